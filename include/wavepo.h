@@ -1,0 +1,178 @@
+/*
+ * wavepo.h -- C ABI of the GB300-native physical-optics (PO) far-field engine.
+ *
+ * The reference (WaveFiber3d) has no library interface: its PO path is a set
+ * of header-only host functions that each driver main() calls in a fixed
+ * order (compareMie/sphere.cu:581-936).  Every entry point below states the
+ * reference function(s) it replaces.  All of them
+ *   - take plain pointers and sizes (no C++ or framework types),
+ *   - order their GPU work on the caller's CUDA stream (`stream`, may be NULL
+ *     for the legacy default stream),
+ *   - report errors through po_status and never exit the process (the
+ *     reference calls exit() from checkCudaErrors, util/helper_cuda.h:583-595).
+ * Device pointers must be valid on the current CUDA device.
+ */
+#ifndef WAVEPO_H
+#define WAVEPO_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PO_MAX_DEPTH 10
+
+typedef enum po_status {
+  PO_OK = 0,
+  PO_ERR_INVALID_ARGUMENT = 1,
+  PO_ERR_CUDA = 2,
+  PO_ERR_OUT_OF_MEMORY = 3,
+  PO_ERR_UNSUPPORTED = 4,
+  PO_ERR_TIMEOUT = 5,
+  PO_ERR_INTERNAL = 6
+} po_status;
+
+/* Arithmetic of the far-field sums. */
+typedef enum po_precision {
+  PO_PREC_FP32 = 0,       /* FP32 sums, FP64 phase arguments where they are large */
+  PO_PREC_FP64 = 1,       /* plain FP64 everywhere (depth 0 only) */
+  PO_PREC_SPLIT_BF16 = 2, /* tensor-core hi+lo BF16 products, FP32 accumulation */
+  PO_PREC_SPLIT_FP16 = 3  /* tensor-core hi+lo FP16 products, FP32 accumulation */
+} po_precision;
+
+/* How the elevation axis is interpolated between tree levels. */
+typedef enum po_theta_mode {
+  /* theta sampled over [-pi/2, 3pi/2) (the sphere covered twice), so that the
+   * trigonometric interpolation sees a smooth 2pi-periodic function */
+  PO_THETA_DOUBLE_COVER = 0,
+  /* as util/interpolation.h:48-77: theta over [-pi/2, pi/2) treated as
+   * pi-periodic (accurate only when the pattern is small at both poles) */
+  PO_THETA_REFERENCE = 1
+} po_theta_mode;
+
+/* Polarisation mask: 'M' (TM) and 'E' (TE) of compareMie/sphere.cu:551-579. */
+#define PO_POL_TM 1
+#define PO_POL_TE 2
+
+typedef struct po_config {
+  int max_depth;                    /* octree depth, 0 = direct sum (sphere.cu:25) */
+  int n_theta[PO_MAX_DEPTH + 1];    /* elevation samples over pi per level; [0] = output grid */
+  int n_phi[PO_MAX_DEPTH + 1];      /* azimuth samples over 2pi per level; [0] = output grid */
+  float box_min[3], box_max[3];     /* root bounding box (sphere.cu:212-216) */
+  int precision;                    /* po_precision */
+  int theta_mode;                   /* po_theta_mode */
+  int nyquist_quirk;                /* PO_THETA_REFERENCE only: split the theta Nyquist bin
+                                       only where interpolation.h:66's launch reaches */
+  double distance;                  /* observer distance Dis of the prefactors (sphere.cu:46) */
+} po_config;
+
+typedef struct po_geometry {
+  int64_t n;                        /* number of surface points */
+  const float *x, *y, *z;           /* positions (m), SoA (sphere.cu:94-125) */
+  const float *nx, *ny, *nz;        /* unit outward normals */
+  const float *area;                /* area per point (m^2) */
+  int on_device;                    /* 1: device pointers, 0: host pointers */
+} po_geometry;
+
+typedef struct po_illum {
+  int n_lambda;                     /* wavelengths (m): sphere.cu:486-490 loops over these */
+  const double *lambda_m;
+  int n_inc;                        /* incident directions (radians, elevation/azimuth as */
+  const double *theta_i;            /*   treePO.cu:559-564 and sphere.cu:544-562)          */
+  const double *phi_i;
+  int pol_mask;                     /* PO_POL_TM | PO_POL_TE */
+  double eta_re, eta_im;            /* complex index of refraction of the scatterer */
+  double sigma;                     /* Gaussian beam width (m), tangentplane.h:33-34 */
+} po_illum;
+
+typedef struct po_report {
+  double ms_total;                  /* device time of the whole solve (CUDA events) */
+  double ms_build;                  /* octree build */
+  double ms_leaf;                   /* leaf / direct far-field sums */
+  double ms_aggregate;              /* interpolation + translation + child sums */
+  double ms_intensity;              /* projection, intensity, output copy */
+  int64_t n_leaves;                 /* active nodes at the deepest level */
+  int64_t n_nodes_total;            /* active nodes over all levels */
+  int root_theta, root_phi;         /* root grid actually used (output x supersampling) */
+  int64_t workspace_bytes;          /* device workspace held by the context */
+  int64_t kernel_launches;          /* kernels launched by the solve */
+} po_report;
+
+typedef struct po_ctx po_ctx;
+
+/* ---- configuration helpers --------------------------------------------- */
+
+/* Fills cfg with defaults and the per-level grids of the reference rule
+ * n(i) = ceil(k d_i + beta (k d_i)^(1/3)), k = 2 pi / lambda_min,
+ * d_i = 0.5^i * extent * ratio (compareMie/sphere.cu:345-352,
+ * fibersim/treePO.cu:353-359).  Level 0 is the n_theta_out x n_phi_out grid. */
+po_status po_config_init(po_config *cfg, int max_depth, int n_theta_out, int n_phi_out,
+                         const float box_min[3], const float box_max[3], double theta_extent,
+                         double phi_extent, double ratio, double beta, double lambda_min);
+
+const char *po_status_string(po_status s);
+/* Message of the last failing call on this host thread (never NULL). */
+const char *po_last_error(void);
+
+/* ---- whole solve (replaces the driver main() of sphere.cu / ellipsoid.cu /
+ *      treePO.cu from the octree build to the intensity write, :212-936) --- */
+
+po_status po_create(po_ctx **ctx, const po_config *cfg);
+po_status po_destroy(po_ctx *ctx);
+/* intensity: [n_lambda][n_inc][n_pol][n_theta[0]][n_phi[0]] float32, host or
+ * device memory (out_on_device).  Polarisations in the order TM, TE. */
+po_status po_solve(po_ctx *ctx, const po_geometry *geom, const po_illum *illum, float *intensity,
+                   int out_on_device, void *stream, po_report *report);
+
+/* ---- single steps of the path (device pointers) ------------------------ */
+
+/* util/tangentplane.h:84-92 (computeLocalTangentPlane) and, when scale != 0,
+ * util/fields.h:123 (field_times_area) and :147 (multiply_current_factor) with
+ * the prefactors of compareMie/sphere.cu:491-494.
+ * currents: n x [Jx,Jy,Jz,Mx,My,Mz] complex64 (float2 pairs), point-major. */
+po_status po_tangent_plane_currents(int64_t n, const float *x, const float *y, const float *z,
+                                    const float *nx, const float *ny, const float *nz, const float *area,
+                                    double lambda_m, double theta_i, double phi_i, int pol, double eta_re,
+                                    double eta_im, double sigma, double distance, int scale, float *currents,
+                                    void *stream);
+
+/* util/tree.h:289-715 (build_octree_kernel) + compareMie/sphere.cu:255-307.
+ * perm[i] = input index of the point at tree position i (the stable octant
+ * order of the reference).  heap_range, if not NULL, receives (begin, end)
+ * for every node of the full 8-ary heap of (8^(depth+1)-1)/7 nodes, in the
+ * reference's heap order. */
+po_status po_build_octree(int64_t n, const float *x, const float *y, const float *z, const float box_min[3],
+                          const float box_max[3], int depth, int32_t *perm, int32_t *heap_range, void *stream);
+
+/* current_times_green_center + thrust::reduce over all points
+ * (util/fields.h:2-50, compareMie/sphere.cu:603-658 at depth 0):
+ * F_c(s) = sum_p exp(+i k s.(x_p - center)) cur_p[c] on an n_theta x n_phi grid.
+ * currents: n x 6 complex64 (as above); fields out: [6][n_theta][n_phi] complex64
+ * (the reference's separate Ex..Hz arrays).  precision: PO_PREC_FP32 or PO_PREC_FP64. */
+po_status po_far_field_direct(int64_t n, const float *x, const float *y, const float *z, const float *currents,
+                              double k, const double center[3], int n_theta, int n_phi, int precision,
+                              float *fields, void *stream);
+
+/* util/interpolation.h:82-93 (copyandinterp -> interpFFT): trigonometric
+ * upsampling of `batch` patterns [th_c][ph_c] -> [th_p][ph_p] (complex64),
+ * phi first, then theta, with hand-written shared-memory FFTs.
+ * theta_mode PO_THETA_REFERENCE treats theta as pi-periodic exactly as the
+ * reference; PO_THETA_DOUBLE_COVER expects th_c / th_p samples over 2pi.
+ * Scratch of batch*th_c*ph_p complex64 is taken from the stream-ordered
+ * allocator. */
+po_status po_interp_fft(const float *in, int th_c, int ph_c, float *out, int th_p, int ph_p, int batch,
+                        int theta_mode, int nyquist_quirk, void *stream);
+
+/* util/fields.h:172-204 (computeintensity): projection onto the transverse
+ * plane and |E - Z0 s x H|^2.  fields: [6][n_theta][n_phi] complex64. */
+po_status po_compute_intensity(const float *fields, int n_theta, int n_phi, float *intensity, void *stream);
+
+/* Library build identification (sm arch, version). */
+const char *po_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* WAVEPO_H */

@@ -1,0 +1,262 @@
+"""GPU parity of every step of the PO path against the FP64 oracle and the
+reference's own CUDA outputs (tests/golden/ref_*.bin).
+
+Tolerances (relative L2 over the whole output):
+  currents, direct sums, intensity, interpolation : 1e-5 (FP32 engine vs FP64)
+  octree                                           : bit-exact
+  tree solve vs FP64 direct sum (double cover)     : 1e-4
+  tree solve, reference theta mode vs oracle tree  : 1e-4
+  anything vs the reference's FP32 CUDA build      : 1e-4
+"""
+import math
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, case_illum, load_case_geometry
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+if not torch.cuda.is_available():
+    pytest.skip("needs a CUDA GPU", allow_module_level=True)
+
+import oracle  # noqa: E402
+from wavefiber3d_gb300 import api, geometry  # noqa: E402
+
+TOL_FP32 = 1e-5
+TOL_TREE = 1e-4
+
+
+def rel(a, b):
+    a = np.asarray(a, dtype=np.complex128 if np.iscomplexobj(a) else np.float64)
+    b = np.asarray(b, dtype=np.complex128 if np.iscomplexobj(b) else np.float64)
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def ref_fixture(name, dtype=np.float32):
+    p = GOLDEN / f"{name}.bin"
+    if not p.exists():
+        pytest.fail(f"golden fixture {p.name} missing")
+    return np.fromfile(p, dtype=dtype)
+
+
+def illum_of(case):
+    il = case["illum"]
+    pol = api.PO_POL_TE if il["mode"] == "E" else api.PO_POL_TM
+    return api.Illumination([il["lambda_m"]], [il["theta_i"]], [il["phi_i"]], pol, complex(*il["eta"]), il["sigma"])
+
+
+def cur_gpu(cloud, il, scale):
+    return api.compute_local_tangent_plane(cloud.x, cloud.y, cloud.z, cloud.nx, cloud.ny, cloud.nz, cloud.area,
+                                           il.lambda_m, il.theta_i, il.phi_i, "E" if il.mode_te else "M",
+                                           complex(il.eta_re, il.eta_im), il.sigma, 1.0, scale).cpu().numpy()
+
+
+# ------------------------------------------------------------------ currents
+@pytest.mark.parametrize("name", ["ref_currents_sphere_M", "ref_currents_ellipsoid_E"])
+@pytest.mark.parametrize("scale", [False, True])
+def test_currents_vs_oracle(cases, name, scale):
+    c = cases[name]
+    cloud, il = load_case_geometry(c), case_illum(c)
+    g = cur_gpu(cloud, il, scale)
+    o = oracle.currents(cloud, il, scale=scale)
+    assert rel(g, o) < TOL_FP32
+    # shadowed points carry no current (tangentplane.h:64-67)
+    lit = np.abs(o).sum(1) > 0
+    assert np.all(np.abs(g[~lit]) == 0)
+
+
+@pytest.mark.parametrize("name", ["ref_currents_sphere_M", "ref_currents_ellipsoid_E"])
+def test_currents_vs_reference_build(cases, name):
+    c = cases[name]
+    cloud, il = load_case_geometry(c), case_illum(c)
+    g = cur_gpu(cloud, il, False)
+    r = ref_fixture(name).reshape(-1, 12).astype(np.float64).view(np.complex128)
+    assert rel(g, r) < TOL_FP32
+
+
+# ------------------------------------------------------------------- octree
+def _octree_case(cloud, box, depth):
+    perm, hr = api.build_octree(cloud.x, cloud.y, cloud.z, box[:3], box[3:], depth)
+    operm, orng, _ = oracle.octree(cloud, box[:3], box[3:], depth)
+    assert np.array_equal(perm.cpu().numpy(), operm)
+    assert np.array_equal(hr.cpu().numpy(), orng)
+
+
+@pytest.mark.parametrize("depth", [0, 1, 3, 5])
+def test_octree_vs_oracle(cases, depth):
+    c = cases["ref_octree_ellipsoid_d3"]
+    _octree_case(load_case_geometry(c), c["box"], depth)
+
+
+def test_octree_boundary_points():
+    # points exactly on the float split planes and outside the root box
+    rng = np.random.default_rng(7)
+    box = [-1.0, -1.0, -1.0, 1.0, 1.0, 1.0]
+    pts = rng.choice(np.array([-1.0, -0.5, -0.25, 0.0, 0.25, 0.5, 0.999, 1.0, 1.5, -1.5], np.float32), size=(3, 4000))
+    z = np.zeros(4000, np.float32)
+    cloud = geometry.PointCloud(pts[0], pts[1], pts[2], z, z, z + 1, z + 1)
+    for depth in (1, 2, 4):
+        _octree_case(cloud, box, depth)
+
+
+def test_octree_vs_reference_build(cases):
+    c = cases["ref_octree_ellipsoid_d3"]
+    cloud = load_case_geometry(c)
+    n, d = cloud.n, c["depth"]
+    raw = ref_fixture(c["name"], np.uint8)
+    geo = np.frombuffer(raw[: 28 * n].tobytes(), dtype=np.float32).reshape(7, n)
+    rng = np.frombuffer(raw[28 * n:].tobytes(), dtype=np.int32).reshape(-1, 2)
+    perm, hr = api.build_octree(cloud.x, cloud.y, cloud.z, c["box"][:3], c["box"][3:], d)
+    perm = perm.cpu().numpy()
+    assert np.array_equal(cloud.soa()[:, perm], geo)
+    assert np.array_equal(hr.cpu().numpy(), rng)
+
+
+# ------------------------------------------------------------ interpolation
+@pytest.mark.parametrize("src,dst,quirk", [((20, 30), (33, 300), True), ((20, 30), (33, 300), False),
+                                           ((21, 25), (40, 64), True), ((16, 16), (16, 16), True),
+                                           ((37, 37), (48, 96), True), ((24, 50), (394, 197), False),
+                                           ((7, 11), (13, 1440), True)])
+def test_interp_vs_oracle(src, dst, quirk):
+    rng = np.random.default_rng(src[0] * 1000 + dst[1])
+    z = (rng.standard_normal(src) + 1j * rng.standard_normal(src)).astype(np.complex64)
+    g = api.copyandinterp(torch.from_numpy(z), dst[0], dst[1], api.PO_THETA_REFERENCE, quirk).cpu().numpy()
+    o = oracle.interp(z.astype(np.complex128), dst[0], dst[1], quirk)
+    assert rel(g, o) < TOL_FP32
+
+
+def test_interp_batched_matches_single():
+    rng = np.random.default_rng(3)
+    z = (rng.standard_normal((5, 12, 18)) + 1j * rng.standard_normal((5, 12, 18))).astype(np.complex64)
+    b = api.copyandinterp(torch.from_numpy(z), 30, 40).cpu().numpy()
+    for i in range(5):
+        s = api.copyandinterp(torch.from_numpy(z[i]), 30, 40).cpu().numpy()
+        assert np.array_equal(b[i], s)
+
+
+@pytest.mark.parametrize("name", ["ref_interp_even", "ref_interp_odd"])
+def test_interp_vs_reference_build(cases, name):
+    c = cases[name]
+    z = np.fromfile(GOLDEN / c["input"], dtype=np.complex64).reshape(c["src"])
+    g = api.copyandinterp(torch.from_numpy(z), *c["dst"], api.PO_THETA_REFERENCE, True).cpu().numpy()
+    r = ref_fixture(name).view(np.complex64).reshape(c["dst"])
+    assert rel(g, r) < TOL_FP32
+
+
+# ------------------------------------------------------ direct sum, intensity
+@pytest.mark.parametrize("prec,tol", [(api.PO_PREC_FP32, TOL_FP32), (api.PO_PREC_FP64, 1e-6)])
+def test_direct_sum_vs_oracle(cases, prec, tol):
+    c = cases["ref_currents_ellipsoid_E"]
+    cloud, il = load_case_geometry(c), case_illum(c)
+    cur = oracle.currents(cloud, il, scale=True)
+    k = 2 * math.pi / il.lambda_m
+    ctr = (0.1e-6, -0.2e-6, 0.05e-6)
+    g = api.current_times_green_center(cloud.x, cloud.y, cloud.z, torch.from_numpy(cur.astype(np.complex64)), k, ctr,
+                                       24, 48, prec).cpu().numpy()
+    o = oracle.far_field(cloud, cur, k, ctr, 24, 48)  # [dir][6]
+    assert rel(g.reshape(6, -1).T, o) < tol
+
+
+def test_intensity_vs_oracle():
+    rng = np.random.default_rng(11)
+    f = (rng.standard_normal((6, 20, 36)) + 1j * rng.standard_normal((6, 20, 36))) * 1e-6
+    g = api.compute_intensity(torch.from_numpy(f.astype(np.complex64))).cpu().numpy()
+    o = oracle.intensity(f.reshape(6, -1).T.copy(), 20, 36)
+    assert rel(g, o) < TOL_FP32
+
+
+# ---------------------------------------------------------------- full solve
+def _solve(cloud, cfg, illum, device_io=False):
+    with api.Solver(cfg) as s:
+        if device_io:
+            g = torch.from_numpy(cloud.soa()).cuda()
+            out = s.solve(tuple(g[k] for k in range(7)), illum).cpu().numpy()
+        else:
+            out = s.solve(cloud, illum)
+        return out, s.last_report
+
+
+@pytest.mark.parametrize("prec,tol", [(api.PO_PREC_FP32, TOL_FP32), (api.PO_PREC_FP64, 1e-6)])
+def test_solve_depth0_vs_oracle(cases, prec, tol):
+    c = cases["ref_solve_sphere_d0"]
+    cloud, il = load_case_geometry(c), case_illum(c)
+    cfg = api.Config(0, [48], [96], c["box"][:3], c["box"][3:], precision=prec)
+    out, _ = _solve(cloud, cfg, illum_of(c))
+    o = oracle.solve_direct(cloud, il, 48, 96)
+    assert rel(out.reshape(48, 96), o) < tol
+
+
+@pytest.mark.parametrize("name", ["ref_solve_sphere_d3", "ref_solve_ellipsoid_d2", "ref_solve_sphere_quirk_d1"])
+def test_solve_tree_vs_fp64_direct(cases, name):
+    c = cases[name]
+    cloud, il = load_case_geometry(c), case_illum(c)
+    cfg = api.Config(c["depth"], c["n_theta"], c["n_phi"], c["box"][:3], c["box"][3:])
+    out, rep = _solve(cloud, cfg, illum_of(c), device_io=True)
+    ctr = [(c["box"][i] + c["box"][i + 3]) / 2 for i in range(3)]
+    o = oracle.solve_direct(cloud, il, c["n_theta"][0], c["n_phi"][0], center=ctr)
+    assert rel(out.reshape(o.shape), o) < TOL_TREE, rep
+
+
+@pytest.mark.parametrize("name", ["ref_solve_sphere_d3", "ref_solve_ellipsoid_d2", "ref_solve_sphere_quirk_d1"])
+def test_solve_reference_mode_vs_oracle_tree(cases, name):
+    c = cases[name]
+    cloud, il = load_case_geometry(c), case_illum(c)
+    cfg = api.Config(c["depth"], c["n_theta"], c["n_phi"], c["box"][:3], c["box"][3:],
+                     theta_mode=api.PO_THETA_REFERENCE, nyquist_quirk=True)
+    out, _ = _solve(cloud, cfg, illum_of(c))
+    o = oracle.solve_tree(cloud, il, c["box"][:3], c["box"][3:], c["depth"], c["n_theta"], c["n_phi"], True)
+    assert rel(out.reshape(o.shape), o) < TOL_TREE
+
+
+@pytest.mark.parametrize("name", ["ref_solve_sphere_d0", "ref_solve_sphere_d3", "ref_solve_ellipsoid_d2",
+                                  "ref_solve_sphere_quirk_d1"])
+def test_solve_vs_reference_build(cases, name):
+    c = cases[name]
+    cloud = load_case_geometry(c)
+    cfg = api.Config(c["depth"], c["n_theta"], c["n_phi"], c["box"][:3], c["box"][3:],
+                     theta_mode=api.PO_THETA_REFERENCE, nyquist_quirk=True)
+    out, _ = _solve(cloud, cfg, illum_of(c))
+    r = ref_fixture(name).reshape(c["n_theta"][0], c["n_phi"][0])
+    assert rel(out.reshape(r.shape), r) < TOL_TREE
+
+
+def test_batched_patterns_match_single_solves():
+    cloud = geometry.ellipsoid((1.5e-6, 1.0e-6, 0.8e-6), 3000)
+    box = [-1.65e-6, -1.1e-6, -0.88e-6, 1.65e-6, 1.1e-6, 0.88e-6]
+    cfg = api.Config.reference_rule(2, 32, 64, box[:3], box[3:], 1.6e-6, 3.0e-6, 1.2)
+    lams, ths, phs = [450e-9, 600e-9], [0.2, -0.4, 1.0], [0.3, 2.0, -1.0]
+    il = api.Illumination(lams, ths, phs, api.PO_POL_TM | api.PO_POL_TE, 1.55 + 0.1j, 2e-6)
+    with api.Solver(cfg) as s:
+        allp = s.solve(cloud, il)
+        for li, lam in enumerate(lams):
+            for ii in range(3):
+                for pi, pol in enumerate((api.PO_POL_TM, api.PO_POL_TE)):
+                    one = s.solve(cloud, api.Illumination([lam], [ths[ii]], [phs[ii]], pol, 1.55 + 0.1j, 2e-6))
+                    assert rel(allp[li, ii, pi], one[0, 0, 0]) < 1e-6
+
+
+def test_empty_and_single_point():
+    box = [-1e-6] * 3 + [1e-6] * 3
+    il = api.Illumination([500e-9], [0.3], [0.2])
+    for depth in (0, 2):
+        cfg = api.Config.reference_rule(depth, 16, 32, box[:3], box[3:], 2e-6, 2e-6, 1.3)
+        z = np.zeros(0, np.float32)
+        out, _ = _solve(geometry.PointCloud(z, z, z, z, z, z, z), cfg, il)
+        assert np.all(out == 0)
+        one = geometry.PointCloud([0.3e-6], [-0.2e-6], [0.1e-6], [-1.0], [0.0], [0.0], [1e-14])
+        out, _ = _solve(one, cfg, il)
+        o = oracle.solve_direct(one, oracle.make_illum(500e-9, 0.3, 0.2), 16, 32)
+        assert rel(out.reshape(16, 32), o) < TOL_TREE
+
+
+def test_invalid_arguments_raise():
+    box = [-1e-6] * 3 + [1e-6] * 3
+    with pytest.raises(api.WavePOError):
+        api.Solver(api.Config(2, [16, 40, 20], [32, 40, 50], box[:3], box[3:]))  # grids grow with depth
+    with pytest.raises(api.WavePOError):
+        api.Solver(api.Config(1, [16, 8], [32, 8], box[:3], box[:3]))  # empty box
+    cfg = api.Config.reference_rule(1, 16, 32, box[:3], box[3:], 2e-6, 2e-6, 1.3)
+    with api.Solver(cfg) as s, pytest.raises(api.WavePOError):
+        s.solve(geometry.fibonacci_sphere(1e-6, 100), api.Illumination([-5e-7], [0.0], [0.0]))

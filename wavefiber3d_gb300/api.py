@@ -1,0 +1,275 @@
+"""Python mirror of the reference's PO operators, running on the CUDA library.
+
+Names follow the reference's host functions so that a driver written against
+util/*.h maps one to one:
+
+  compute_local_tangent_plane   util/tangentplane.h:84   (+ field_times_area fields.h:123,
+                                                          multiply_current_factor fields.h:147)
+  build_octree                  util/tree.h:290          (+ active lists, sphere.cu:255-307)
+  current_times_green_center    util/fields.h:41 + per-node thrust::reduce (depth 0)
+  copyandinterp                 util/interpolation.h:82
+  compute_intensity             util/fields.h:172
+  Solver.solve                  the driver main() of compareMie/sphere.cu:212-936
+
+Arrays are torch tensors on the current CUDA device (PyTorch is used only for
+device memory and streams).  Errors raise WavePOError instead of exiting the
+process as the reference does (util/helper_cuda.h:583-595).
+"""
+from __future__ import annotations
+
+import ctypes
+import dataclasses
+import math
+from typing import Sequence
+
+import numpy as np
+
+from . import _lib
+from ._lib import (PO_POL_TE, PO_POL_TM, PO_PREC_FP32, PO_PREC_FP64, PO_THETA_DOUBLE_COVER, PO_THETA_REFERENCE,
+                   WavePOError, check)
+
+__all__ = ["Config", "Illumination", "Solver", "compute_local_tangent_plane", "build_octree",
+           "current_times_green_center", "copyandinterp", "compute_intensity", "wavelength_from_index",
+           "incidence_from_index", "WavePOError", "PO_POL_TM", "PO_POL_TE", "PO_PREC_FP32", "PO_PREC_FP64",
+           "PO_THETA_DOUBLE_COVER", "PO_THETA_REFERENCE"]
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def _stream_ptr(stream=None):
+    torch = _torch()
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return ctypes.c_void_p(s.cuda_stream)
+
+
+def _dev(t, dtype=None):
+    torch = _torch()
+    if not isinstance(t, torch.Tensor):
+        t = torch.as_tensor(np.asarray(t))
+    if dtype is not None:
+        t = t.to(dtype)
+    return t.cuda().contiguous()
+
+
+def _ptr(t):
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def wavelength_from_index(i: int, n: int = 25, lo_nm: float = 400.0, hi_nm: float = 700.0) -> float:
+    """Reference wavelength list (compareMie/sphere.cu:489): lo + (hi-lo)/n * i nm, in metres."""
+    return (lo_nm + (hi_nm - lo_nm) / n * i) * 1e-9
+
+
+def incidence_from_index(theta_index: int, phi_index: int, n_theta: int = 180, n_phi: int = 360):
+    """Incident angles of fibersim/treePO.cu:559-564 from the 180 x 360 index grid."""
+    th = -math.pi / 2 + 1e-10 + math.pi / n_theta * theta_index
+    ph = 2 * math.pi / n_phi * phi_index
+    return th, ph
+
+
+@dataclasses.dataclass
+class Config:
+    """Mirror of po_config.  Use Config.reference_rule for the reference's grids."""
+    max_depth: int
+    n_theta: Sequence[int]
+    n_phi: Sequence[int]
+    box_min: Sequence[float]
+    box_max: Sequence[float]
+    precision: int = PO_PREC_FP32
+    theta_mode: int = PO_THETA_DOUBLE_COVER
+    nyquist_quirk: bool = True
+    distance: float = 1.0
+
+    @classmethod
+    def reference_rule(cls, max_depth, n_theta_out, n_phi_out, box_min, box_max, theta_extent, phi_extent,
+                       ratio, beta=6.0, lambda_min=0.4e-6, **kw):
+        c = _lib.po_config()
+        bmin = (ctypes.c_float * 3)(*box_min)
+        bmax = (ctypes.c_float * 3)(*box_max)
+        check(_lib.load().po_config_init(ctypes.byref(c), max_depth, n_theta_out, n_phi_out, bmin, bmax,
+                                         theta_extent, phi_extent, ratio, beta, lambda_min))
+        return cls(max_depth, list(c.n_theta[:max_depth + 1]), list(c.n_phi[:max_depth + 1]), list(box_min),
+                   list(box_max), **kw)
+
+    def to_c(self) -> _lib.po_config:
+        c = _lib.po_config()
+        c.max_depth = self.max_depth
+        for i, (t, p) in enumerate(zip(self.n_theta, self.n_phi)):
+            c.n_theta[i] = int(t)
+            c.n_phi[i] = int(p)
+        for a in range(3):
+            c.box_min[a] = float(self.box_min[a])
+            c.box_max[a] = float(self.box_max[a])
+        c.precision = int(self.precision)
+        c.theta_mode = int(self.theta_mode)
+        c.nyquist_quirk = 1 if self.nyquist_quirk else 0
+        c.distance = float(self.distance)
+        return c
+
+
+@dataclasses.dataclass
+class Illumination:
+    """Mirror of po_illum: every (wavelength, incidence, polarisation) is one pattern."""
+    wavelengths_m: Sequence[float]
+    theta_i: Sequence[float]
+    phi_i: Sequence[float]
+    pol_mask: int = PO_POL_TM
+    eta: complex = 1.55 + 0j
+    sigma: float = 1e-2
+
+    @property
+    def n_patterns(self) -> int:
+        npol = (1 if self.pol_mask & PO_POL_TM else 0) + (1 if self.pol_mask & PO_POL_TE else 0)
+        return len(self.wavelengths_m) * len(self.theta_i) * npol
+
+    def to_c(self):
+        lam = np.ascontiguousarray(self.wavelengths_m, dtype=np.float64)
+        th = np.ascontiguousarray(self.theta_i, dtype=np.float64)
+        ph = np.ascontiguousarray(self.phi_i, dtype=np.float64)
+        if th.shape != ph.shape:
+            raise ValueError("theta_i and phi_i must have the same length")
+        il = _lib.po_illum(lam.size, lam.ctypes.data, th.size, th.ctypes.data, ph.ctypes.data, int(self.pol_mask),
+                           float(np.real(self.eta)), float(np.imag(self.eta)), float(self.sigma))
+        return il, (lam, th, ph)
+
+
+class Solver:
+    """Whole PO solve (po_create / po_solve / po_destroy)."""
+
+    def __init__(self, config: Config):
+        self.config = config
+        self._c = config.to_c()
+        h = ctypes.c_void_p()
+        check(_lib.load().po_create(ctypes.byref(h), ctypes.byref(self._c)))
+        self._h = h
+        self.last_report: dict = {}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib.load().po_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def out_shape(self, illum: Illumination):
+        npol = (1 if illum.pol_mask & PO_POL_TM else 0) + (1 if illum.pol_mask & PO_POL_TE else 0)
+        return (len(illum.wavelengths_m), len(illum.theta_i), npol, int(self.config.n_theta[0]),
+                int(self.config.n_phi[0]))
+
+    def solve(self, cloud, illum: Illumination, out=None, stream=None):
+        """cloud: PointCloud (host numpy) or a (7, n) float32 CUDA tensor / tuple of 7 CUDA tensors.
+        Returns intensity [L][I][P][n_theta][n_phi] float32 (numpy for host geometry without `out`,
+        else the CUDA tensor `out` or a new CUDA tensor)."""
+        torch = _torch()
+        il, keep = illum.to_c()
+        host = hasattr(cloud, "soa")
+        if host:
+            soa = np.ascontiguousarray(cloud.soa(), dtype=np.float32)
+            n = soa.shape[1]
+            base = soa.ctypes.data
+            ptrs = [base + 4 * n * k for k in range(7)]
+            g = _lib.po_geometry(n, *ptrs, 0)
+        else:
+            arrs = [cloud[k] for k in range(7)]
+            for a in arrs:
+                if not (a.is_cuda and a.dtype == torch.float32 and a.is_contiguous()):
+                    raise ValueError("device geometry must be 7 contiguous float32 CUDA arrays")
+            n = arrs[0].numel()
+            g = _lib.po_geometry(n, *[a.data_ptr() for a in arrs], 1)
+        rep = _lib.po_report()
+        shape = self.out_shape(illum)
+        if out is None and host:
+            res = np.empty(shape, dtype=np.float32)
+            check(_lib.load().po_solve(self._h, ctypes.byref(g), ctypes.byref(il), res.ctypes.data, 0,
+                                       _stream_ptr(stream), ctypes.byref(rep)))
+        else:
+            res = out if out is not None else torch.empty(shape, dtype=torch.float32, device="cuda")
+            if not (res.is_cuda and res.is_contiguous() and res.numel() == int(np.prod(shape))):
+                raise ValueError(f"out must be a contiguous CUDA tensor with {int(np.prod(shape))} elements")
+            check(_lib.load().po_solve(self._h, ctypes.byref(g), ctypes.byref(il), ctypes.c_void_p(res.data_ptr()),
+                                       1, _stream_ptr(stream), ctypes.byref(rep)))
+        self.last_report = rep.as_dict()
+        del keep
+        return res
+
+
+def compute_local_tangent_plane(x, y, z, nx, ny, nz, area, wavelength_m, theta_i, phi_i, mode="M", eta=1.55 + 0j,
+                                sigma=1e-2, distance=1.0, scale=True, stream=None):
+    """Surface currents (n, 6) complex64 [Jx,Jy,Jz,Mx,My,Mz]: computeLocalTangentPlane
+    (tangentplane.h:84) and, if `scale`, field_times_area and multiply_current_factor."""
+    torch = _torch()
+    t = [_dev(a, torch.float32) for a in (x, y, z, nx, ny, nz, area)]
+    n = t[0].numel()
+    out = torch.empty((n, 6), dtype=torch.complex64, device="cuda")
+    pol = PO_POL_TE if mode in ("E", "TE", PO_POL_TE) else PO_POL_TM
+    check(_lib.load().po_tangent_plane_currents(n, *[_ptr(a) for a in t], wavelength_m, theta_i, phi_i, pol,
+                                                float(np.real(eta)), float(np.imag(eta)), sigma, distance,
+                                                1 if scale else 0, _ptr(out), _stream_ptr(stream)))
+    return out
+
+
+def build_octree(x, y, z, box_min, box_max, depth: int, heap_ranges: bool = True, stream=None):
+    """Octree of util/tree.h:290: returns (perm, heap_range) where perm[i] is the input
+    index of the point at tree position i and heap_range[h] = (begin, end) of heap node h."""
+    torch = _torch()
+    t = [_dev(a, torch.float32) for a in (x, y, z)]
+    n = t[0].numel()
+    perm = torch.empty(max(n, 1), dtype=torch.int32, device="cuda")
+    nn = (8 ** (depth + 1) - 1) // 7
+    hr = torch.empty((nn, 2), dtype=torch.int32, device="cuda") if heap_ranges else None
+    bmin = (ctypes.c_float * 3)(*box_min)
+    bmax = (ctypes.c_float * 3)(*box_max)
+    check(_lib.load().po_build_octree(n, *[_ptr(a) for a in t], bmin, bmax, depth, _ptr(perm),
+                                      _ptr(hr) if hr is not None else None, _stream_ptr(stream)))
+    return perm[:n], hr
+
+
+def current_times_green_center(x, y, z, currents, k, center, n_theta, n_phi, precision=PO_PREC_FP32, stream=None):
+    """Depth-0 far field: sum_p exp(+i k s.(x_p - center)) currents_p on the
+    n_theta x n_phi grid; returns (6, n_theta, n_phi) complex64."""
+    torch = _torch()
+    t = [_dev(a, torch.float32) for a in (x, y, z)]
+    cur = _dev(currents, torch.complex64)
+    n = t[0].numel()
+    out = torch.empty((6, n_theta, n_phi), dtype=torch.complex64, device="cuda")
+    c = (ctypes.c_double * 3)(*center)
+    check(_lib.load().po_far_field_direct(n, *[_ptr(a) for a in t], _ptr(cur), float(k), c, n_theta, n_phi,
+                                          precision, _ptr(out), _stream_ptr(stream)))
+    return out
+
+
+def copyandinterp(patterns, th_p, ph_p, theta_mode=PO_THETA_REFERENCE, nyquist_quirk=True, stream=None):
+    """Trigonometric upsampling of (batch, th_c, ph_c) complex patterns (interpolation.h:82)."""
+    torch = _torch()
+    p = _dev(patterns, torch.complex64)
+    squeeze = p.dim() == 2
+    if squeeze:
+        p = p.unsqueeze(0)
+    b, th_c, ph_c = p.shape
+    out = torch.empty((b, th_p, ph_p), dtype=torch.complex64, device="cuda")
+    check(_lib.load().po_interp_fft(_ptr(p), th_c, ph_c, _ptr(out), th_p, ph_p, b, theta_mode,
+                                    1 if nyquist_quirk else 0, _stream_ptr(stream)))
+    return out[0] if squeeze else out
+
+
+def compute_intensity(fields, stream=None):
+    """computeintensity (fields.h:172): (6, n_theta, n_phi) complex -> (n_theta, n_phi) float32."""
+    torch = _torch()
+    f = _dev(fields, torch.complex64)
+    _, nth, nph = f.shape
+    out = torch.empty((nth, nph), dtype=torch.float32, device="cuda")
+    check(_lib.load().po_compute_intensity(_ptr(f), nth, nph, _ptr(out), _stream_ptr(stream)))
+    return out

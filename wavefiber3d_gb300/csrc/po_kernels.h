@@ -1,0 +1,69 @@
+// po_kernels.h -- kernel launchers shared between the engine's translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "po_common.cuh"
+#include "wavepo.h"
+
+namespace wavepo {
+
+constexpr int kMaxStages = 24;
+
+// Stockham FFT plan: radix sequence and offset of the W_n table in the
+// engine's twiddle buffer.
+struct FftPlan {
+  int n = 0;
+  int tw = 0;
+  int nstages = 0;
+  int radix[kMaxStages];
+};
+
+int fft_plan(int n, int *radix);
+FftPlan make_plan(int n, int tw_offset);
+po_status launch_twiddles(int n, float2 *out, cudaStream_t st);
+
+// currents: out[slot][n][6] complex (T pairs)
+po_status launch_currents_f32(int64_t n, const float *const g[7], const SlotParams<float> *slots_dev, int n_slots,
+                              float *out, cudaStream_t st);
+po_status launch_currents_f64(int64_t n, const float *const g[7], const SlotParams<double> *slots_dev, int n_slots,
+                              double *out, cudaStream_t st);
+
+// leaf far fields: out[slot][leaf][comp][dir]; slots grouped by wavelength (G per lambda)
+po_status launch_leaf(const float *const g[7], const int32_t *leaf_begin, const double *leaf_center,
+                      int64_t n_leaves, const SlotParams<float> *slots_dev, int n_lambda, int G,
+                      const float4 *dirs, int ndir, float2 *out, cudaStream_t st);
+
+int direct_splits(int64_t n, int ndir, int n_lambda, int sm_count);
+// FP32 depth-0 sum about c0: out[slot][comp][dir]; cur[slot][n][6]
+po_status launch_direct_f32(int64_t n, const float *x, const float *y, const float *z, const float2 *cur,
+                            double *tile_ctr, const double *k_per_lambda, int n_lambda, int G,
+                            const double c0[3], const float4 *dirs, const double *dirs_d, int ndir, int nsplit,
+                            float2 *partial, float2 *out, cudaStream_t st);
+// FP64 depth-0 sum (k per slot): out[slot][comp][dir]
+po_status launch_direct_f64(int64_t n, const float *x, const float *y, const float *z, const double2 *cur,
+                            const double *k_per_slot, int n_slots, const double c0[3], const double *dirs_d,
+                            int ndir, int nsplit, double2 *partial, double2 *out, cudaStream_t st);
+
+// complex64 <-> complex128 copies of n complex values
+po_status launch_widen(const float *in, double2 *out, int64_t n, cudaStream_t st);
+po_status launch_narrow(const double2 *in, float2 *out, int64_t n, cudaStream_t st);
+
+// interpolation passes
+po_status launch_interp_rows(const float2 *src, float2 *dst, int64_t nrows, const FftPlan &pin, const FftPlan &pout,
+                             const float2 *twiddles, float scale, int sm_count, cudaStream_t st);
+po_status launch_interp_cols(const float2 *mid, float2 *parent, const int32_t *child_table, int64_t n_parent,
+                             int64_t n_child, int phi, const FftPlan &pin, const FftPlan &pout,
+                             const float2 *twiddles, const float4 *trans, int n_slots, int G, int quirk_reach,
+                             float scale, int ncomp, cudaStream_t st);
+po_status launch_trans_table(const double *k_per_lambda, int n_lambda, int nth, int Tp, int phi, const double a[3],
+                             float4 *out, cudaStream_t st);
+
+// intensity: fields [slot][comp][T][Phi] (root, possibly supersampled by
+// (mt, mp)) -> out [slot][nth][nph]
+po_status launch_intensity_f32(const float2 *fields, int n_slots, int T, int Phi, int nth, int nph, int mt, int mp,
+                               float *out, cudaStream_t st);
+po_status launch_intensity_f64(const double2 *fields, int n_slots, int nth, int nph, float *out, cudaStream_t st);
+
+}  // namespace wavepo

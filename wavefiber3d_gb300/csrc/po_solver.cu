@@ -1,0 +1,644 @@
+// po_solver.cu -- host orchestration of the PO solve and the C ABI.
+//
+// One call of po_solve does what the reference's driver main() does from the
+// octree build to the intensity write (compareMie/sphere.cu:212-936,
+// fibersim/treePO.cu:230-961), for every wavelength, incidence and
+// polarisation at once:
+//   geometry (H2D if host) -> octree (po_octree.cu) -> sorted geometry
+//   depth 0 : currents -> direct sum (FP32 tiles or FP64) -> intensity
+//   depth d : leaf sums (currents fused) -> for each level: row FFTs, column
+//             FFTs + translation + child sum -> intensity of the root
+// All work is ordered on the caller's stream; the only host synchronisation
+// is the read-back of the per-level node counts after the octree build.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "po_common.cuh"
+#include "po_internal.h"
+#include "po_kernels.h"
+
+namespace wavepo {
+
+thread_local int64_t g_launch_count = 0;
+static thread_local std::string g_last_error = "";
+
+void set_error(const std::string &msg) { g_last_error = msg; }
+po_status fail(po_status s, const std::string &msg) {
+  g_last_error = msg;
+  return s;
+}
+po_status cuda_fail(cudaError_t e, const char *what) {
+  g_last_error = std::string("CUDA error ") + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ") in " + what;
+  return e == cudaErrorMemoryAllocation ? PO_ERR_OUT_OF_MEMORY : PO_ERR_CUDA;
+}
+
+namespace {
+
+struct DevBuf {
+  void *p = nullptr;
+  size_t bytes = 0;
+  po_status ensure(size_t b) {
+    if (b <= bytes && p) return PO_OK;
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+    cudaError_t e = cudaMalloc(&p, b ? b : 256);
+    if (e != cudaSuccess) {
+      p = nullptr;
+      return cuda_fail(e, "cudaMalloc(workspace)");
+    }
+    bytes = b ? b : 256;
+    return PO_OK;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  template <typename T>
+  T *as() const { return (T *)p; }
+};
+
+__global__ void k_leaf_centers(const uint32_t *__restrict__ prefix, int64_t count, int depth, double3 lo0,
+                               double3 hi0, double *__restrict__ out) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  uint32_t key = prefix[i];
+  double lo[3] = {lo0.x, lo0.y, lo0.z}, hi[3] = {hi0.x, hi0.y, hi0.z};
+  for (int l = 1; l <= depth; ++l) {
+    uint32_t o = (key >> (3 * (depth - l))) & 7u;
+    double m[3] = {0.5 * (lo[0] + hi[0]), 0.5 * (lo[1] + hi[1]), 0.5 * (lo[2] + hi[2])};
+    if (o & 1u) lo[0] = m[0]; else hi[0] = m[0];
+    if (o & 2u) hi[1] = m[1]; else lo[1] = m[1];
+    if (o & 4u) hi[2] = m[2]; else lo[2] = m[2];
+  }
+  out[3 * i] = 0.5 * (lo[0] + hi[0]);
+  out[3 * i + 1] = 0.5 * (lo[1] + hi[1]);
+  out[3 * i + 2] = 0.5 * (lo[2] + hi[2]);
+}
+
+std::vector<float4> host_dirs_f4(int T, int Phi, int nth) {
+  std::vector<float4> v((size_t)T * Phi);
+  for (int it = 0; it < T; ++it)
+    for (int ip = 0; ip < Phi; ++ip) {
+      double s[3];
+      grid_direction(it, ip, nth, Phi, s);
+      v[(size_t)it * Phi + ip] = make_float4((float)s[0], (float)s[1], (float)s[2], 0.f);
+    }
+  return v;
+}
+
+std::vector<double> host_dirs_d(int T, int Phi, int nth) {
+  std::vector<double> v((size_t)T * Phi * 3);
+  for (int it = 0; it < T; ++it)
+    for (int ip = 0; ip < Phi; ++ip) grid_direction(it, ip, nth, Phi, &v[((size_t)it * Phi + ip) * 3]);
+  return v;
+}
+
+int ceil_div(int a, int b) { return (a + b - 1) / b; }
+
+}  // namespace
+
+}  // namespace wavepo
+
+using namespace wavepo;
+
+struct po_ctx {
+  po_config cfg;
+  int device = 0;
+  int sm_count = 152;
+  int depth = 0;
+  int cover = 2;
+  int mt = 1, mp = 1;
+  int nth[PO_MAX_DEPTH + 1];  // samples over pi per level (root: output * mt)
+  int T[PO_MAX_DEPTH + 1];    // theta samples per level (cover * nth)
+  int Phi[PO_MAX_DEPTH + 1];
+  std::map<int, int> tw_offset;
+  DevBuf twiddles;
+  DevBuf geom_in, geom_sorted, octree_ws, leaf_ctr, dirs, dirs_d, trans, levelA, levelB, mid, slots, kvals, out,
+      cur, partial, tile_ctr;
+  cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+};
+
+extern "C" {
+
+const char *po_version(void) { return "wavepo 0.1 (sm_103a)"; }
+
+const char *po_status_string(po_status s) {
+  switch (s) {
+    case PO_OK: return "ok";
+    case PO_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case PO_ERR_CUDA: return "CUDA error";
+    case PO_ERR_OUT_OF_MEMORY: return "out of device memory";
+    case PO_ERR_UNSUPPORTED: return "unsupported configuration";
+    case PO_ERR_TIMEOUT: return "device wait timed out";
+    case PO_ERR_INTERNAL: return "internal error";
+  }
+  return "unknown status";
+}
+
+const char *po_last_error(void) {
+  static thread_local std::string copy;
+  copy = g_last_error;
+  return copy.c_str();
+}
+
+po_status po_config_init(po_config *cfg, int max_depth, int n_theta_out, int n_phi_out, const float box_min[3],
+                         const float box_max[3], double theta_extent, double phi_extent, double ratio, double beta,
+                         double lambda_min) {
+  if (!cfg || !box_min || !box_max) return fail(PO_ERR_INVALID_ARGUMENT, "null argument");
+  if (max_depth < 0 || max_depth > PO_MAX_DEPTH) return fail(PO_ERR_INVALID_ARGUMENT, "max_depth out of range");
+  if (n_theta_out <= 0 || n_phi_out <= 0) return fail(PO_ERR_INVALID_ARGUMENT, "output grid must be positive");
+  if (!(lambda_min > 0) || !(ratio > 0)) return fail(PO_ERR_INVALID_ARGUMENT, "lambda_min and ratio must be > 0");
+  std::memset(cfg, 0, sizeof(*cfg));
+  cfg->max_depth = max_depth;
+  cfg->n_theta[0] = n_theta_out;
+  cfg->n_phi[0] = n_phi_out;
+  const double kmin = kTwoPi / lambda_min;
+  for (int i = 1; i <= max_depth; ++i) {
+    // compareMie/sphere.cu:346-350: d is a float
+    float dth = (float)(std::pow(0.5, i) * (double)((float)theta_extent * (float)ratio));
+    float dph = (float)(std::pow(0.5, i) * (double)((float)phi_extent * (float)ratio));
+    double a = kmin * dth, b = kmin * dph;
+    cfg->n_theta[i] = (int)std::ceil(a + beta * std::pow(a, 1.0 / 3.0));
+    cfg->n_phi[i] = (int)std::ceil(b + beta * std::pow(b, 1.0 / 3.0));
+  }
+  for (int a = 0; a < 3; ++a) {
+    cfg->box_min[a] = box_min[a];
+    cfg->box_max[a] = box_max[a];
+  }
+  cfg->precision = PO_PREC_FP32;
+  cfg->theta_mode = PO_THETA_DOUBLE_COVER;
+  cfg->nyquist_quirk = 1;
+  cfg->distance = 1.0;
+  return PO_OK;
+}
+
+po_status po_create(po_ctx **out, const po_config *cfg) {
+  if (!out || !cfg) return fail(PO_ERR_INVALID_ARGUMENT, "null argument");
+  *out = nullptr;
+  const int d = cfg->max_depth;
+  if (d < 0 || d > PO_MAX_DEPTH) return fail(PO_ERR_INVALID_ARGUMENT, "max_depth out of range");
+  for (int l = 0; l <= d; ++l)
+    if (cfg->n_theta[l] <= 0 || cfg->n_phi[l] <= 0)
+      return fail(PO_ERR_INVALID_ARGUMENT, "every level needs positive n_theta and n_phi");
+  for (int l = 1; l < d; ++l)
+    if (cfg->n_theta[l] < cfg->n_theta[l + 1] || cfg->n_phi[l] < cfg->n_phi[l + 1])
+      return fail(PO_ERR_INVALID_ARGUMENT, "level grids must not grow with depth (the interpolation only upsamples)");
+  for (int a = 0; a < 3; ++a)
+    if (!(cfg->box_max[a] > cfg->box_min[a])) return fail(PO_ERR_INVALID_ARGUMENT, "empty bounding box");
+  if (cfg->precision < 0 || cfg->precision > 3) return fail(PO_ERR_INVALID_ARGUMENT, "unknown precision");
+  if (cfg->precision == PO_PREC_FP64 && d != 0)
+    return fail(PO_ERR_UNSUPPORTED, "the plain FP64 path is the depth-0 direct sum");
+  if (cfg->precision == PO_PREC_SPLIT_BF16 || cfg->precision == PO_PREC_SPLIT_FP16)
+    return fail(PO_ERR_UNSUPPORTED, "split tensor-core precision is not available in this build");
+  if (cfg->theta_mode != PO_THETA_DOUBLE_COVER && cfg->theta_mode != PO_THETA_REFERENCE)
+    return fail(PO_ERR_INVALID_ARGUMENT, "unknown theta mode");
+  if (!(cfg->distance > 0)) return fail(PO_ERR_INVALID_ARGUMENT, "distance must be > 0");
+  int dev = 0;
+  PO_CUDA(cudaGetDevice(&dev));
+  po_ctx *c = new po_ctx();
+  c->cfg = *cfg;
+  c->device = dev;
+  cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, dev);
+  c->depth = d;
+  c->cover = cfg->theta_mode == PO_THETA_DOUBLE_COVER ? 2 : 1;
+  c->mt = c->mp = 1;
+  if (d >= 1) {
+    c->mt = ceil_div(cfg->n_theta[1], cfg->n_theta[0]);
+    c->mp = ceil_div(cfg->n_phi[1], cfg->n_phi[0]);
+  }
+  for (int l = 0; l <= d; ++l) {
+    c->nth[l] = l == 0 ? cfg->n_theta[0] * c->mt : cfg->n_theta[l];
+    c->Phi[l] = l == 0 ? cfg->n_phi[0] * c->mp : cfg->n_phi[l];
+    c->T[l] = (d == 0) ? cfg->n_theta[0] : c->cover * c->nth[l];
+  }
+  // twiddle tables for every transform length of the level chain
+  std::vector<int> lens;
+  for (int l = 0; l < d; ++l) {
+    lens.push_back(c->Phi[l + 1]);
+    lens.push_back(c->Phi[l]);
+    lens.push_back(c->T[l + 1]);
+    lens.push_back(c->T[l]);
+  }
+  std::sort(lens.begin(), lens.end());
+  lens.erase(std::unique(lens.begin(), lens.end()), lens.end());
+  int total = 0;
+  for (int n : lens) {
+    c->tw_offset[n] = total;
+    total += n;
+  }
+  po_status s = c->twiddles.ensure(sizeof(float2) * (size_t)std::max(total, 1));
+  if (s != PO_OK) { delete c; return s; }
+  for (int n : lens) {
+    s = launch_twiddles(n, c->twiddles.as<float2>() + c->tw_offset[n], 0);
+    if (s != PO_OK) { delete c; return s; }
+  }
+  for (auto &e : c->ev) {
+    if (cudaEventCreate(&e) != cudaSuccess) { delete c; return fail(PO_ERR_CUDA, "cudaEventCreate"); }
+  }
+  if (cudaDeviceSynchronize() != cudaSuccess) { delete c; return fail(PO_ERR_CUDA, "twiddle set-up failed"); }
+  *out = c;
+  return PO_OK;
+}
+
+po_status po_destroy(po_ctx *c) {
+  if (!c) return PO_OK;
+  for (DevBuf *b : {&c->twiddles, &c->geom_in, &c->geom_sorted, &c->octree_ws, &c->leaf_ctr, &c->dirs, &c->dirs_d,
+                    &c->trans, &c->levelA, &c->levelB, &c->mid, &c->slots, &c->kvals, &c->out, &c->cur, &c->partial,
+                    &c->tile_ctr})
+    b->release();
+  for (auto &e : c->ev)
+    if (e) cudaEventDestroy(e);
+  delete c;
+  return PO_OK;
+}
+
+static po_status solve_impl(po_ctx *c, const po_geometry *g, const po_illum *il, float *intensity, int out_on_device,
+                            cudaStream_t st, po_report *rep) {
+  const po_config &cfg = c->cfg;
+  const int d = c->depth;
+  const int64_t n = g->n;
+  const int npol = ((il->pol_mask & PO_POL_TM) ? 1 : 0) + ((il->pol_mask & PO_POL_TE) ? 1 : 0);
+  const int L = il->n_lambda, I = il->n_inc, G = I * npol, S = L * G;
+  const int nth_out = cfg.n_theta[0], nph_out = cfg.n_phi[0];
+  const int64_t nd_out = (int64_t)nth_out * nph_out;
+  const int64_t launches0 = g_launch_count;
+  PO_CUDA(cudaEventRecord(c->ev[0], st));
+
+  // ---- geometry on the device
+  const float *gin[7];
+  if (g->on_device) {
+    const float *src[7] = {g->x, g->y, g->z, g->nx, g->ny, g->nz, g->area};
+    for (int k = 0; k < 7; ++k) gin[k] = src[k];
+  } else {
+    PO_TRY(c->geom_in.ensure(sizeof(float) * 7 * (size_t)std::max<int64_t>(n, 1)));
+    const float *src[7] = {g->x, g->y, g->z, g->nx, g->ny, g->nz, g->area};
+    for (int k = 0; k < 7; ++k) {
+      float *dst = c->geom_in.as<float>() + (size_t)k * n;
+      if (n > 0) PO_CUDA(cudaMemcpyAsync(dst, src[k], sizeof(float) * n, cudaMemcpyHostToDevice, st));
+      gin[k] = dst;
+    }
+  }
+
+  // ---- output buffer
+  float *out_dev = intensity;
+  if (!out_on_device) {
+    PO_TRY(c->out.ensure(sizeof(float) * (size_t)S * nd_out));
+    out_dev = c->out.as<float>();
+  }
+
+  // per-slot parameters, slot = (lambda, incidence, polarisation)
+  std::vector<double> kl(L), ks(S);
+  for (int l = 0; l < L; ++l) kl[l] = kTwoPi / il->lambda_m[l];
+  const bool fp64 = cfg.precision == PO_PREC_FP64;
+  std::vector<SlotParams<float>> sp32;
+  std::vector<SlotParams<double>> sp64;
+  for (int l = 0; l < L; ++l)
+    for (int i = 0; i < I; ++i)
+      for (int p = 0; p < 2; ++p) {
+        int bit = p == 0 ? PO_POL_TM : PO_POL_TE;
+        if (!(il->pol_mask & bit)) continue;
+        ks[sp32.size()] = kl[l];
+        sp32.push_back(make_slot<float>(il->lambda_m[l], il->theta_i[i], il->phi_i[i], p == 1, il->eta_re,
+                                        il->eta_im, il->sigma, cfg.distance, true));
+        sp64.push_back(make_slot<double>(il->lambda_m[l], il->theta_i[i], il->phi_i[i], p == 1, il->eta_re,
+                                         il->eta_im, il->sigma, cfg.distance, true));
+      }
+  PO_TRY(c->slots.ensure(std::max(sizeof(SlotParams<float>), sizeof(SlotParams<double>)) * S));
+  PO_TRY(c->kvals.ensure(sizeof(double) * (L + S)));
+  PO_CUDA(cudaMemcpyAsync(c->kvals.as<double>(), kl.data(), sizeof(double) * L, cudaMemcpyHostToDevice, st));
+  PO_CUDA(cudaMemcpyAsync(c->kvals.as<double>() + L, ks.data(), sizeof(double) * S, cudaMemcpyHostToDevice, st));
+  if (fp64)
+    PO_CUDA(cudaMemcpyAsync(c->slots.p, sp64.data(), sizeof(SlotParams<double>) * S, cudaMemcpyHostToDevice, st));
+  else
+    PO_CUDA(cudaMemcpyAsync(c->slots.p, sp32.data(), sizeof(SlotParams<float>) * S, cudaMemcpyHostToDevice, st));
+  const double *k_lambda = c->kvals.as<double>();
+  const double *k_slot = k_lambda + L;
+
+  // root centre (tree.h:116-120, float box)
+  double c0[3];
+  for (int a = 0; a < 3; ++a) c0[a] = (double)(0.5f * (cfg.box_min[a] + cfg.box_max[a]));
+
+  if (fp64) {
+    // ---- plain FP64 direct sum (the "plain method"): no tree, no sort
+    PO_CUDA(cudaEventRecord(c->ev[1], st));
+    PO_TRY(c->cur.ensure(sizeof(double2) * 6 * (size_t)S * std::max<int64_t>(n, 1)));
+    PO_TRY(launch_currents_f64(n, gin, c->slots.as<SlotParams<double>>(), S, c->cur.as<double>(), st));
+    PO_CUDA(cudaEventRecord(c->ev[2], st));
+    std::vector<double> dd = host_dirs_d(nth_out, nph_out, nth_out);
+    PO_TRY(c->dirs_d.ensure(sizeof(double) * dd.size()));
+    PO_CUDA(cudaMemcpyAsync(c->dirs_d.p, dd.data(), sizeof(double) * dd.size(), cudaMemcpyHostToDevice, st));
+    int nsplit = std::max(1, std::min<int>(64, (int)((c->sm_count * 8 + S * ceil_div((int)nd_out, 128) - 1) /
+                                                      std::max<int64_t>(1, S * ceil_div((int)nd_out, 128)))));
+    nsplit = (int)std::min<int64_t>(nsplit, std::max<int64_t>(1, n));
+    PO_TRY(c->partial.ensure(sizeof(double2) * 6 * (size_t)S * nd_out * nsplit));
+    PO_TRY(c->levelA.ensure(sizeof(double2) * 6 * (size_t)S * nd_out));
+    PO_TRY(launch_direct_f64(n, gin[0], gin[1], gin[2], c->cur.as<double2>(), k_slot, S, c0, c->dirs_d.as<double>(),
+                             (int)nd_out, nsplit, c->partial.as<double2>(), c->levelA.as<double2>(), st));
+    PO_CUDA(cudaEventRecord(c->ev[3], st));
+    PO_CUDA(cudaEventRecord(c->ev[4], st));
+    PO_TRY(launch_intensity_f64(c->levelA.as<double2>(), S, nth_out, nph_out, out_dev, st));
+  } else {
+    // ---- octree (depth 0 still sorts the points so that direct-sum tiles are compact)
+    PO_CUDA(cudaEventRecord(c->ev[1], st));
+    const int tdepth = d > 0 ? d : 6;
+    size_t wsb = octree_workspace_bytes(n, tdepth);
+    PO_TRY(c->octree_ws.ensure(wsb));
+    OctreeBuffers tree;
+    PO_TRY(build_octree(gin[0], gin[1], gin[2], n, cfg.box_min, cfg.box_max, tdepth, c->octree_ws.p, wsb, &tree, st));
+    PO_TRY(c->geom_sorted.ensure(sizeof(float) * 7 * (size_t)std::max<int64_t>(n, 1)));
+    float *gs[7];
+    for (int k = 0; k < 7; ++k) gs[k] = c->geom_sorted.as<float>() + (size_t)k * n;
+    PO_TRY(gather_points(n, tree.perm, gin, gs, st));
+    const float *gsc[7] = {gs[0], gs[1], gs[2], gs[3], gs[4], gs[5], gs[6]};
+    PO_CUDA(cudaEventRecord(c->ev[2], st));
+    if (rep) {
+      rep->n_leaves = tree.level[tdepth].count;
+      int64_t tot = 0;
+      for (int l = 0; l <= tdepth; ++l) tot += tree.level[l].count;
+      rep->n_nodes_total = tot;
+    }
+    if (d == 0) {
+      PO_TRY(c->cur.ensure(sizeof(float2) * 6 * (size_t)S * std::max<int64_t>(n, 1)));
+      PO_TRY(launch_currents_f32(n, gsc, c->slots.as<SlotParams<float>>(), S, c->cur.as<float>(), st));
+      std::vector<float4> df = host_dirs_f4(nth_out, nph_out, nth_out);
+      std::vector<double> dd = host_dirs_d(nth_out, nph_out, nth_out);
+      PO_TRY(c->dirs.ensure(sizeof(float4) * df.size()));
+      PO_TRY(c->dirs_d.ensure(sizeof(double) * dd.size()));
+      PO_CUDA(cudaMemcpyAsync(c->dirs.p, df.data(), sizeof(float4) * df.size(), cudaMemcpyHostToDevice, st));
+      PO_CUDA(cudaMemcpyAsync(c->dirs_d.p, dd.data(), sizeof(double) * dd.size(), cudaMemcpyHostToDevice, st));
+      int nsplit = direct_splits(n, (int)nd_out, L, c->sm_count);
+      PO_TRY(c->tile_ctr.ensure(sizeof(double) * 3 * (size_t)((n + 127) / 128 + 1)));
+      PO_TRY(c->partial.ensure(sizeof(float2) * 6 * (size_t)S * nd_out * nsplit));
+      PO_TRY(c->levelA.ensure(sizeof(float2) * 6 * (size_t)S * nd_out));
+      PO_TRY(launch_direct_f32(n, gs[0], gs[1], gs[2], c->cur.as<float2>(), c->tile_ctr.as<double>(), k_lambda, L, G,
+                               c0, c->dirs.as<float4>(), c->dirs_d.as<double>(), (int)nd_out, nsplit,
+                               c->partial.as<float2>(), c->levelA.as<float2>(), st));
+      PO_CUDA(cudaEventRecord(c->ev[3], st));
+      PO_CUDA(cudaEventRecord(c->ev[4], st));
+      PO_TRY(launch_intensity_f32(c->levelA.as<float2>(), S, nth_out, nph_out, nth_out, nph_out, 1, 1, out_dev, st));
+    } else {
+      // ---- hierarchical solve
+      const int64_t nleaf = tree.level[d].count;
+      PO_TRY(c->leaf_ctr.ensure(sizeof(double) * 3 * (size_t)std::max<int64_t>(nleaf, 1)));
+      double3 lo = make_double3(cfg.box_min[0], cfg.box_min[1], cfg.box_min[2]);
+      double3 hi = make_double3(cfg.box_max[0], cfg.box_max[1], cfg.box_max[2]);
+      k_leaf_centers<<<(unsigned)((nleaf + 255) / 256), 256, 0, st>>>(tree.level[d].prefix, nleaf, d, lo, hi,
+                                                                       c->leaf_ctr.as<double>());
+      count_launch();
+      // buffer sizes
+      size_t lvl_max = 0, mid_max = 0;
+      for (int l = 0; l <= d; ++l)
+        lvl_max = std::max(lvl_max, (size_t)S * tree.level[l].count * 6 * (size_t)c->T[l] * c->Phi[l]);
+      for (int l = 0; l < d; ++l)
+        mid_max = std::max(mid_max, (size_t)S * tree.level[l + 1].count * 6 * (size_t)c->T[l + 1] * c->Phi[l]);
+      PO_TRY(c->levelA.ensure(sizeof(float2) * lvl_max));
+      PO_TRY(c->levelB.ensure(sizeof(float2) * lvl_max));
+      PO_TRY(c->mid.ensure(sizeof(float2) * std::max<size_t>(mid_max, 1)));
+      // translation tables (per level, per wavelength)
+      size_t tr_total = 0;
+      std::vector<size_t> tr_off(d);
+      for (int l = 0; l < d; ++l) {
+        tr_off[l] = tr_total;
+        tr_total += (size_t)L * c->T[l] * c->Phi[l];
+      }
+      PO_TRY(c->trans.ensure(sizeof(float4) * std::max<size_t>(tr_total, 1)));
+      for (int l = 0; l < d; ++l) {
+        double a[3];
+        for (int q = 0; q < 3; ++q) a[q] = ((double)cfg.box_max[q] - (double)cfg.box_min[q]) / std::ldexp(1.0, l + 2);
+        PO_TRY(launch_trans_table(k_lambda, L, c->nth[l], c->T[l], c->Phi[l], a, c->trans.as<float4>() + tr_off[l],
+                                  st));
+      }
+      // leaf directions
+      std::vector<float4> df = host_dirs_f4(c->T[d], c->Phi[d], c->nth[d]);
+      PO_TRY(c->dirs.ensure(sizeof(float4) * df.size()));
+      PO_CUDA(cudaMemcpyAsync(c->dirs.p, df.data(), sizeof(float4) * df.size(), cudaMemcpyHostToDevice, st));
+      PO_TRY(launch_leaf(gsc, tree.level[d].begin, c->leaf_ctr.as<double>(), nleaf, c->slots.as<SlotParams<float>>(),
+                         L, G, c->dirs.as<float4>(), c->T[d] * c->Phi[d], c->levelA.as<float2>(), st));
+      PO_CUDA(cudaEventRecord(c->ev[3], st));
+      float2 *cur_lvl = c->levelA.as<float2>(), *nxt = c->levelB.as<float2>();
+      for (int l = d - 1; l >= 0; --l) {
+        const int64_t nc = tree.level[l + 1].count, np = tree.level[l].count;
+        FftPlan prow_in = make_plan(c->Phi[l + 1], c->tw_offset[c->Phi[l + 1]]);
+        FftPlan prow_out = make_plan(c->Phi[l], c->tw_offset[c->Phi[l]]);
+        FftPlan pcol_in = make_plan(c->T[l + 1], c->tw_offset[c->T[l + 1]]);
+        FftPlan pcol_out = make_plan(c->T[l], c->tw_offset[c->T[l]]);
+        int64_t nrows = (int64_t)S * nc * 6 * c->T[l + 1];
+        PO_TRY(launch_interp_rows(cur_lvl, c->mid.as<float2>(), nrows, prow_in, prow_out, c->twiddles.as<float2>(),
+                                  1.0f / (float)c->Phi[l + 1], c->sm_count, st));
+        int reach = 0x7fffffff;
+        if (c->cover == 1 && cfg.nyquist_quirk) reach = 256 * (c->T[l + 1] / 256 + 1);
+        PO_TRY(launch_interp_cols(c->mid.as<float2>(), nxt, tree.level[l].child, np, nc, c->Phi[l], pcol_in, pcol_out,
+                                  c->twiddles.as<float2>(), c->trans.as<float4>() + tr_off[l], S, G, reach,
+                                  1.0f / (float)c->T[l + 1], 6, st));
+        std::swap(cur_lvl, nxt);
+      }
+      PO_CUDA(cudaEventRecord(c->ev[4], st));
+      PO_TRY(launch_intensity_f32(cur_lvl, S, c->T[0], c->Phi[0], nth_out, nph_out, c->mt, c->mp, out_dev, st));
+    }
+  }
+  if (!out_on_device)
+    PO_CUDA(cudaMemcpyAsync(intensity, out_dev, sizeof(float) * (size_t)S * nd_out, cudaMemcpyDeviceToHost, st));
+  PO_CUDA(cudaEventRecord(c->ev[5], st));
+  if (rep || !out_on_device) PO_CUDA(cudaEventSynchronize(c->ev[5]));
+  PO_CUDA(cudaGetLastError());
+  if (rep) {
+    float t[5];
+    cudaEventElapsedTime(&t[0], c->ev[0], c->ev[5]);
+    cudaEventElapsedTime(&t[1], c->ev[1], c->ev[2]);
+    cudaEventElapsedTime(&t[2], c->ev[2], c->ev[3]);
+    cudaEventElapsedTime(&t[3], c->ev[3], c->ev[4]);
+    cudaEventElapsedTime(&t[4], c->ev[4], c->ev[5]);
+    rep->ms_total = t[0];
+    rep->ms_build = t[1];
+    rep->ms_leaf = t[2];
+    rep->ms_aggregate = t[3];
+    rep->ms_intensity = t[4];
+    rep->root_theta = c->nth[0];
+    rep->root_phi = c->Phi[0];
+    int64_t ws = 0;
+    for (DevBuf *b : {&c->twiddles, &c->geom_in, &c->geom_sorted, &c->octree_ws, &c->leaf_ctr, &c->dirs, &c->dirs_d,
+                      &c->trans, &c->levelA, &c->levelB, &c->mid, &c->slots, &c->kvals, &c->out, &c->cur, &c->partial,
+                      &c->tile_ctr})
+      ws += (int64_t)b->bytes;
+    rep->workspace_bytes = ws;
+    rep->kernel_launches = g_launch_count - launches0;
+  }
+  return PO_OK;
+}
+
+po_status po_solve(po_ctx *c, const po_geometry *g, const po_illum *il, float *intensity, int out_on_device,
+                   void *stream, po_report *rep) {
+  if (!c || !g || !il || !intensity) return fail(PO_ERR_INVALID_ARGUMENT, "null argument");
+  if (g->n < 0 || g->n > 2000000000LL) return fail(PO_ERR_INVALID_ARGUMENT, "point count out of range");
+  if (g->n > 0 && (!g->x || !g->y || !g->z || !g->nx || !g->ny || !g->nz || !g->area))
+    return fail(PO_ERR_INVALID_ARGUMENT, "null geometry array");
+  if (il->n_lambda <= 0 || !il->lambda_m) return fail(PO_ERR_INVALID_ARGUMENT, "no wavelengths");
+  if (il->n_inc <= 0 || !il->theta_i || !il->phi_i) return fail(PO_ERR_INVALID_ARGUMENT, "no incident directions");
+  if ((il->pol_mask & (PO_POL_TM | PO_POL_TE)) == 0 || (il->pol_mask & ~(PO_POL_TM | PO_POL_TE)))
+    return fail(PO_ERR_INVALID_ARGUMENT, "pol_mask must select TM and/or TE");
+  for (int l = 0; l < il->n_lambda; ++l)
+    if (!(il->lambda_m[l] > 0) || !std::isfinite(il->lambda_m[l]))
+      return fail(PO_ERR_INVALID_ARGUMENT, "wavelengths must be positive");
+  if (!(il->sigma > 0)) return fail(PO_ERR_INVALID_ARGUMENT, "beam sigma must be > 0");
+  const int npol = ((il->pol_mask & PO_POL_TM) ? 1 : 0) + ((il->pol_mask & PO_POL_TE) ? 1 : 0);
+  if ((int64_t)il->n_lambda * il->n_inc * npol > 65535) return fail(PO_ERR_UNSUPPORTED, "too many patterns per call");
+  int dev = 0;
+  PO_CUDA(cudaGetDevice(&dev));
+  if (dev != c->device) return fail(PO_ERR_INVALID_ARGUMENT, "context was created on another device");
+  if (rep) std::memset(rep, 0, sizeof(*rep));
+  return solve_impl(c, g, il, intensity, out_on_device, (cudaStream_t)stream, rep);
+}
+
+// ---------------------------------------------------------------- single steps
+po_status po_tangent_plane_currents(int64_t n, const float *x, const float *y, const float *z, const float *nx,
+                                    const float *ny, const float *nz, const float *area, double lambda_m,
+                                    double theta_i, double phi_i, int pol, double eta_re, double eta_im, double sigma,
+                                    double distance, int scale, float *currents, void *stream) {
+  if (n < 0) return fail(PO_ERR_INVALID_ARGUMENT, "negative point count");
+  if (n == 0) return PO_OK;
+  if (!x || !y || !z || !nx || !ny || !nz || !currents || (scale && !area))
+    return fail(PO_ERR_INVALID_ARGUMENT, "null pointer");
+  if (pol != PO_POL_TM && pol != PO_POL_TE) return fail(PO_ERR_INVALID_ARGUMENT, "pol must be PO_POL_TM or PO_POL_TE");
+  if (!(lambda_m > 0) || !(sigma > 0) || (scale && !(distance > 0)))
+    return fail(PO_ERR_INVALID_ARGUMENT, "lambda, sigma and distance must be > 0");
+  cudaStream_t st = (cudaStream_t)stream;
+  SlotParams<float> p = make_slot<float>(lambda_m, theta_i, phi_i, pol == PO_POL_TE, eta_re, eta_im, sigma,
+                                         scale ? distance : 1.0, scale != 0);
+  SlotParams<float> *dp = nullptr;
+  PO_CUDA(cudaMallocAsync((void **)&dp, sizeof(p), st));
+  cudaError_t e = cudaMemcpyAsync(dp, &p, sizeof(p), cudaMemcpyHostToDevice, st);
+  const float *g[7] = {x, y, z, nx, ny, nz, scale ? area : nullptr};
+  po_status s = e == cudaSuccess ? launch_currents_f32(n, g, dp, 1, currents, st) : cuda_fail(e, "cudaMemcpyAsync");
+  cudaFreeAsync(dp, st);
+  if (s == PO_OK) PO_CUDA(cudaStreamSynchronize(st));  // the host slot struct goes out of scope
+  return s;
+}
+
+po_status po_build_octree(int64_t n, const float *x, const float *y, const float *z, const float box_min[3],
+                          const float box_max[3], int depth, int32_t *perm, int32_t *heap_range, void *stream) {
+  if (n < 0 || (n > 0 && (!x || !y || !z || !perm)) || !box_min || !box_max)
+    return fail(PO_ERR_INVALID_ARGUMENT, "null pointer or negative count");
+  if (depth < 0 || depth > 7) return fail(PO_ERR_INVALID_ARGUMENT, "depth must be in [0, 7] for the heap layout");
+  cudaStream_t st = (cudaStream_t)stream;
+  size_t wsb = octree_workspace_bytes(n, depth);
+  void *ws = nullptr;
+  PO_CUDA(cudaMallocAsync(&ws, wsb, st));
+  OctreeBuffers t;
+  po_status s = build_octree(x, y, z, n, box_min, box_max, depth, ws, wsb, &t, st);
+  if (s == PO_OK && n > 0) {
+    cudaError_t e = cudaMemcpyAsync(perm, t.perm, sizeof(int32_t) * n, cudaMemcpyDeviceToDevice, st);
+    if (e != cudaSuccess) s = cuda_fail(e, "cudaMemcpyAsync(perm)");
+  }
+  if (s == PO_OK && heap_range) s = octree_heap_ranges(t, heap_range, st);
+  cudaFreeAsync(ws, st);
+  if (s == PO_OK) PO_CUDA(cudaStreamSynchronize(st));
+  return s;
+}
+
+po_status po_far_field_direct(int64_t n, const float *x, const float *y, const float *z, const float *currents,
+                              double k, const double center[3], int n_theta, int n_phi, int precision, float *fields,
+                              void *stream) {
+  if (n < 0 || n_theta <= 0 || n_phi <= 0 || !center || !fields || (n > 0 && (!x || !y || !z || !currents)))
+    return fail(PO_ERR_INVALID_ARGUMENT, "invalid argument");
+  if (!(k > 0)) return fail(PO_ERR_INVALID_ARGUMENT, "k must be > 0");
+  if (precision != PO_PREC_FP32 && precision != PO_PREC_FP64)
+    return fail(PO_ERR_UNSUPPORTED, "direct sum precision must be FP32 or FP64");
+  cudaStream_t st = (cudaStream_t)stream;
+  const int64_t nd = (int64_t)n_theta * n_phi;
+  std::vector<float4> df = host_dirs_f4(n_theta, n_phi, n_theta);
+  std::vector<double> dd = host_dirs_d(n_theta, n_phi, n_theta);
+  void *bdirs = nullptr, *bdd = nullptr, *bk = nullptr, *bpart = nullptr, *btile = nullptr, *bacc = nullptr;
+  po_status s = PO_OK;
+  int nsplit = precision == PO_PREC_FP32 ? direct_splits(n, (int)nd, 1, 152) : 8;
+  if (n > 0 && nsplit > n) nsplit = (int)n;
+  size_t vb = precision == PO_PREC_FP32 ? sizeof(float2) : sizeof(double2);
+#define A(ptr, bytes)                                             \
+  do {                                                            \
+    cudaError_t _e = cudaMallocAsync(&ptr, (bytes), st);          \
+    if (_e != cudaSuccess && s == PO_OK) s = cuda_fail(_e, "cudaMallocAsync"); \
+  } while (0)
+  A(bdirs, sizeof(float4) * df.size());
+  A(bdd, sizeof(double) * dd.size());
+  A(bk, sizeof(double));
+  A(bpart, vb * 6 * nd * nsplit);
+  A(btile, sizeof(double) * 3 * ((n + 127) / 128 + 1));
+  A(bacc, precision == PO_PREC_FP64 ? sizeof(double2) * 6 * (n > 0 ? n : 1) + sizeof(double2) * 6 * nd : 16);
+#undef A
+  if (s == PO_OK) {
+    cudaMemcpyAsync(bdirs, df.data(), sizeof(float4) * df.size(), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(bdd, dd.data(), sizeof(double) * dd.size(), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(bk, &k, sizeof(double), cudaMemcpyHostToDevice, st);
+    if (precision == PO_PREC_FP32) {
+      s = launch_direct_f32(n, x, y, z, (const float2 *)currents, (double *)btile, (const double *)bk, 1, 1, center,
+                            (const float4 *)bdirs, (const double *)bdd, (int)nd, nsplit, (float2 *)bpart,
+                            (float2 *)fields, st);
+    } else {
+      // widen the float currents, sum in double, narrow the fields
+      double2 *cur64 = (double2 *)bacc, *f64 = cur64 + 6 * (n > 0 ? n : 1);
+      s = launch_widen(currents, cur64, 6 * n, st);
+      if (s == PO_OK)
+        s = launch_direct_f64(n, x, y, z, cur64, (const double *)bk, 1, center, (const double *)bdd, (int)nd, nsplit,
+                              (double2 *)bpart, f64, st);
+      if (s == PO_OK) s = launch_narrow(f64, (float2 *)fields, 6 * nd, st);
+    }
+  }
+  for (void *p : {bdirs, bdd, bk, bpart, btile, bacc})
+    if (p) cudaFreeAsync(p, st);
+  if (s == PO_OK) PO_CUDA(cudaStreamSynchronize(st));
+  return s;
+}
+
+po_status po_interp_fft(const float *in, int th_c, int ph_c, float *out, int th_p, int ph_p, int batch, int theta_mode,
+                        int nyquist_quirk, void *stream) {
+  if (!in || !out || th_c <= 0 || ph_c <= 0 || batch < 0) return fail(PO_ERR_INVALID_ARGUMENT, "invalid argument");
+  if (th_p < th_c || ph_p < ph_c) return fail(PO_ERR_INVALID_ARGUMENT, "the interpolation only upsamples");
+  if (theta_mode != PO_THETA_DOUBLE_COVER && theta_mode != PO_THETA_REFERENCE)
+    return fail(PO_ERR_INVALID_ARGUMENT, "unknown theta mode");
+  if (batch == 0) return PO_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  std::vector<int> lens = {ph_c, ph_p, th_c, th_p};
+  std::sort(lens.begin(), lens.end());
+  lens.erase(std::unique(lens.begin(), lens.end()), lens.end());
+  std::map<int, int> off;
+  int total = 0;
+  for (int n : lens) { off[n] = total; total += n; }
+  void *tw = nullptr, *mid = nullptr;
+  po_status s = PO_OK;
+  cudaError_t e = cudaMallocAsync(&tw, sizeof(float2) * total, st);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMallocAsync(twiddles)");
+  e = cudaMallocAsync(&mid, sizeof(float2) * (size_t)batch * th_c * ph_p, st);
+  if (e != cudaSuccess) { cudaFreeAsync(tw, st); return cuda_fail(e, "cudaMallocAsync(scratch)"); }
+  for (int n : lens)
+    if (s == PO_OK) s = launch_twiddles(n, (float2 *)tw + off[n], st);
+  int sm = 152;
+  cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, 0);
+  if (s == PO_OK)
+    s = launch_interp_rows((const float2 *)in, (float2 *)mid, (int64_t)batch * th_c, make_plan(ph_c, off[ph_c]),
+                           make_plan(ph_p, off[ph_p]), (const float2 *)tw, 1.0f / (float)ph_c, sm, st);
+  int reach = (theta_mode == PO_THETA_REFERENCE && nyquist_quirk) ? 256 * (th_c / 256 + 1) : 0x7fffffff;
+  if (s == PO_OK)
+    s = launch_interp_cols((const float2 *)mid, (float2 *)out, nullptr, batch, batch, ph_p, make_plan(th_c, off[th_c]),
+                           make_plan(th_p, off[th_p]), (const float2 *)tw, nullptr, 1, 1, reach, 1.0f / (float)th_c, 1,
+                           st);
+  cudaFreeAsync(mid, st);
+  cudaFreeAsync(tw, st);
+  if (s == PO_OK) PO_CUDA(cudaStreamSynchronize(st));
+  return s;
+}
+
+po_status po_compute_intensity(const float *fields, int n_theta, int n_phi, float *intensity, void *stream) {
+  if (!fields || !intensity || n_theta <= 0 || n_phi <= 0) return fail(PO_ERR_INVALID_ARGUMENT, "invalid argument");
+  return launch_intensity_f32((const float2 *)fields, 1, n_theta, n_phi, n_theta, n_phi, 1, 1, intensity,
+                              (cudaStream_t)stream);
+}
+
+}  // extern "C"
