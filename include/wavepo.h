@@ -97,6 +97,12 @@ typedef struct po_report {
   int root_theta, root_phi;         /* root grid actually used (output x supersampling) */
   int64_t workspace_bytes;          /* device workspace held by the context */
   int64_t kernel_launches;          /* kernels launched by the solve */
+  double ms_leaf_kernel;            /* the leaf (or direct-sum) kernel launches alone */
+  double ms_rows;                   /* all row (phi) interpolation launches */
+  double ms_cols;                   /* all column (theta) interpolation + child-sum launches */
+  int n_leaf_launches, n_row_launches, n_col_launches;
+  double leaf_point_dirs;           /* sum over leaves of points x leaf directions x patterns */
+  double rows_bytes, cols_bytes;    /* algorithmic bytes (pattern reads + writes) of the passes */
 } po_report;
 
 typedef struct po_ctx po_ctx;

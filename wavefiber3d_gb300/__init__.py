@@ -11,8 +11,9 @@ __version__ = "0.1.0"
 
 
 def __getattr__(name):
-    # the CUDA-backed API is imported lazily so that geometry/grids work without the library
+    # the CUDA-backed API is imported on first use so that geometry/grids work without the library
     if name in ("api", "Solver", "Config", "Illumination"):
-        from . import api
-        return api if name == "api" else getattr(api, name)
+        import importlib
+        mod = importlib.import_module(__name__ + ".api")
+        return mod if name == "api" else getattr(mod, name)
     raise AttributeError(name)

@@ -56,7 +56,10 @@ class po_report(ctypes.Structure):
                 ("ms_aggregate", ctypes.c_double), ("ms_intensity", ctypes.c_double),
                 ("n_leaves", ctypes.c_int64), ("n_nodes_total", ctypes.c_int64),
                 ("root_theta", ctypes.c_int), ("root_phi", ctypes.c_int),
-                ("workspace_bytes", ctypes.c_int64), ("kernel_launches", ctypes.c_int64)]
+                ("workspace_bytes", ctypes.c_int64), ("kernel_launches", ctypes.c_int64),
+                ("ms_leaf_kernel", ctypes.c_double), ("ms_rows", ctypes.c_double), ("ms_cols", ctypes.c_double),
+                ("n_leaf_launches", ctypes.c_int), ("n_row_launches", ctypes.c_int), ("n_col_launches", ctypes.c_int),
+                ("leaf_point_dirs", ctypes.c_double), ("rows_bytes", ctypes.c_double), ("cols_bytes", ctypes.c_double)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}

@@ -184,11 +184,12 @@ class Solver:
             g = _lib.po_geometry(n, *ptrs, 0)
         else:
             arrs = [cloud[k] for k in range(7)]
+            on_dev = arrs[0].is_cuda
             for a in arrs:
-                if not (a.is_cuda and a.dtype == torch.float32 and a.is_contiguous()):
-                    raise ValueError("device geometry must be 7 contiguous float32 CUDA arrays")
+                if not (a.is_cuda == on_dev and a.dtype == torch.float32 and a.is_contiguous()):
+                    raise ValueError("geometry must be 7 contiguous float32 arrays, all on the GPU or all on the host")
             n = arrs[0].numel()
-            g = _lib.po_geometry(n, *[a.data_ptr() for a in arrs], 1)
+            g = _lib.po_geometry(n, *[a.data_ptr() for a in arrs], 1 if on_dev else 0)
         rep = _lib.po_report()
         shape = self.out_shape(illum)
         if out is None and host:
@@ -197,10 +198,10 @@ class Solver:
                                        _stream_ptr(stream), ctypes.byref(rep)))
         else:
             res = out if out is not None else torch.empty(shape, dtype=torch.float32, device="cuda")
-            if not (res.is_cuda and res.is_contiguous() and res.numel() == int(np.prod(shape))):
-                raise ValueError(f"out must be a contiguous CUDA tensor with {int(np.prod(shape))} elements")
+            if not (res.is_contiguous() and res.dtype == torch.float32 and res.numel() == int(np.prod(shape))):
+                raise ValueError(f"out must be a contiguous float32 tensor with {int(np.prod(shape))} elements")
             check(_lib.load().po_solve(self._h, ctypes.byref(g), ctypes.byref(il), ctypes.c_void_p(res.data_ptr()),
-                                       1, _stream_ptr(stream), ctypes.byref(rep)))
+                                       1 if res.is_cuda else 0, _stream_ptr(stream), ctypes.byref(rep)))
         self.last_report = rep.as_dict()
         del keep
         return res

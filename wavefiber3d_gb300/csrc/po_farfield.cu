@@ -17,6 +17,8 @@
 // large part of the argument never passes through float.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "po_common.cuh"
 #include "po_internal.h"
 #include "po_kernels.h"
@@ -72,16 +74,17 @@ __global__ void __launch_bounds__(kLeafThreads) k_leaf(
     const float *__restrict__ nx, const float *__restrict__ ny, const float *__restrict__ nz,
     const float *__restrict__ area, const int32_t *__restrict__ leaf_begin, const double *__restrict__ leaf_center,
     const SlotParams<float> *__restrict__ slots, const float4 *__restrict__ dirs, int ndir, int64_t n_leaves,
-    float2 *__restrict__ out) {
+    int Gtot, int g0, float2 *__restrict__ out) {
   __shared__ float4 s_u[kLeafChunk];
   __shared__ float2 s_cur[kLeafChunk][G * 6];
   const int64_t leaf = blockIdx.x;
   const int lam = blockIdx.y;
   const int b = leaf_begin[leaf], e = leaf_begin[leaf + 1];
   const double cxd = leaf_center[3 * leaf], cyd = leaf_center[3 * leaf + 1], czd = leaf_center[3 * leaf + 2];
-  const double k0 = slots[lam * G].k0d;
+  const SlotParams<float> *sl = slots + lam * Gtot + g0;
+  const double k0 = sl[0].k0d;
   const int64_t slot_stride = n_leaves * 6 * (int64_t)ndir;
-  float2 *obase = out + (int64_t)lam * G * slot_stride + leaf * 6 * (int64_t)ndir;
+  float2 *obase = out + ((int64_t)lam * Gtot + g0) * slot_stride + leaf * 6 * (int64_t)ndir;
   const int per_pass = kLeafThreads * DPT;
   for (int c0 = b; c0 < e; c0 += kLeafChunk) {
     const int cnt = min(kLeafChunk, e - c0);
@@ -95,7 +98,7 @@ __global__ void __launch_bounds__(kLeafThreads) k_leaf(
 #pragma unroll
       for (int g = 0; g < G; ++g) {
         cx<float> c[6];
-        tangent_plane<float>(slots[lam * G + g], px, py, pz, qx, qy, qz, ar, c);
+        tangent_plane<float>(sl[g], px, py, pz, qx, qy, qz, ar, c);
 #pragma unroll
         for (int k = 0; k < 6; ++k) s_cur[q][g * 6 + k] = make_float2(c[k].re, c[k].im);
       }
@@ -156,20 +159,24 @@ po_status launch_leaf(const float *const g[7], const int32_t *leaf_begin, const 
                       int64_t n_leaves, const SlotParams<float> *slots_dev, int n_lambda, int G,
                       const float4 *dirs, int ndir, float2 *out, cudaStream_t st) {
   if (n_leaves <= 0 || n_lambda <= 0) return PO_OK;
+  if (n_lambda > 65535) return fail(PO_ERR_UNSUPPORTED, "too many wavelengths for one launch");
   dim3 grid((unsigned)n_leaves, (unsigned)n_lambda);
+  // the slots of a wavelength share its phases; they go through the kernel in
+  // chunks of at most 4 (register budget of the accumulators)
+  for (int g0 = 0; g0 < G; g0 += 4) {
+    const int gc = std::min(4, G - g0);
 #define PO_LEAF(GG, DD)                                                                                     \
   k_leaf<GG, DD><<<grid, kLeafThreads, 0, st>>>(g[0], g[1], g[2], g[3], g[4], g[5], g[6], leaf_begin,      \
-                                               leaf_center, slots_dev, dirs, ndir, n_leaves, out)
-  switch (G) {
-    case 1: PO_LEAF(1, 4); break;
-    case 2: PO_LEAF(2, 2); break;
-    case 3: PO_LEAF(3, 1); break;
-    case 4: PO_LEAF(4, 1); break;
-    default: return fail(PO_ERR_UNSUPPORTED, "FP32 leaf kernel supports at most 4 incidence x polarisation slots "
-                                             "per wavelength; use a split tensor-core precision for more");
-  }
+                                               leaf_center, slots_dev, dirs, ndir, n_leaves, G, g0, out)
+    switch (gc) {
+      case 1: PO_LEAF(1, 4); break;
+      case 2: PO_LEAF(2, 2); break;
+      case 3: PO_LEAF(3, 1); break;
+      default: PO_LEAF(4, 1); break;
+    }
 #undef PO_LEAF
-  count_launch();
+    count_launch();
+  }
   PO_CUDA(cudaGetLastError());
   return PO_OK;
 }
@@ -215,7 +222,7 @@ __global__ void __launch_bounds__(kDirThreads) k_direct_f32(
     int64_t n, const float *__restrict__ x, const float *__restrict__ y, const float *__restrict__ z,
     const float2 *__restrict__ cur /* [slot][n][6] */, const double *__restrict__ tile_ctr,
     const double *__restrict__ k_per_lambda, double c0x, double c0y, double c0z, const float4 *__restrict__ dirs,
-    const double *__restrict__ dirs_d, int ndir, int tiles_per_split, int n_slots_total,
+    const double *__restrict__ dirs_d, int ndir, int tiles_per_split, int n_slots_total, int Gtot, int g0,
     float2 *__restrict__ partial) {
   __shared__ float4 s_u[kDirTile];
   __shared__ float2 s_cur[kDirTile][G * 6];
@@ -249,7 +256,7 @@ __global__ void __launch_bounds__(kDirThreads) k_direct_f32(
 #pragma unroll
       for (int g = 0; g < G; ++g)
 #pragma unroll
-        for (int k = 0; k < 6; ++k) s_cur[q][g * 6 + k] = cur[(((int64_t)lam * G + g) * n + p) * 6 + k];
+        for (int k = 0; k < 6; ++k) s_cur[q][g * 6 + k] = cur[(((int64_t)lam * Gtot + g0 + g) * n + p) * 6 + k];
     }
     __syncthreads();
 #pragma unroll
@@ -285,7 +292,7 @@ __global__ void __launch_bounds__(kDirThreads) k_direct_f32(
     for (int g = 0; g < G; ++g)
 #pragma unroll
       for (int k = 0; k < 6; ++k)
-        partial[(((int64_t)split * n_slots_total + (int64_t)lam * G + g) * 6 + k) * ndir + dd[q]] =
+        partial[(((int64_t)split * n_slots_total + (int64_t)lam * Gtot + g0 + g) * 6 + k) * ndir + dd[q]] =
             make_float2(tr[q][g * 6 + k], ti[q][g * 6 + k]);
   }
 }
@@ -402,18 +409,20 @@ po_status launch_direct_f32(int64_t n, const float *x, const float *y, const flo
   int tps = (int)((ntiles + nsplit - 1) / nsplit);
   dim3 grid((unsigned)((ndir + kDirThreads * kDirDPT - 1) / (kDirThreads * kDirDPT)), (unsigned)nsplit,
             (unsigned)n_lambda);
+  for (int g0 = 0; g0 < G; g0 += 4) {
+    const int gc = std::min(4, G - g0);
 #define PO_DIR(GG)                                                                                             \
   k_direct_f32<GG><<<grid, kDirThreads, 0, st>>>(n, x, y, z, cur, tile_ctr, k_per_lambda, c0[0], c0[1], c0[2], \
-                                                 dirs, dirs_d, ndir, tps, S, partial)
-  switch (G) {
-    case 1: PO_DIR(1); break;
-    case 2: PO_DIR(2); break;
-    case 3: PO_DIR(3); break;
-    case 4: PO_DIR(4); break;
-    default: return fail(PO_ERR_UNSUPPORTED, "FP32 direct kernel supports at most 4 slots per wavelength");
-  }
+                                                 dirs, dirs_d, ndir, tps, S, G, g0, partial)
+    switch (gc) {
+      case 1: PO_DIR(1); break;
+      case 2: PO_DIR(2); break;
+      case 3: PO_DIR(3); break;
+      default: PO_DIR(4); break;
+    }
 #undef PO_DIR
-  count_launch();
+    count_launch();
+  }
   int64_t per = (int64_t)S * 6 * ndir;
   k_sum_splits<float2><<<(unsigned)((per + 255) / 256), 256, 0, st>>>(partial, nsplit, per, out);
   count_launch();

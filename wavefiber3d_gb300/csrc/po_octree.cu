@@ -18,6 +18,7 @@
 // of tree.h:379-414.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdio>
 #include <vector>
 
@@ -311,6 +312,8 @@ struct Carver {
   }
 };
 
+int64_t level_capacity(int64_t n, int l);
+
 int64_t level_capacity(int64_t n, int l) {
   int64_t c = 1;
   for (int i = 0; i < l && c < n; ++i) c *= 8;
@@ -320,50 +323,65 @@ int64_t level_capacity(int64_t n, int l) {
 
 }  // namespace
 
-size_t octree_workspace_bytes(int64_t n, int depth) {
-  size_t b = 0;
-  int64_t nn = n > 0 ? n : 1;
-  b += 4 * align256(sizeof(uint32_t) * nn);                 // keys a/b, idx a/b
-  b += 2 * align256(sizeof(int32_t) * nn);                  // flags, pos
-  int64_t nb = (nn + kSortTile - 1) / kSortTile;
-  b += 2 * align256(sizeof(int32_t) * 256 * nb);            // hist, offs
-  b += align256(sizeof(int32_t) * ((nn * 1 + kScanThreads * 4 - 1) / (kScanThreads * 4) + 1) * 2 + 256 * nb);
-  b += align256(sizeof(int64_t) * (PO_MAX_DEPTH + 1));      // counts
+// Layout of the octree workspace; with a null base it only measures.
+struct OctreeLayout {
+  uint32_t *ka, *kb;
+  int32_t *va, *vb, *flag, *pos, *hist, *offs, *sums;
+  int64_t *counts;
+  OctreeLevel level[PO_MAX_DEPTH + 1];
+  size_t bytes;
+  bool ok;
+};
+
+OctreeLayout carve_octree(void *ws, size_t ws_bytes, int64_t n, int depth) {
+  OctreeLayout L;
+  Carver cv{(char *)ws, ws ? ws_bytes : (size_t)-1};
+  const int64_t nn = n > 0 ? n : 1;
+  const int64_t nb = (nn + kSortTile - 1) / kSortTile;
+  L.ka = cv.take<uint32_t>(nn);
+  L.kb = cv.take<uint32_t>(nn);
+  L.va = cv.take<int32_t>(nn);
+  L.vb = cv.take<int32_t>(nn);
+  L.flag = cv.take<int32_t>(nn);
+  L.pos = cv.take<int32_t>(nn);
+  L.hist = cv.take<int32_t>(256 * nb);
+  L.offs = cv.take<int32_t>(256 * nb);
+  // block sums of the device scan: the largest scanned array is max(n, 256 * nb)
+  L.sums = cv.take<int32_t>((std::max(nn, 256 * nb) + kScanThreads * 4 - 1) / (kScanThreads * 4) + 1);
+  L.counts = cv.take<int64_t>(PO_MAX_DEPTH + 1);
   for (int l = 0; l <= depth; ++l) {
     int64_t c = level_capacity(nn, l);
-    b += align256(sizeof(int32_t) * (c + 1));               // begin
-    b += align256(sizeof(int32_t) * c);                     // parent
-    b += align256(sizeof(uint32_t) * c);                    // prefix
-    if (l < depth) b += align256(sizeof(int32_t) * c * 8);  // child
+    L.level[l].begin = cv.take<int32_t>(c + 1);
+    L.level[l].parent = cv.take<int32_t>(c);
+    L.level[l].prefix = cv.take<uint32_t>(c);
+    L.level[l].child = l < depth ? cv.take<int32_t>(c * 8) : nullptr;
+    L.level[l].count = 0;
   }
-  return b + 4096;
+  L.ok = cv.ok;
+  L.bytes = (size_t)(cv.p - (char *)ws);
+  return L;
 }
+
+size_t octree_workspace_bytes(int64_t n, int depth) { return carve_octree(nullptr, 0, n, depth).bytes + 256; }
 
 po_status build_octree(const float *x, const float *y, const float *z, int64_t n, const float box_min[3],
                        const float box_max[3], int depth, void *ws, size_t ws_bytes, OctreeBuffers *out,
                        cudaStream_t st) {
   if (depth < 0 || depth > PO_MAX_DEPTH) return fail(PO_ERR_INVALID_ARGUMENT, "octree depth out of range");
   if (n < 0 || n > INT32_MAX - 1) return fail(PO_ERR_INVALID_ARGUMENT, "point count out of range");
-  Carver cv{(char *)ws, ws_bytes};
+  if (!ws) return fail(PO_ERR_INVALID_ARGUMENT, "null octree workspace");
+  OctreeLayout lay = carve_octree(ws, ws_bytes, n, depth);
+  if (!lay.ok) return fail(PO_ERR_INVALID_ARGUMENT, "octree workspace too small");
   int64_t nn = n > 0 ? n : 1;
-  uint32_t *ka = cv.take<uint32_t>(nn), *kb = cv.take<uint32_t>(nn);
-  int32_t *va = cv.take<int32_t>(nn), *vb = cv.take<int32_t>(nn);
-  int32_t *flag = cv.take<int32_t>(nn), *pos = cv.take<int32_t>(nn);
   int64_t nb = (nn + kSortTile - 1) / kSortTile;
-  int32_t *hist = cv.take<int32_t>(256 * nb), *offs = cv.take<int32_t>(256 * nb);
-  int32_t *sums = cv.take<int32_t>(((nn + kScanThreads * 4 - 1) / (kScanThreads * 4) + 1) * 2 + 256 * nb);
-  int64_t *counts = cv.take<int64_t>(PO_MAX_DEPTH + 1);
+  uint32_t *ka = lay.ka, *kb = lay.kb;
+  int32_t *va = lay.va, *vb = lay.vb, *flag = lay.flag, *pos = lay.pos, *hist = lay.hist, *offs = lay.offs;
+  int32_t *sums = lay.sums;
+  int64_t *counts = lay.counts;
   OctreeBuffers t;
   t.depth = depth;
   t.n = n;
-  for (int l = 0; l <= depth; ++l) {
-    int64_t c = level_capacity(nn, l);
-    t.level[l].begin = cv.take<int32_t>(c + 1);
-    t.level[l].parent = cv.take<int32_t>(c);
-    t.level[l].prefix = cv.take<uint32_t>(c);
-    t.level[l].child = l < depth ? cv.take<int32_t>(c * 8) : nullptr;
-  }
-  if (!cv.ok) return fail(PO_ERR_INVALID_ARGUMENT, "octree workspace too small");
+  for (int l = 0; l <= depth; ++l) t.level[l] = lay.level[l];
 
   const int T = 256;
   if (n > 0) {

@@ -125,6 +125,8 @@ struct po_ctx {
   DevBuf geom_in, geom_sorted, octree_ws, leaf_ctr, dirs, dirs_d, trans, levelA, levelB, mid, slots, kvals, out,
       cur, partial, tile_ctr;
   cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  // per kernel class: [0..1] leaf/direct kernel, then rows and cols per level
+  cudaEvent_t kev[2 + 4 * PO_MAX_DEPTH] = {};
 };
 
 extern "C" {
@@ -244,6 +246,9 @@ po_status po_create(po_ctx **out, const po_config *cfg) {
   for (auto &e : c->ev) {
     if (cudaEventCreate(&e) != cudaSuccess) { delete c; return fail(PO_ERR_CUDA, "cudaEventCreate"); }
   }
+  for (auto &e : c->kev) {
+    if (cudaEventCreate(&e) != cudaSuccess) { delete c; return fail(PO_ERR_CUDA, "cudaEventCreate"); }
+  }
   if (cudaDeviceSynchronize() != cudaSuccess) { delete c; return fail(PO_ERR_CUDA, "twiddle set-up failed"); }
   *out = c;
   return PO_OK;
@@ -256,6 +261,8 @@ po_status po_destroy(po_ctx *c) {
                     &c->tile_ctr})
     b->release();
   for (auto &e : c->ev)
+    if (e) cudaEventDestroy(e);
+  for (auto &e : c->kev)
     if (e) cudaEventDestroy(e);
   delete c;
   return PO_OK;
@@ -271,6 +278,8 @@ static po_status solve_impl(po_ctx *c, const po_geometry *g, const po_illum *il,
   const int nth_out = cfg.n_theta[0], nph_out = cfg.n_phi[0];
   const int64_t nd_out = (int64_t)nth_out * nph_out;
   const int64_t launches0 = g_launch_count;
+  int n_leaf_launches = 0, n_row_launches = 0, n_col_launches = 0;
+  double leaf_pd = 0, rows_b = 0, cols_b = 0;
   PO_CUDA(cudaEventRecord(c->ev[0], st));
 
   // ---- geometry on the device
@@ -341,8 +350,12 @@ static po_status solve_impl(po_ctx *c, const po_geometry *g, const po_illum *il,
     nsplit = (int)std::min<int64_t>(nsplit, std::max<int64_t>(1, n));
     PO_TRY(c->partial.ensure(sizeof(double2) * 6 * (size_t)S * nd_out * nsplit));
     PO_TRY(c->levelA.ensure(sizeof(double2) * 6 * (size_t)S * nd_out));
+    PO_CUDA(cudaEventRecord(c->kev[0], st));
     PO_TRY(launch_direct_f64(n, gin[0], gin[1], gin[2], c->cur.as<double2>(), k_slot, S, c0, c->dirs_d.as<double>(),
                              (int)nd_out, nsplit, c->partial.as<double2>(), c->levelA.as<double2>(), st));
+    PO_CUDA(cudaEventRecord(c->kev[1], st));
+    n_leaf_launches = 2;
+    leaf_pd = (double)n * nd_out * S;
     PO_CUDA(cudaEventRecord(c->ev[3], st));
     PO_CUDA(cudaEventRecord(c->ev[4], st));
     PO_TRY(launch_intensity_f64(c->levelA.as<double2>(), S, nth_out, nph_out, out_dev, st));
@@ -379,9 +392,13 @@ static po_status solve_impl(po_ctx *c, const po_geometry *g, const po_illum *il,
       PO_TRY(c->tile_ctr.ensure(sizeof(double) * 3 * (size_t)((n + 127) / 128 + 1)));
       PO_TRY(c->partial.ensure(sizeof(float2) * 6 * (size_t)S * nd_out * nsplit));
       PO_TRY(c->levelA.ensure(sizeof(float2) * 6 * (size_t)S * nd_out));
+      PO_CUDA(cudaEventRecord(c->kev[0], st));
       PO_TRY(launch_direct_f32(n, gs[0], gs[1], gs[2], c->cur.as<float2>(), c->tile_ctr.as<double>(), k_lambda, L, G,
                                c0, c->dirs.as<float4>(), c->dirs_d.as<double>(), (int)nd_out, nsplit,
                                c->partial.as<float2>(), c->levelA.as<float2>(), st));
+      PO_CUDA(cudaEventRecord(c->kev[1], st));
+      n_leaf_launches = 2 + (G + 3) / 4;
+      leaf_pd = (double)n * nd_out * S;
       PO_CUDA(cudaEventRecord(c->ev[3], st));
       PO_CUDA(cudaEventRecord(c->ev[4], st));
       PO_TRY(launch_intensity_f32(c->levelA.as<float2>(), S, nth_out, nph_out, nth_out, nph_out, 1, 1, out_dev, st));
@@ -391,9 +408,11 @@ static po_status solve_impl(po_ctx *c, const po_geometry *g, const po_illum *il,
       PO_TRY(c->leaf_ctr.ensure(sizeof(double) * 3 * (size_t)std::max<int64_t>(nleaf, 1)));
       double3 lo = make_double3(cfg.box_min[0], cfg.box_min[1], cfg.box_min[2]);
       double3 hi = make_double3(cfg.box_max[0], cfg.box_max[1], cfg.box_max[2]);
-      k_leaf_centers<<<(unsigned)((nleaf + 255) / 256), 256, 0, st>>>(tree.level[d].prefix, nleaf, d, lo, hi,
-                                                                       c->leaf_ctr.as<double>());
-      count_launch();
+      if (nleaf > 0) {
+        k_leaf_centers<<<(unsigned)((nleaf + 255) / 256), 256, 0, st>>>(tree.level[d].prefix, nleaf, d, lo, hi,
+                                                                         c->leaf_ctr.as<double>());
+        count_launch();
+      }
       // buffer sizes
       size_t lvl_max = 0, mid_max = 0;
       for (int l = 0; l <= d; ++l)
@@ -421,8 +440,12 @@ static po_status solve_impl(po_ctx *c, const po_geometry *g, const po_illum *il,
       std::vector<float4> df = host_dirs_f4(c->T[d], c->Phi[d], c->nth[d]);
       PO_TRY(c->dirs.ensure(sizeof(float4) * df.size()));
       PO_CUDA(cudaMemcpyAsync(c->dirs.p, df.data(), sizeof(float4) * df.size(), cudaMemcpyHostToDevice, st));
+      PO_CUDA(cudaEventRecord(c->kev[0], st));
       PO_TRY(launch_leaf(gsc, tree.level[d].begin, c->leaf_ctr.as<double>(), nleaf, c->slots.as<SlotParams<float>>(),
                          L, G, c->dirs.as<float4>(), c->T[d] * c->Phi[d], c->levelA.as<float2>(), st));
+      PO_CUDA(cudaEventRecord(c->kev[1], st));
+      n_leaf_launches = nleaf > 0 ? (G + 3) / 4 : 0;
+      leaf_pd = (double)n * c->T[d] * c->Phi[d] * S;
       PO_CUDA(cudaEventRecord(c->ev[3], st));
       float2 *cur_lvl = c->levelA.as<float2>(), *nxt = c->levelB.as<float2>();
       for (int l = d - 1; l >= 0; --l) {
@@ -432,13 +455,21 @@ static po_status solve_impl(po_ctx *c, const po_geometry *g, const po_illum *il,
         FftPlan pcol_in = make_plan(c->T[l + 1], c->tw_offset[c->T[l + 1]]);
         FftPlan pcol_out = make_plan(c->T[l], c->tw_offset[c->T[l]]);
         int64_t nrows = (int64_t)S * nc * 6 * c->T[l + 1];
+        PO_CUDA(cudaEventRecord(c->kev[2 + 4 * l], st));
         PO_TRY(launch_interp_rows(cur_lvl, c->mid.as<float2>(), nrows, prow_in, prow_out, c->twiddles.as<float2>(),
                                   1.0f / (float)c->Phi[l + 1], c->sm_count, st));
+        PO_CUDA(cudaEventRecord(c->kev[3 + 4 * l], st));
+        rows_b += 8.0 * nrows * (c->Phi[l + 1] + c->Phi[l]);
+        cols_b += 8.0 * S * 6 * ((double)nc * c->T[l + 1] * c->Phi[l] + (double)np * c->T[l] * c->Phi[l]);
+        if (nrows > 0) ++n_row_launches;
+        if (np > 0) ++n_col_launches;
+        PO_CUDA(cudaEventRecord(c->kev[4 + 4 * l], st));
         int reach = 0x7fffffff;
         if (c->cover == 1 && cfg.nyquist_quirk) reach = 256 * (c->T[l + 1] / 256 + 1);
         PO_TRY(launch_interp_cols(c->mid.as<float2>(), nxt, tree.level[l].child, np, nc, c->Phi[l], pcol_in, pcol_out,
                                   c->twiddles.as<float2>(), c->trans.as<float4>() + tr_off[l], S, G, reach,
                                   1.0f / (float)c->T[l + 1], 6, st));
+        PO_CUDA(cudaEventRecord(c->kev[5 + 4 * l], st));
         std::swap(cur_lvl, nxt);
       }
       PO_CUDA(cudaEventRecord(c->ev[4], st));
@@ -471,6 +502,20 @@ static po_status solve_impl(po_ctx *c, const po_geometry *g, const po_illum *il,
       ws += (int64_t)b->bytes;
     rep->workspace_bytes = ws;
     rep->kernel_launches = g_launch_count - launches0;
+    rep->n_leaf_launches = n_leaf_launches;
+    rep->n_row_launches = n_row_launches;
+    rep->n_col_launches = n_col_launches;
+    rep->leaf_point_dirs = leaf_pd;
+    rep->rows_bytes = rows_b;
+    rep->cols_bytes = cols_b;
+    float tk = 0;
+    if (n_leaf_launches > 0 && cudaEventElapsedTime(&tk, c->kev[0], c->kev[1]) == cudaSuccess) rep->ms_leaf_kernel = tk;
+    if (!fp64 && d > 0)
+      for (int l = 0; l < d; ++l) {
+        if (cudaEventElapsedTime(&tk, c->kev[2 + 4 * l], c->kev[3 + 4 * l]) == cudaSuccess) rep->ms_rows += tk;
+        if (cudaEventElapsedTime(&tk, c->kev[4 + 4 * l], c->kev[5 + 4 * l]) == cudaSuccess) rep->ms_cols += tk;
+      }
+    cudaGetLastError();
   }
   return PO_OK;
 }
