@@ -170,6 +170,23 @@ po_status po_far_field_direct(int64_t n, const float *x, const float *y, const f
 po_status po_interp_fft(const float *in, int th_c, int ph_c, float *out, int th_p, int ph_p, int batch,
                         int theta_mode, int nyquist_quirk, void *stream);
 
+/* No counterpart in the reference.  The interpolation of po_interp_fft for
+ * callers that must not allocate or free device memory while they run (host
+ * applications that own a fixed device-memory budget, plugins, code paths that
+ * cannot afford an allocator call or its failure).  Its scratch is one fixed
+ * device array of PO_NOALLOC_SCRATCH_BYTES per GPU that loads this library,
+ * held until the process exits; a call needs
+ *   batch*th_c*ph_p*8 bytes + the twiddle tables (8 bytes per sample of each
+ *   distinct length among th_c, ph_c, th_p, ph_p, rounded up to 256 bytes)
+ * and larger requests are rejected with PO_ERR_INVALID_ARGUMENT.  The first
+ * call on a device looks up the array's device address (make it before any
+ * stream capture).  All calls share the array: calls that overlap on the GPU
+ * race.  The output is complete in stream order; the call does not
+ * synchronise. */
+#define PO_NOALLOC_SCRATCH_BYTES (16u << 20)
+po_status po_interp_fft_noalloc(const float *in, int th_c, int ph_c, float *out, int th_p, int ph_p, int batch,
+                                int theta_mode, int nyquist_quirk, void *stream);
+
 /* util/fields.h:172-204 (computeintensity): projection onto the transverse
  * plane and |E - Z0 s x H|^2.  fields: [6][n_theta][n_phi] complex64. */
 po_status po_compute_intensity(const float *fields, int n_theta, int n_phi, float *intensity, void *stream);

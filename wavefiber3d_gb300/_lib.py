@@ -67,7 +67,7 @@ class po_report(ctypes.Structure):
 
 EXPORTS = ("po_config_init", "po_status_string", "po_last_error", "po_create", "po_destroy", "po_solve",
            "po_tangent_plane_currents", "po_build_octree", "po_far_field_direct", "po_interp_fft",
-           "po_compute_intensity", "po_version")
+           "po_compute_intensity", "po_version", "po_interp_fft_noalloc")
 
 _lib = None
 
@@ -95,6 +95,7 @@ def load():
     L.po_build_octree.argtypes = [i64, vp, vp, vp, vp, vp, i32, vp, vp, vp]
     L.po_far_field_direct.argtypes = [i64, vp, vp, vp, vp, dbl, vp, i32, i32, i32, vp, vp]
     L.po_interp_fft.argtypes = [vp, i32, i32, vp, i32, i32, i32, i32, i32, vp]
+    L.po_interp_fft_noalloc.argtypes = [vp, i32, i32, vp, i32, i32, i32, i32, i32, vp]
     L.po_compute_intensity.argtypes = [vp, i32, i32, vp, vp]
     for name in EXPORTS:
         f = getattr(L, name)
