@@ -65,7 +65,17 @@ typedef struct po_config {
   int nyquist_quirk;                /* PO_THETA_REFERENCE only: split the theta Nyquist bin
                                        only where interpolation.h:66's launch reaches */
   double distance;                  /* observer distance Dis of the prefactors (sphere.cu:46) */
+  int interp_method;                /* po_interp_method of the theta pass between levels */
 } po_config;
+
+/* How the theta interpolation + translation + child sum between tree levels
+ * is computed (the phi interpolation always uses the shared-memory FFTs). */
+typedef enum po_interp_method {
+  PO_INTERP_FFT = 0,    /* shared-memory batched FFTs (any theta mode) */
+  PO_INTERP_TENSOR = 1  /* the level's trigonometric interpolation matrix as a split hi+lo
+                           BF16 tensor-core product (double-cover theta only; reference
+                           theta mode falls back to the FFTs) */
+} po_interp_method;
 
 typedef struct po_geometry {
   int64_t n;                        /* number of surface points */

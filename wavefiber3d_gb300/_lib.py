@@ -17,6 +17,7 @@ PO_OK = 0
 PO_PREC_FP32, PO_PREC_FP64, PO_PREC_SPLIT_BF16, PO_PREC_SPLIT_FP16 = 0, 1, 2, 3
 PO_THETA_DOUBLE_COVER, PO_THETA_REFERENCE = 0, 1
 PO_POL_TM, PO_POL_TE = 1, 2
+PO_INTERP_FFT, PO_INTERP_TENSOR = 0, 1
 
 STATUS_NAMES = {0: "PO_OK", 1: "PO_ERR_INVALID_ARGUMENT", 2: "PO_ERR_CUDA", 3: "PO_ERR_OUT_OF_MEMORY",
                 4: "PO_ERR_UNSUPPORTED", 5: "PO_ERR_TIMEOUT", 6: "PO_ERR_INTERNAL"}
@@ -34,7 +35,7 @@ class po_config(ctypes.Structure):
                 ("n_phi", ctypes.c_int * (PO_MAX_DEPTH + 1)),
                 ("box_min", ctypes.c_float * 3), ("box_max", ctypes.c_float * 3),
                 ("precision", ctypes.c_int), ("theta_mode", ctypes.c_int), ("nyquist_quirk", ctypes.c_int),
-                ("distance", ctypes.c_double)]
+                ("distance", ctypes.c_double), ("interp_method", ctypes.c_int)]
 
 
 class po_geometry(ctypes.Structure):

@@ -25,13 +25,13 @@ from typing import Sequence
 import numpy as np
 
 from . import _lib
-from ._lib import (PO_POL_TE, PO_POL_TM, PO_PREC_FP32, PO_PREC_FP64, PO_THETA_DOUBLE_COVER, PO_THETA_REFERENCE,
-                   WavePOError, check)
+from ._lib import (PO_INTERP_FFT, PO_INTERP_TENSOR, PO_POL_TE, PO_POL_TM, PO_PREC_FP32, PO_PREC_FP64,
+                   PO_THETA_DOUBLE_COVER, PO_THETA_REFERENCE, WavePOError, check)
 
 __all__ = ["Config", "Illumination", "Solver", "compute_local_tangent_plane", "build_octree",
            "current_times_green_center", "copyandinterp", "compute_intensity", "wavelength_from_index",
            "incidence_from_index", "WavePOError", "PO_POL_TM", "PO_POL_TE", "PO_PREC_FP32", "PO_PREC_FP64",
-           "PO_THETA_DOUBLE_COVER", "PO_THETA_REFERENCE"]
+           "PO_THETA_DOUBLE_COVER", "PO_THETA_REFERENCE", "PO_INTERP_FFT", "PO_INTERP_TENSOR"]
 
 
 def _torch():
@@ -82,6 +82,7 @@ class Config:
     theta_mode: int = PO_THETA_DOUBLE_COVER
     nyquist_quirk: bool = True
     distance: float = 1.0
+    interp_method: int = PO_INTERP_TENSOR
 
     @classmethod
     def reference_rule(cls, max_depth, n_theta_out, n_phi_out, box_min, box_max, theta_extent, phi_extent,
@@ -107,6 +108,7 @@ class Config:
         c.theta_mode = int(self.theta_mode)
         c.nyquist_quirk = 1 if self.nyquist_quirk else 0
         c.distance = float(self.distance)
+        c.interp_method = int(self.interp_method)
         return c
 
 

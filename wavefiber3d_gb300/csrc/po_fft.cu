@@ -117,19 +117,23 @@ __device__ __forceinline__ void small_dft(float2 *v, bool inv) {
   for (int r = 0; r < R; ++r) v[r] = out[r];
 }
 
+// One Stockham stage of radix R over butterflies j = glane, glane+L, ...
+// tab[j] packs the output base idxD = (j/Ns)*Ns*R + j%Ns (low 16 bits) and
+// the twiddle base (j%Ns)*N/(Ns*R) (high 16 bits), precomputed per CTA so
+// that no integer division runs per butterfly.
 template <int R>
 __device__ __forceinline__ void stage_bfly(const float2 *a, float2 *b, int N, int Ns, const float2 *W, bool inv,
-                                           int lane, int nl) {
+                                           int glane, int L, const uint32_t *tab) {
   const int NR = N / R;
-  const int twstep = N / (Ns * R);
-  for (int j = lane; j < NR; j += nl) {
-    const int jm = j % Ns;
+  for (int j = glane; j < NR; j += L) {
+    const uint32_t e = tab[j];
+    const int idxD = (int)(e & 0xffffu), twb = (int)(e >> 16);
     float2 v[R];
 #pragma unroll
     for (int r = 0; r < R; ++r) v[r] = a[j + r * NR];
     if (Ns > 1) {
 #pragma unroll
-      for (int r = 1; r < R; ++r) v[r] = cmul(v[r], tw(W, r * jm * twstep, inv));
+      for (int r = 1; r < R; ++r) v[r] = cmul(v[r], tw(W, r * twb, inv));
     }
     if (R == 2) {
       float2 t0 = cadd(v[0], v[1]), t1 = csub(v[0], v[1]);
@@ -146,9 +150,30 @@ __device__ __forceinline__ void stage_bfly(const float2 *a, float2 *b, int N, in
     } else {
       small_dft<R>(v, inv);
     }
-    const int idxD = (j / Ns) * Ns * R + jm;
 #pragma unroll
     for (int r = 0; r < R; ++r) b[idxD + r * Ns] = v[r];
+  }
+}
+
+// Number of table entries of a plan (sum over stages of N/R).
+__host__ __device__ __forceinline__ int stage_table_size(const FftPlan &p) {
+  int t = 0;
+  for (int s = 0; s < p.nstages; ++s) t += p.n / p.radix[s];
+  return t;
+}
+
+// Fills the per-stage butterfly tables of plan p (all threads of the CTA).
+__device__ void build_stage_table(const FftPlan &p, uint32_t *tab) {
+  int Ns = 1, off = 0;
+  for (int s = 0; s < p.nstages; ++s) {
+    const int R = p.radix[s], NR = p.n / R, twstep = p.n / (Ns * R);
+    for (int j = threadIdx.x; j < NR; j += blockDim.x) {
+      const int jm = j % Ns;
+      const int idxD = (j / Ns) * Ns * R + jm;
+      tab[off + j] = (uint32_t)idxD | ((uint32_t)(jm * twstep) << 16);
+    }
+    off += NR;
+    Ns *= R;
   }
 }
 
@@ -178,20 +203,24 @@ __device__ __forceinline__ void stage_generic(const float2 *a, float2 *b, int N,
   }
 }
 
-// Full transform of length p.n by `nl` lanes of one warp (sync = __syncwarp).
-// Data starts in `a`; returns the buffer holding the result.
-__device__ float2 *fft_warp(float2 *a, float2 *b, const FftPlan &p, const float2 *W, bool inv, int lane) {
+// Transform of length p.n by the L lanes of one lane group (glane in [0, L)).
+// All groups of a warp run the same plan in lockstep, so a warp-wide
+// __syncwarp separates the stages.  Data starts in `a`; returns the buffer
+// holding the result.  tab: the plan's stage tables (build_stage_table).
+__device__ float2 *fft_group(float2 *a, float2 *b, const FftPlan &p, const float2 *W, bool inv, int glane, int L,
+                             const uint32_t *tab) {
   int Ns = 1;
   for (int s = 0; s < p.nstages; ++s) {
     const int R = p.radix[s];
     switch (R) {
-      case 2: stage_bfly<2>(a, b, p.n, Ns, W, inv, lane, 32); break;
-      case 3: stage_bfly<3>(a, b, p.n, Ns, W, inv, lane, 32); break;
-      case 4: stage_bfly<4>(a, b, p.n, Ns, W, inv, lane, 32); break;
-      case 5: stage_bfly<5>(a, b, p.n, Ns, W, inv, lane, 32); break;
-      case 7: stage_bfly<7>(a, b, p.n, Ns, W, inv, lane, 32); break;
-      default: stage_generic(a, b, p.n, Ns, R, W, inv, lane, 32); break;
+      case 2: stage_bfly<2>(a, b, p.n, Ns, W, inv, glane, L, tab); break;
+      case 3: stage_bfly<3>(a, b, p.n, Ns, W, inv, glane, L, tab); break;
+      case 4: stage_bfly<4>(a, b, p.n, Ns, W, inv, glane, L, tab); break;
+      case 5: stage_bfly<5>(a, b, p.n, Ns, W, inv, glane, L, tab); break;
+      case 7: stage_bfly<7>(a, b, p.n, Ns, W, inv, glane, L, tab); break;
+      default: stage_generic(a, b, p.n, Ns, R, W, inv, glane, L); break;
     }
+    tab += p.n / R;
     __syncwarp();
     float2 *t = a;
     a = b;
@@ -202,18 +231,22 @@ __device__ float2 *fft_warp(float2 *a, float2 *b, const FftPlan &p, const float2
 }
 
 // Zero pad of a spectrum X (length n) into Y (length nf), interpolation.h:20-37.
-// split: apply the Nyquist halving of setvalue (interpolation.h:2-9).
-__device__ __forceinline__ void pad_spectrum(const float2 *X, int n, float2 *Y, int nf, bool split, int lane) {
+// split: apply the Nyquist halving of setvalue (interpolation.h:2-9).  When
+// nf == n both halves land on one bin; the reference then keeps half of it
+// (split = true), the exact trigonometric interpolant keeps all of it, which
+// callers request by passing split = false for that case.
+__device__ __forceinline__ void pad_spectrum(const float2 *X, int n, float2 *Y, int nf, bool split, int glane,
+                                             int L) {
   const int nyq = (n + 2) / 2;  // ceil((n+1)/2)
   const int sh = nf - n;
-  for (int k = lane; k < nf; k += 32) {
+  for (int k = glane; k < nf; k += L) {
     float2 v = make_float2(0.f, 0.f);
     if (k < nyq) v = X[k];
     else if (k >= nyq + sh) v = X[k - sh];
     Y[k] = v;
   }
   __syncwarp();
-  if (split && (n % 2 == 0) && lane == 0) {
+  if (split && (n % 2 == 0) && glane == 0) {
     float2 t = Y[nyq - 1];
     t.x *= 0.5f;
     t.y *= 0.5f;
@@ -223,125 +256,175 @@ __device__ __forceinline__ void pad_spectrum(const float2 *X, int n, float2 *Y, 
   __syncwarp();
 }
 
+// lanes per transform: enough butterflies per lane to amortise a stage
+int group_lanes(int nmax) {
+  int want = (nmax + 15) / 16, L = 2;
+  while (L < want && L < 32) L <<= 1;
+  return L;
+}
+
 // ------------------------------------------------------------- row pass
-// rows: src [nrows][n_in] -> dst [nrows][n_out], both complex64.
+// rows: src [nrows][n_in] -> dst [nrows][n_out], both complex64.  A CTA
+// processes NG = blockDim/L consecutive rows per iteration (one lane group per
+// row); consecutive rows are contiguous, so loads and stores are coalesced
+// through shared memory.
 __global__ void k_interp_rows(const float2 *__restrict__ src, float2 *__restrict__ dst, int64_t nrows, FftPlan pin,
-                              FftPlan pout, const float2 *__restrict__ twiddles, float scale) {
+                              FftPlan pout, const float2 *__restrict__ twiddles, float scale, int L, int ref_nyquist) {
   extern __shared__ float2 smem[];
-  const int nw = blockDim.x >> 5, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int nmax = max(pin.n, pout.n);
-  float2 *Win = smem, *Wout = smem + pin.n;
-  float2 *bufA = Wout + pout.n + (size_t)w * 2 * nmax, *bufB = bufA + nmax;
-  for (int k = threadIdx.x; k < pin.n; k += blockDim.x) Win[k] = twiddles[pin.tw + k];
-  for (int k = threadIdx.x; k < pout.n; k += blockDim.x) Wout[k] = twiddles[pout.tw + k];
-  __syncthreads();
-  for (int64_t row = (int64_t)blockIdx.x * nw + w; row < nrows; row += (int64_t)gridDim.x * nw) {
-    const float2 *s = src + row * pin.n;
-    for (int k = lane; k < pin.n; k += 32) bufA[k] = s[k];
-    __syncwarp();
-    float2 *X = fft_warp(bufA, bufB, pin, Win, false, lane);
-    float2 *Y = (X == bufA) ? bufB : bufA;
-    pad_spectrum(X, pin.n, Y, pout.n, true, lane);  // every row is reached (interpolation.h:34-37)
-    float2 *Z = fft_warp(Y, X, pout, Wout, true, lane);
-    float2 *d = dst + row * pout.n;
-    for (int k = lane; k < pout.n; k += 32) {
-      float2 v = Z[k];
-      d[k] = make_float2(v.x * scale, v.y * scale);
+  const int NG = blockDim.x / L, gid = threadIdx.x / L, glane = threadIdx.x % L;
+  const int nin = pin.n, nout = pout.n, nmax = max(nin, nout);
+  const int stride = 2 * nmax + 1;  // odd: lane groups start in different banks
+  float2 *Win = smem, *Wout = smem + nin;
+  float2 *bufs = Wout + nout;
+  uint32_t *tin = (uint32_t *)(bufs + (size_t)NG * stride);
+  uint32_t *tout = tin + stage_table_size(pin);
+  float2 *bufA = bufs + (size_t)gid * stride, *bufB = bufA + nmax;
+  for (int k = threadIdx.x; k < nin; k += blockDim.x) Win[k] = twiddles[pin.tw + k];
+  for (int k = threadIdx.x; k < nout; k += blockDim.x) Wout[k] = twiddles[pout.tw + k];
+  build_stage_table(pin, tin);
+  build_stage_table(pout, tout);
+  for (int64_t base = (int64_t)blockIdx.x * NG; base < nrows; base += (int64_t)gridDim.x * NG) {
+    const int nr = (int)min((int64_t)NG, nrows - base);
+    __syncthreads();
+    const float2 *s = src + base * nin;
+    for (int e = threadIdx.x; e < NG * nin; e += blockDim.x) {
+      int g = e / nin, k = e - g * nin;
+      bufs[(size_t)g * stride + k] = g < nr ? s[e] : make_float2(0.f, 0.f);
     }
-    __syncwarp();
+    __syncthreads();
+    float2 *X = fft_group(bufA, bufB, pin, Win, false, glane, L, tin);
+    float2 *Y = (X == bufA) ? bufB : bufA;
+    // every row is reached by the reference's split (interpolation.h:34-37)
+    pad_spectrum(X, nin, Y, nout, ref_nyquist || nin != nout, glane, L);
+    float2 *Z = fft_group(Y, X, pout, Wout, true, glane, L, tout);
+    // the result sits in bufA or bufB of every group (same parity for all)
+    const int zoff = (Z == bufA) ? 0 : nmax;
+    __syncthreads();
+    float2 *d = dst + base * nout;
+    for (int e = threadIdx.x; e < nr * nout; e += blockDim.x) {
+      int g = e / nout, k = e - g * nout;
+      float2 v = bufs[(size_t)g * stride + zoff + k];
+      d[e] = make_float2(v.x * scale, v.y * scale);
+    }
   }
 }
 
-int rows_warps(int nmax, int nin, int nout) {
-  size_t tw = sizeof(float2) * (size_t)(nin + nout);
-  size_t per = sizeof(float2) * 2 * (size_t)nmax;
-  int w = 8;
-  while (w > 1 && tw + per * w > 200 * 1024) w >>= 1;
-  return w;
+static size_t rows_smem(const FftPlan &pin, const FftPlan &pout, int NG) {
+  const int nmax = std::max(pin.n, pout.n);
+  return sizeof(float2) * ((size_t)pin.n + pout.n + (size_t)NG * (2 * nmax + 1)) +
+         sizeof(uint32_t) * (stage_table_size(pin) + stage_table_size(pout)) + 16;
 }
 
 po_status launch_interp_rows(const float2 *src, float2 *dst, int64_t nrows, const FftPlan &pin, const FftPlan &pout,
-                             const float2 *twiddles, float scale, int sm_count, cudaStream_t st) {
+                             const float2 *twiddles, float scale, int sm_count, int ref_nyquist, cudaStream_t st) {
   if (nrows <= 0) return PO_OK;
   const int nmax = std::max(pin.n, pout.n);
-  const int w = rows_warps(nmax, pin.n, pout.n);
-  size_t smem = sizeof(float2) * ((size_t)pin.n + pout.n + (size_t)w * 2 * nmax);
+  const int L = group_lanes(nmax);
+  int threads = 256;
+  while (rows_smem(pin, pout, threads / L) > 72 * 1024 && threads > std::max(32, L)) threads >>= 1;
+  const size_t smem = rows_smem(pin, pout, threads / L);
   if (smem > 227 * 1024) return fail(PO_ERR_UNSUPPORTED, "angular grid too large for the shared-memory FFT");
   PO_CUDA(cudaFuncSetAttribute(k_interp_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  int64_t blocks = (nrows + w - 1) / w;
-  int64_t cap = (int64_t)sm_count * 16;
+  const int NG = threads / L;
+  int64_t blocks = (nrows + NG - 1) / NG;
+  int64_t cap = (int64_t)sm_count * 32;
   if (blocks > cap) blocks = cap;
-  k_interp_rows<<<(unsigned)blocks, 32 * w, smem, st>>>(src, dst, nrows, pin, pout, twiddles, scale);
+  k_interp_rows<<<(unsigned)blocks, threads, smem, st>>>(src, dst, nrows, pin, pout, twiddles, scale, L, ref_nyquist);
   count_launch();
   PO_CUDA(cudaGetLastError());
   return PO_OK;
 }
 
 // ---------------------------------------------------- column pass + sum
-// mid   : [slot][child][comp][Tc][Phi] (output of the row pass)
-// parent: [slot][node][comp][Tp][Phi]
-// trans : [lambda][Tp*Phi] float4 (r_x, r_y, r_z, 0) reduced axis phases
-// One warp owns one phi column; a CTA owns `nw` consecutive columns of one
-// (parent node, component, slot).
+// mid   : [slot][child][comp][Rc][Phi]   (row-pass output, Rc stored theta rows)
+// parent: [slot][node][comp][Rp][Phi]
+// trans : [lambda][Rp*Phi] float4 (r_x, r_y, r_z, 0) reduced axis phases
+// Without `mirror`, Rc = Tc and Rp = Tp: whole theta columns are stored.
+// With `mirror` (double cover, Phi even), a level stores rows 0..n_theta only
+// (Rc = Tc/2 + 1); row t > n_theta of column j is row Tc - t of column
+// j + Phi/2 (the same direction), so a CTA takes columns in pairs
+// (j, j + Phi/2) and rebuilds both full columns from the two stored halves.
+// A CTA owns NG = 2^lgNG columns of one (parent node, component, slot); one
+// lane group of L lanes transforms one column.
 __global__ void k_interp_cols(const float2 *__restrict__ mid, float2 *__restrict__ parent,
                               const int32_t *__restrict__ child_table, int64_t n_parent, int64_t n_child, int phi,
-                              FftPlan pin, FftPlan pout, const float2 *__restrict__ twiddles,
-                              const float4 *__restrict__ trans, int G, int quirk_reach, float scale, int ncomp) {
+                              int Rc, int Rp, FftPlan pin, FftPlan pout, const float2 *__restrict__ twiddles,
+                              const float4 *__restrict__ trans, int G, int quirk_reach, float scale, int ncomp,
+                              int mirror, int L, int lgNG, int ref_nyquist) {
   extern __shared__ float2 smem[];
-  const int nw = blockDim.x >> 5, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int NG = 1 << lgNG, gid = threadIdx.x / L, glane = threadIdx.x % L;
   const int Tc = pin.n, Tp = pout.n;
-  const int nmax = max(Tc, Tp);
+  const int nmax = max(Tc, Tp), stride = 2 * nmax + 1, ts = NG + 1;
   float2 *Win = smem, *Wout = smem + Tc;
-  float2 *tile = Wout + Tp;                       // [Tc][nw]
-  float2 *acc = tile + (size_t)Tc * nw;           // [nw][Tp]
-  float2 *bufA = acc + (size_t)nw * Tp + (size_t)w * 2 * nmax, *bufB = bufA + nmax;
-  float2 *myacc = acc + (size_t)w * Tp;
-  const int ntile = (phi + nw - 1) / nw;
-  const int j0 = (int)(blockIdx.x % ntile) * nw;
+  float2 *tile = Wout + Tp;                 // [Rc][NG + 1]
+  float2 *acc = tile + (size_t)Rc * ts;     // [NG][Rp + 1]
+  float2 *bufs = acc + (size_t)NG * (Rp + 1);
+  uint32_t *tin = (uint32_t *)(bufs + (size_t)NG * stride);
+  uint32_t *tout = tin + stage_table_size(pin);
+  float2 *bufA = bufs + (size_t)gid * stride, *bufB = bufA + nmax;
+  float2 *myacc = acc + (size_t)gid * (Rp + 1);
+  // columns of this CTA
+  const int TW = mirror ? NG / 2 : NG;          // distinct column starts per tile
+  const int span = mirror ? phi / 2 : phi;      // columns covered by tile starts
+  const int ntile = (span + TW - 1) / TW;
+  const int j0 = (int)(blockIdx.x % ntile) * TW;
   const int64_t pc = blockIdx.x / ntile;  // parent * ncomp + comp
   const int64_t p = pc / ncomp;
   const int comp = (int)(pc % ncomp);
   const int slot = blockIdx.z;
   const int lam = slot / G;
-  const int j = j0 + w;
-  const bool col_ok = j < phi;
+  // the column this thread's group owns and the column this thread loads/stores
+  // in the cooperative tile loops (blockDim is a multiple of NG, so it is fixed)
+  const int gl = threadIdx.x & (NG - 1);
+  auto col_of = [&](int g) { return mirror ? (g < TW ? j0 + g : j0 + (g - TW) + phi / 2) : j0 + g; };
+  auto base_of = [&](int g) { return mirror ? j0 + (g < TW ? g : g - TW) : j0 + g; };
+  const int j = col_of(gid);
+  const bool ok = base_of(gid) < span;
+  const int jl = col_of(gl);
+  const bool okl = base_of(gl) < span;
+  const int partner = mirror ? (gid < TW ? gid + TW : gid - TW) : gid;
+  const int nth_c = Tc / 2;
+  const int rstep = blockDim.x >> lgNG;
   for (int k = threadIdx.x; k < Tc; k += blockDim.x) Win[k] = twiddles[pin.tw + k];
   for (int k = threadIdx.x; k < Tp; k += blockDim.x) Wout[k] = twiddles[pout.tw + k];
-  for (int k = lane; k < Tp; k += 32) myacc[k] = make_float2(0.f, 0.f);
-  const bool split = (j < quirk_reach);
-  const float4 *tr = trans ? trans + (int64_t)lam * Tp * phi : nullptr;
+  build_stage_table(pin, tin);
+  build_stage_table(pout, tout);
+  for (int k = glane; k < Rp; k += L) myacc[k] = make_float2(0.f, 0.f);
+  const bool split = (j < quirk_reach) && (ref_nyquist || Tc != Tp);
+  const float4 *tr = trans ? trans + (int64_t)lam * Rp * phi : nullptr;
   // child_table == nullptr: plain interpolation of pattern p (one "child", no phase shift)
   const int nchild_slots = child_table ? 8 : 1;
   for (int o = 0; o < nchild_slots; ++o) {
     const int32_t c = child_table ? child_table[p * 8 + o] : (int32_t)p;
     if (c < 0) continue;
     __syncthreads();
-    // coalesced tile load: row t, columns j0..j0+nw
-    const float2 *m = mid + (((int64_t)slot * n_child + c) * ncomp + comp) * (int64_t)Tc * phi;
-    for (int e = threadIdx.x; e < Tc * nw; e += blockDim.x) {
-      int t = e / nw, q = e % nw;
-      int jj = j0 + q;
-      tile[t * nw + q] = (jj < phi) ? m[(int64_t)t * phi + jj] : make_float2(0.f, 0.f);
-    }
+    const float2 *m = mid + (((int64_t)slot * n_child + c) * ncomp + comp) * (int64_t)Rc * phi;
+    for (int t = threadIdx.x >> lgNG; t < Rc; t += rstep)
+      tile[t * ts + gl] = okl ? m[(int64_t)t * phi + jl] : make_float2(0.f, 0.f);
     __syncthreads();
-    for (int t = lane; t < Tc; t += 32) bufA[t] = tile[t * nw + w];
+    if (mirror) {
+      for (int t = glane; t < Tc; t += L)
+        bufA[t] = t <= nth_c ? tile[t * ts + gid] : tile[(Tc - t) * ts + partner];
+    } else {
+      for (int t = glane; t < Tc; t += L) bufA[t] = tile[t * ts + gid];
+    }
     __syncwarp();
-    float2 *X = fft_warp(bufA, bufB, pin, Win, false, lane);
+    float2 *X = fft_group(bufA, bufB, pin, Win, false, glane, L, tin);
     float2 *Y = (X == bufA) ? bufB : bufA;
-    pad_spectrum(X, Tc, Y, Tp, split, lane);
-    float2 *Z = fft_warp(Y, X, pout, Wout, true, lane);
+    pad_spectrum(X, Tc, Y, Tp, split, glane, L);
+    float2 *Z = fft_group(Y, X, pout, Wout, true, glane, L, tout);
     // child centre - parent centre = (sx*a_x, sy*a_y, sz*a_z) with the octant signs of tree.h:672-687
     const float sgx = (o & 1) ? 1.f : -1.f, sgy = (o & 2) ? -1.f : 1.f, sgz = (o & 4) ? -1.f : 1.f;
-    if (col_ok && trans == nullptr) {
-      for (int t = lane; t < Tp; t += 32) {
+    if (ok && tr == nullptr) {
+      for (int t = glane; t < Rp; t += L) {
         float2 v = Z[t];
         float2 a = myacc[t];
         a.x += scale * v.x;
         a.y += scale * v.y;
         myacc[t] = a;
       }
-    } else if (col_ok) {
-      for (int t = lane; t < Tp; t += 32) {
+    } else if (ok) {
+      for (int t = glane; t < Rp; t += L) {
         float4 r = tr[(int64_t)t * phi + j];
         float ph = fmaf(sgx, r.x, fmaf(sgy, r.y, sgz * r.z));
         float sn, cs;
@@ -356,41 +439,47 @@ __global__ void k_interp_cols(const float2 *__restrict__ mid, float2 *__restrict
     __syncwarp();
   }
   __syncthreads();
-  float2 *out = parent + (((int64_t)slot * n_parent + p) * ncomp + comp) * (int64_t)Tp * phi;
-  for (int e = threadIdx.x; e < Tp * nw; e += blockDim.x) {
-    int t = e / nw, q = e % nw;
-    int jj = j0 + q;
-    if (jj < phi) out[(int64_t)t * phi + jj] = acc[(size_t)q * Tp + t];
-  }
+  float2 *out = parent + (((int64_t)slot * n_parent + p) * ncomp + comp) * (int64_t)Rp * phi;
+  if (okl)
+    for (int t = threadIdx.x >> lgNG; t < Rp; t += rstep) out[(int64_t)t * phi + jl] = acc[(size_t)gl * (Rp + 1) + t];
 }
 
-int cols_warps(int tc, int tp) {
-  int nmax = std::max(tc, tp);
-  int w = 8;
-  while (w > 1) {
-    size_t b = sizeof(float2) * ((size_t)tc + tp + (size_t)tc * w + (size_t)w * tp + (size_t)w * 2 * nmax);
-    if (b <= 200 * 1024) break;
-    w >>= 1;
-  }
-  return w;
+static size_t cols_smem(const FftPlan &pin, const FftPlan &pout, int Rc, int Rp, int NG) {
+  const int nmax = std::max(pin.n, pout.n);
+  return sizeof(float2) * ((size_t)pin.n + pout.n + (size_t)Rc * (NG + 1) + (size_t)NG * (Rp + 1) +
+                           (size_t)NG * (2 * nmax + 1)) +
+         sizeof(uint32_t) * (stage_table_size(pin) + stage_table_size(pout)) + 16;
 }
 
 po_status launch_interp_cols(const float2 *mid, float2 *parent, const int32_t *child_table, int64_t n_parent,
-                             int64_t n_child, int phi, const FftPlan &pin, const FftPlan &pout,
+                             int64_t n_child, int phi, int Rc, int Rp, const FftPlan &pin, const FftPlan &pout,
                              const float2 *twiddles, const float4 *trans, int n_slots, int G, int quirk_reach,
-                             float scale, int ncomp, cudaStream_t st) {
+                             float scale, int ncomp, int mirror, int ref_nyquist, cudaStream_t st) {
   if (n_parent <= 0 || n_slots <= 0) return PO_OK;
-  const int w = cols_warps(pin.n, pout.n);
+  if (mirror && (phi % 2 != 0 || pin.n % 2 != 0 || pout.n % 2 != 0 || Rc != pin.n / 2 + 1 || Rp != pout.n / 2 + 1))
+    return fail(PO_ERR_INTERNAL, "mirrored column pass needs even sizes and half-stored rows");
+  if (!mirror && (Rc != pin.n || Rp != pout.n)) return fail(PO_ERR_INTERNAL, "row counts must match the transforms");
   const int nmax = std::max(pin.n, pout.n);
-  size_t smem = sizeof(float2) * ((size_t)pin.n + pout.n + (size_t)pin.n * w + (size_t)w * pout.n +
-                                  (size_t)w * 2 * nmax);
+  const int L = group_lanes(nmax);
+  int threads = 256;
+  // fewer columns per CTA when one tile would mostly hang over the grid edge
+  const int span = mirror ? phi / 2 : phi;
+  while (threads > 2 * L && (threads / L) / (mirror ? 2 : 1) >= 2 * span) threads >>= 1;
+  while (cols_smem(pin, pout, Rc, Rp, threads / L) > 72 * 1024 && threads > std::max(64, 2 * L)) threads >>= 1;
+  const int NG = threads / L;
+  const size_t smem = cols_smem(pin, pout, Rc, Rp, NG);
   if (smem > 227 * 1024) return fail(PO_ERR_UNSUPPORTED, "angular grid too large for the shared-memory FFT");
+  if (mirror && NG < 2) return fail(PO_ERR_UNSUPPORTED, "mirrored column pass needs two lane groups per CTA");
+  int lg = 0;
+  while ((1 << lg) < NG) ++lg;
   PO_CUDA(cudaFuncSetAttribute(k_interp_cols, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  int64_t gx = (int64_t)((phi + w - 1) / w) * n_parent * ncomp;
+  const int TW = mirror ? NG / 2 : NG;
+  int64_t gx = (int64_t)((span + TW - 1) / TW) * n_parent * ncomp;
   if (gx > 2147483647LL || n_slots > 65535) return fail(PO_ERR_UNSUPPORTED, "too many nodes for one launch");
   dim3 grid((unsigned)gx, 1u, (unsigned)n_slots);
-  k_interp_cols<<<grid, 32 * w, smem, st>>>(mid, parent, child_table, n_parent, n_child, phi, pin, pout, twiddles,
-                                            trans, G, quirk_reach, scale, ncomp);
+  k_interp_cols<<<grid, threads, smem, st>>>(mid, parent, child_table, n_parent, n_child, phi, Rc, Rp, pin, pout,
+                                             twiddles, trans, G, quirk_reach, scale, ncomp, mirror, L, lg,
+                                             ref_nyquist);
   count_launch();
   PO_CUDA(cudaGetLastError());
   return PO_OK;
@@ -399,11 +488,11 @@ po_status launch_interp_cols(const float2 *mid, float2 *parent, const int32_t *c
 // ----------------------------------------------------- translation table
 // r_a = (k * a_a * s_a) mod 2pi for a = x, y, z and every direction of a
 // Tp x Phi grid (theta rows may run into the second cover), per wavelength.
-__global__ void k_trans_table(const double *__restrict__ k_per_lambda, int n_lambda, int nth, int Tp, int phi,
+__global__ void k_trans_table(const double *__restrict__ k_per_lambda, int n_lambda, int nth, int Rp, int phi,
                               double ax, double ay, double az, float4 *__restrict__ out) {
   int64_t d = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   int lam = blockIdx.y;
-  int64_t nd = (int64_t)Tp * phi;
+  int64_t nd = (int64_t)Rp * phi;
   if (d >= nd || lam >= n_lambda) return;
   int it = (int)(d / phi), ip = (int)(d % phi);
   double s[3];
@@ -420,12 +509,12 @@ __global__ void k_trans_table(const double *__restrict__ k_per_lambda, int n_lam
   out[(int64_t)lam * nd + d] = make_float4(r[0], r[1], r[2], 0.f);
 }
 
-po_status launch_trans_table(const double *k_per_lambda, int n_lambda, int nth, int Tp, int phi, const double a[3],
+po_status launch_trans_table(const double *k_per_lambda, int n_lambda, int nth, int Rp, int phi, const double a[3],
                              float4 *out, cudaStream_t st) {
-  int64_t nd = (int64_t)Tp * phi;
+  int64_t nd = (int64_t)Rp * phi;
   if (nd <= 0 || n_lambda <= 0) return PO_OK;
   dim3 grid((unsigned)((nd + 255) / 256), (unsigned)n_lambda);
-  k_trans_table<<<grid, 256, 0, st>>>(k_per_lambda, n_lambda, nth, Tp, phi, a[0], a[1], a[2], out);
+  k_trans_table<<<grid, 256, 0, st>>>(k_per_lambda, n_lambda, nth, Rp, phi, a[0], a[1], a[2], out);
   count_launch();
   PO_CUDA(cudaGetLastError());
   return PO_OK;

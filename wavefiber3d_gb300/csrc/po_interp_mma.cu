@@ -1,0 +1,251 @@
+// po_interp_mma.cu -- theta interpolation + translation + child sum as a
+// split-precision tensor-core product.
+//
+// The theta half of util/interpolation.h:47-77 (FFT along theta, zero pad with
+// the Nyquist split, inverse FFT, scale 1/n) is one fixed linear map per tree
+// level: out[t'] = sum_t K_n(t'/Tp - t/Tc) x[t] with the real trigonometric
+// kernel
+//   K_n(v) = (1/n) [1 + 2 sum_{k=1}^{n/2-1} cos(2 pi k v) + cos(pi n v)]   (n even)
+//   K_n(v) = (1/n) sin(pi n v) / sin(pi v)                                 (n odd).
+// With the double cover stored as rows 0..n_theta (see k_interp_cols), a
+// parent column j is A h_j + B h_{j+Phi/2}: a GEMM with K = 2 Rc whose
+// operands are the level's constant matrix [A | B] and the child's stored
+// half columns.  Both are split into bf16 hi + lo parts and multiplied as
+// hi*hi + hi*lo + lo*hi with FP32 accumulation (mma.sync m16n8k16), which
+// keeps ~16 bits of every operand.  The epilogue multiplies each child's
+// result by exp(i k s.(c_child - c_parent)) and sums the children into the
+// parent in shared memory.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "po_common.cuh"
+#include "po_internal.h"
+#include "po_kernels.h"
+
+namespace wavepo {
+
+// ------------------------------------------------------------ host side
+static double trig_kernel(int n, double v) {
+  double f = v - std::nearbyint(v);
+  if (std::fabs(f) < 1e-15) return 1.0;
+  double x = 2.0 * kPi * v;
+  if (n % 2) return std::sin(0.5 * n * x) / (n * std::sin(0.5 * x));
+  // even n: Dirichlet sum up to n/2-1 plus the split Nyquist cosine
+  double d = std::sin(0.5 * (n - 1) * x) / std::sin(0.5 * x);
+  return (d + std::cos(0.5 * n * x)) / n;
+}
+
+static uint16_t bf16_rne(float f) {
+  uint32_t u;
+  std::memcpy(&u, &f, 4);
+  if ((u & 0x7f800000u) == 0x7f800000u) return (uint16_t)(u >> 16);
+  uint32_t r = u + 0x7fffu + ((u >> 16) & 1u);
+  return (uint16_t)(r >> 16);
+}
+static float bf16_to_f(uint16_t h) {
+  uint32_t u = (uint32_t)h << 16;
+  float f;
+  std::memcpy(&f, &u, 4);
+  return f;
+}
+
+// A operand of one level in mma.sync fragment order:
+//   [mtile][kstep][lane] { hi[4] b32, lo[4] b32 }  (32 bytes per lane)
+// Rows: parent rows t' < Rp.  Columns (K): own half column rows 0..Rc-1, then
+// (mirror) the partner half column rows 0..Rc-1.
+size_t theta_matrix_words(int Rp, int Kp) { return (size_t)((Rp + 15) / 16) * (Kp / 16) * 32 * 8; }
+
+void build_theta_matrix(int Tc, int Tp, int Rc, int Rp, int mirror, int Kp, std::vector<uint32_t> &out) {
+  const int K = mirror ? 2 * Rc : Rc;
+  const int nth_c = Tc / 2;
+  std::vector<double> M((size_t)Rp * Kp, 0.0);
+  for (int r = 0; r < Rp; ++r) {
+    for (int t = 0; t < Rc; ++t) M[(size_t)r * Kp + t] = trig_kernel(Tc, (double)r / Tp - (double)t / Tc);
+    if (mirror)
+      for (int s = 1; s < nth_c; ++s) M[(size_t)r * Kp + Rc + s] = trig_kernel(Tc, (double)r / Tp - (double)(Tc - s) / Tc);
+  }
+  (void)K;
+  const int MT = (Rp + 15) / 16, KS = Kp / 16;
+  out.assign(theta_matrix_words(Rp, Kp), 0u);
+  for (int mt = 0; mt < MT; ++mt)
+    for (int ks = 0; ks < KS; ++ks)
+      for (int lane = 0; lane < 32; ++lane) {
+        const int g = lane >> 2, tq = lane & 3;
+        const int rows[4] = {mt * 16 + g, mt * 16 + g + 8, mt * 16 + g, mt * 16 + g + 8};
+        const int cols[4] = {ks * 16 + 2 * tq, ks * 16 + 2 * tq, ks * 16 + 2 * tq + 8, ks * 16 + 2 * tq + 8};
+        uint32_t *dst = &out[(((size_t)mt * KS + ks) * 32 + lane) * 8];
+        for (int q = 0; q < 4; ++q) {
+          uint16_t h[2], l[2];
+          for (int e = 0; e < 2; ++e) {
+            int r = rows[q], c = cols[q] + e;
+            double v = (r < Rp && c < Kp) ? M[(size_t)r * Kp + c] : 0.0;
+            h[e] = bf16_rne((float)v);
+            l[e] = bf16_rne((float)(v - (double)bf16_to_f(h[e])));
+          }
+          dst[q] = (uint32_t)h[0] | ((uint32_t)h[1] << 16);
+          dst[4 + q] = (uint32_t)l[0] | ((uint32_t)l[1] << 16);
+        }
+      }
+}
+
+// ---------------------------------------------------------- device side
+__device__ __forceinline__ void mma_bf16(float *d, const uint32_t *a, const uint32_t *b) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+__device__ __forceinline__ void split_bf16x2(float x0, float x1, uint32_t &hi, uint32_t &lo) {
+  __nv_bfloat16 h0 = __float2bfloat16_rn(x0), h1 = __float2bfloat16_rn(x1);
+  __nv_bfloat16 l0 = __float2bfloat16_rn(x0 - __bfloat162float(h0));
+  __nv_bfloat16 l1 = __float2bfloat16_rn(x1 - __bfloat162float(h1));
+  hi = (uint32_t)__bfloat16_as_ushort(h0) | ((uint32_t)__bfloat16_as_ushort(h1) << 16);
+  lo = (uint32_t)__bfloat16_as_ushort(l0) | ((uint32_t)__bfloat16_as_ushort(l1) << 16);
+}
+
+// CTA: one (parent node, component, slot) and NCC complex columns (NCC/2
+// mirror pairs).  4 warps; warp w owns the 16-row tiles w, w+4, ...
+// B operand (child half columns) is staged per child in fragment order:
+//   Bf[kstep][ntile][lane] = {hi0, hi1, lo0, lo1}  (n = 2*column + re/im)
+template <int NCC>
+__global__ void __launch_bounds__(128) k_interp_cols_mma(
+    const float2 *__restrict__ mid, float2 *__restrict__ parent, const int32_t *__restrict__ child_table,
+    int64_t n_parent, int64_t n_child, int phi, int Rc, int Rp, int Kp, int mirror,
+    const uint4 *__restrict__ Afrag, const float4 *__restrict__ trans, int G, float scale_unused) {
+  constexpr int NT = NCC / 4;  // n-tiles of 8 (re, im interleaved)
+  extern __shared__ uint4 smem_u4[];
+  const int KS = Kp / 16, MT = (Rp + 15) / 16;
+  uint4 *Bf = smem_u4;                                       // [KS][NT][32]
+  float2 *tile = (float2 *)(Bf + (size_t)KS * NT * 32);      // [Rc][NCC]
+  float2 *acc = tile + (size_t)Rc * NCC;                     // [Rp][NCC]
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, tq = lane & 3;
+  const int TW = mirror ? NCC / 2 : NCC;
+  const int span = mirror ? phi / 2 : phi;
+  const int ntile = (span + TW - 1) / TW;
+  const int j0 = (int)(blockIdx.x % ntile) * TW;
+  const int64_t pc = blockIdx.x / ntile;
+  const int64_t p = pc / 6;
+  const int comp = (int)(pc % 6);
+  const int slot = blockIdx.z, lam = slot / G;
+  auto col_of = [&](int q) { return mirror ? (q < TW ? j0 + q : j0 + (q - TW) + phi / 2) : j0 + q; };
+  auto ok_of = [&](int q) { return (mirror ? j0 + (q < TW ? q : q - TW) : j0 + q) < span; };
+  auto partner_of = [&](int q) { return mirror ? (q < TW ? q + TW : q - TW) : q; };
+  for (int e = threadIdx.x; e < Rp * NCC; e += blockDim.x) acc[e] = make_float2(0.f, 0.f);
+  const float4 *tr = trans + (int64_t)lam * Rp * phi;
+  for (int o = 0; o < 8; ++o) {
+    const int32_t c = child_table[p * 8 + o];
+    if (c < 0) continue;
+    __syncthreads();
+    const float2 *m = mid + (((int64_t)slot * n_child + c) * 6 + comp) * (int64_t)Rc * phi;
+    for (int e = threadIdx.x; e < Rc * NCC; e += blockDim.x) {
+      int t = e / NCC, q = e - t * NCC;
+      tile[e] = ok_of(q) ? m[(int64_t)t * phi + col_of(q)] : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    // B fragments: rows kk of the stacked operand [own half; partner half]
+    for (int e = threadIdx.x; e < KS * NT * 32; e += blockDim.x) {
+      const int ln = e & 31, nt = (e >> 5) % NT, ks = (e >> 5) / NT;
+      const int n = nt * 8 + (ln >> 2), q = n >> 1, part = n & 1;
+      const int kb = ks * 16 + 2 * (ln & 3);
+      float v[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int kk = kb + (u & 1) + (u >> 1) * 8;
+        float2 x = make_float2(0.f, 0.f);
+        if (kk < Rc) x = tile[kk * NCC + q];
+        else if (mirror && kk < 2 * Rc) x = tile[(kk - Rc) * NCC + partner_of(q)];
+        v[u] = part ? x.y : x.x;
+      }
+      uint32_t h0, l0, h1, l1;
+      split_bf16x2(v[0], v[1], h0, l0);
+      split_bf16x2(v[2], v[3], h1, l1);
+      Bf[e] = make_uint4(h0, h1, l0, l1);
+    }
+    __syncthreads();
+    const float sgx = (o & 1) ? 1.f : -1.f, sgy = (o & 2) ? -1.f : 1.f, sgz = (o & 4) ? -1.f : 1.f;
+    for (int mt = warp; mt < MT; mt += 4) {
+      float d[NT][4];
+#pragma unroll
+      for (int nt = 0; nt < NT; ++nt) d[nt][0] = d[nt][1] = d[nt][2] = d[nt][3] = 0.f;
+      const uint4 *ap = Afrag + ((size_t)mt * KS) * 64 + lane * 2;
+      for (int ks = 0; ks < KS; ++ks) {
+        const uint4 ah = __ldg(ap + (size_t)ks * 64), al = __ldg(ap + (size_t)ks * 64 + 1);
+        const uint32_t a_hi[4] = {ah.x, ah.y, ah.z, ah.w}, a_lo[4] = {al.x, al.y, al.z, al.w};
+#pragma unroll
+        for (int nt = 0; nt < NT; ++nt) {
+          const uint4 b = Bf[((size_t)ks * NT + nt) * 32 + lane];
+          const uint32_t b_hi[2] = {b.x, b.y}, b_lo[2] = {b.z, b.w};
+          mma_bf16(d[nt], a_hi, b_hi);
+          mma_bf16(d[nt], a_hi, b_lo);
+          mma_bf16(d[nt], a_lo, b_hi);
+        }
+      }
+      // epilogue: rows r0 = mt*16+g (d0,d1) and r0+8 (d2,d3); complex column q = nt*4+tq
+#pragma unroll
+      for (int nt = 0; nt < NT; ++nt) {
+        const int q = nt * 4 + tq;
+        if (!ok_of(q)) continue;
+        const int j = col_of(q);
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const int r = mt * 16 + g + 8 * h;
+          if (r >= Rp) continue;
+          const float4 rr = tr[(int64_t)r * phi + j];
+          float sn, cs;
+          sincos_small(fmaf(sgx, rr.x, fmaf(sgy, rr.y, sgz * rr.z)), &sn, &cs);
+          const float vr = d[nt][2 * h], vi = d[nt][2 * h + 1];
+          float2 a = acc[r * NCC + q];
+          a.x += vr * cs - vi * sn;
+          a.y += vr * sn + vi * cs;
+          acc[r * NCC + q] = a;
+        }
+      }
+    }
+  }
+  __syncthreads();
+  float2 *out = parent + (((int64_t)slot * n_parent + p) * 6 + comp) * (int64_t)Rp * phi;
+  for (int e = threadIdx.x; e < Rp * NCC; e += blockDim.x) {
+    int t = e / NCC, q = e - t * NCC;
+    if (ok_of(q)) out[(int64_t)t * phi + col_of(q)] = acc[e];
+  }
+}
+
+static size_t cols_mma_smem(int ncc, int Rc, int Rp, int Kp) {
+  return sizeof(uint4) * (size_t)(Kp / 16) * (ncc / 4) * 32 + sizeof(float2) * ((size_t)Rc * ncc + (size_t)Rp * ncc);
+}
+
+po_status launch_interp_cols_mma(const float2 *mid, float2 *parent, const int32_t *child_table, int64_t n_parent,
+                                 int64_t n_child, int phi, int Rc, int Rp, int Kp, int mirror, const uint32_t *Afrag,
+                                 const float4 *trans, int n_slots, int G, cudaStream_t st) {
+  if (n_parent <= 0 || n_slots <= 0) return PO_OK;
+  if (Kp % 16 || Kp < (mirror ? 2 * Rc : Rc)) return fail(PO_ERR_INTERNAL, "theta matrix K padding");
+  int ncc = 16;
+  if (cols_mma_smem(ncc, Rc, Rp, Kp) > 100 * 1024 || (mirror ? phi / 2 : phi) <= 4) ncc = 8;
+  const size_t smem = cols_mma_smem(ncc, Rc, Rp, Kp);
+  if (smem > 227 * 1024) return fail(PO_ERR_UNSUPPORTED, "angular grid too large for the tensor-core interpolation");
+  const int TW = mirror ? ncc / 2 : ncc;
+  const int span = mirror ? phi / 2 : phi;
+  int64_t gx = (int64_t)((span + TW - 1) / TW) * n_parent * 6;
+  if (gx > 2147483647LL || n_slots > 65535) return fail(PO_ERR_UNSUPPORTED, "too many nodes for one launch");
+  dim3 grid((unsigned)gx, 1u, (unsigned)n_slots);
+  if (ncc == 16) {
+    PO_CUDA(cudaFuncSetAttribute(k_interp_cols_mma<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_interp_cols_mma<16><<<grid, 128, smem, st>>>(mid, parent, child_table, n_parent, n_child, phi, Rc, Rp, Kp,
+                                                   mirror, (const uint4 *)Afrag, trans, G, 0.f);
+  } else {
+    PO_CUDA(cudaFuncSetAttribute(k_interp_cols_mma<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_interp_cols_mma<8><<<grid, 128, smem, st>>>(mid, parent, child_table, n_parent, n_child, phi, Rc, Rp, Kp,
+                                                  mirror, (const uint4 *)Afrag, trans, G, 0.f);
+  }
+  count_launch();
+  PO_CUDA(cudaGetLastError());
+  return PO_OK;
+}
+
+}  // namespace wavepo

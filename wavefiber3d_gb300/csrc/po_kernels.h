@@ -4,6 +4,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <vector>
+
 #include "po_common.cuh"
 #include "wavepo.h"
 
@@ -51,13 +53,21 @@ po_status launch_widen(const float *in, double2 *out, int64_t n, cudaStream_t st
 po_status launch_narrow(const double2 *in, float2 *out, int64_t n, cudaStream_t st);
 
 // interpolation passes
+// ref_nyquist: equal sizes keep the reference's halved Nyquist bin (else exact)
 po_status launch_interp_rows(const float2 *src, float2 *dst, int64_t nrows, const FftPlan &pin, const FftPlan &pout,
-                             const float2 *twiddles, float scale, int sm_count, cudaStream_t st);
+                             const float2 *twiddles, float scale, int sm_count, int ref_nyquist, cudaStream_t st);
+// Rc/Rp: stored theta rows of child/parent patterns (mirror: Tc/2+1, Tp/2+1)
 po_status launch_interp_cols(const float2 *mid, float2 *parent, const int32_t *child_table, int64_t n_parent,
-                             int64_t n_child, int phi, const FftPlan &pin, const FftPlan &pout,
+                             int64_t n_child, int phi, int Rc, int Rp, const FftPlan &pin, const FftPlan &pout,
                              const float2 *twiddles, const float4 *trans, int n_slots, int G, int quirk_reach,
-                             float scale, int ncomp, cudaStream_t st);
-po_status launch_trans_table(const double *k_per_lambda, int n_lambda, int nth, int Tp, int phi, const double a[3],
+                             float scale, int ncomp, int mirror, int ref_nyquist, cudaStream_t st);
+// tensor-core theta pass (po_interp_mma.cu)
+size_t theta_matrix_words(int Rp, int Kp);
+void build_theta_matrix(int Tc, int Tp, int Rc, int Rp, int mirror, int Kp, std::vector<uint32_t> &out);
+po_status launch_interp_cols_mma(const float2 *mid, float2 *parent, const int32_t *child_table, int64_t n_parent,
+                                 int64_t n_child, int phi, int Rc, int Rp, int Kp, int mirror, const uint32_t *Afrag,
+                                 const float4 *trans, int n_slots, int G, cudaStream_t st);
+po_status launch_trans_table(const double *k_per_lambda, int n_lambda, int nth, int Rp, int phi, const double a[3],
                              float4 *out, cudaStream_t st);
 
 // intensity: fields [slot][comp][T][Phi] (root, possibly supersampled by

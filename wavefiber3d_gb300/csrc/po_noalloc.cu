@@ -92,9 +92,11 @@ extern "C" po_status po_interp_fft_noalloc(const float *in, int th_c, int ph_c, 
   PO_CUDA(cudaGetDevice(&dev));
   cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, dev);
   PO_TRY(launch_interp_rows((const float2 *)in, mid, (int64_t)batch * th_c, make_plan(ph_c, offset_of(ph_c)),
-                            make_plan(ph_p, offset_of(ph_p)), tw, 1.0f / (float)ph_c, sm, st));
+                            make_plan(ph_p, offset_of(ph_p)), tw, 1.0f / (float)ph_c, sm,
+                            theta_mode == PO_THETA_REFERENCE ? 1 : 0, st));
   int reach = (theta_mode == PO_THETA_REFERENCE && nyquist_quirk) ? 256 * (th_c / 256 + 1) : 0x7fffffff;
-  PO_TRY(launch_interp_cols(mid, (float2 *)out, nullptr, batch, batch, ph_p, make_plan(th_c, offset_of(th_c)),
-                            make_plan(th_p, offset_of(th_p)), tw, nullptr, 1, 1, reach, 1.0f / (float)th_c, 1, st));
+  PO_TRY(launch_interp_cols(mid, (float2 *)out, nullptr, batch, batch, ph_p, th_c, th_p,
+                            make_plan(th_c, offset_of(th_c)), make_plan(th_p, offset_of(th_p)), tw, nullptr, 1, 1,
+                            reach, 1.0f / (float)th_c, 1, 0, theta_mode == PO_THETA_REFERENCE ? 1 : 0, st));
   return PO_OK;
 }

@@ -104,6 +104,17 @@ std::vector<double> host_dirs_d(int T, int Phi, int nth) {
 
 int ceil_div(int a, int b) { return (a + b - 1) / b; }
 
+// smallest n' >= n with no prime factor above 7 (and even if requested)
+int smooth_at_least(int n, bool even) {
+  for (int m = std::max(n, 1);; ++m) {
+    if (even && (m % 2)) continue;
+    int k = m;
+    for (int p : {2, 3, 5, 7})
+      while (k % p == 0) k /= p;
+    if (k == 1) return m;
+  }
+}
+
 }  // namespace
 
 }  // namespace wavepo
@@ -118,8 +129,14 @@ struct po_ctx {
   int cover = 2;
   int mt = 1, mp = 1;
   int nth[PO_MAX_DEPTH + 1];  // samples over pi per level (root: output * mt)
-  int T[PO_MAX_DEPTH + 1];    // theta samples per level (cover * nth)
+  int T[PO_MAX_DEPTH + 1];    // theta transform length per level (cover * nth)
+  int R[PO_MAX_DEPTH + 1];    // theta rows stored per level (mirror: nth + 1, else T)
   int Phi[PO_MAX_DEPTH + 1];
+  int mirror = 0;             // double cover stored as rows 0..nth (see k_interp_cols)
+  bool tensor_theta = false;  // theta pass on the tensor cores (po_interp_mma.cu)
+  size_t amat_off[PO_MAX_DEPTH] = {};
+  int amat_kp[PO_MAX_DEPTH] = {};
+  DevBuf amat;
   std::map<int, int> tw_offset;
   DevBuf twiddles;
   DevBuf geom_in, geom_sorted, octree_ws, leaf_ctr, dirs, dirs_d, trans, levelA, levelB, mid, slots, kvals, out,
@@ -180,6 +197,7 @@ po_status po_config_init(po_config *cfg, int max_depth, int n_theta_out, int n_p
   cfg->theta_mode = PO_THETA_DOUBLE_COVER;
   cfg->nyquist_quirk = 1;
   cfg->distance = 1.0;
+  cfg->interp_method = PO_INTERP_TENSOR;
   return PO_OK;
 }
 
@@ -204,6 +222,8 @@ po_status po_create(po_ctx **out, const po_config *cfg) {
   if (cfg->theta_mode != PO_THETA_DOUBLE_COVER && cfg->theta_mode != PO_THETA_REFERENCE)
     return fail(PO_ERR_INVALID_ARGUMENT, "unknown theta mode");
   if (!(cfg->distance > 0)) return fail(PO_ERR_INVALID_ARGUMENT, "distance must be > 0");
+  if (cfg->interp_method != PO_INTERP_FFT && cfg->interp_method != PO_INTERP_TENSOR)
+    return fail(PO_ERR_INVALID_ARGUMENT, "unknown interpolation method");
   int dev = 0;
   PO_CUDA(cudaGetDevice(&dev));
   po_ctx *c = new po_ctx();
@@ -213,14 +233,29 @@ po_status po_create(po_ctx **out, const po_config *cfg) {
   c->depth = d;
   c->cover = cfg->theta_mode == PO_THETA_DOUBLE_COVER ? 2 : 1;
   c->mt = c->mp = 1;
+  c->mirror = (d >= 1 && c->cover == 2) ? 1 : 0;
+  int lvl_th[PO_MAX_DEPTH + 1], lvl_ph[PO_MAX_DEPTH + 1];
+  for (int l = 0; l <= d; ++l) {
+    lvl_th[l] = cfg->n_theta[l];
+    lvl_ph[l] = cfg->n_phi[l];
+    // double cover: inner levels are rounded up to FFT-friendly sizes (7-smooth,
+    // even in phi so that phi + pi is a grid line); more samples never lower
+    // the accuracy of the interpolation
+    if (c->mirror && l >= 1) {
+      lvl_th[l] = smooth_at_least(lvl_th[l], false);
+      lvl_ph[l] = smooth_at_least(lvl_ph[l], true);
+    }
+  }
   if (d >= 1) {
-    c->mt = ceil_div(cfg->n_theta[1], cfg->n_theta[0]);
-    c->mp = ceil_div(cfg->n_phi[1], cfg->n_phi[0]);
+    c->mt = ceil_div(lvl_th[1], lvl_th[0]);
+    c->mp = ceil_div(lvl_ph[1], lvl_ph[0]);
+    if (c->mirror && (c->mp * lvl_ph[0]) % 2) ++c->mp;
   }
   for (int l = 0; l <= d; ++l) {
-    c->nth[l] = l == 0 ? cfg->n_theta[0] * c->mt : cfg->n_theta[l];
-    c->Phi[l] = l == 0 ? cfg->n_phi[0] * c->mp : cfg->n_phi[l];
+    c->nth[l] = l == 0 ? lvl_th[0] * c->mt : lvl_th[l];
+    c->Phi[l] = l == 0 ? lvl_ph[0] * c->mp : lvl_ph[l];
     c->T[l] = (d == 0) ? cfg->n_theta[0] : c->cover * c->nth[l];
+    c->R[l] = c->mirror ? c->nth[l] + 1 : c->T[l];
   }
   // twiddle tables for every transform length of the level chain
   std::vector<int> lens;
@@ -249,6 +284,23 @@ po_status po_create(po_ctx **out, const po_config *cfg) {
   for (auto &e : c->kev) {
     if (cudaEventCreate(&e) != cudaSuccess) { delete c; return fail(PO_ERR_CUDA, "cudaEventCreate"); }
   }
+  // constant theta-interpolation matrices of every level (tensor-core path)
+  c->tensor_theta = cfg->interp_method == PO_INTERP_TENSOR && c->mirror;
+  if (c->tensor_theta) {
+    std::vector<uint32_t> all, one;
+    for (int l = 0; l < d; ++l) {
+      const int K = c->mirror ? 2 * c->R[l + 1] : c->R[l + 1];
+      c->amat_kp[l] = (K + 15) / 16 * 16;
+      build_theta_matrix(c->T[l + 1], c->T[l], c->R[l + 1], c->R[l], c->mirror, c->amat_kp[l], one);
+      c->amat_off[l] = all.size();
+      all.insert(all.end(), one.begin(), one.end());
+    }
+    s = c->amat.ensure(sizeof(uint32_t) * std::max<size_t>(all.size(), 1));
+    if (s == PO_OK && !all.empty() &&
+        cudaMemcpy(c->amat.p, all.data(), sizeof(uint32_t) * all.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+      s = fail(PO_ERR_CUDA, "upload of the interpolation matrices");
+    if (s != PO_OK) { po_destroy(c); return s; }
+  }
   if (cudaDeviceSynchronize() != cudaSuccess) { delete c; return fail(PO_ERR_CUDA, "twiddle set-up failed"); }
   *out = c;
   return PO_OK;
@@ -258,7 +310,7 @@ po_status po_destroy(po_ctx *c) {
   if (!c) return PO_OK;
   for (DevBuf *b : {&c->twiddles, &c->geom_in, &c->geom_sorted, &c->octree_ws, &c->leaf_ctr, &c->dirs, &c->dirs_d,
                     &c->trans, &c->levelA, &c->levelB, &c->mid, &c->slots, &c->kvals, &c->out, &c->cur, &c->partial,
-                    &c->tile_ctr})
+                    &c->tile_ctr, &c->amat})
     b->release();
   for (auto &e : c->ev)
     if (e) cudaEventDestroy(e);
@@ -416,9 +468,9 @@ static po_status solve_impl(po_ctx *c, const po_geometry *g, const po_illum *il,
       // buffer sizes
       size_t lvl_max = 0, mid_max = 0;
       for (int l = 0; l <= d; ++l)
-        lvl_max = std::max(lvl_max, (size_t)S * tree.level[l].count * 6 * (size_t)c->T[l] * c->Phi[l]);
+        lvl_max = std::max(lvl_max, (size_t)S * tree.level[l].count * 6 * (size_t)c->R[l] * c->Phi[l]);
       for (int l = 0; l < d; ++l)
-        mid_max = std::max(mid_max, (size_t)S * tree.level[l + 1].count * 6 * (size_t)c->T[l + 1] * c->Phi[l]);
+        mid_max = std::max(mid_max, (size_t)S * tree.level[l + 1].count * 6 * (size_t)c->R[l + 1] * c->Phi[l]);
       PO_TRY(c->levelA.ensure(sizeof(float2) * lvl_max));
       PO_TRY(c->levelB.ensure(sizeof(float2) * lvl_max));
       PO_TRY(c->mid.ensure(sizeof(float2) * std::max<size_t>(mid_max, 1)));
@@ -427,25 +479,25 @@ static po_status solve_impl(po_ctx *c, const po_geometry *g, const po_illum *il,
       std::vector<size_t> tr_off(d);
       for (int l = 0; l < d; ++l) {
         tr_off[l] = tr_total;
-        tr_total += (size_t)L * c->T[l] * c->Phi[l];
+        tr_total += (size_t)L * c->R[l] * c->Phi[l];
       }
       PO_TRY(c->trans.ensure(sizeof(float4) * std::max<size_t>(tr_total, 1)));
       for (int l = 0; l < d; ++l) {
         double a[3];
         for (int q = 0; q < 3; ++q) a[q] = ((double)cfg.box_max[q] - (double)cfg.box_min[q]) / std::ldexp(1.0, l + 2);
-        PO_TRY(launch_trans_table(k_lambda, L, c->nth[l], c->T[l], c->Phi[l], a, c->trans.as<float4>() + tr_off[l],
+        PO_TRY(launch_trans_table(k_lambda, L, c->nth[l], c->R[l], c->Phi[l], a, c->trans.as<float4>() + tr_off[l],
                                   st));
       }
       // leaf directions
-      std::vector<float4> df = host_dirs_f4(c->T[d], c->Phi[d], c->nth[d]);
+      std::vector<float4> df = host_dirs_f4(c->R[d], c->Phi[d], c->nth[d]);
       PO_TRY(c->dirs.ensure(sizeof(float4) * df.size()));
       PO_CUDA(cudaMemcpyAsync(c->dirs.p, df.data(), sizeof(float4) * df.size(), cudaMemcpyHostToDevice, st));
       PO_CUDA(cudaEventRecord(c->kev[0], st));
       PO_TRY(launch_leaf(gsc, tree.level[d].begin, c->leaf_ctr.as<double>(), nleaf, c->slots.as<SlotParams<float>>(),
-                         L, G, c->dirs.as<float4>(), c->T[d] * c->Phi[d], c->levelA.as<float2>(), st));
+                         L, G, c->dirs.as<float4>(), c->R[d] * c->Phi[d], c->levelA.as<float2>(), st));
       PO_CUDA(cudaEventRecord(c->kev[1], st));
       n_leaf_launches = nleaf > 0 ? (G + 3) / 4 : 0;
-      leaf_pd = (double)n * c->T[d] * c->Phi[d] * S;
+      leaf_pd = (double)n * c->R[d] * c->Phi[d] * S;
       PO_CUDA(cudaEventRecord(c->ev[3], st));
       float2 *cur_lvl = c->levelA.as<float2>(), *nxt = c->levelB.as<float2>();
       for (int l = d - 1; l >= 0; --l) {
@@ -454,26 +506,33 @@ static po_status solve_impl(po_ctx *c, const po_geometry *g, const po_illum *il,
         FftPlan prow_out = make_plan(c->Phi[l], c->tw_offset[c->Phi[l]]);
         FftPlan pcol_in = make_plan(c->T[l + 1], c->tw_offset[c->T[l + 1]]);
         FftPlan pcol_out = make_plan(c->T[l], c->tw_offset[c->T[l]]);
-        int64_t nrows = (int64_t)S * nc * 6 * c->T[l + 1];
+        int64_t nrows = (int64_t)S * nc * 6 * c->R[l + 1];
         PO_CUDA(cudaEventRecord(c->kev[2 + 4 * l], st));
+        const int refnq = c->cover == 1 ? 1 : 0;
         PO_TRY(launch_interp_rows(cur_lvl, c->mid.as<float2>(), nrows, prow_in, prow_out, c->twiddles.as<float2>(),
-                                  1.0f / (float)c->Phi[l + 1], c->sm_count, st));
+                                  1.0f / (float)c->Phi[l + 1], c->sm_count, refnq, st));
         PO_CUDA(cudaEventRecord(c->kev[3 + 4 * l], st));
         rows_b += 8.0 * nrows * (c->Phi[l + 1] + c->Phi[l]);
-        cols_b += 8.0 * S * 6 * ((double)nc * c->T[l + 1] * c->Phi[l] + (double)np * c->T[l] * c->Phi[l]);
+        cols_b += 8.0 * S * 6 * ((double)nc * c->R[l + 1] * c->Phi[l] + (double)np * c->R[l] * c->Phi[l]);
         if (nrows > 0) ++n_row_launches;
         if (np > 0) ++n_col_launches;
         PO_CUDA(cudaEventRecord(c->kev[4 + 4 * l], st));
         int reach = 0x7fffffff;
         if (c->cover == 1 && cfg.nyquist_quirk) reach = 256 * (c->T[l + 1] / 256 + 1);
-        PO_TRY(launch_interp_cols(c->mid.as<float2>(), nxt, tree.level[l].child, np, nc, c->Phi[l], pcol_in, pcol_out,
-                                  c->twiddles.as<float2>(), c->trans.as<float4>() + tr_off[l], S, G, reach,
-                                  1.0f / (float)c->T[l + 1], 6, st));
+        if (c->tensor_theta)
+          PO_TRY(launch_interp_cols_mma(c->mid.as<float2>(), nxt, tree.level[l].child, np, nc, c->Phi[l], c->R[l + 1],
+                                        c->R[l], c->amat_kp[l], c->mirror, c->amat.as<uint32_t>() + c->amat_off[l],
+                                        c->trans.as<float4>() + tr_off[l], S, G, st));
+        else
+          PO_TRY(launch_interp_cols(c->mid.as<float2>(), nxt, tree.level[l].child, np, nc, c->Phi[l], c->R[l + 1],
+                                    c->R[l], pcol_in, pcol_out, c->twiddles.as<float2>(),
+                                    c->trans.as<float4>() + tr_off[l], S, G, reach, 1.0f / (float)c->T[l + 1], 6,
+                                    c->mirror, refnq, st));
         PO_CUDA(cudaEventRecord(c->kev[5 + 4 * l], st));
         std::swap(cur_lvl, nxt);
       }
       PO_CUDA(cudaEventRecord(c->ev[4], st));
-      PO_TRY(launch_intensity_f32(cur_lvl, S, c->T[0], c->Phi[0], nth_out, nph_out, c->mt, c->mp, out_dev, st));
+      PO_TRY(launch_intensity_f32(cur_lvl, S, c->R[0], c->Phi[0], nth_out, nph_out, c->mt, c->mp, out_dev, st));
     }
   }
   if (!out_on_device)
@@ -668,12 +727,13 @@ po_status po_interp_fft(const float *in, int th_c, int ph_c, float *out, int th_
   cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, 0);
   if (s == PO_OK)
     s = launch_interp_rows((const float2 *)in, (float2 *)mid, (int64_t)batch * th_c, make_plan(ph_c, off[ph_c]),
-                           make_plan(ph_p, off[ph_p]), (const float2 *)tw, 1.0f / (float)ph_c, sm, st);
+                           make_plan(ph_p, off[ph_p]), (const float2 *)tw, 1.0f / (float)ph_c, sm,
+                           theta_mode == PO_THETA_REFERENCE ? 1 : 0, st);
   int reach = (theta_mode == PO_THETA_REFERENCE && nyquist_quirk) ? 256 * (th_c / 256 + 1) : 0x7fffffff;
   if (s == PO_OK)
-    s = launch_interp_cols((const float2 *)mid, (float2 *)out, nullptr, batch, batch, ph_p, make_plan(th_c, off[th_c]),
-                           make_plan(th_p, off[th_p]), (const float2 *)tw, nullptr, 1, 1, reach, 1.0f / (float)th_c, 1,
-                           st);
+    s = launch_interp_cols((const float2 *)mid, (float2 *)out, nullptr, batch, batch, ph_p, th_c, th_p,
+                           make_plan(th_c, off[th_c]), make_plan(th_p, off[th_p]), (const float2 *)tw, nullptr, 1, 1,
+                           reach, 1.0f / (float)th_c, 1, 0, theta_mode == PO_THETA_REFERENCE ? 1 : 0, st);
   cudaFreeAsync(mid, st);
   cudaFreeAsync(tw, st);
   if (s == PO_OK) PO_CUDA(cudaStreamSynchronize(st));
