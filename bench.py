@@ -48,12 +48,17 @@ SIGMA = 1e-2
 WORKLOAD = "ellipsoid 8x5x5um, 400k points, depth 5, 25 wavelengths x 1 incidence x TM, 180x360 grid"
 
 
-def make_workload():
+PRECISIONS = {"fp32": 0, "split_bf16": 2}
+INTERP = {"fft": 0, "tensor": 1}
+
+
+def make_workload(precision: str = "fp32", interp: str = "tensor"):
     from wavefiber3d_gb300 import api, geometry
     cloud = geometry.ellipsoid(RADII, N_POINTS)
     bmin = [-1.1 * r for r in RADII]
     bmax = [1.1 * r for r in RADII]
-    cfg = api.Config.reference_rule(DEPTH, N_THETA, N_PHI, bmin, bmax, 16e-6, 16e-6, 1.3)
+    cfg = api.Config.reference_rule(DEPTH, N_THETA, N_PHI, bmin, bmax, 16e-6, 16e-6, 1.3,
+                                    precision=PRECISIONS[precision], interp_method=INTERP[interp])
     illum = api.Illumination(LAMBDAS, [0.0], [0.0], api.PO_POL_TM, ETA, SIGMA)
     return cloud, cfg, illum
 
@@ -165,7 +170,7 @@ def run_engine(args, world, rank, local):
     bf16_peak = peaks.get("bf16_tflops", 1900.0)
     peak_src = "measured" if peaks else "fallback"
 
-    cloud, cfg, illum = make_workload()
+    cloud, cfg, illum = make_workload(args.precision, args.interp)
     pd_step = point_dirs_per_step(illum)
     st = torch.cuda.current_stream()
     g_dev = torch.from_numpy(cloud.soa()).to(dev)
@@ -259,11 +264,13 @@ def run_engine(args, world, rank, local):
             "higher_is_better": True,
             "scaling": "weak",
             "vs_baseline": None,
-            "dtype": "f32 (f64 phase arguments)",
+            "dtype": "f32 (f64 phase arguments)" if args.precision == "fp32" else
+                     "split bf16 hi+lo leaf products, f32 accumulation (f64 phase arguments)",
             "data": "synthetic (seeded ellipsoid, analytic normals)",
             "config": {"workload": WORKLOAD, "points": N_POINTS, "directions": N_THETA * N_PHI,
                        "wavelengths": len(LAMBDAS), "incidences": 1, "polarisations": 1, "depth": DEPTH,
                        "level_grids": [list(cfg.n_theta), list(cfg.n_phi)], "theta_mode": "double cover",
+                       "precision": args.precision, "theta_interpolation": args.interp,
                        "l2": "flushed between steps (256 MiB write, outside the timed events)",
                        "parallelism": f"replicas x{world}"},
             "patterns_per_s": illum.n_patterns * world / (ms_step_max * 1e-3),
@@ -325,6 +332,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["engine", "reference"], default="engine")
     ap.add_argument("--cpu-dirs", type=int, default=2048, help="directions of the FP64 CPU sample")
+    ap.add_argument("--precision", choices=sorted(PRECISIONS), default="fp32")
+    ap.add_argument("--interp", choices=sorted(INTERP), default="tensor")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "engine":
         args.warmup = 3

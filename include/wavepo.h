@@ -37,8 +37,10 @@ typedef enum po_status {
 typedef enum po_precision {
   PO_PREC_FP32 = 0,       /* FP32 sums, FP64 phase arguments where they are large */
   PO_PREC_FP64 = 1,       /* plain FP64 everywhere (depth 0 only) */
-  PO_PREC_SPLIT_BF16 = 2, /* tensor-core hi+lo BF16 products, FP32 accumulation */
-  PO_PREC_SPLIT_FP16 = 3  /* tensor-core hi+lo FP16 products, FP32 accumulation */
+  PO_PREC_SPLIT_BF16 = 2, /* leaf sums as tensor-core hi+lo BF16 products, FP32 accumulation
+                             (depth 0 keeps the FP32 direct sum) */
+  PO_PREC_SPLIT_FP16 = 3  /* reserved: rejected with PO_ERR_UNSUPPORTED (the currents need
+                             per-tile scaling to fit the FP16 range) */
 } po_precision;
 
 /* How the elevation axis is interpolated between tree levels. */

@@ -260,3 +260,31 @@ def test_invalid_arguments_raise():
     cfg = api.Config.reference_rule(1, 16, 32, box[:3], box[3:], 2e-6, 2e-6, 1.3)
     with api.Solver(cfg) as s, pytest.raises(api.WavePOError):
         s.solve(geometry.fibonacci_sphere(1e-6, 100), api.Illumination([-5e-7], [0.0], [0.0]))
+
+
+# ------------------------------------------------ split-precision tensor path
+@pytest.mark.parametrize("name", ["ref_solve_sphere_d3", "ref_solve_ellipsoid_d2"])
+def test_split_bf16_leaf_vs_fp64_direct(cases, name):
+    c = cases[name]
+    cloud, il = load_case_geometry(c), case_illum(c)
+    cfg = api.Config(c["depth"], c["n_theta"], c["n_phi"], c["box"][:3], c["box"][3:],
+                     precision=api.PO_PREC_SPLIT_BF16)
+    out, _ = _solve(cloud, cfg, illum_of(c))
+    ctr = [(c["box"][i] + c["box"][i + 3]) / 2 for i in range(3)]
+    o = oracle.solve_direct(cloud, il, c["n_theta"][0], c["n_phi"][0], center=ctr)
+    assert rel(out.reshape(o.shape), o) < TOL_TREE
+
+
+def test_split_bf16_many_slots_match_fp32():
+    """Seven incidences x two polarisations per wavelength (14 slots: the
+    tensor-core leaf kernel's slot groups) against the FP32 CUDA-core path."""
+    cloud = geometry.ellipsoid((1.5e-6, 1.0e-6, 0.8e-6), 3000)
+    box = [-1.65e-6, -1.1e-6, -0.88e-6, 1.65e-6, 1.1e-6, 0.88e-6]
+    th = list(np.linspace(-1.2, 1.2, 7))
+    ph = list(np.linspace(0.1, 5.9, 7))
+    il = api.Illumination([450e-9, 620e-9], th, ph, api.PO_POL_TM | api.PO_POL_TE, 1.55 + 0.1j, 2e-6)
+    outs = []
+    for prec in (api.PO_PREC_FP32, api.PO_PREC_SPLIT_BF16):
+        cfg = api.Config.reference_rule(2, 32, 64, box[:3], box[3:], 1.6e-6, 3.0e-6, 1.2, precision=prec)
+        outs.append(_solve(cloud, cfg, il)[0])
+    assert rel(outs[1], outs[0]) < 1e-4

@@ -26,11 +26,11 @@ import numpy as np
 
 from . import _lib
 from ._lib import (PO_INTERP_FFT, PO_INTERP_TENSOR, PO_POL_TE, PO_POL_TM, PO_PREC_FP32, PO_PREC_FP64,
-                   PO_THETA_DOUBLE_COVER, PO_THETA_REFERENCE, WavePOError, check)
+                   PO_PREC_SPLIT_BF16, PO_THETA_DOUBLE_COVER, PO_THETA_REFERENCE, WavePOError, check)
 
 __all__ = ["Config", "Illumination", "Solver", "compute_local_tangent_plane", "build_octree",
            "current_times_green_center", "copyandinterp", "compute_intensity", "wavelength_from_index",
-           "incidence_from_index", "WavePOError", "PO_POL_TM", "PO_POL_TE", "PO_PREC_FP32", "PO_PREC_FP64",
+           "incidence_from_index", "WavePOError", "PO_POL_TM", "PO_POL_TE", "PO_PREC_FP32", "PO_PREC_FP64", "PO_PREC_SPLIT_BF16",
            "PO_THETA_DOUBLE_COVER", "PO_THETA_REFERENCE", "PO_INTERP_FFT", "PO_INTERP_TENSOR"]
 
 

@@ -248,4 +248,114 @@ po_status launch_interp_cols_mma(const float2 *mid, float2 *parent, const int32_
   return PO_OK;
 }
 
+// ---------------------------------------------------------------- row pass
+// The phi half of interpFFT (interpolation.h:17-45) is out[r][j'] =
+// sum_j K_{Phi_c}(j'/Phi_p - j/Phi_c) in[r][j] for every stored row r.  As a
+// GEMM the A operand stacks 8 complex rows as 16 real rows (real parts in
+// rows 0-7, imaginary parts in rows 8-15), so a lane's A fragment is two
+// contiguous 16-byte loads of one input row and its D fragment is two
+// complex outputs of one output row.  B = the level's phi matrix, transposed,
+// in fragment order  Bm[ntile][kstep][lane] = {hi0, hi1, lo0, lo1}.
+size_t phi_matrix_words(int Pp, int Kp) { return (size_t)((Pp + 7) / 8) * (Kp / 16) * 32 * 4; }
+
+void build_phi_matrix(int Pc, int Pp, int Kp, std::vector<uint32_t> &out) {
+  const int NTt = (Pp + 7) / 8, KS = Kp / 16;
+  out.assign(phi_matrix_words(Pp, Kp), 0u);
+  for (int nt = 0; nt < NTt; ++nt)
+    for (int ks = 0; ks < KS; ++ks)
+      for (int lane = 0; lane < 32; ++lane) {
+        const int n = nt * 8 + (lane >> 2), kb = ks * 16 + 2 * (lane & 3);
+        const int ks4[4] = {kb, kb + 1, kb + 8, kb + 9};
+        uint16_t h[4], l[4];
+        for (int u = 0; u < 4; ++u) {
+          double v = (n < Pp && ks4[u] < Pc) ? trig_kernel(Pc, (double)n / Pp - (double)ks4[u] / Pc) : 0.0;
+          h[u] = bf16_rne((float)v);
+          l[u] = bf16_rne((float)(v - (double)bf16_to_f(h[u])));
+        }
+        uint32_t *dst = &out[(((size_t)nt * KS + ks) * 32 + lane) * 4];
+        dst[0] = (uint32_t)h[0] | ((uint32_t)h[1] << 16);
+        dst[1] = (uint32_t)h[2] | ((uint32_t)h[3] << 16);
+        dst[2] = (uint32_t)l[0] | ((uint32_t)l[1] << 16);
+        dst[3] = (uint32_t)l[2] | ((uint32_t)l[3] << 16);
+      }
+}
+
+// One warp per block of 8 rows; n-tiles in groups of kRowNG (accumulators in
+// registers); the B fragments come from shared memory when they fit.
+constexpr int kRowNG = 8;
+__global__ void __launch_bounds__(128) k_interp_rows_mma(const float2 *__restrict__ src, float2 *__restrict__ dst,
+                                                         int64_t nrows, int Pc, int Pp, int Kp,
+                                                         const uint4 *__restrict__ Bm, int b_in_smem) {
+  extern __shared__ uint4 bsm[];
+  const int KS = Kp / 16, NTt = (Pp + 7) / 8;
+  if (b_in_smem) {
+    for (int e = threadIdx.x; e < NTt * KS * 32; e += blockDim.x) bsm[e] = Bm[e];
+    __syncthreads();
+  }
+  const uint4 *B = b_in_smem ? bsm : Bm;
+  const int lane = threadIdx.x & 31, g = lane >> 2, tq = lane & 3;
+  const int64_t nblk = (nrows + 7) / 8;
+  for (int64_t blk = (int64_t)blockIdx.x * 4 + (threadIdx.x >> 5); blk < nblk; blk += (int64_t)gridDim.x * 4) {
+    const int64_t r = blk * 8 + g;
+    const bool rok = r < nrows;
+    const float2 *in = src + (rok ? r : 0) * (int64_t)Pc;
+    float2 *out = dst + (rok ? r : 0) * (int64_t)Pp;
+    for (int ng = 0; ng < NTt; ng += kRowNG) {
+      float acc[kRowNG][4];
+#pragma unroll
+      for (int q = 0; q < kRowNG; ++q) acc[q][0] = acc[q][1] = acc[q][2] = acc[q][3] = 0.f;
+      for (int ks = 0; ks < KS; ++ks) {
+        const int k0 = ks * 16 + 2 * tq;
+        float2 v[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int k = k0 + (u & 1) + (u >> 1) * 8;
+          v[u] = (rok && k < Pc) ? in[k] : make_float2(0.f, 0.f);
+        }
+        uint32_t ahi[4], alo[4];
+        split_bf16x2(v[0].x, v[1].x, ahi[0], alo[0]);  // row g (real parts), k0, k0+1
+        split_bf16x2(v[0].y, v[1].y, ahi[1], alo[1]);  // row g+8 (imaginary parts)
+        split_bf16x2(v[2].x, v[3].x, ahi[2], alo[2]);  // row g, k0+8, k0+9
+        split_bf16x2(v[2].y, v[3].y, ahi[3], alo[3]);
+#pragma unroll
+        for (int q = 0; q < kRowNG; ++q) {
+          const int nt = ng + q;
+          if (nt >= NTt) break;
+          const uint4 bv = B[((size_t)nt * KS + ks) * 32 + lane];
+          const uint32_t bhi[2] = {bv.x, bv.y}, blo[2] = {bv.z, bv.w};
+          mma_bf16(acc[q], ahi, bhi);
+          mma_bf16(acc[q], ahi, blo);
+          mma_bf16(acc[q], alo, bhi);
+        }
+      }
+      if (rok) {
+#pragma unroll
+        for (int q = 0; q < kRowNG; ++q) {
+          const int j = (ng + q) * 8 + 2 * tq;
+          if (j < Pp) out[j] = make_float2(acc[q][0], acc[q][2]);
+          if (j + 1 < Pp) out[j + 1] = make_float2(acc[q][1], acc[q][3]);
+        }
+      }
+    }
+  }
+}
+
+po_status launch_interp_rows_mma(const float2 *src, float2 *dst, int64_t nrows, int Pc, int Pp, int Kp,
+                                 const uint32_t *Bm, int sm_count, cudaStream_t st) {
+  if (nrows <= 0) return PO_OK;
+  if (Kp % 16 || Kp < Pc) return fail(PO_ERR_INTERNAL, "phi matrix K padding");
+  const size_t bbytes = sizeof(uint32_t) * phi_matrix_words(Pp, Kp);
+  const bool b_smem = bbytes <= 48 * 1024;
+  const size_t smem = b_smem ? bbytes : 0;
+  if (smem) PO_CUDA(cudaFuncSetAttribute(k_interp_rows_mma, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int64_t blocks = ((nrows + 7) / 8 + 3) / 4;
+  const int64_t cap = (int64_t)sm_count * 16;
+  if (blocks > cap) blocks = cap;
+  k_interp_rows_mma<<<(unsigned)blocks, 128, smem, st>>>(src, dst, nrows, Pc, Pp, Kp, (const uint4 *)Bm,
+                                                         b_smem ? 1 : 0);
+  count_launch();
+  PO_CUDA(cudaGetLastError());
+  return PO_OK;
+}
+
 }  // namespace wavepo

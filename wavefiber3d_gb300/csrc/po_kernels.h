@@ -37,6 +37,11 @@ po_status launch_leaf(const float *const g[7], const int32_t *leaf_begin, const 
                       int64_t n_leaves, const SlotParams<float> *slots_dev, int n_lambda, int G,
                       const float4 *dirs, int ndir, float2 *out, cudaStream_t st);
 
+// split hi+lo BF16 tensor-core leaf sums (po_leaf_mma.cu); same layout as launch_leaf
+po_status launch_leaf_mma(const float *const g[7], const int32_t *leaf_begin, const double *leaf_center,
+                          int64_t n_leaves, const SlotParams<float> *slots_dev, int n_lambda, int G,
+                          const float4 *dirs, int ndir, float2 *out, cudaStream_t st);
+
 int direct_splits(int64_t n, int ndir, int n_lambda, int sm_count);
 // FP32 depth-0 sum about c0: out[slot][comp][dir]; cur[slot][n][6]
 po_status launch_direct_f32(int64_t n, const float *x, const float *y, const float *z, const float2 *cur,
@@ -67,6 +72,11 @@ void build_theta_matrix(int Tc, int Tp, int Rc, int Rp, int mirror, int Kp, std:
 po_status launch_interp_cols_mma(const float2 *mid, float2 *parent, const int32_t *child_table, int64_t n_parent,
                                  int64_t n_child, int phi, int Rc, int Rp, int Kp, int mirror, const uint32_t *Afrag,
                                  const float4 *trans, int n_slots, int G, cudaStream_t st);
+// tensor-core phi pass (po_interp_mma.cu)
+size_t phi_matrix_words(int Pp, int Kp);
+void build_phi_matrix(int Pc, int Pp, int Kp, std::vector<uint32_t> &out);
+po_status launch_interp_rows_mma(const float2 *src, float2 *dst, int64_t nrows, int Pc, int Pp, int Kp,
+                                 const uint32_t *Bm, int sm_count, cudaStream_t st);
 po_status launch_trans_table(const double *k_per_lambda, int n_lambda, int nth, int Rp, int phi, const double a[3],
                              float4 *out, cudaStream_t st);
 

@@ -136,7 +136,9 @@ struct po_ctx {
   bool tensor_theta = false;  // theta pass on the tensor cores (po_interp_mma.cu)
   size_t amat_off[PO_MAX_DEPTH] = {};
   int amat_kp[PO_MAX_DEPTH] = {};
-  DevBuf amat;
+  size_t bmat_off[PO_MAX_DEPTH] = {};
+  int bmat_kp[PO_MAX_DEPTH] = {};
+  DevBuf amat, bmat;
   std::map<int, int> tw_offset;
   DevBuf twiddles;
   DevBuf geom_in, geom_sorted, octree_ws, leaf_ctr, dirs, dirs_d, trans, levelA, levelB, mid, slots, kvals, out,
@@ -217,8 +219,9 @@ po_status po_create(po_ctx **out, const po_config *cfg) {
   if (cfg->precision < 0 || cfg->precision > 3) return fail(PO_ERR_INVALID_ARGUMENT, "unknown precision");
   if (cfg->precision == PO_PREC_FP64 && d != 0)
     return fail(PO_ERR_UNSUPPORTED, "the plain FP64 path is the depth-0 direct sum");
-  if (cfg->precision == PO_PREC_SPLIT_BF16 || cfg->precision == PO_PREC_SPLIT_FP16)
-    return fail(PO_ERR_UNSUPPORTED, "split tensor-core precision is not available in this build");
+  if (cfg->precision == PO_PREC_SPLIT_FP16)
+    return fail(PO_ERR_UNSUPPORTED,
+                "split FP16 needs per-tile scaling of the currents (FP16 range); use PO_PREC_SPLIT_BF16");
   if (cfg->theta_mode != PO_THETA_DOUBLE_COVER && cfg->theta_mode != PO_THETA_REFERENCE)
     return fail(PO_ERR_INVALID_ARGUMENT, "unknown theta mode");
   if (!(cfg->distance > 0)) return fail(PO_ERR_INVALID_ARGUMENT, "distance must be > 0");
@@ -300,6 +303,19 @@ po_status po_create(po_ctx **out, const po_config *cfg) {
         cudaMemcpy(c->amat.p, all.data(), sizeof(uint32_t) * all.size(), cudaMemcpyHostToDevice) != cudaSuccess)
       s = fail(PO_ERR_CUDA, "upload of the interpolation matrices");
     if (s != PO_OK) { po_destroy(c); return s; }
+    // phi matrices (row pass)
+    all.clear();
+    for (int l = 0; l < d; ++l) {
+      c->bmat_kp[l] = (c->Phi[l + 1] + 15) / 16 * 16;
+      build_phi_matrix(c->Phi[l + 1], c->Phi[l], c->bmat_kp[l], one);
+      c->bmat_off[l] = all.size();
+      all.insert(all.end(), one.begin(), one.end());
+    }
+    s = c->bmat.ensure(sizeof(uint32_t) * std::max<size_t>(all.size(), 1));
+    if (s == PO_OK && !all.empty() &&
+        cudaMemcpy(c->bmat.p, all.data(), sizeof(uint32_t) * all.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+      s = fail(PO_ERR_CUDA, "upload of the interpolation matrices");
+    if (s != PO_OK) { po_destroy(c); return s; }
   }
   if (cudaDeviceSynchronize() != cudaSuccess) { delete c; return fail(PO_ERR_CUDA, "twiddle set-up failed"); }
   *out = c;
@@ -310,7 +326,7 @@ po_status po_destroy(po_ctx *c) {
   if (!c) return PO_OK;
   for (DevBuf *b : {&c->twiddles, &c->geom_in, &c->geom_sorted, &c->octree_ws, &c->leaf_ctr, &c->dirs, &c->dirs_d,
                     &c->trans, &c->levelA, &c->levelB, &c->mid, &c->slots, &c->kvals, &c->out, &c->cur, &c->partial,
-                    &c->tile_ctr, &c->amat})
+                    &c->tile_ctr, &c->amat, &c->bmat})
     b->release();
   for (auto &e : c->ev)
     if (e) cudaEventDestroy(e);
@@ -493,8 +509,14 @@ static po_status solve_impl(po_ctx *c, const po_geometry *g, const po_illum *il,
       PO_TRY(c->dirs.ensure(sizeof(float4) * df.size()));
       PO_CUDA(cudaMemcpyAsync(c->dirs.p, df.data(), sizeof(float4) * df.size(), cudaMemcpyHostToDevice, st));
       PO_CUDA(cudaEventRecord(c->kev[0], st));
-      PO_TRY(launch_leaf(gsc, tree.level[d].begin, c->leaf_ctr.as<double>(), nleaf, c->slots.as<SlotParams<float>>(),
-                         L, G, c->dirs.as<float4>(), c->R[d] * c->Phi[d], c->levelA.as<float2>(), st));
+      if (cfg.precision == PO_PREC_SPLIT_BF16)
+        PO_TRY(launch_leaf_mma(gsc, tree.level[d].begin, c->leaf_ctr.as<double>(), nleaf,
+                               c->slots.as<SlotParams<float>>(), L, G, c->dirs.as<float4>(), c->R[d] * c->Phi[d],
+                               c->levelA.as<float2>(), st));
+      else
+        PO_TRY(launch_leaf(gsc, tree.level[d].begin, c->leaf_ctr.as<double>(), nleaf,
+                           c->slots.as<SlotParams<float>>(), L, G, c->dirs.as<float4>(), c->R[d] * c->Phi[d],
+                           c->levelA.as<float2>(), st));
       PO_CUDA(cudaEventRecord(c->kev[1], st));
       n_leaf_launches = nleaf > 0 ? (G + 3) / 4 : 0;
       leaf_pd = (double)n * c->R[d] * c->Phi[d] * S;
@@ -509,8 +531,12 @@ static po_status solve_impl(po_ctx *c, const po_geometry *g, const po_illum *il,
         int64_t nrows = (int64_t)S * nc * 6 * c->R[l + 1];
         PO_CUDA(cudaEventRecord(c->kev[2 + 4 * l], st));
         const int refnq = c->cover == 1 ? 1 : 0;
-        PO_TRY(launch_interp_rows(cur_lvl, c->mid.as<float2>(), nrows, prow_in, prow_out, c->twiddles.as<float2>(),
-                                  1.0f / (float)c->Phi[l + 1], c->sm_count, refnq, st));
+        if (c->tensor_theta)
+          PO_TRY(launch_interp_rows_mma(cur_lvl, c->mid.as<float2>(), nrows, c->Phi[l + 1], c->Phi[l], c->bmat_kp[l],
+                                        c->bmat.as<uint32_t>() + c->bmat_off[l], c->sm_count, st));
+        else
+          PO_TRY(launch_interp_rows(cur_lvl, c->mid.as<float2>(), nrows, prow_in, prow_out, c->twiddles.as<float2>(),
+                                    1.0f / (float)c->Phi[l + 1], c->sm_count, refnq, st));
         PO_CUDA(cudaEventRecord(c->kev[3 + 4 * l], st));
         rows_b += 8.0 * nrows * (c->Phi[l + 1] + c->Phi[l]);
         cols_b += 8.0 * S * 6 * ((double)nc * c->R[l + 1] * c->Phi[l] + (double)np * c->R[l] * c->Phi[l]);
