@@ -293,6 +293,128 @@ def run_engine(args, world, rank, local):
     return result
 
 
+# ---------------------------------------------------------------- fiber workload
+FIBER_RADII = (25e-6, 20e-6)
+FIBER_LENGTH = 60e-6
+FIBER_DEPTH = 7
+FIBER_SIGMA = 10e-6          # Gaussian beam width of the reference's fiber presets 0/1 (treePO.cu:47)
+FIBER_INC = 64               # theta sweep at phi_i = 0: theta_i = -pi/2 + 1e-10 + pi/180 * idx, idx = 58..121
+FIBER_WORKLOAD = ("fiber segment 25x20um x 60um, cuticle 5um/0.4um/3deg + Gaussian noise 0.05um/1um, "
+                  "0.05um spacing (3.40M points), depth 7, 64 incidences x TM per wavelength, 180x360 grid")
+
+
+def fiber_incidences():
+    idx = np.arange(58, 58 + FIBER_INC)
+    return list(-math.pi / 2 + 1e-10 + math.pi / 180 * idx), [0.0] * FIBER_INC
+
+
+def run_fiber(args, world, rank, local):
+    """Split-precision hierarchical solve of the fiber segment against the plain
+    FP64 direct sum on the same GPU (timed on every 64th point and scaled by
+    the point count, which the direct sum is linear in)."""
+    import torch
+
+    from wavefiber3d_gb300 import api, geometry
+    import __graft_entry__
+    __graft_entry__.build()
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    st = torch.cuda.current_stream()
+    hf = geometry.fiber_height_field(FIBER_RADII, FIBER_LENGTH, seed=11)
+    t0 = time.perf_counter()
+    g_dev = api.height_field_points(hf)  # the GPU height-field sampler (util/geometry.h:76-179)
+    torch.cuda.synchronize()
+    t_geom = time.perf_counter() - t0
+    n = g_dev.shape[1]
+    geom_dev = tuple(g_dev[k] for k in range(7))
+    bmin = [-1.1 * FIBER_RADII[0], -1.1 * FIBER_RADII[1], -0.55 * FIBER_LENGTH]  # treePO.cu:96-98
+    bmax = [-v for v in bmin]
+    lams = LAMBDAS[: args.fiber_lambdas]
+    th, ph = fiber_incidences()
+    illum = api.Illumination(lams, th, ph, api.PO_POL_TM, ETA, FIBER_SIGMA)
+    cfg = api.Config.reference_rule(FIBER_DEPTH, N_THETA, N_PHI, bmin, bmax, FIBER_LENGTH,
+                                    2 * max(FIBER_RADII), 1.2, precision=PRECISIONS[args.precision],
+                                    interp_method=INTERP[args.interp])  # treePO.cu:353-359
+    solver = api.Solver(cfg)
+    out = torch.empty(solver.out_shape(illum), dtype=torch.float32, device=dev)
+    for _ in range(max(1, min(args.warmup, 1))):
+        solver.solve(geom_dev, illum, out=out)
+    torch.cuda.synchronize()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    reps = []
+    clocks = ClockSampler(local)
+    for i in range(args.steps):
+        evs[i][0].record(st)
+        solver.solve(geom_dev, illum, out=out)
+        evs[i][1].record(st)
+        reps.append(dict(solver.last_report))
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms_hier = statistics.mean(a.elapsed_time(b) for a, b in evs)
+    solver.close()
+
+    # plain FP64 direct sum, same GPU, same wavelengths and incidences, every 64th point
+    stride = 64
+    sub = g_dev[:, ::stride].contiguous()
+    n_sub = sub.shape[1]
+    cfg64 = api.Config(0, [N_THETA], [N_PHI], bmin, bmax, precision=api.PO_PREC_FP64)
+    il64 = api.Illumination(lams[:1], th, ph, api.PO_POL_TM, ETA, FIBER_SIGMA)
+    with api.Solver(cfg64) as s64:
+        o64 = torch.empty(s64.out_shape(il64), dtype=torch.float32, device=dev)
+        s64.solve(tuple(sub[k] for k in range(7)), il64, out=o64)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        s64.solve(tuple(sub[k] for k in range(7)), il64, out=o64)
+        e1.record(st)
+        torch.cuda.synchronize()
+        ms64_sub = e0.elapsed_time(e1)
+    ms64_full = ms64_sub * (n / n_sub) * len(lams)  # linear in points and wavelengths
+
+    # accuracy: FP64 oracle on the host for two incidences, sampled directions
+    import oracle
+    cloud = geometry.PointCloud.from_soa(g_dev.cpu().numpy())
+    dirs = sample_directions(args.fiber_dirs)
+    errs = []
+    for ii in (0, FIBER_INC - 1):
+        il = oracle.make_illum(lams[0], th[ii], ph[ii], "M", ETA, FIBER_SIGMA)
+        cur = oracle.currents(cloud, il)
+        ctr = [0.5 * (a + b) for a, b in zip(np.float32(bmin), np.float32(bmax))]
+        f = oracle.far_field_sampled(cloud, cur, 2 * math.pi / lams[0], ctr, N_THETA, N_PHI, dirs)
+        ref = oracle.intensity_sampled(f, N_THETA, N_PHI, dirs)
+        got = out[0, ii, 0].reshape(-1).cpu().numpy()[dirs].astype(np.float64)
+        errs.append(float(np.linalg.norm(got - ref) / np.linalg.norm(ref)))
+    pd = float(n) * N_THETA * N_PHI * illum.n_patterns
+    r = reps[-1]
+    return {
+        "metric": "Gpoint-dirs/s (equivalent depth-0 terms) of the split-precision tree solve vs the plain FP64 "
+                  "direct sum on the same GPU",
+        "value": pd / (ms_hier * 1e-3) / 1e9, "unit": "Gpoint-dirs/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": 1, "ms_per_step": ms_hier, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "split bf16 hi+lo products, f32 accumulation (f64 phase arguments)" if args.precision == "split_bf16"
+                 else "f32 (f64 phase arguments)",
+        "data": "synthetic (seeded fiber height field, sampled on the GPU)",
+        "config": {"workload": FIBER_WORKLOAD, "points": n, "numel": hf.numel, "numelvert": hf.numelvert,
+                   "wavelengths": len(lams), "incidences": FIBER_INC, "depth": FIBER_DEPTH,
+                   "level_grids": [list(cfg.n_theta), list(cfg.n_phi)], "precision": args.precision,
+                   "theta_interpolation": args.interp, "beam_sigma_m": FIBER_SIGMA,
+                   "l2": "inputs and patterns far larger than L2"},
+        "patterns_per_s": illum.n_patterns / (ms_hier * 1e-3),
+        "plain_fp64_direct": {"ms_per_step_scaled": ms64_full, "ms_measured": ms64_sub, "points_measured": n_sub,
+                              "note": f"FP64 depth-0 sum on every {stride}th point, scaled by {n / n_sub:.2f} "
+                                      f"(points) x {len(lams)} (wavelengths)",
+                              "value": pd / (ms64_full * 1e-3) / 1e9},
+        "speedup_vs_plain_fp64": ms64_full / ms_hier,
+        "rel_l2_vs_fp64": max(errs), "rel_l2_per_incidence": errs,
+        "accuracy_sample": f"{dirs.size} seeded directions, lambda={lams[0] * 1e9:.0f} nm, incidences 0 and "
+                           f"{FIBER_INC - 1}, FP64 oracle on the host",
+        "geometry_build_ms": t_geom * 1e3,
+        "gpu_launches": int(sum(x["kernel_launches"] for x in reps)),
+        "clocks": clk,
+        "report": r,
+    }
+
+
 def run_reference(args, world, rank):
     """CPU implementation of the path (FP64 direct sum restatement), all host cores."""
     if rank != 0:
@@ -334,11 +456,21 @@ def main():
     ap.add_argument("--cpu-dirs", type=int, default=2048, help="directions of the FP64 CPU sample")
     ap.add_argument("--precision", choices=sorted(PRECISIONS), default="fp32")
     ap.add_argument("--interp", choices=sorted(INTERP), default="tensor")
+    ap.add_argument("--workload", choices=["ellipsoid", "fiber"], default="ellipsoid",
+                    help="ellipsoid: the headline 400k-point depth-5 workload; fiber: the 3.4M-point fiber "
+                         "segment (split precision vs plain FP64 on the same GPU)")
+    ap.add_argument("--fiber-lambdas", type=int, default=1, help="wavelengths per fiber step (400 nm first)")
+    ap.add_argument("--fiber-dirs", type=int, default=512, help="directions of the fiber accuracy sample")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "engine":
         args.warmup = 3
     world, rank, local = dist_setup(args)
-    res = run_reference(args, world, rank) if args.impl == "reference" else run_engine(args, world, rank, local)
+    if args.impl == "reference":
+        res = run_reference(args, world, rank)
+    elif args.workload == "fiber":
+        res = run_fiber(args, world, rank, local) if rank == 0 else None
+    else:
+        res = run_engine(args, world, rank, local)
     if rank == 0 and res is not None:
         print(json.dumps(res), flush=True)
     if world > 1:

@@ -68,6 +68,9 @@ typedef struct po_config {
                                        only where interpolation.h:66's launch reaches */
   double distance;                  /* observer distance Dis of the prefactors (sphere.cu:46) */
   int interp_method;                /* po_interp_method of the theta pass between levels */
+  int64_t max_workspace_bytes;      /* device workspace cap of one solve; the patterns are
+                                       processed in chunks of slots that fit (0 = half of
+                                       the device's memory) */
 } po_config;
 
 /* How the theta interpolation + translation + child sum between tree levels
@@ -113,6 +116,8 @@ typedef struct po_report {
   double ms_rows;                   /* all row (phi) interpolation launches */
   double ms_cols;                   /* all column (theta) interpolation + child-sum launches */
   int n_leaf_launches, n_row_launches, n_col_launches;
+  int n_chunks;                     /* slot chunks the patterns were processed in */
+  int chunk_slots;                  /* patterns per chunk (the last may be smaller) */
   double leaf_point_dirs;           /* sum over leaves of points x leaf directions x patterns */
   double rows_bytes, cols_bytes;    /* algorithmic bytes (pattern reads + writes) of the passes */
 } po_report;
@@ -202,6 +207,23 @@ po_status po_interp_fft_noalloc(const float *in, int th_c, int ph_c, float *out,
 /* util/fields.h:172-204 (computeintensity): projection onto the transverse
  * plane and |E - Z0 s x H|^2.  fields: [6][n_theta][n_phi] complex64. */
 po_status po_compute_intensity(const float *fields, int n_theta, int n_phi, float *intensity, void *stream);
+
+/* util/geometry.h:3-75 and :76-179 (set_sourcepoint, full ring and ring
+ * segment; the segment form is the one fibersim/treePO.cu:132 calls): a fiber
+ * surface given as a quad grid of vertices -> one surface sample per quad.
+ * height: device float32 [2][numel][numelvert], plane 0 = x, plane 1 = y of
+ * vertex (j, i) at j*numelvert + i (fibersim/treePO.cu:83-86 file layout);
+ * z_i = i*unitz - period/2.  Quads i in [0, numelvert), j in
+ * [ring_begin, ring_end] (the full ring is 0 .. numel-1); outputs (device,
+ * (ring_end-ring_begin+1)*numelvert floats each) at i*(ring_end-ring_begin+1)
+ * + (j-ring_begin): vertex average, area 0.5(|a1| + |a2|) of the two triangle
+ * cross products, unit normal along a1 + a2.  Results equal the reference's
+ * float arithmetic bit for bit.  A vertex at the origin, which the reference
+ * rejects with exit(1), returns PO_ERR_INVALID_ARGUMENT.  Synchronises the
+ * stream (reads the status flag). */
+po_status po_height_field_points(const float *height, int numel, int numelvert, float period, float unitz,
+                                 int ring_begin, int ring_end, float *x, float *y, float *z, float *nx, float *ny,
+                                 float *nz, float *area, void *stream);
 
 /* Library build identification (sm arch, version). */
 const char *po_version(void);

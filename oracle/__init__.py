@@ -64,6 +64,9 @@ def lib():
                                                                           ctypes.c_int, i32p, i32p, ctypes.c_int, f64p]
         L.po_oracle_solve_tree.restype = ctypes.c_int
         L.po_oracle_fresnel.argtypes = [ctypes.c_double] * 5 + [f64p, f64p]
+        L.po_oracle_height_field.argtypes = [f32p, ctypes.c_int, ctypes.c_int, ctypes.c_float, ctypes.c_float,
+                                             ctypes.c_int, ctypes.c_int] + [f32p] * 7
+        L.po_oracle_height_field.restype = ctypes.c_int
         L.po_oracle_z0.restype = ctypes.c_double
         L.po_oracle_num_threads.restype = ctypes.c_int
         _lib = L
@@ -179,3 +182,15 @@ def rel_l2(a, b) -> float:
     a = np.asarray(a, dtype=np.float64)
     b = np.asarray(b, dtype=np.float64)
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def height_field(hf, ring_begin: int = 0, ring_end=None):
+    """util/geometry.h:76-179 restated in float (po_oracle_geometry.c).
+    Returns ((7, n) float32 x, y, z, nx, ny, nz, area; origin-vertex flag)."""
+    ring_end = hf.numel - 1 if ring_end is None else ring_end
+    n = (ring_end - ring_begin + 1) * hf.numelvert
+    out = np.zeros((7, n), dtype=np.float32)
+    xy = np.ascontiguousarray(hf.xy, dtype=np.float32)
+    bad = lib().po_oracle_height_field(xy.ravel(), hf.numel, hf.numelvert, hf.period, hf.unitz, ring_begin,
+                                       ring_end, *[out[k] for k in range(7)])
+    return out, bool(bad)

@@ -45,6 +45,7 @@ struct binary_function {
 #include "util/fields.h"
 #include "util/interpolation.h"
 #include "util/tree.h"
+#include "util/geometry.h"
 
 static std::vector<float> read_f32(const char *path, size_t count) {
   std::vector<float> v(count);
@@ -461,13 +462,34 @@ static int cmd_solve(char **a) {
   return 0;
 }
 
+// util/geometry.h:76-179 (host code): height field -> samples, written as
+// float32 [7][n] (x, y, z, nx, ny, nz, area).  Runs without a GPU.
+static int cmd_heightfield(char **a) {
+  const char *path = a[0];
+  int numel = atoi(a[1]), numelvert = atoi(a[2]);
+  float period = (float)atof(a[3]), unitz = (float)atof(a[4]);
+  int start = atoi(a[5]), end = atoi(a[6]);
+  const char *outpath = a[7];
+  std::vector<float> h = read_f32(path, (size_t)2 * numel * numelvert);
+  int n = (end - start + 1) * numelvert;
+  hostFvec x(n), y(n), z(n), area(n), nx(n), ny(n), nz(n);
+  set_sourcepoint(0.f, 0.f, period, unitz, x, y, z, area, nx, ny, nz, numel, numelvert, h.data(), start, end);
+  std::vector<float> out((size_t)7 * n);
+  const hostFvec *cols[7] = {&x, &y, &z, &nx, &ny, &nz, &area};
+  for (int k = 0; k < 7; ++k)
+    for (int i = 0; i < n; ++i) out[(size_t)k * n + i] = (*cols[k])[i];
+  write_bytes(outpath, out.data(), sizeof(float) * out.size());
+  return 0;
+}
+
 int main(int argc, char **argv) {
-  if (argc < 2) { fprintf(stderr, "usage: ref_harness currents|interp|octree|solve ...\n"); return 2; }
+  if (argc < 2) { fprintf(stderr, "usage: ref_harness currents|interp|octree|solve|heightfield ...\n"); return 2; }
   std::string c = argv[1];
   if (c == "currents" && argc >= 12) return cmd_currents(argv + 2);
   if (c == "interp" && argc >= 8) return cmd_interp(argv + 2);
   if (c == "octree" && argc >= 12) return cmd_octree(argv + 2);
   if (c == "solve" && argc >= 12) return cmd_solve(argv + 2);
+  if (c == "heightfield" && argc >= 10) return cmd_heightfield(argv + 2);
   fprintf(stderr, "bad arguments\n");
   return 2;
 }

@@ -27,3 +27,13 @@ def case_illum(case):
     import oracle
     il = case["illum"]
     return oracle.make_illum(il["lambda_m"], il["theta_i"], il["phi_i"], il["mode"], complex(*il["eta"]), il["sigma"])
+
+
+def load_case_height_field(case):
+    """(HeightField, ring_begin, ring_end) of a height-field case."""
+    from wavefiber3d_gb300.geometry import HeightField
+    h = case["height"]
+    hf = HeightField.load(GOLDEN / h["file"], h["numel"], h["numelvert"], h["period"])
+    assert hf.unitz == h["unitz"]
+    end = case["ring"][1] if case["ring"][1] >= 0 else h["numel"] - 1
+    return hf, case["ring"][0], end

@@ -33,6 +33,7 @@ from wavefiber3d_gb300 import geometry, grids  # noqa: E402
 
 SPHERE = dict(file="geom_sphere_r1um_n2000.bin", n=2000)
 ELLIPSOID = dict(file="geom_ellipsoid_n3000.bin", n=3000)
+HEIGHT = dict(file="hf_fiber_small.bin", radii=[2.0e-6, 1.6e-6], length=1.2e-6, spacing=0.1e-6, seed=7)
 SPHERE_BOX = [-1.1e-6, -1.1e-6, -1.1e-6, 1.1e-6, 1.1e-6, 1.1e-6]
 ELL_BOX = [-1.65e-6, -1.1e-6, -0.88e-6, 1.65e-6, 1.1e-6, 0.88e-6]
 KZ = dict(theta_i=math.pi / 2, phi_i=math.pi)  # incidence along +z, E along x in mode M
@@ -57,7 +58,18 @@ def _cases():
              n_theta=[48, 40], n_phi=[300, 40], illum=illum_a),
         dict(name="ref_interp_even", kind="interp", input="interp_in_20x30.bin", src=[20, 30], dst=[33, 300]),
         dict(name="ref_interp_odd", kind="interp", input="interp_in_21x25.bin", src=[21, 25], dst=[40, 64]),
+        dict(name="ref_heightfield_full", kind="heightfield", height=HEIGHT, ring=[0, -1]),
+        dict(name="ref_heightfield_segment", kind="heightfield", height=HEIGHT, ring=[20, 70]),
+        dict(name="ref_heightfield_wrap", kind="heightfield", height=HEIGHT, ring=[90, -1]),
     ]
+
+
+def small_height_field():
+    """The seeded fiber-like height field of the height-field cases."""
+    h = HEIGHT
+    return geometry.fiber_height_field(radii=h["radii"], length=h["length"], spacing=h["spacing"],
+                                       scale_spacing=0.5e-6, scale_step=0.04e-6, noise_sigma=0.01e-6,
+                                       noise_corr=0.2e-6, seed=h["seed"])
 
 
 def make_inputs():
@@ -69,6 +81,9 @@ def make_inputs():
             th, ph = c["src"]
             z = (rng.standard_normal((th, ph)) + 1j * rng.standard_normal((th, ph))).astype(np.complex64)
             z.tofile(HERE / c["input"])
+    hf = small_height_field()
+    hf.save(HERE / HEIGHT["file"])
+    HEIGHT["numel"], HEIGHT["numelvert"], HEIGHT["period"], HEIGHT["unitz"] = hf.numel, hf.numelvert, hf.period, hf.unitz
     (HERE / "cases.json").write_text(json.dumps(_cases(), indent=1) + "\n")
 
 
@@ -83,6 +98,11 @@ def _harness_args(c):
         args = ["octree", str(HERE / g["file"]), str(g["n"])] + [repr(v) for v in c["box"]] + [str(c["depth"])]
     elif c["kind"] == "interp":
         args = ["interp", str(HERE / c["input"])] + [str(v) for v in c["src"] + c["dst"]]
+    elif c["kind"] == "heightfield":
+        h = c["height"]
+        end = c["ring"][1] if c["ring"][1] >= 0 else h["numel"] - 1
+        args = ["heightfield", str(HERE / h["file"]), str(h["numel"]), str(h["numelvert"]), repr(h["period"]),
+                repr(h["unitz"]), str(c["ring"][0]), str(end)]
     elif c["kind"] == "solve":
         il = c["illum"]
         args = ["solve", str(HERE / g["file"]), str(g["n"])] + [repr(v) for v in c["box"]] + [str(c["depth"])]
@@ -93,10 +113,14 @@ def _harness_args(c):
     return args
 
 
-def run(outdir: Path):
+def run(outdir: Path, kinds=None):
+    """Runs the harness on every case (or the cases of the given kinds; the
+    height-field cases are host code and run without a GPU)."""
     outdir.mkdir(parents=True, exist_ok=True)
     exe = ROOT / "oracle" / "_ref" / "ref_harness"
     for c in json.loads((HERE / "cases.json").read_text()):
+        if kinds and c["kind"] not in kinds:
+            continue
         out = outdir / (c["name"] + ".bin")
         cmd = [str(exe)] + _harness_args(c) + [str(out)]
         print(" ".join(cmd), flush=True)
@@ -107,7 +131,7 @@ if __name__ == "__main__":
     if len(sys.argv) >= 2 and sys.argv[1] == "inputs":
         make_inputs()
     elif len(sys.argv) >= 3 and sys.argv[1] == "run":
-        run(Path(sys.argv[2]))
+        run(Path(sys.argv[2]), sys.argv[3:])
     else:
         print(__doc__)
         sys.exit(2)

@@ -83,3 +83,11 @@ def test_single_step_argument_checks(lib):
     assert lib.po_build_octree(-1, None, None, None, None, None, 2, None, None, None) == 1
     assert lib.po_tangent_plane_currents(-5, *([None] * 7), 5e-7, 0.0, 0.0, 1, 1.55, 0.0, 1e-2, 1.0, 1, None,
                                          None) == 1
+    # height field: null arrays, empty grids and bad ring segments
+    fake = ctypes.c_void_p(16)
+    assert lib.po_height_field_points(None, 8, 4, 1e-6, 2.5e-7, 0, 7, *([fake] * 7), None) == 1
+    assert lib.po_height_field_points(fake, 1, 4, 1e-6, 2.5e-7, 0, 0, *([fake] * 7), None) == 1
+    assert lib.po_height_field_points(fake, 8, 0, 1e-6, 2.5e-7, 0, 7, *([fake] * 7), None) == 1
+    assert lib.po_height_field_points(fake, 8, 4, 1e-6, 2.5e-7, 5, 4, *([fake] * 7), None) == 1
+    assert lib.po_height_field_points(fake, 8, 4, 1e-6, 2.5e-7, 0, 8, *([fake] * 7), None) == 1
+    assert lib.po_height_field_points(fake, 8, 4, 1e-6, 0.0, 0, 7, *([fake] * 7), None) == 1

@@ -240,3 +240,41 @@ def test_oracle_solve_pinned_to_reference(cases, name):
     r = fixture(name).reshape(c["n_theta"][0], c["n_phi"][0])
     o = oracle.solve_tree(cloud, il, c["box"][:3], c["box"][3:], c["depth"], c["n_theta"], c["n_phi"], True)
     assert rel(o, r) < 1e-4
+
+
+# ------------------------------------------------- height field (geometry.h)
+@pytest.mark.parametrize("name", ["ref_heightfield_full", "ref_heightfield_segment", "ref_heightfield_wrap"])
+def test_height_field_oracle_vs_reference_build(cases, name):
+    """The float restatement equals the reference's own set_sourcepoint bit for bit."""
+    from conftest import load_case_height_field
+    hf, b, e = load_case_height_field(cases[name])
+    out, bad = oracle.height_field(hf, b, e)
+    ref = fixture(name).reshape(7, -1)
+    assert not bad
+    assert out.shape == ref.shape
+    assert np.array_equal(out.view(np.uint32), ref.view(np.uint32))
+
+
+def test_height_field_oracle_geometry():
+    """Independent float64 check: samples on the surface, unit normals pointing
+    outwards, areas summing to the lateral area of the segment."""
+    hf = geometry.fiber_height_field(radii=(2e-6, 1.6e-6), length=1.0e-6, spacing=0.02e-6, scale_step=0.0,
+                                     noise_sigma=1e-12, seed=1)
+    out, bad = oracle.height_field(hf)
+    assert not bad
+    x, y, z, nx, ny, nz, a = out.astype(np.float64)
+    assert np.allclose(np.sqrt(nx * nx + ny * ny + nz * nz), 1.0, atol=1e-6)
+    assert np.all(nx * x / 4e-12 + ny * y / 2.56e-12 > 0)  # outward (ellipse gradient)
+    # the last axial row of quads repeats row numelvert-1 (geometry.h:100-103): the band is numelvert*unitz high
+    lateral = geometry.ellipse_perimeter(2e-6, 1.6e-6) * hf.numelvert * hf.unitz
+    assert abs(a.sum() / lateral - 1) < 2e-3
+    assert abs(z.min() - (-hf.period / 2 + hf.unitz / 2)) < 1e-12
+
+
+def test_height_field_origin_vertex_flagged():
+    hf = geometry.fiber_height_field(radii=(2e-6, 1.6e-6), length=0.5e-6, spacing=0.1e-6, seed=2)
+    hf.xy[:, 5, 3] = 0.0
+    _, bad = oracle.height_field(hf)
+    assert bad
+    _, bad = oracle.height_field(hf, 20, 40)  # the zero vertex is outside the segment
+    assert not bad

@@ -35,7 +35,8 @@ class po_config(ctypes.Structure):
                 ("n_phi", ctypes.c_int * (PO_MAX_DEPTH + 1)),
                 ("box_min", ctypes.c_float * 3), ("box_max", ctypes.c_float * 3),
                 ("precision", ctypes.c_int), ("theta_mode", ctypes.c_int), ("nyquist_quirk", ctypes.c_int),
-                ("distance", ctypes.c_double), ("interp_method", ctypes.c_int)]
+                ("distance", ctypes.c_double), ("interp_method", ctypes.c_int),
+                ("max_workspace_bytes", ctypes.c_int64)]
 
 
 class po_geometry(ctypes.Structure):
@@ -60,6 +61,7 @@ class po_report(ctypes.Structure):
                 ("workspace_bytes", ctypes.c_int64), ("kernel_launches", ctypes.c_int64),
                 ("ms_leaf_kernel", ctypes.c_double), ("ms_rows", ctypes.c_double), ("ms_cols", ctypes.c_double),
                 ("n_leaf_launches", ctypes.c_int), ("n_row_launches", ctypes.c_int), ("n_col_launches", ctypes.c_int),
+                ("n_chunks", ctypes.c_int), ("chunk_slots", ctypes.c_int),
                 ("leaf_point_dirs", ctypes.c_double), ("rows_bytes", ctypes.c_double), ("cols_bytes", ctypes.c_double)]
 
     def as_dict(self):
@@ -68,7 +70,7 @@ class po_report(ctypes.Structure):
 
 EXPORTS = ("po_config_init", "po_status_string", "po_last_error", "po_create", "po_destroy", "po_solve",
            "po_tangent_plane_currents", "po_build_octree", "po_far_field_direct", "po_interp_fft",
-           "po_compute_intensity", "po_version", "po_interp_fft_noalloc")
+           "po_compute_intensity", "po_version", "po_interp_fft_noalloc", "po_height_field_points")
 
 _lib = None
 
@@ -98,6 +100,7 @@ def load():
     L.po_interp_fft.argtypes = [vp, i32, i32, vp, i32, i32, i32, i32, i32, vp]
     L.po_interp_fft_noalloc.argtypes = [vp, i32, i32, vp, i32, i32, i32, i32, i32, vp]
     L.po_compute_intensity.argtypes = [vp, i32, i32, vp, vp]
+    L.po_height_field_points.argtypes = [vp, i32, i32, ctypes.c_float, ctypes.c_float, i32, i32] + [vp] * 8
     for name in EXPORTS:
         f = getattr(L, name)
         if name not in ("po_status_string", "po_last_error", "po_version"):

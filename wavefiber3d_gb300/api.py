@@ -83,6 +83,7 @@ class Config:
     nyquist_quirk: bool = True
     distance: float = 1.0
     interp_method: int = PO_INTERP_TENSOR
+    max_workspace_bytes: int = 0
 
     @classmethod
     def reference_rule(cls, max_depth, n_theta_out, n_phi_out, box_min, box_max, theta_extent, phi_extent,
@@ -109,6 +110,7 @@ class Config:
         c.nyquist_quirk = 1 if self.nyquist_quirk else 0
         c.distance = float(self.distance)
         c.interp_method = int(self.interp_method)
+        c.max_workspace_bytes = int(self.max_workspace_bytes)
         return c
 
 
@@ -276,3 +278,21 @@ def compute_intensity(fields, stream=None):
     out = torch.empty((nth, nph), dtype=torch.float32, device="cuda")
     check(_lib.load().po_compute_intensity(_ptr(f), nth, nph, _ptr(out), _stream_ptr(stream)))
     return out
+
+
+def height_field_points(hf, ring_begin: int = 0, ring_end=None, stream=None):
+    """Surface samples of a fiber height field (util/geometry.h:76-179,
+    set_sourcepoint): one sample per quad of the ring segment
+    [ring_begin, ring_end] (default: the full ring).  ``hf`` is a
+    geometry.HeightField.  Returns a (7, n) float32 CUDA tensor in the order
+    x, y, z, nx, ny, nz, area, n = (ring_end - ring_begin + 1) * numelvert,
+    sample (j, i) at i * (ring_end - ring_begin + 1) + (j - ring_begin)."""
+    torch = _torch()
+    ring_end = hf.numel - 1 if ring_end is None else int(ring_end)
+    h = _dev(hf.xy, torch.float32)
+    n = (ring_end - ring_begin + 1) * hf.numelvert
+    out = torch.empty((7, max(n, 1)), dtype=torch.float32, device="cuda")
+    check(_lib.load().po_height_field_points(_ptr(h), hf.numel, hf.numelvert, float(hf.period), float(hf.unitz),
+                                             int(ring_begin), ring_end, *[_ptr(out[k]) for k in range(7)],
+                                             _stream_ptr(stream)))
+    return out[:, :n]

@@ -80,6 +80,11 @@ po_status launch_interp_rows_mma(const float2 *src, float2 *dst, int64_t nrows, 
 po_status launch_trans_table(const double *k_per_lambda, int n_lambda, int nth, int Rp, int phi, const double a[3],
                              float4 *out, cudaStream_t st);
 
+// height field [2][numel][numelvert] -> samples of quads (i, j in [ring_begin, ring_end]);
+// out = {x, y, z, nx, ny, nz, area}; err |= 1 on a vertex at the origin (po_geometry.cu)
+po_status launch_height_field(const float *height, int numel, int numelvert, float period, float unitz, int ring_begin,
+                              int ring_end, float *const out[7], int *err, cudaStream_t st);
+
 // intensity: fields [slot][comp][T][Phi] (root, possibly supersampled by
 // (mt, mp)) -> out [slot][nth][nph]
 po_status launch_intensity_f32(const float2 *fields, int n_slots, int T, int Phi, int nth, int nph, int mt, int mp,

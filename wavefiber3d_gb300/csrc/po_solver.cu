@@ -336,6 +336,39 @@ po_status po_destroy(po_ctx *c) {
   return PO_OK;
 }
 
+// A contiguous range of pattern slots processed together: either whole
+// wavelengths (gc == G) or a run of the slots of one wavelength.
+struct SlotChunk {
+  int s0, ns;  // first slot, slot count
+  int l0, nl;  // first wavelength, wavelength count
+  int gc;      // slots per wavelength inside the chunk
+};
+
+static std::vector<SlotChunk> plan_chunks(int L, int G, int chunk_slots) {
+  std::vector<SlotChunk> v;
+  const int S = L * G;
+  if (chunk_slots >= G) {
+    chunk_slots = (chunk_slots / G) * G;
+    for (int s0 = 0; s0 < S; s0 += chunk_slots) {
+      int ns = std::min(chunk_slots, S - s0);
+      v.push_back({s0, ns, s0 / G, ns / G, G});
+    }
+  } else {
+    for (int l = 0; l < L; ++l)
+      for (int g0 = 0; g0 < G; g0 += chunk_slots) {
+        int ns = std::min(chunk_slots, G - g0);
+        v.push_back({l * G + g0, ns, l, 1, ns});
+      }
+  }
+  return v;
+}
+
+static int chunk_slot_count(int64_t budget, double bytes_per_slot, int S) {
+  if (!(bytes_per_slot > 0)) return S;
+  double c = std::floor((double)budget / bytes_per_slot);
+  return (int)std::max(1.0, std::min((double)S, c));
+}
+
 static po_status solve_impl(po_ctx *c, const po_geometry *g, const po_illum *il, float *intensity, int out_on_device,
                             cudaStream_t st, po_report *rep) {
   const po_config &cfg = c->cfg;
@@ -348,7 +381,15 @@ static po_status solve_impl(po_ctx *c, const po_geometry *g, const po_illum *il,
   const int64_t launches0 = g_launch_count;
   int n_leaf_launches = 0, n_row_launches = 0, n_col_launches = 0;
   double leaf_pd = 0, rows_b = 0, cols_b = 0;
+  double t_leaf = 0, t_agg = 0, t_int = 0, t_leafk = 0, t_rows = 0, t_cols = 0;
   PO_CUDA(cudaEventRecord(c->ev[0], st));
+
+  int64_t budget = cfg.max_workspace_bytes;
+  if (budget <= 0) {
+    size_t fr = 0, tot = 0;
+    PO_CUDA(cudaMemGetInfo(&fr, &tot));
+    budget = (int64_t)(tot / 2);
+  }
 
   // ---- geometry on the device
   const float *gin[7];
@@ -404,29 +445,59 @@ static po_status solve_impl(po_ctx *c, const po_geometry *g, const po_illum *il,
   double c0[3];
   for (int a = 0; a < 3; ++a) c0[a] = (double)(0.5f * (cfg.box_min[a] + cfg.box_max[a]));
 
+  // Accumulates the device times of one chunk (needs its events complete).
+  auto chunk_times = [&](bool tree_levels) {
+    float t = 0;
+    if (cudaEventElapsedTime(&t, c->kev[0], c->kev[1]) == cudaSuccess) { t_leafk += t; t_leaf += t; }
+    if (cudaEventElapsedTime(&t, c->kev[1], c->ev[3]) == cudaSuccess) t_agg += t;
+    if (cudaEventElapsedTime(&t, c->ev[3], c->ev[4]) == cudaSuccess) t_int += t;
+    if (tree_levels)
+      for (int l = 0; l < d; ++l) {
+        if (cudaEventElapsedTime(&t, c->kev[2 + 4 * l], c->kev[3 + 4 * l]) == cudaSuccess) t_rows += t;
+        if (cudaEventElapsedTime(&t, c->kev[4 + 4 * l], c->kev[5 + 4 * l]) == cudaSuccess) t_cols += t;
+      }
+    cudaGetLastError();
+  };
+  std::vector<SlotChunk> chunks;
+
   if (fp64) {
     // ---- plain FP64 direct sum (the "plain method"): no tree, no sort
     PO_CUDA(cudaEventRecord(c->ev[1], st));
-    PO_TRY(c->cur.ensure(sizeof(double2) * 6 * (size_t)S * std::max<int64_t>(n, 1)));
-    PO_TRY(launch_currents_f64(n, gin, c->slots.as<SlotParams<double>>(), S, c->cur.as<double>(), st));
     PO_CUDA(cudaEventRecord(c->ev[2], st));
+    auto splits = [&](int ns) {
+      int64_t tiles = (int64_t)ns * ceil_div((int)nd_out, 128);
+      int s = (int)std::max<int64_t>(1, std::min<int64_t>(64, (c->sm_count * 8 + tiles - 1) / std::max<int64_t>(1, tiles)));
+      return (int)std::min<int64_t>(s, std::max<int64_t>(1, n));
+    };
+    int cs = chunk_slot_count(budget, 96.0 * (double)(n + nd_out * (1 + splits(1))), S);
+    cs = chunk_slot_count(budget, 96.0 * (double)(n + nd_out * (1 + splits(cs))), S);
+    chunks = plan_chunks(L, G, cs);
+    const int ns_max = chunks.front().ns, nsplit_max = splits(std::min(ns_max, chunks.back().ns));
+    PO_TRY(c->cur.ensure(sizeof(double2) * 6 * (size_t)ns_max * std::max<int64_t>(n, 1)));
     std::vector<double> dd = host_dirs_d(nth_out, nph_out, nth_out);
     PO_TRY(c->dirs_d.ensure(sizeof(double) * dd.size()));
     PO_CUDA(cudaMemcpyAsync(c->dirs_d.p, dd.data(), sizeof(double) * dd.size(), cudaMemcpyHostToDevice, st));
-    int nsplit = std::max(1, std::min<int>(64, (int)((c->sm_count * 8 + S * ceil_div((int)nd_out, 128) - 1) /
-                                                      std::max<int64_t>(1, S * ceil_div((int)nd_out, 128)))));
-    nsplit = (int)std::min<int64_t>(nsplit, std::max<int64_t>(1, n));
-    PO_TRY(c->partial.ensure(sizeof(double2) * 6 * (size_t)S * nd_out * nsplit));
-    PO_TRY(c->levelA.ensure(sizeof(double2) * 6 * (size_t)S * nd_out));
-    PO_CUDA(cudaEventRecord(c->kev[0], st));
-    PO_TRY(launch_direct_f64(n, gin[0], gin[1], gin[2], c->cur.as<double2>(), k_slot, S, c0, c->dirs_d.as<double>(),
-                             (int)nd_out, nsplit, c->partial.as<double2>(), c->levelA.as<double2>(), st));
-    PO_CUDA(cudaEventRecord(c->kev[1], st));
-    n_leaf_launches = 2;
+    PO_TRY(c->partial.ensure(sizeof(double2) * 6 * (size_t)ns_max * nd_out * nsplit_max));
+    PO_TRY(c->levelA.ensure(sizeof(double2) * 6 * (size_t)ns_max * nd_out));
+    for (const SlotChunk &ch : chunks) {
+      PO_CUDA(cudaEventRecord(c->kev[0], st));
+      PO_TRY(launch_currents_f64(n, gin, c->slots.as<SlotParams<double>>() + ch.s0, ch.ns, c->cur.as<double>(), st));
+      const int nsplit = std::min(splits(ch.ns), nsplit_max);
+      PO_TRY(launch_direct_f64(n, gin[0], gin[1], gin[2], c->cur.as<double2>(), k_slot + ch.s0, ch.ns, c0,
+                               c->dirs_d.as<double>(), (int)nd_out, nsplit, c->partial.as<double2>(),
+                               c->levelA.as<double2>(), st));
+      PO_CUDA(cudaEventRecord(c->kev[1], st));
+      PO_CUDA(cudaEventRecord(c->ev[3], st));
+      PO_TRY(launch_intensity_f64(c->levelA.as<double2>(), ch.ns, nth_out, nph_out, out_dev + (size_t)ch.s0 * nd_out,
+                                  st));
+      PO_CUDA(cudaEventRecord(c->ev[4], st));
+      n_leaf_launches += 3;
+      if (rep) {
+        PO_CUDA(cudaEventSynchronize(c->ev[4]));
+        chunk_times(false);
+      }
+    }
     leaf_pd = (double)n * nd_out * S;
-    PO_CUDA(cudaEventRecord(c->ev[3], st));
-    PO_CUDA(cudaEventRecord(c->ev[4], st));
-    PO_TRY(launch_intensity_f64(c->levelA.as<double2>(), S, nth_out, nph_out, out_dev, st));
   } else {
     // ---- octree (depth 0 still sorts the points so that direct-sum tiles are compact)
     PO_CUDA(cudaEventRecord(c->ev[1], st));
@@ -448,28 +519,41 @@ static po_status solve_impl(po_ctx *c, const po_geometry *g, const po_illum *il,
       rep->n_nodes_total = tot;
     }
     if (d == 0) {
-      PO_TRY(c->cur.ensure(sizeof(float2) * 6 * (size_t)S * std::max<int64_t>(n, 1)));
-      PO_TRY(launch_currents_f32(n, gsc, c->slots.as<SlotParams<float>>(), S, c->cur.as<float>(), st));
       std::vector<float4> df = host_dirs_f4(nth_out, nph_out, nth_out);
       std::vector<double> dd = host_dirs_d(nth_out, nph_out, nth_out);
       PO_TRY(c->dirs.ensure(sizeof(float4) * df.size()));
       PO_TRY(c->dirs_d.ensure(sizeof(double) * dd.size()));
       PO_CUDA(cudaMemcpyAsync(c->dirs.p, df.data(), sizeof(float4) * df.size(), cudaMemcpyHostToDevice, st));
       PO_CUDA(cudaMemcpyAsync(c->dirs_d.p, dd.data(), sizeof(double) * dd.size(), cudaMemcpyHostToDevice, st));
-      int nsplit = direct_splits(n, (int)nd_out, L, c->sm_count);
+      int cs = chunk_slot_count(budget, 48.0 * (double)(n + nd_out * (1 + direct_splits(n, (int)nd_out, 1, c->sm_count))), S);
+      chunks = plan_chunks(L, G, cs);
+      const int ns_max = chunks.front().ns;
+      int nsplit_max = 1;
+      for (const SlotChunk &ch : chunks)
+        nsplit_max = std::max(nsplit_max, direct_splits(n, (int)nd_out, ch.nl, c->sm_count));
+      PO_TRY(c->cur.ensure(sizeof(float2) * 6 * (size_t)ns_max * std::max<int64_t>(n, 1)));
       PO_TRY(c->tile_ctr.ensure(sizeof(double) * 3 * (size_t)((n + 127) / 128 + 1)));
-      PO_TRY(c->partial.ensure(sizeof(float2) * 6 * (size_t)S * nd_out * nsplit));
-      PO_TRY(c->levelA.ensure(sizeof(float2) * 6 * (size_t)S * nd_out));
-      PO_CUDA(cudaEventRecord(c->kev[0], st));
-      PO_TRY(launch_direct_f32(n, gs[0], gs[1], gs[2], c->cur.as<float2>(), c->tile_ctr.as<double>(), k_lambda, L, G,
-                               c0, c->dirs.as<float4>(), c->dirs_d.as<double>(), (int)nd_out, nsplit,
-                               c->partial.as<float2>(), c->levelA.as<float2>(), st));
-      PO_CUDA(cudaEventRecord(c->kev[1], st));
-      n_leaf_launches = 2 + (G + 3) / 4;
+      PO_TRY(c->partial.ensure(sizeof(float2) * 6 * (size_t)ns_max * nd_out * nsplit_max));
+      PO_TRY(c->levelA.ensure(sizeof(float2) * 6 * (size_t)ns_max * nd_out));
+      for (const SlotChunk &ch : chunks) {
+        PO_CUDA(cudaEventRecord(c->kev[0], st));
+        PO_TRY(launch_currents_f32(n, gsc, c->slots.as<SlotParams<float>>() + ch.s0, ch.ns, c->cur.as<float>(), st));
+        int nsplit = direct_splits(n, (int)nd_out, ch.nl, c->sm_count);
+        PO_TRY(launch_direct_f32(n, gs[0], gs[1], gs[2], c->cur.as<float2>(), c->tile_ctr.as<double>(),
+                                 k_lambda + ch.l0, ch.nl, ch.gc, c0, c->dirs.as<float4>(), c->dirs_d.as<double>(),
+                                 (int)nd_out, nsplit, c->partial.as<float2>(), c->levelA.as<float2>(), st));
+        PO_CUDA(cudaEventRecord(c->kev[1], st));
+        PO_CUDA(cudaEventRecord(c->ev[3], st));
+        PO_TRY(launch_intensity_f32(c->levelA.as<float2>(), ch.ns, nth_out, nph_out, nth_out, nph_out, 1, 1,
+                                    out_dev + (size_t)ch.s0 * nd_out, st));
+        PO_CUDA(cudaEventRecord(c->ev[4], st));
+        n_leaf_launches += 3 + (ch.gc + 3) / 4;
+        if (rep) {
+          PO_CUDA(cudaEventSynchronize(c->ev[4]));
+          chunk_times(false);
+        }
+      }
       leaf_pd = (double)n * nd_out * S;
-      PO_CUDA(cudaEventRecord(c->ev[3], st));
-      PO_CUDA(cudaEventRecord(c->ev[4], st));
-      PO_TRY(launch_intensity_f32(c->levelA.as<float2>(), S, nth_out, nph_out, nth_out, nph_out, 1, 1, out_dev, st));
     } else {
       // ---- hierarchical solve
       const int64_t nleaf = tree.level[d].count;
@@ -481,15 +565,17 @@ static po_status solve_impl(po_ctx *c, const po_geometry *g, const po_illum *il,
                                                                          c->leaf_ctr.as<double>());
         count_launch();
       }
-      // buffer sizes
+      // pattern buffers per slot: two level buffers + the row-pass output
       size_t lvl_max = 0, mid_max = 0;
       for (int l = 0; l <= d; ++l)
-        lvl_max = std::max(lvl_max, (size_t)S * tree.level[l].count * 6 * (size_t)c->R[l] * c->Phi[l]);
+        lvl_max = std::max(lvl_max, (size_t)tree.level[l].count * 6 * (size_t)c->R[l] * c->Phi[l]);
       for (int l = 0; l < d; ++l)
-        mid_max = std::max(mid_max, (size_t)S * tree.level[l + 1].count * 6 * (size_t)c->R[l + 1] * c->Phi[l]);
-      PO_TRY(c->levelA.ensure(sizeof(float2) * lvl_max));
-      PO_TRY(c->levelB.ensure(sizeof(float2) * lvl_max));
-      PO_TRY(c->mid.ensure(sizeof(float2) * std::max<size_t>(mid_max, 1)));
+        mid_max = std::max(mid_max, (size_t)tree.level[l + 1].count * 6 * (size_t)c->R[l + 1] * c->Phi[l]);
+      chunks = plan_chunks(L, G, chunk_slot_count(budget, 8.0 * (2.0 * lvl_max + mid_max), S));
+      const int ns_max = chunks.front().ns;
+      PO_TRY(c->levelA.ensure(sizeof(float2) * lvl_max * ns_max));
+      PO_TRY(c->levelB.ensure(sizeof(float2) * lvl_max * ns_max));
+      PO_TRY(c->mid.ensure(sizeof(float2) * std::max<size_t>(mid_max * ns_max, 1)));
       // translation tables (per level, per wavelength)
       size_t tr_total = 0;
       std::vector<size_t> tr_off(d);
@@ -508,57 +594,65 @@ static po_status solve_impl(po_ctx *c, const po_geometry *g, const po_illum *il,
       std::vector<float4> df = host_dirs_f4(c->R[d], c->Phi[d], c->nth[d]);
       PO_TRY(c->dirs.ensure(sizeof(float4) * df.size()));
       PO_CUDA(cudaMemcpyAsync(c->dirs.p, df.data(), sizeof(float4) * df.size(), cudaMemcpyHostToDevice, st));
-      PO_CUDA(cudaEventRecord(c->kev[0], st));
-      if (cfg.precision == PO_PREC_SPLIT_BF16)
-        PO_TRY(launch_leaf_mma(gsc, tree.level[d].begin, c->leaf_ctr.as<double>(), nleaf,
-                               c->slots.as<SlotParams<float>>(), L, G, c->dirs.as<float4>(), c->R[d] * c->Phi[d],
-                               c->levelA.as<float2>(), st));
-      else
-        PO_TRY(launch_leaf(gsc, tree.level[d].begin, c->leaf_ctr.as<double>(), nleaf,
-                           c->slots.as<SlotParams<float>>(), L, G, c->dirs.as<float4>(), c->R[d] * c->Phi[d],
-                           c->levelA.as<float2>(), st));
-      PO_CUDA(cudaEventRecord(c->kev[1], st));
-      n_leaf_launches = nleaf > 0 ? (G + 3) / 4 : 0;
-      leaf_pd = (double)n * c->R[d] * c->Phi[d] * S;
-      PO_CUDA(cudaEventRecord(c->ev[3], st));
-      float2 *cur_lvl = c->levelA.as<float2>(), *nxt = c->levelB.as<float2>();
-      for (int l = d - 1; l >= 0; --l) {
-        const int64_t nc = tree.level[l + 1].count, np = tree.level[l].count;
-        FftPlan prow_in = make_plan(c->Phi[l + 1], c->tw_offset[c->Phi[l + 1]]);
-        FftPlan prow_out = make_plan(c->Phi[l], c->tw_offset[c->Phi[l]]);
-        FftPlan pcol_in = make_plan(c->T[l + 1], c->tw_offset[c->T[l + 1]]);
-        FftPlan pcol_out = make_plan(c->T[l], c->tw_offset[c->T[l]]);
-        int64_t nrows = (int64_t)S * nc * 6 * c->R[l + 1];
-        PO_CUDA(cudaEventRecord(c->kev[2 + 4 * l], st));
-        const int refnq = c->cover == 1 ? 1 : 0;
-        if (c->tensor_theta)
-          PO_TRY(launch_interp_rows_mma(cur_lvl, c->mid.as<float2>(), nrows, c->Phi[l + 1], c->Phi[l], c->bmat_kp[l],
-                                        c->bmat.as<uint32_t>() + c->bmat_off[l], c->sm_count, st));
+      const int refnq = c->cover == 1 ? 1 : 0;
+      for (const SlotChunk &ch : chunks) {
+        const SlotParams<float> *sp = c->slots.as<SlotParams<float>>() + ch.s0;
+        PO_CUDA(cudaEventRecord(c->kev[0], st));
+        if (cfg.precision == PO_PREC_SPLIT_BF16)
+          PO_TRY(launch_leaf_mma(gsc, tree.level[d].begin, c->leaf_ctr.as<double>(), nleaf, sp, ch.nl, ch.gc,
+                                 c->dirs.as<float4>(), c->R[d] * c->Phi[d], c->levelA.as<float2>(), st));
         else
-          PO_TRY(launch_interp_rows(cur_lvl, c->mid.as<float2>(), nrows, prow_in, prow_out, c->twiddles.as<float2>(),
-                                    1.0f / (float)c->Phi[l + 1], c->sm_count, refnq, st));
-        PO_CUDA(cudaEventRecord(c->kev[3 + 4 * l], st));
-        rows_b += 8.0 * nrows * (c->Phi[l + 1] + c->Phi[l]);
-        cols_b += 8.0 * S * 6 * ((double)nc * c->R[l + 1] * c->Phi[l] + (double)np * c->R[l] * c->Phi[l]);
-        if (nrows > 0) ++n_row_launches;
-        if (np > 0) ++n_col_launches;
-        PO_CUDA(cudaEventRecord(c->kev[4 + 4 * l], st));
-        int reach = 0x7fffffff;
-        if (c->cover == 1 && cfg.nyquist_quirk) reach = 256 * (c->T[l + 1] / 256 + 1);
-        if (c->tensor_theta)
-          PO_TRY(launch_interp_cols_mma(c->mid.as<float2>(), nxt, tree.level[l].child, np, nc, c->Phi[l], c->R[l + 1],
-                                        c->R[l], c->amat_kp[l], c->mirror, c->amat.as<uint32_t>() + c->amat_off[l],
-                                        c->trans.as<float4>() + tr_off[l], S, G, st));
-        else
-          PO_TRY(launch_interp_cols(c->mid.as<float2>(), nxt, tree.level[l].child, np, nc, c->Phi[l], c->R[l + 1],
-                                    c->R[l], pcol_in, pcol_out, c->twiddles.as<float2>(),
-                                    c->trans.as<float4>() + tr_off[l], S, G, reach, 1.0f / (float)c->T[l + 1], 6,
-                                    c->mirror, refnq, st));
-        PO_CUDA(cudaEventRecord(c->kev[5 + 4 * l], st));
-        std::swap(cur_lvl, nxt);
+          PO_TRY(launch_leaf(gsc, tree.level[d].begin, c->leaf_ctr.as<double>(), nleaf, sp, ch.nl, ch.gc,
+                             c->dirs.as<float4>(), c->R[d] * c->Phi[d], c->levelA.as<float2>(), st));
+        PO_CUDA(cudaEventRecord(c->kev[1], st));
+        n_leaf_launches += nleaf > 0 ? (ch.gc + 3) / 4 : 0;
+        float2 *cur_lvl = c->levelA.as<float2>(), *nxt = c->levelB.as<float2>();
+        for (int l = d - 1; l >= 0; --l) {
+          const int64_t nc = tree.level[l + 1].count, np = tree.level[l].count;
+          const float4 *trans = c->trans.as<float4>() + tr_off[l] + (size_t)ch.l0 * c->R[l] * c->Phi[l];
+          int64_t nrows = (int64_t)ch.ns * nc * 6 * c->R[l + 1];
+          PO_CUDA(cudaEventRecord(c->kev[2 + 4 * l], st));
+          if (c->tensor_theta) {
+            PO_TRY(launch_interp_rows_mma(cur_lvl, c->mid.as<float2>(), nrows, c->Phi[l + 1], c->Phi[l],
+                                          c->bmat_kp[l], c->bmat.as<uint32_t>() + c->bmat_off[l], c->sm_count, st));
+          } else {
+            FftPlan prow_in = make_plan(c->Phi[l + 1], c->tw_offset[c->Phi[l + 1]]);
+            FftPlan prow_out = make_plan(c->Phi[l], c->tw_offset[c->Phi[l]]);
+            PO_TRY(launch_interp_rows(cur_lvl, c->mid.as<float2>(), nrows, prow_in, prow_out,
+                                      c->twiddles.as<float2>(), 1.0f / (float)c->Phi[l + 1], c->sm_count, refnq, st));
+          }
+          PO_CUDA(cudaEventRecord(c->kev[3 + 4 * l], st));
+          rows_b += 8.0 * nrows * (c->Phi[l + 1] + c->Phi[l]);
+          cols_b += 8.0 * ch.ns * 6 * ((double)nc * c->R[l + 1] * c->Phi[l] + (double)np * c->R[l] * c->Phi[l]);
+          if (nrows > 0) ++n_row_launches;
+          if (np > 0) ++n_col_launches;
+          PO_CUDA(cudaEventRecord(c->kev[4 + 4 * l], st));
+          if (c->tensor_theta) {
+            PO_TRY(launch_interp_cols_mma(c->mid.as<float2>(), nxt, tree.level[l].child, np, nc, c->Phi[l],
+                                          c->R[l + 1], c->R[l], c->amat_kp[l], c->mirror,
+                                          c->amat.as<uint32_t>() + c->amat_off[l], trans, ch.ns, ch.gc, st));
+          } else {
+            FftPlan pcol_in = make_plan(c->T[l + 1], c->tw_offset[c->T[l + 1]]);
+            FftPlan pcol_out = make_plan(c->T[l], c->tw_offset[c->T[l]]);
+            int reach = 0x7fffffff;
+            if (c->cover == 1 && cfg.nyquist_quirk) reach = 256 * (c->T[l + 1] / 256 + 1);
+            PO_TRY(launch_interp_cols(c->mid.as<float2>(), nxt, tree.level[l].child, np, nc, c->Phi[l],
+                                      c->R[l + 1], c->R[l], pcol_in, pcol_out, c->twiddles.as<float2>(), trans,
+                                      ch.ns, ch.gc, reach, 1.0f / (float)c->T[l + 1], 6, c->mirror, refnq, st));
+          }
+          PO_CUDA(cudaEventRecord(c->kev[5 + 4 * l], st));
+          std::swap(cur_lvl, nxt);
+        }
+        PO_CUDA(cudaEventRecord(c->ev[3], st));
+        PO_TRY(launch_intensity_f32(cur_lvl, ch.ns, c->R[0], c->Phi[0], nth_out, nph_out, c->mt, c->mp,
+                                    out_dev + (size_t)ch.s0 * nd_out, st));
+        PO_CUDA(cudaEventRecord(c->ev[4], st));
+        if (rep) {
+          PO_CUDA(cudaEventSynchronize(c->ev[4]));
+          chunk_times(true);
+        }
       }
-      PO_CUDA(cudaEventRecord(c->ev[4], st));
-      PO_TRY(launch_intensity_f32(cur_lvl, S, c->R[0], c->Phi[0], nth_out, nph_out, c->mt, c->mp, out_dev, st));
+      leaf_pd = (double)n * c->R[d] * c->Phi[d] * S;
     }
   }
   if (!out_on_device)
@@ -567,17 +661,14 @@ static po_status solve_impl(po_ctx *c, const po_geometry *g, const po_illum *il,
   if (rep || !out_on_device) PO_CUDA(cudaEventSynchronize(c->ev[5]));
   PO_CUDA(cudaGetLastError());
   if (rep) {
-    float t[5];
+    float t[2];
     cudaEventElapsedTime(&t[0], c->ev[0], c->ev[5]);
     cudaEventElapsedTime(&t[1], c->ev[1], c->ev[2]);
-    cudaEventElapsedTime(&t[2], c->ev[2], c->ev[3]);
-    cudaEventElapsedTime(&t[3], c->ev[3], c->ev[4]);
-    cudaEventElapsedTime(&t[4], c->ev[4], c->ev[5]);
     rep->ms_total = t[0];
     rep->ms_build = t[1];
-    rep->ms_leaf = t[2];
-    rep->ms_aggregate = t[3];
-    rep->ms_intensity = t[4];
+    rep->ms_leaf = t_leaf;
+    rep->ms_aggregate = t_agg;
+    rep->ms_intensity = t_int;
     rep->root_theta = c->nth[0];
     rep->root_phi = c->Phi[0];
     int64_t ws = 0;
@@ -590,16 +681,14 @@ static po_status solve_impl(po_ctx *c, const po_geometry *g, const po_illum *il,
     rep->n_leaf_launches = n_leaf_launches;
     rep->n_row_launches = n_row_launches;
     rep->n_col_launches = n_col_launches;
+    rep->n_chunks = (int)chunks.size();
+    rep->chunk_slots = chunks.empty() ? 0 : chunks.front().ns;
     rep->leaf_point_dirs = leaf_pd;
     rep->rows_bytes = rows_b;
     rep->cols_bytes = cols_b;
-    float tk = 0;
-    if (n_leaf_launches > 0 && cudaEventElapsedTime(&tk, c->kev[0], c->kev[1]) == cudaSuccess) rep->ms_leaf_kernel = tk;
-    if (!fp64 && d > 0)
-      for (int l = 0; l < d; ++l) {
-        if (cudaEventElapsedTime(&tk, c->kev[2 + 4 * l], c->kev[3 + 4 * l]) == cudaSuccess) rep->ms_rows += tk;
-        if (cudaEventElapsedTime(&tk, c->kev[4 + 4 * l], c->kev[5 + 4 * l]) == cudaSuccess) rep->ms_cols += tk;
-      }
+    rep->ms_leaf_kernel = t_leafk;
+    rep->ms_rows = t_rows;
+    rep->ms_cols = t_cols;
     cudaGetLastError();
   }
   return PO_OK;
