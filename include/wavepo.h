@@ -225,6 +225,16 @@ po_status po_height_field_points(const float *height, int numel, int numelvert, 
                                  int ring_begin, int ring_end, float *x, float *y, float *z, float *nx, float *ny,
                                  float *nz, float *area, void *stream);
 
+/* util/fields.h:206-234 (average_cpu): box average of n_patterns float32
+ * patterns [nth_in][nph_in] onto [nth_out][nph_out] (device pointers), phi
+ * first, then theta.  As in the reference the ratios are the integer
+ * quotients nth_in / nth_out and nph_in / nph_out, so when they do not divide
+ * evenly only the first ratio*n_out rows / columns contribute (for the fiber
+ * preset 450 x 880 -> 180 x 360: ratios 2 and 2, rows 0..359 and columns
+ * 0..719).  Results equal the reference's float arithmetic bit for bit. */
+po_status po_average_pattern(const float *in, int nth_in, int nph_in, float *out, int nth_out, int nph_out,
+                             int n_patterns, void *stream);
+
 /* Library build identification (sm arch, version). */
 const char *po_version(void);
 

@@ -67,6 +67,7 @@ def lib():
         L.po_oracle_height_field.argtypes = [f32p, ctypes.c_int, ctypes.c_int, ctypes.c_float, ctypes.c_float,
                                              ctypes.c_int, ctypes.c_int] + [f32p] * 7
         L.po_oracle_height_field.restype = ctypes.c_int
+        L.po_oracle_average.argtypes = [f32p, ctypes.c_int, ctypes.c_int, f32p, ctypes.c_int, ctypes.c_int]
         L.po_oracle_z0.restype = ctypes.c_double
         L.po_oracle_num_threads.restype = ctypes.c_int
         _lib = L
@@ -194,3 +195,11 @@ def height_field(hf, ring_begin: int = 0, ring_end=None):
     bad = lib().po_oracle_height_field(xy.ravel(), hf.numel, hf.numelvert, hf.period, hf.unitz, ring_begin,
                                        ring_end, *[out[k] for k in range(7)])
     return out, bool(bad)
+
+
+def average(pattern, nth_out: int, nph_out: int) -> np.ndarray:
+    """util/fields.h:206-234 (average_cpu) restated in float."""
+    p = np.ascontiguousarray(pattern, dtype=np.float32)
+    out = np.zeros((nth_out, nph_out), dtype=np.float32)
+    lib().po_oracle_average(p.ravel(), p.shape[0], p.shape[1], out.ravel(), nth_out, nph_out)
+    return out

@@ -11,9 +11,13 @@
  * with -ffp-contract=off so that no multiply-add is fused on any host.
  * Returns 0, or 1 when a vertex lies at the origin (geometry.h:110-114 prints
  * an error and exits there).
+ *
+ * Also restates util/fields.h:206-234 (average_cpu), the box average of a
+ * fine pattern onto a coarse grid, in float and in the reference's order.
  */
 #include <math.h>
 #include <stdint.h>
+#include <stdlib.h>
 
 typedef struct {
   float x, y, z;
@@ -64,4 +68,21 @@ int po_oracle_height_field(const float *height, int numel, int numelvert, float 
     }
   }
   return bad;
+}
+
+/* util/fields.h:206-234: ratios by integer division (std::ceil of an int
+   quotient), phi pass into a zeroed row buffer, then the theta pass into a
+   zeroed output. */
+void po_oracle_average(const float *in, int nth_in, int nph_in, float *out, int nth_out, int nph_out) {
+  int rp = nph_in / nph_out, rt = nth_in / nth_out;
+  float *rows = (float *)calloc((size_t)nth_in * nph_out, sizeof(float));
+  for (int i = 0; i < nth_in; ++i)
+    for (int j = 0; j < nph_out; ++j)
+      for (int k = 0; k < rp; ++k) rows[(size_t)i * nph_out + j] += in[(size_t)i * nph_in + j * rp + k] / (float)rp;
+  for (int i = 0; i < nth_out; ++i)
+    for (int j = 0; j < nph_out; ++j) {
+      out[(size_t)i * nph_out + j] = 0.f;
+      for (int k = 0; k < rt; ++k) out[(size_t)i * nph_out + j] += rows[(size_t)(i * rt + k) * nph_out + j] / (float)rt;
+    }
+  free(rows);
 }

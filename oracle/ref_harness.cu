@@ -482,14 +482,29 @@ static int cmd_heightfield(char **a) {
   return 0;
 }
 
+// util/fields.h:206-234 (average_cpu, host code): float32 [nth_in][nph_in]
+// -> [nth_out][nph_out].  Runs without a GPU.
+static int cmd_average(char **a) {
+  const char *path = a[0];
+  int nth_in = atoi(a[1]), nph_in = atoi(a[2]), nth_out = atoi(a[3]), nph_out = atoi(a[4]);
+  const char *outpath = a[5];
+  std::vector<float> v = read_f32(path, (size_t)nth_in * nph_in);
+  hostFvec in(v.begin(), v.end()), out((size_t)nth_out * nph_out, 0.f);
+  average_cpu(in, out, nth_out, nth_in, nph_out, nph_in);
+  std::vector<float> o(out.begin(), out.end());
+  write_bytes(outpath, o.data(), sizeof(float) * o.size());
+  return 0;
+}
+
 int main(int argc, char **argv) {
-  if (argc < 2) { fprintf(stderr, "usage: ref_harness currents|interp|octree|solve|heightfield ...\n"); return 2; }
+  if (argc < 2) { fprintf(stderr, "usage: ref_harness currents|interp|octree|solve|heightfield|average ...\n"); return 2; }
   std::string c = argv[1];
   if (c == "currents" && argc >= 12) return cmd_currents(argv + 2);
   if (c == "interp" && argc >= 8) return cmd_interp(argv + 2);
   if (c == "octree" && argc >= 12) return cmd_octree(argv + 2);
   if (c == "solve" && argc >= 12) return cmd_solve(argv + 2);
   if (c == "heightfield" && argc >= 10) return cmd_heightfield(argv + 2);
+  if (c == "average" && argc >= 8) return cmd_average(argv + 2);
   fprintf(stderr, "bad arguments\n");
   return 2;
 }

@@ -58,6 +58,9 @@ def _cases():
              n_theta=[48, 40], n_phi=[300, 40], illum=illum_a),
         dict(name="ref_interp_even", kind="interp", input="interp_in_20x30.bin", src=[20, 30], dst=[33, 300]),
         dict(name="ref_interp_odd", kind="interp", input="interp_in_21x25.bin", src=[21, 25], dst=[40, 64]),
+        dict(name="ref_average_leftover", kind="average", input="avg_in_45x88.bin", src=[45, 88], dst=[18, 36]),
+        dict(name="ref_average_even", kind="average", input="avg_in_90x144.bin", src=[90, 144], dst=[18, 36]),
+        dict(name="ref_average_ragged", kind="average", input="avg_in_7x13.bin", src=[7, 13], dst=[3, 4]),
         dict(name="ref_heightfield_full", kind="heightfield", height=HEIGHT, ring=[0, -1]),
         dict(name="ref_heightfield_segment", kind="heightfield", height=HEIGHT, ring=[20, 70]),
         dict(name="ref_heightfield_wrap", kind="heightfield", height=HEIGHT, ring=[90, -1]),
@@ -81,6 +84,11 @@ def make_inputs():
             th, ph = c["src"]
             z = (rng.standard_normal((th, ph)) + 1j * rng.standard_normal((th, ph))).astype(np.complex64)
             z.tofile(HERE / c["input"])
+    rng = np.random.default_rng(20231204)
+    for c in _cases():
+        if c["kind"] == "average":
+            th, ph = c["src"]
+            rng.exponential(1.0, (th, ph)).astype(np.float32).tofile(HERE / c["input"])
     hf = small_height_field()
     hf.save(HERE / HEIGHT["file"])
     HEIGHT["numel"], HEIGHT["numelvert"], HEIGHT["period"], HEIGHT["unitz"] = hf.numel, hf.numelvert, hf.period, hf.unitz
@@ -98,6 +106,8 @@ def _harness_args(c):
         args = ["octree", str(HERE / g["file"]), str(g["n"])] + [repr(v) for v in c["box"]] + [str(c["depth"])]
     elif c["kind"] == "interp":
         args = ["interp", str(HERE / c["input"])] + [str(v) for v in c["src"] + c["dst"]]
+    elif c["kind"] == "average":
+        args = ["average", str(HERE / c["input"])] + [str(v) for v in c["src"] + c["dst"]]
     elif c["kind"] == "heightfield":
         h = c["height"]
         end = c["ring"][1] if c["ring"][1] >= 0 else h["numel"] - 1

@@ -66,3 +66,24 @@ def test_height_field_errors():
     with pytest.raises(WavePOError, match="origin"):
         api.height_field_points(bad)
     api.height_field_points(bad, 20, 40)  # the zero vertex lies outside this segment
+
+
+# ------------------------------------------------------- pattern averaging
+@pytest.mark.parametrize("name", ["ref_average_leftover", "ref_average_even", "ref_average_ragged"])
+def test_average_vs_reference_build(cases, name):
+    c = cases[name]
+    inp = np.fromfile(GOLDEN / c["input"], dtype=np.float32).reshape(c["src"])
+    out = api.average_pattern(inp, *c["dst"]).cpu().numpy()
+    ref = np.fromfile(GOLDEN / f"{name}.bin", dtype=np.float32).reshape(c["dst"])
+    assert np.array_equal(bits(out), bits(ref))
+
+
+def test_average_batched_fiber_preset_vs_oracle():
+    """450 x 880 -> 180 x 360 (the fiber preset), three patterns in one launch."""
+    rng = np.random.default_rng(9)
+    p = rng.exponential(1.0, (3, 450, 880)).astype(np.float32)
+    out = api.average_pattern(p, 180, 360).cpu().numpy()
+    for b in range(3):
+        assert np.array_equal(bits(out[b]), bits(oracle.average(p[b], 180, 360)))
+    with pytest.raises(WavePOError, match="INVALID_ARGUMENT"):
+        api.average_pattern(p[0], 451, 360)

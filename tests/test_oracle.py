@@ -278,3 +278,25 @@ def test_height_field_origin_vertex_flagged():
     assert bad
     _, bad = oracle.height_field(hf, 20, 40)  # the zero vertex is outside the segment
     assert not bad
+
+
+# ------------------------------------------------ pattern averaging (fields.h)
+@pytest.mark.parametrize("name", ["ref_average_leftover", "ref_average_even", "ref_average_ragged"])
+def test_average_oracle_vs_reference_build(cases, name):
+    c = cases[name]
+    inp = np.fromfile(GOLDEN / c["input"], dtype=np.float32).reshape(c["src"])
+    out = oracle.average(inp, *c["dst"])
+    ref = fixture(name).reshape(c["dst"])
+    assert np.array_equal(out.view(np.uint32), ref.view(np.uint32))
+
+
+def test_average_oracle_uses_leading_samples_only():
+    """Integer ratios (fields.h:210-211): 45 -> 18 rows averages rows 0..35 in pairs."""
+    p = np.zeros((45, 88), np.float32)
+    p[36:, :] = 1e9
+    p[:, 72:] = 1e9
+    out = oracle.average(p, 18, 36)
+    assert np.all(out == 0)
+    q = np.arange(45 * 88, dtype=np.float32).reshape(45, 88)
+    want = q[:36, :72].reshape(18, 2, 36, 2).mean(axis=(1, 3))
+    assert np.allclose(oracle.average(q, 18, 36), want, rtol=1e-6)

@@ -296,3 +296,17 @@ def height_field_points(hf, ring_begin: int = 0, ring_end=None, stream=None):
                                              int(ring_begin), ring_end, *[_ptr(out[k]) for k in range(7)],
                                              _stream_ptr(stream)))
     return out[:, :n]
+
+
+def average_pattern(patterns, nth_out: int = 180, nph_out: int = 360, stream=None):
+    """Box average of (..., nth_in, nph_in) float32 patterns onto nth_out x
+    nph_out (util/fields.h:206-234, average_cpu, with its integer ratios)."""
+    torch = _torch()
+    p = _dev(patterns, torch.float32)
+    lead = p.shape[:-2]
+    nth_in, nph_in = p.shape[-2:]
+    b = int(np.prod(lead)) if lead else 1
+    out = torch.empty((*lead, nth_out, nph_out), dtype=torch.float32, device="cuda")
+    check(_lib.load().po_average_pattern(_ptr(p), nth_in, nph_in, _ptr(out), nth_out, nph_out, b,
+                                         _stream_ptr(stream)))
+    return out

@@ -2,7 +2,10 @@
 
 Every translation unit under csrc/ is compiled for sm_103a only
 (-gencode arch=compute_103a,code=sm_103a) in parallel, then linked into one
-shared library with a C ABI (include/wavepo.h).
+shared library with a C ABI (include/wavepo.h).  The drop-in command-line
+drivers (cli/wavepo_cli.cpp: wavepo_sphere, wavepo_ellipsoid,
+wavepo_ellipsoid_simple, wavepo_treepo) are linked against it into the same
+folder.
 """
 from __future__ import annotations
 
@@ -46,6 +49,31 @@ def _compile(src: Path, verbose_ptxas: bool) -> Path:
     return obj
 
 
+CLI_SRC = PKG / "cli" / "wavepo_cli.cpp"
+CLIS = {"wavepo_sphere": "SPHERE", "wavepo_ellipsoid": "ELLIPSOID", "wavepo_ellipsoid_simple": "ELLIPSOID_SIMPLE",
+        "wavepo_treepo": "TREEPO"}
+
+
+def _build_cli(name: str, define: str) -> Path:
+    exe = BUILD / name
+    cmd = [nvcc(), "-O2", "-std=c++17", f"-DWAVEPO_CLI_{define}", "-I", str(ROOT / "include"), str(CLI_SRC), "-o",
+           str(exe), "-L", str(BUILD), "-lwavepo", "-Xlinker", "-rpath,$ORIGIN", "-lcudart"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"nvcc failed for {name}:\n{r.stderr}")
+    return exe
+
+
+def build_cli(force: bool = False) -> list:
+    """Links the drop-in drivers against libwavepo.so (after build())."""
+    t = LIB.stat().st_mtime
+    todo = [n for n in CLIS if force or not (BUILD / n).exists() or (BUILD / n).stat().st_mtime < max(
+        t, CLI_SRC.stat().st_mtime, (ROOT / "include" / "wavepo.h").stat().st_mtime)]
+    with cf.ThreadPoolExecutor(max_workers=max(1, len(todo))) as ex:
+        list(ex.map(lambda n: _build_cli(n, CLIS[n]), todo))
+    return [BUILD / n for n in CLIS]
+
+
 def build(force: bool = False, verbose_ptxas: bool = False) -> Path:
     BUILD.mkdir(exist_ok=True)
     srcs = sources()
@@ -53,6 +81,7 @@ def build(force: bool = False, verbose_ptxas: bool = False) -> Path:
     if LIB.exists() and not force and not verbose_ptxas:
         t = LIB.stat().st_mtime
         if all(p.stat().st_mtime <= t for p in deps):
+            build_cli()
             return LIB
     with cf.ThreadPoolExecutor(max_workers=min(len(srcs), os.cpu_count() or 4)) as ex:
         objs = list(ex.map(lambda s: _compile(s, verbose_ptxas), srcs))
@@ -62,6 +91,7 @@ def build(force: bool = False, verbose_ptxas: bool = False) -> Path:
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr}")
     tmp.replace(LIB)
+    build_cli(force=True)
     return LIB
 
 

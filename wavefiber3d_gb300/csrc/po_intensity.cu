@@ -89,4 +89,45 @@ po_status launch_intensity_f64(const double2 *fields, int n_slots, int nth, int 
   return PO_OK;
 }
 
+// util/fields.h:206-234 (average_cpu): box average of a fine pattern onto a
+// coarse grid, phi first, then theta, with the reference's integer ratios
+// r = n_in / n_out (integer division, so only the first r*n_out samples of each
+// axis take part) and its float evaluation order:
+//   row(i', j) = sum_k in[i'][j*rp + k] / rp,  out(i, j) = sum_k row(i*rt + k, j) / rt.
+__global__ void k_average(const float *__restrict__ in, int nth_in, int nph_in, float *__restrict__ out, int nth_out,
+                          int nph_out, int rt, int rp) {
+  int64_t d = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  int64_t nd = (int64_t)nth_out * nph_out;
+  if (d >= nd) return;
+  const float *src = in + (int64_t)blockIdx.y * nth_in * nph_in;
+  int i = (int)(d / nph_out), j = (int)(d % nph_out);
+  float acc = 0.f;
+  for (int kt = 0; kt < rt; ++kt) {
+    const float *row = src + (int64_t)(i * rt + kt) * nph_in + (int64_t)j * rp;
+    float s = 0.f;
+    for (int kp = 0; kp < rp; ++kp) s = __fadd_rn(s, __fdiv_rn(row[kp], (float)rp));
+    acc = __fadd_rn(acc, __fdiv_rn(s, (float)rt));
+  }
+  out[(int64_t)blockIdx.y * nd + d] = acc;
+}
+
 }  // namespace wavepo
+
+using namespace wavepo;
+
+extern "C" po_status po_average_pattern(const float *in, int nth_in, int nph_in, float *out, int nth_out,
+                                        int nph_out, int n_patterns, void *stream) {
+  if (!in || !out) return fail(PO_ERR_INVALID_ARGUMENT, "null pointer");
+  if (nth_out <= 0 || nph_out <= 0 || n_patterns < 0 || n_patterns > 65535)
+    return fail(PO_ERR_INVALID_ARGUMENT, "output grid must be positive and n_patterns in [0, 65535]");
+  if (nth_in < nth_out || nph_in < nph_out)
+    return fail(PO_ERR_INVALID_ARGUMENT, "the input grid must be at least as fine as the output grid");
+  if (n_patterns == 0) return PO_OK;
+  const int rt = nth_in / nth_out, rp = nph_in / nph_out;
+  const int64_t nd = (int64_t)nth_out * nph_out;
+  dim3 grid((unsigned)((nd + 255) / 256), (unsigned)n_patterns);
+  k_average<<<grid, 256, 0, (cudaStream_t)stream>>>(in, nth_in, nph_in, out, nth_out, nph_out, rt, rp);
+  count_launch();
+  PO_CUDA(cudaGetLastError());
+  return PO_OK;
+}
