@@ -148,6 +148,23 @@ po_status po_destroy(po_ctx *ctx);
 po_status po_solve(po_ctx *ctx, const po_geometry *geom, const po_illum *illum, float *intensity,
                    int out_on_device, void *stream, po_report *report);
 
+/* No counterpart in the reference (it has no gradients).  Gradient of a
+ * scalar loss L with respect to every surface sample, given dL/dI on the
+ * output grid: dl_di [n_lambda][n_inc][n_pol][n_theta[0]][n_phi[0]] float32
+ * (device).  grad (device, float32 [7][n], overwritten) receives dL/dx,
+ * dL/dy, dL/dz, dL/dnx, dL/dny, dL/dnz, dL/darea in the input point order;
+ * normals are differentiated as given (no renormalisation).  The forward
+ * solve is recomputed (intensity, if not NULL, receives it on the device);
+ * then the root adjoint, the exact transpose of the tree aggregation (or of
+ * the depth-0 sum) and the derivative of the tangent-plane currents give the
+ * gradient of the discrete map the engine evaluates.  Needs double-cover
+ * theta and PO_INTERP_TENSOR when max_depth > 0 (else PO_ERR_UNSUPPORTED);
+ * PO_PREC_FP64 runs the whole chain in FP64 (depth 0).  The gradient is
+ * piecewise: the octree assignment and the lit/shadow switch of every point
+ * are held fixed. */
+po_status po_grad(po_ctx *ctx, const po_geometry *geom, const po_illum *illum, const float *dl_di, float *grad,
+                  float *intensity, void *stream, po_report *report);
+
 /* ---- single steps of the path (device pointers) ------------------------ */
 
 /* util/tangentplane.h:84-92 (computeLocalTangentPlane) and, when scale != 0,
@@ -224,6 +241,16 @@ po_status po_compute_intensity(const float *fields, int n_theta, int n_phi, floa
 po_status po_height_field_points(const float *height, int numel, int numelvert, float period, float unitz,
                                  int ring_begin, int ring_end, float *x, float *y, float *z, float *nx, float *ny,
                                  float *nz, float *area, void *stream);
+
+/* No counterpart in the reference.  Adjoint of po_height_field_points:
+ * given dL/d(sample) (device float32 [7][n] in the sample order of
+ * po_height_field_points: x, y, z, nx, ny, nz, area), writes dL/d(vertex)
+ * into grad_height (device float32 [2][numel][numelvert], overwritten;
+ * vertices outside the ring segment get 0).  Derivatives are taken in FP64
+ * per quad and accumulated with atomics. */
+po_status po_height_field_adjoint(const float *height, int numel, int numelvert, float period, float unitz,
+                                  int ring_begin, int ring_end, const float *grad_samples, float *grad_height,
+                                  void *stream);
 
 /* util/fields.h:206-234 (average_cpu): box average of n_patterns float32
  * patterns [nth_in][nph_in] onto [nth_out][nph_out] (device pointers), phi

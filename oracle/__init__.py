@@ -67,6 +67,8 @@ def lib():
         L.po_oracle_height_field.argtypes = [f32p, ctypes.c_int, ctypes.c_int, ctypes.c_float, ctypes.c_float,
                                              ctypes.c_int, ctypes.c_int] + [f32p] * 7
         L.po_oracle_height_field.restype = ctypes.c_int
+        L.po_oracle_solve_direct_d.argtypes = [ctypes.c_int64] + [f64p] * 7 + [ctypes.POINTER(Illum), f64p,
+                                                                              ctypes.c_int, ctypes.c_int, f64p]
         L.po_oracle_average.argtypes = [f32p, ctypes.c_int, ctypes.c_int, f32p, ctypes.c_int, ctypes.c_int]
         L.po_oracle_z0.restype = ctypes.c_double
         L.po_oracle_num_threads.restype = ctypes.c_int
@@ -202,4 +204,14 @@ def average(pattern, nth_out: int, nph_out: int) -> np.ndarray:
     p = np.ascontiguousarray(pattern, dtype=np.float32)
     out = np.zeros((nth_out, nph_out), dtype=np.float32)
     lib().po_oracle_average(p.ravel(), p.shape[0], p.shape[1], out.ravel(), nth_out, nph_out)
+    return out
+
+
+def solve_direct_f64(samples, il: Illum, n_theta: int, n_phi: int, center=(0.0, 0.0, 0.0)) -> np.ndarray:
+    """Depth-0 FP64 solve of (7, n) float64 samples (x, y, z, nx, ny, nz, area)."""
+    a = np.ascontiguousarray(samples, dtype=np.float64)
+    out = np.zeros((n_theta, n_phi), dtype=np.float64)
+    c = np.ascontiguousarray(center, dtype=np.float64)
+    lib().po_oracle_solve_direct_d(a.shape[1], *[np.ascontiguousarray(a[k]) for k in range(7)], ctypes.byref(il),
+                                   c, n_theta, n_phi, out)
     return out

@@ -272,6 +272,47 @@ void po_oracle_solve_direct(int64_t n, const float *x, const float *y, const flo
   free(fld);
 }
 
+/* The depth-0 solve with FP64 samples (positions, normals, areas as double):
+ * the same model as po_oracle_solve_direct, for central finite differences
+ * whose steps a float32 coordinate could not resolve. */
+void po_oracle_solve_direct_d(int64_t n, const double *x, const double *y, const double *z, const double *nx,
+                              const double *ny, const double *nz, const double *area, const po_oracle_illum *il,
+                              const double *center, int nth, int nph, double *intensity) {
+  double wavedir[3], edir[3], hdir[3];
+  po_oracle_incident(il->theta_i, il->phi_i, il->mode_te, wavedir, edir, hdir);
+  double k0 = 2.0 * M_PI / il->lambda_m, z0 = orc_z0();
+  cdbl ef, hf;
+  prefactors(k0, il->dis, &ef, &hf);
+  cdbl eta = il->eta_re + I * il->eta_im;
+  cdbl *cur = (cdbl *)malloc(sizeof(cdbl) * 6 * (size_t)(n > 0 ? n : 1));
+  double *fld = (double *)malloc(sizeof(double) * 12 * (size_t)nth * nph);
+#pragma omp parallel for schedule(static)
+  for (int64_t p = 0; p < n; ++p) {
+    double src[3] = {x[p], y[p], z[p]}, nrm[3] = {nx[p], ny[p], nz[p]};
+    tangent_plane_point(wavedir, edir, hdir, 1.0, eta, z0, il->sigma, k0, il->mode_te, src, nrm, cur + 6 * p);
+    for (int c = 0; c < 6; ++c) cur[6 * p + c] *= area[p] * (c < 3 ? ef : hf);
+  }
+  int64_t nd = (int64_t)nth * nph;
+#pragma omp parallel for schedule(dynamic, 16)
+  for (int64_t d = 0; d < nd; ++d) {
+    double s[3];
+    direction((int)(d / nph), (int)(d % nph), nth, nph, s);
+    cdbl acc[6] = {0, 0, 0, 0, 0, 0};
+    for (int64_t p = 0; p < n; ++p) {
+      double ph = k0 * ((x[p] - center[0]) * s[0] + (y[p] - center[1]) * s[1] + (z[p] - center[2]) * s[2]);
+      cdbl g = cos(ph) + I * sin(ph);
+      for (int k = 0; k < 6; ++k) acc[k] += cur[6 * p + k] * g;
+    }
+    for (int k = 0; k < 6; ++k) {
+      fld[d * 12 + 2 * k] = creal(acc[k]);
+      fld[d * 12 + 2 * k + 1] = cimag(acc[k]);
+    }
+  }
+  po_oracle_intensity(nth, nph, fld, intensity);
+  free(cur);
+  free(fld);
+}
+
 /* Sampled variant for timing and for large cases: only the listed flat
  * direction indices of the nth x nph grid are evaluated (fields out: [m][6]). */
 void po_oracle_far_field_sampled(int64_t n, const float *x, const float *y, const float *z,

@@ -71,7 +71,7 @@ class po_report(ctypes.Structure):
 EXPORTS = ("po_config_init", "po_status_string", "po_last_error", "po_create", "po_destroy", "po_solve",
            "po_tangent_plane_currents", "po_build_octree", "po_far_field_direct", "po_interp_fft",
            "po_compute_intensity", "po_version", "po_interp_fft_noalloc", "po_height_field_points",
-           "po_average_pattern")
+           "po_average_pattern", "po_grad", "po_height_field_adjoint")
 
 _lib = None
 
@@ -101,6 +101,9 @@ def load():
     L.po_interp_fft.argtypes = [vp, i32, i32, vp, i32, i32, i32, i32, i32, vp]
     L.po_interp_fft_noalloc.argtypes = [vp, i32, i32, vp, i32, i32, i32, i32, i32, vp]
     L.po_compute_intensity.argtypes = [vp, i32, i32, vp, vp]
+    L.po_grad.argtypes = [vp, ctypes.POINTER(po_geometry), ctypes.POINTER(po_illum), vp, vp, vp, vp,
+                          ctypes.POINTER(po_report)]
+    L.po_height_field_adjoint.argtypes = [vp, i32, i32, ctypes.c_float, ctypes.c_float, i32, i32, vp, vp, vp]
     L.po_average_pattern.argtypes = [vp, i32, i32, vp, i32, i32, i32, vp]
     L.po_height_field_points.argtypes = [vp, i32, i32, ctypes.c_float, ctypes.c_float, i32, i32] + [vp] * 8
     for name in EXPORTS:

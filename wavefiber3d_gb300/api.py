@@ -210,6 +210,32 @@ class Solver:
         del keep
         return res
 
+    def grad(self, samples, illum: Illumination, dl_di, with_intensity: bool = False, stream=None):
+        """Gradient of a loss with respect to the surface samples (po_grad).
+
+        samples: (7, n) float32 CUDA tensor (x, y, z, nx, ny, nz, area);
+        dl_di: dL/dI shaped like the solve output.  Returns the (7, n) float32
+        gradient (and the recomputed intensity if with_intensity)."""
+        torch = _torch()
+        g7 = samples.to(device="cuda", dtype=torch.float32).contiguous()
+        n = g7.shape[1]
+        g = _lib.po_geometry(n, *[g7[k].data_ptr() for k in range(7)], 1)
+        il, keep = illum.to_c()
+        shape = self.out_shape(illum)
+        w = dl_di.to(device="cuda", dtype=torch.float32).contiguous()
+        if w.numel() != int(np.prod(shape)):
+            raise ValueError(f"dl_di must have {int(np.prod(shape))} elements")
+        grad = torch.empty((7, max(n, 1)), dtype=torch.float32, device="cuda")
+        inten = torch.empty(shape, dtype=torch.float32, device="cuda") if with_intensity else None
+        rep = _lib.po_report()
+        check(_lib.load().po_grad(self._h, ctypes.byref(g), ctypes.byref(il), ctypes.c_void_p(w.data_ptr()),
+                                  ctypes.c_void_p(grad.data_ptr()),
+                                  ctypes.c_void_p(inten.data_ptr()) if inten is not None else None,
+                                  _stream_ptr(stream), ctypes.byref(rep)))
+        self.last_report = rep.as_dict()
+        del keep
+        return (grad[:, :n], inten) if with_intensity else grad[:, :n]
+
 
 def compute_local_tangent_plane(x, y, z, nx, ny, nz, area, wavelength_m, theta_i, phi_i, mode="M", eta=1.55 + 0j,
                                 sigma=1e-2, distance=1.0, scale=True, stream=None):
@@ -309,4 +335,29 @@ def average_pattern(patterns, nth_out: int = 180, nph_out: int = 360, stream=Non
     out = torch.empty((*lead, nth_out, nph_out), dtype=torch.float32, device="cuda")
     check(_lib.load().po_average_pattern(_ptr(p), nth_in, nph_in, _ptr(out), nth_out, nph_out, b,
                                          _stream_ptr(stream)))
+    return out
+
+
+def height_field_points_tensor(xy, period: float, unitz: float, ring_begin: int, ring_end: int, stream=None):
+    """po_height_field_points on a (2, numel, numelvert) float32 CUDA tensor; returns (7, n)."""
+    torch = _torch()
+    x = xy.to(device="cuda", dtype=torch.float32).contiguous()
+    numel, numelvert = int(x.shape[1]), int(x.shape[2])
+    n = (ring_end - ring_begin + 1) * numelvert
+    out = torch.empty((7, max(n, 1)), dtype=torch.float32, device="cuda")
+    check(_lib.load().po_height_field_points(_ptr(x), numel, numelvert, float(period), float(unitz), int(ring_begin),
+                                             int(ring_end), *[_ptr(out[k]) for k in range(7)], _stream_ptr(stream)))
+    return out[:, :n]
+
+
+def height_field_adjoint(xy, period: float, unitz: float, ring_begin: int, ring_end: int, grad_samples, stream=None):
+    """dL/d(vertex xy) (2, numel, numelvert) from dL/d(samples) (7, n)."""
+    torch = _torch()
+    x = xy.to(device="cuda", dtype=torch.float32).contiguous()
+    numel, numelvert = int(x.shape[1]), int(x.shape[2])
+    g = grad_samples.to(device="cuda", dtype=torch.float32).contiguous()
+    out = torch.empty_like(x)
+    check(_lib.load().po_height_field_adjoint(_ptr(x), numel, numelvert, float(period), float(unitz),
+                                              int(ring_begin), int(ring_end), _ptr(g), _ptr(out),
+                                              _stream_ptr(stream)))
     return out

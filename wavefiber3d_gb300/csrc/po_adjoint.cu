@@ -1,0 +1,480 @@
+// po_adjoint.cu -- gradient of far-field intensity with respect to the surface
+// samples (positions, normals, areas).
+//
+// The forward map of the engine is F = T(C(x, n, a)): tangent-plane currents
+// C per point (util/tangentplane.h:19-80), leaf or depth-0 far-field sums
+// F(s) = sum_p exp(i k s.(x_p - c)) C_p (util/fields.h:2-50), then the linear
+// tree aggregation T, and the intensity I = |E - Z0 s x H|^2 of the
+// transverse projection (util/fields.h:172-204).  For a scalar loss with
+// dL/dI given on the output grid, dL = 2 Re sum G^H dF with
+//   G(s) = dL/dI(s) [E'; Z0 s x E'],   E' = P(s) F(s)            (root adjoint)
+// at the root; the aggregation passes its exact transpose down to the leaves
+// (po_interp_mma.cu); at a leaf (or the whole cloud at depth 0)
+//   A_p   = sum_s G(s) exp(-i k s.(x_p - c)),
+//   A_p^a = sum_s s_a G(s) exp(-i k s.(x_p - c))   (a = x, y, z)
+// and
+//   dL/dx_p,a += -2 k Im(A_p^a^H C_p)          (phase of the far-field sum)
+//   dL/dq     += 2 Re(A_p^H dC_p/dq)            (q in x, y, z, n, area)
+// The Jacobian dC_p/dq of the tangent-plane model is taken in FP64 forward
+// mode (dual numbers with 7 tangents), per point and pattern.  Only the root
+// fields of the forward pass are kept; nothing of the intermediate levels is
+// stored, because the transposed aggregation is linear.
+#include <cuda_runtime.h>
+
+#include "po_common.cuh"
+#include "po_internal.h"
+#include "po_kernels.h"
+
+namespace wavepo {
+
+// ------------------------------------------------ FP64 forward-mode duals
+constexpr int kNT = 7;  // tangents: x, y, z, nx, ny, nz, area
+
+struct D7 {
+  double v;
+  double d[kNT];
+};
+
+__device__ __forceinline__ D7 dconst(double v) {
+  D7 r;
+  r.v = v;
+#pragma unroll
+  for (int i = 0; i < kNT; ++i) r.d[i] = 0.0;
+  return r;
+}
+__device__ __forceinline__ D7 dvar(double v, int i) {
+  D7 r = dconst(v);
+  r.d[i] = 1.0;
+  return r;
+}
+// f(u) with f(u.v) = fv and f'(u.v) = fp
+__device__ __forceinline__ D7 dchain(const D7 &u, double fv, double fp) {
+  D7 r;
+  r.v = fv;
+#pragma unroll
+  for (int i = 0; i < kNT; ++i) r.d[i] = fp * u.d[i];
+  return r;
+}
+__device__ __forceinline__ D7 operator+(const D7 &a, const D7 &b) {
+  D7 r;
+  r.v = a.v + b.v;
+#pragma unroll
+  for (int i = 0; i < kNT; ++i) r.d[i] = a.d[i] + b.d[i];
+  return r;
+}
+__device__ __forceinline__ D7 operator-(const D7 &a, const D7 &b) {
+  D7 r;
+  r.v = a.v - b.v;
+#pragma unroll
+  for (int i = 0; i < kNT; ++i) r.d[i] = a.d[i] - b.d[i];
+  return r;
+}
+__device__ __forceinline__ D7 operator-(const D7 &a) { return dchain(a, -a.v, -1.0); }
+__device__ __forceinline__ D7 operator*(const D7 &a, const D7 &b) {
+  D7 r;
+  r.v = a.v * b.v;
+#pragma unroll
+  for (int i = 0; i < kNT; ++i) r.d[i] = a.d[i] * b.v + a.v * b.d[i];
+  return r;
+}
+__device__ __forceinline__ D7 operator*(const D7 &a, double s) { return dchain(a, a.v * s, s); }
+__device__ __forceinline__ D7 operator*(double s, const D7 &a) { return dchain(a, a.v * s, s); }
+__device__ __forceinline__ D7 operator/(const D7 &a, const D7 &b) {
+  D7 r;
+  const double ib = 1.0 / b.v;
+  r.v = a.v * ib;
+#pragma unroll
+  for (int i = 0; i < kNT; ++i) r.d[i] = (a.d[i] - r.v * b.d[i]) * ib;
+  return r;
+}
+__device__ __forceinline__ D7 dsqrt(const D7 &a) {
+  const double s = sqrt(a.v);
+  return dchain(a, s, s > 0 ? 0.5 / s : 0.0);
+}
+__device__ __forceinline__ D7 dexp(const D7 &a) {
+  const double e = exp(a.v);
+  return dchain(a, e, e);
+}
+__device__ __forceinline__ D7 dacos(const D7 &a) {
+  const double q = 1.0 - a.v * a.v;
+  return dchain(a, acos(a.v), q > 0 ? -1.0 / sqrt(q) : 0.0);
+}
+__device__ __forceinline__ D7 dabs(const D7 &a) { return a.v < 0 ? -a : a; }
+__device__ __forceinline__ D7 dsin(const D7 &a) { return dchain(a, sin(a.v), cos(a.v)); }
+
+using CD = cx<D7>;
+__device__ __forceinline__ CD cd(double re, double im) { return {dconst(re), dconst(im)}; }
+__device__ __forceinline__ CD operator*(const CD &a, const CD &b) {
+  return {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re};
+}
+__device__ __forceinline__ CD operator*(const CD &a, const D7 &s) { return {a.re * s, a.im * s}; }
+__device__ __forceinline__ CD operator*(const CD &a, double s) { return {a.re * s, a.im * s}; }
+__device__ __forceinline__ CD operator+(const CD &a, const CD &b) { return {a.re + b.re, a.im + b.im}; }
+__device__ __forceinline__ CD operator-(const CD &a, const CD &b) { return {a.re - b.re, a.im - b.im}; }
+__device__ __forceinline__ CD cddiv(const CD &a, const CD &b) {
+  D7 d = b.re * b.re + b.im * b.im;
+  return {(a.re * b.re + a.im * b.im) / d, (a.im * b.re - a.re * b.im) / d};
+}
+// principal square root (as csqrt_ of po_common.cuh)
+__device__ __forceinline__ CD cdsqrt(const CD &z) {
+  const D7 r = dsqrt(z.re * z.re + z.im * z.im);
+  const D7 ha = (r + z.re) * 0.5, hb = (r - z.re) * 0.5;
+  const D7 a = ha.v > 0 ? dsqrt(ha) : dconst(0.0);
+  const D7 b = hb.v > 0 ? dsqrt(hb) : dconst(0.0);
+  return {a, z.im.v < 0 ? -b : b};
+}
+// util/util.h:365-382 with a dual angle and constant indices
+__device__ __forceinline__ CD d_cos_internal(const CD &n, const D7 &theta) {
+  D7 s = dsin(theta);
+  CD q = cddiv({s, dconst(0.0)}, n);
+  q = cddiv(q * s, n);
+  return cdsqrt({dconst(1.0) - q.re, -q.im});
+}
+__device__ __forceinline__ CD d_rs(const D7 &theta, const CD &n0, const CD &nt) {
+  CD p0 = n0 * d_cos_internal(n0, theta);
+  CD pt = nt * d_cos_internal(cddiv(nt, n0), theta);
+  return cddiv(p0 - pt, p0 + pt);
+}
+__device__ __forceinline__ CD d_rp(const D7 &theta, const CD &n0, const CD &nt) {
+  CD q0 = cddiv(d_cos_internal(n0, theta), n0);
+  CD qt = cddiv(d_cos_internal(nt, theta), nt);
+  return cddiv(q0 - qt, q0 + qt);
+}
+
+// The tangent-plane model of tangent_plane() (po_common.cuh) in FP64 on dual
+// inputs: the same branches (taken on the float-rounded values, as the
+// forward kernels take them), differentiated.  out[0..2] = J, out[3..5] = M.
+__device__ void tangent_plane_jvp(const SlotParams<double> &P, float px, float py, float pz, float qx, float qy,
+                                  float qz, float area, CD out[6]) {
+  const D7 X = dvar(px, 0), Y = dvar(py, 1), Z = dvar(pz, 2);
+  const D7 nr[3] = {dvar(qx, 3), dvar(qy, 4), dvar(qz, 5)};
+  const D7 Ar = dvar(area, 6);
+  const double kd[3] = {P.wavedir[0], P.wavedir[1], P.wavedir[2]};
+  const D7 dotvalue = nr[0] * kd[0] + nr[1] * kd[1] + nr[2] * kd[2];
+  CD Ei[3] = {cd(0, 0), cd(0, 0), cd(0, 0)}, Hi[3] = {cd(0, 0), cd(0, 0), cd(0, 0)};
+  CD Es[3] = {cd(0, 0), cd(0, 0), cd(0, 0)}, Hs[3] = {cd(0, 0), cd(0, 0), cd(0, 0)};
+  const float dot_f = (float)(kd[0] * qx + kd[1] * qy + kd[2] * qz);
+  if (dot_f <= 0.0f) {
+    // incident phase exp(-i k0 w.x) and beam exp(-z^2 / (2 sigma^2))
+    const D7 arg = (X * P.wd[0] + Y * P.wd[1] + Z * P.wd[2]) * (-P.k0d);
+    double sn, cs;
+    sincos(arg.v, &sn, &cs);
+    const CD e = {dchain(arg, cs, -sn), dchain(arg, sn, cs)};
+    const D7 beam = dexp(-(Z * Z) * P.inv_two_sigma2);
+    const CD Ei0 = e * beam;
+    const CD Hi0 = Ei0 * (1.0 / P.z0);
+    for (int c = 0; c < 3; ++c) {
+      Ei[c] = Ei0 * P.edir[c];
+      Hi[c] = Hi0 * P.hdir[c];
+    }
+    const CD eta_in = cd(1, 0), eta_out = cd(P.eta_re, P.eta_im);
+    if (fabsf(fabsf(dot_f) - 1.0f) < 1e-10f) {  // tangentplane.h:39-49
+      const CD R = P.te ? cddiv(eta_out - eta_in, eta_in + eta_out) : cddiv(eta_in - eta_out, eta_in + eta_out);
+      for (int c = 0; c < 3; ++c) {
+        Es[c] = Ei[c] * R;
+        Hs[c] = Hi[c] * R;
+      }
+    } else {  // tangentplane.h:51-62
+      D7 rp[3] = {nr[2] * kd[1] - nr[1] * kd[2], nr[0] * kd[2] - nr[2] * kd[0], nr[1] * kd[0] - nr[0] * kd[1]};
+      const D7 inv = dconst(1.0) / dsqrt(rp[0] * rp[0] + rp[1] * rp[1] + rp[2] * rp[2]);
+      for (int c = 0; c < 3; ++c) rp[c] = rp[c] * inv;
+      const CD f = Ei[0] * rp[0] + Ei[1] * rp[1] + Ei[2] * rp[2];
+      CD Eperp[3], Epar[3], Hpar[3], Hperp[3];
+      for (int c = 0; c < 3; ++c) {
+        Eperp[c] = f * rp[c];
+        Epar[c] = Ei[c] - Eperp[c];
+      }
+      const double iz = 1.0 / P.z0;
+      Hpar[0] = (Epar[2] * kd[1] - Epar[1] * kd[2]) * iz;
+      Hpar[1] = (Epar[0] * kd[2] - Epar[2] * kd[0]) * iz;
+      Hpar[2] = (Epar[1] * kd[0] - Epar[0] * kd[1]) * iz;
+      for (int c = 0; c < 3; ++c) Hperp[c] = Hi[c] - Hpar[c];
+      const D7 lphi = dacos(dabs(dotvalue));
+      const CD Rs = d_rs(lphi, eta_in, eta_out);
+      const CD Rp = d_rp(lphi, eta_in, eta_out);
+      for (int c = 0; c < 3; ++c) {
+        Es[c] = Eperp[c] * Rs - Epar[c] * Rp;
+        Hs[c] = Hpar[c] * Rp - Hperp[c] * Rs;
+      }
+    }
+  }
+  CD Et[3], Ht[3];
+  for (int c = 0; c < 3; ++c) {
+    Et[c] = Ei[c] + Es[c];
+    Ht[c] = Hi[c] + Hs[c];
+  }
+  const CD M[3] = {Et[1] * nr[2] - Et[2] * nr[1], Et[2] * nr[0] - Et[0] * nr[2], Et[0] * nr[1] - Et[1] * nr[0]};
+  const CD J[3] = {Ht[2] * nr[1] - Ht[1] * nr[2], Ht[0] * nr[2] - Ht[2] * nr[0], Ht[1] * nr[0] - Ht[0] * nr[1]};
+  const CD ef = {Ar * P.ef_re, Ar * P.ef_im}, hf = {Ar * P.hf_re, Ar * P.hf_im};
+  for (int c = 0; c < 3; ++c) {
+    out[c] = J[c] * ef;
+    out[3 + c] = M[c] * hf;
+  }
+}
+
+// ------------------------------------------------------------ root adjoint
+// G at the sampled root points (output sample (i, k) = root (mt*i, mp*k));
+// every other root sample gets 0.  fields/G: [slot][6][T][Phi].
+template <typename V, typename R>
+__global__ void k_intensity_adjoint(const V *__restrict__ fields, const float *__restrict__ dl_di, int T, int Phi,
+                                    int nth, int nph, int mt, int mp, R z0, V *__restrict__ G) {
+  const int64_t cstride = (int64_t)T * Phi;
+  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int slot = blockIdx.y;
+  if (e >= cstride) return;
+  const int it = (int)(e / Phi), ip = (int)(e % Phi);
+  const V *f = fields + (int64_t)slot * 6 * cstride;
+  V *g = G + (int64_t)slot * 6 * cstride;
+  const bool sampled = (it % mt == 0) && (ip % mp == 0) && it / mt < nth && ip / mp < nph;
+  if (!sampled) {
+#pragma unroll
+    for (int c = 0; c < 6; ++c) g[c * cstride + e] = V{0, 0};
+    return;
+  }
+  const int i = it / mt, k = ip / mp;
+  double sd[3];
+  grid_direction(i, k, nth, nph, sd);
+  const R s[3] = {(R)sd[0], (R)sd[1], (R)sd[2]};
+  V E[3], H[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    E[c] = f[c * cstride + e];
+    H[c] = f[(3 + c) * cstride + e];
+  }
+  // E' = (E - (E.s) s) - Z0 s x (H - (H.s) s) = (E - (E.s) s) - Z0 s x H
+  const R der = E[0].x * s[0] + E[1].x * s[1] + E[2].x * s[2];
+  const R dei = E[0].y * s[0] + E[1].y * s[1] + E[2].y * s[2];
+  R er[3], ei[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    er[c] = E[c].x - der * s[c];
+    ei[c] = E[c].y - dei * s[c];
+  }
+  const R xr[3] = {s[1] * H[2].x - s[2] * H[1].x, s[2] * H[0].x - s[0] * H[2].x, s[0] * H[1].x - s[1] * H[0].x};
+  const R xi[3] = {s[1] * H[2].y - s[2] * H[1].y, s[2] * H[0].y - s[0] * H[2].y, s[0] * H[1].y - s[1] * H[0].y};
+  R pr[3], pi[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    pr[c] = er[c] - z0 * xr[c];
+    pi[c] = ei[c] - z0 * xi[c];
+  }
+  const R w = (R)dl_di[((int64_t)slot * nth + i) * nph + k];
+  // G_E = w E' ; G_H = w Z0 (s x E')
+  g[0 * cstride + e] = V{w * pr[0], w * pi[0]};
+  g[1 * cstride + e] = V{w * pr[1], w * pi[1]};
+  g[2 * cstride + e] = V{w * pr[2], w * pi[2]};
+  const R wz = w * z0;
+  g[3 * cstride + e] = V{wz * (s[1] * pr[2] - s[2] * pr[1]), wz * (s[1] * pi[2] - s[2] * pi[1])};
+  g[4 * cstride + e] = V{wz * (s[2] * pr[0] - s[0] * pr[2]), wz * (s[2] * pi[0] - s[0] * pi[2])};
+  g[5 * cstride + e] = V{wz * (s[0] * pr[1] - s[1] * pr[0]), wz * (s[0] * pi[1] - s[1] * pi[0])};
+}
+
+po_status launch_intensity_adjoint_f32(const float2 *fields, const float *dl_di, int n_slots, int T, int Phi, int nth,
+                                       int nph, int mt, int mp, float2 *G, cudaStream_t st) {
+  const int64_t cs = (int64_t)T * Phi;
+  if (cs <= 0 || n_slots <= 0) return PO_OK;
+  dim3 grid((unsigned)((cs + 255) / 256), (unsigned)n_slots);
+  k_intensity_adjoint<float2, float><<<grid, 256, 0, st>>>(fields, dl_di, T, Phi, nth, nph, mt, mp, (float)z0_host(),
+                                                          G);
+  count_launch();
+  PO_CUDA(cudaGetLastError());
+  return PO_OK;
+}
+
+po_status launch_intensity_adjoint_f64(const double2 *fields, const float *dl_di, int n_slots, int nth, int nph,
+                                       double2 *G, cudaStream_t st) {
+  const int64_t cs = (int64_t)nth * nph;
+  if (cs <= 0 || n_slots <= 0) return PO_OK;
+  dim3 grid((unsigned)((cs + 255) / 256), (unsigned)n_slots);
+  k_intensity_adjoint<double2, double><<<grid, 256, 0, st>>>(fields, dl_di, nth, nph, nth, nph, 1, 1, z0_host(), G);
+  count_launch();
+  PO_CUDA(cudaGetLastError());
+  return PO_OK;
+}
+
+// ------------------------------------------------------- point adjoint
+// One warp per (node, 32-point chunk); 4 warps per CTA.  A node's points are
+// [begin[node], begin[node+1]); its adjoint pattern is
+// G[slot][node * node_stride][6][ndir] about centre[3 * node * center_stride]
+// (node_stride = center_stride = 0 lets all chunks of a depth-0 sum share one
+// pattern and centre).  Every slot of the launch is accumulated into the
+// point's 7 gradients in registers and added to grad[7][n] once.
+constexpr int kAdjWarps = 4;
+constexpr int kAdjTile = 32;  // directions staged per step
+
+template <typename R>
+struct AdjVec;
+template <>
+struct AdjVec<float> {
+  using V = float2;
+};
+template <>
+struct AdjVec<double> {
+  using V = double2;
+};
+
+__device__ __forceinline__ void phase_exp(float ph, float *sn, float *cs) { sincos_small(ph, sn, cs); }
+__device__ __forceinline__ void phase_exp(double ph, double *sn, double *cs) { sincos(ph, sn, cs); }
+
+template <typename R>
+__global__ void __launch_bounds__(32 * kAdjWarps) k_point_adjoint(
+    const float *__restrict__ x, const float *__restrict__ y, const float *__restrict__ z,
+    const float *__restrict__ nx, const float *__restrict__ ny, const float *__restrict__ nz,
+    const float *__restrict__ area, const int32_t *__restrict__ begin, int64_t n_nodes,
+    const double *__restrict__ center, int center_stride, const typename AdjVec<R>::V *__restrict__ G,
+    int64_t node_stride, int64_t slot_stride, const float4 *__restrict__ dirs, const double *__restrict__ dirs_d,
+    int ndir, const SlotParams<double> *__restrict__ slots, int n_lambda, int Gc, int64_t n,
+    double *__restrict__ grad) {
+  using V = typename AdjVec<R>::V;
+  __shared__ V s_g[kAdjWarps][6][kAdjTile];
+  __shared__ R s_d[kAdjWarps][kAdjTile][3];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t node = (int64_t)blockIdx.x * kAdjWarps + warp;
+  if (node >= n_nodes) return;
+  const int b = begin[node], e = begin[node + 1];
+  const double *ctr = center + 3 * node * center_stride;
+  const double cx_ = ctr[0], cy_ = ctr[1], cz_ = ctr[2];
+  for (int c0 = b; c0 < e; c0 += 32) {
+    const int p = c0 + lane;
+    const bool ok = p < e;
+    const float px = ok ? x[p] : 0.f, py = ok ? y[p] : 0.f, pz = ok ? z[p] : 0.f;
+    double gacc[kNT];
+#pragma unroll
+    for (int i = 0; i < kNT; ++i) gacc[i] = 0.0;
+    for (int lam = 0; lam < n_lambda; ++lam) {
+      const double k0 = slots[lam * Gc].k0d;
+      const R ux = (R)(k0 * ((double)px - cx_)), uy = (R)(k0 * ((double)py - cy_)), uz = (R)(k0 * ((double)pz - cz_));
+      for (int g = 0; g < Gc; ++g) {
+        const int slot = lam * Gc + g;
+        const V *gp = G + slot * slot_stride + node * node_stride;
+        R ar[4][6], ai[4][6];
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+#pragma unroll
+          for (int c = 0; c < 6; ++c) ar[a][c] = ai[a][c] = (R)0;
+        for (int d0 = 0; d0 < ndir; d0 += kAdjTile) {
+          __syncwarp();
+          const int d = d0 + lane;
+          if (dirs_d) {  // FP64 directions
+#pragma unroll
+            for (int a = 0; a < 3; ++a) s_d[warp][lane][a] = d < ndir ? (R)dirs_d[3 * (int64_t)d + a] : (R)0;
+          } else {
+            const float4 f = d < ndir ? dirs[d] : make_float4(0.f, 0.f, 0.f, 0.f);
+            s_d[warp][lane][0] = (R)f.x;
+            s_d[warp][lane][1] = (R)f.y;
+            s_d[warp][lane][2] = (R)f.z;
+          }
+#pragma unroll
+          for (int c = 0; c < 6; ++c) s_g[warp][c][lane] = d < ndir ? gp[(int64_t)c * ndir + d] : V{0, 0};
+          __syncwarp();
+          const int cnt = ndir - d0 < kAdjTile ? ndir - d0 : kAdjTile;
+          for (int q = 0; q < cnt; ++q) {
+            const R sx = s_d[warp][q][0], sy = s_d[warp][q][1], sz = s_d[warp][q][2];
+            const R ph = -(ux * sx + uy * sy + uz * sz);
+            R sn, cs;
+            phase_exp(ph, &sn, &cs);
+            const R w[4] = {(R)1, sx, sy, sz};
+#pragma unroll
+            for (int c = 0; c < 6; ++c) {
+              const V gv = s_g[warp][c][q];
+              const R tr = gv.x * cs - gv.y * sn, ti = gv.x * sn + gv.y * cs;
+#pragma unroll
+              for (int a = 0; a < 4; ++a) {
+                ar[a][c] += w[a] * tr;
+                ai[a][c] += w[a] * ti;
+              }
+            }
+          }
+        }
+        if (!ok) continue;
+        CD C[6];
+        tangent_plane_jvp(slots[slot], px, py, pz, nx[p], ny[p], nz[p], area[p], C);
+#pragma unroll
+        for (int i = 0; i < kNT; ++i) {
+          double s = 0.0;
+#pragma unroll
+          for (int c = 0; c < 6; ++c) s += (double)ar[0][c] * C[c].re.d[i] + (double)ai[0][c] * C[c].im.d[i];
+          gacc[i] += 2.0 * s;
+        }
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+          double im = 0.0;  // Im(sum_c conj(A^a_c) C_c)
+#pragma unroll
+          for (int c = 0; c < 6; ++c) im += (double)ar[a + 1][c] * C[c].im.v - (double)ai[a + 1][c] * C[c].re.v;
+          gacc[a] += -2.0 * k0 * im;
+        }
+      }
+    }
+    if (ok) {
+#pragma unroll
+      for (int i = 0; i < kNT; ++i) grad[(int64_t)i * n + p] += gacc[i];
+    }
+  }
+}
+
+template <typename R>
+static po_status launch_point_adjoint_t(const float *const g[7], const int32_t *begin, int64_t n_nodes,
+                                        const double *center, int center_stride, const void *G, int64_t node_stride,
+                                        int64_t slot_stride, const float4 *dirs, const double *dirs_d, int ndir,
+                                        const SlotParams<double> *slots, int n_lambda, int Gc, int64_t n,
+                                        double *grad, cudaStream_t st) {
+  if (n_nodes <= 0 || n_lambda <= 0 || Gc <= 0) return PO_OK;
+  const int64_t blocks = (n_nodes + kAdjWarps - 1) / kAdjWarps;
+  if (blocks > 2147483647LL) return fail(PO_ERR_UNSUPPORTED, "too many nodes for one launch");
+  k_point_adjoint<R><<<(unsigned)blocks, 32 * kAdjWarps, 0, st>>>(
+      g[0], g[1], g[2], g[3], g[4], g[5], g[6], begin, n_nodes, center, center_stride,
+      (const typename AdjVec<R>::V *)G, node_stride, slot_stride, dirs, dirs_d, ndir, slots, n_lambda, Gc, n, grad);
+  count_launch();
+  PO_CUDA(cudaGetLastError());
+  return PO_OK;
+}
+
+po_status launch_point_adjoint_f32(const float *const g[7], const int32_t *begin, int64_t n_nodes,
+                                   const double *center, int center_stride, const float2 *G, int64_t node_stride,
+                                   int64_t slot_stride, const float4 *dirs, int ndir, const SlotParams<double> *slots,
+                                   int n_lambda, int Gc, int64_t n, double *grad, cudaStream_t st) {
+  return launch_point_adjoint_t<float>(g, begin, n_nodes, center, center_stride, G, node_stride, slot_stride, dirs,
+                                       nullptr, ndir, slots, n_lambda, Gc, n, grad, st);
+}
+
+po_status launch_point_adjoint_f64(const float *const g[7], const int32_t *begin, int64_t n_nodes,
+                                   const double *center, int center_stride, const double2 *G, int64_t node_stride,
+                                   int64_t slot_stride, const double *dirs_d, int ndir, const SlotParams<double> *slots,
+                                   int n_lambda, int Gc, int64_t n, double *grad, cudaStream_t st) {
+  return launch_point_adjoint_t<double>(g, begin, n_nodes, center, center_stride, G, node_stride, slot_stride,
+                                        nullptr, dirs_d, ndir, slots, n_lambda, Gc, n, grad, st);
+}
+
+// chunk starts 0, 32, 64, ... n (the depth-0 adjoint treats every 32 points as a node)
+__global__ void k_chunk_begin(int32_t *begin, int64_t nchunk, int64_t n) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i <= nchunk) begin[i] = (int32_t)(i * 32 < n ? i * 32 : n);
+}
+
+po_status launch_chunk_begin(int32_t *begin, int64_t n, cudaStream_t st) {
+  const int64_t nchunk = (n + 31) / 32;
+  k_chunk_begin<<<(unsigned)((nchunk + 256) / 256), 256, 0, st>>>(begin, nchunk, n);
+  count_launch();
+  PO_CUDA(cudaGetLastError());
+  return PO_OK;
+}
+
+// grad_out[k][perm[i]] = (float) grad_sorted[k][i]  (perm = NULL: identity)
+__global__ void k_scatter_grad(const double *__restrict__ gs, const int32_t *__restrict__ perm, int64_t n,
+                               float *__restrict__ out) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int64_t dst = perm ? perm[i] : i;
+#pragma unroll
+  for (int k = 0; k < kNT; ++k) out[(int64_t)k * n + dst] = (float)gs[(int64_t)k * n + i];
+}
+
+po_status launch_scatter_grad(const double *grad_sorted, const int32_t *perm, int64_t n, float *out, cudaStream_t st) {
+  if (n <= 0) return PO_OK;
+  k_scatter_grad<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(grad_sorted, perm, n, out);
+  count_launch();
+  PO_CUDA(cudaGetLastError());
+  return PO_OK;
+}
+
+}  // namespace wavepo

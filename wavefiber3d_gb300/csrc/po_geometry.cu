@@ -109,6 +109,119 @@ __global__ void __launch_bounds__(kTile * kRows) k_height_field(const float *__r
   if (bad) atomicOr(err, 1);
 }
 
+// ---------------------------------------------------------------- adjoint
+// d(sample)/d(vertex xy) of one quad by forward mode in FP64: 8 tangents,
+// (x, y) of p1, p2, p3, p4.
+struct D8 {
+  double v, d[8];
+};
+__device__ __forceinline__ D8 c8(double v) {
+  D8 r;
+  r.v = v;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) r.d[i] = 0.0;
+  return r;
+}
+__device__ __forceinline__ D8 var8(double v, int i) {
+  D8 r = c8(v);
+  r.d[i] = 1.0;
+  return r;
+}
+__device__ __forceinline__ D8 operator+(const D8 &a, const D8 &b) {
+  D8 r;
+  r.v = a.v + b.v;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) r.d[i] = a.d[i] + b.d[i];
+  return r;
+}
+__device__ __forceinline__ D8 operator-(const D8 &a, const D8 &b) {
+  D8 r;
+  r.v = a.v - b.v;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) r.d[i] = a.d[i] - b.d[i];
+  return r;
+}
+__device__ __forceinline__ D8 operator*(const D8 &a, const D8 &b) {
+  D8 r;
+  r.v = a.v * b.v;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) r.d[i] = a.d[i] * b.v + a.v * b.d[i];
+  return r;
+}
+__device__ __forceinline__ D8 scale8(const D8 &a, double s) {
+  D8 r;
+  r.v = a.v * s;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) r.d[i] = a.d[i] * s;
+  return r;
+}
+__device__ __forceinline__ D8 sqrt8(const D8 &a) {
+  D8 r;
+  r.v = sqrt(a.v);
+  const double f = r.v > 0 ? 0.5 / r.v : 0.0;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) r.d[i] = a.d[i] * f;
+  return r;
+}
+__device__ __forceinline__ D8 div8(const D8 &a, const D8 &b) {
+  D8 r;
+  const double ib = 1.0 / b.v;
+  r.v = a.v * ib;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) r.d[i] = (a.d[i] - r.v * b.d[i]) * ib;
+  return r;
+}
+struct V8 {
+  D8 x, y, z;
+};
+__device__ __forceinline__ V8 sub8(const V8 &a, const V8 &b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ V8 cross8(const V8 &a, const V8 &b) {
+  return {a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, b.y * a.x - a.y * b.x};
+}
+__device__ __forceinline__ D8 norm8(const V8 &a) { return sqrt8(a.x * a.x + a.y * a.y + a.z * a.z); }
+
+// One thread per quad: gh[2][numel][numelvert] (double, zeroed) += J^T g.
+__global__ void k_height_field_adjoint(const float *__restrict__ hx, const float *__restrict__ hy, int numel,
+                                       int numelvert, float unitz, float half_period, int ring_begin, int ring_end,
+                                       const float *__restrict__ gs, int64_t n, double *__restrict__ ghx,
+                                       double *__restrict__ ghy) {
+  const int ncol = ring_end - ring_begin + 1;
+  const int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (o >= n) return;
+  const int i = (int)(o / ncol), j = ring_begin + (int)(o % ncol);
+  const int pj = j < numel - 1 ? j + 1 : 0, zi = i < numelvert - 1 ? i + 1 : i;
+  const int64_t v[4] = {(int64_t)j * numelvert + i, (int64_t)pj * numelvert + i, (int64_t)j * numelvert + zi,
+                        (int64_t)pj * numelvert + zi};
+  const double z = (double)__fsub_rn(__fmul_rn((float)i, unitz), half_period);
+  const double zn = (double)__fsub_rn(__fmul_rn((float)(i + 1), unitz), half_period);
+  V8 p[4];
+  for (int q = 0; q < 4; ++q)
+    p[q] = {var8(hx[v[q]], 2 * q), var8(hy[v[q]], 2 * q + 1), c8(q < 2 ? z : zn)};
+  const V8 a1 = cross8(sub8(p[1], p[0]), sub8(p[2], p[0]));
+  const V8 a2 = cross8(sub8(p[3], p[1]), sub8(p[2], p[1]));
+  const V8 sm = {a1.x + a2.x, a1.y + a2.y, a1.z + a2.z};
+  const D8 ns = norm8(sm);
+  const D8 area = scale8(norm8(a1) + norm8(a2), 0.5);
+  const D8 nrm[3] = {div8(sm.x, ns), div8(sm.y, ns), div8(sm.z, ns)};
+  const double g[7] = {gs[o], gs[n + o], gs[2 * n + o], gs[3 * n + o], gs[4 * n + o], gs[5 * n + o], gs[6 * n + o]};
+  double acc[8];
+#pragma unroll
+  for (int t = 0; t < 8; ++t) {
+    // x = mean of the vertex x (tangent 2q), y = mean of the vertex y (2q+1); z has no xy dependence
+    acc[t] = 0.25 * ((t & 1) ? g[1] : g[0]) + g[3] * nrm[0].d[t] + g[4] * nrm[1].d[t] + g[5] * nrm[2].d[t] +
+             g[6] * area.d[t];
+  }
+  for (int q = 0; q < 4; ++q) {
+    atomicAdd(ghx + v[q], acc[2 * q]);
+    atomicAdd(ghy + v[q], acc[2 * q + 1]);
+  }
+}
+
+__global__ void k_narrow_f64(const double *__restrict__ in, float *__restrict__ out, int64_t n) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) out[i] = (float)in[i];
+}
+
 }  // namespace
 
 po_status launch_height_field(const float *height, int numel, int numelvert, float period, float unitz, int ring_begin,
@@ -152,5 +265,36 @@ extern "C" po_status po_height_field_points(const float *height, int numel, int 
   }
   cudaFreeAsync(err, st);
   if (s == PO_OK && h_err) return fail(PO_ERR_INVALID_ARGUMENT, "height field has a vertex at the origin (x == y == 0)");
+  return s;
+}
+
+extern "C" po_status po_height_field_adjoint(const float *height, int numel, int numelvert, float period, float unitz,
+                                             int ring_begin, int ring_end, const float *grad_samples,
+                                             float *grad_height, void *stream) {
+  if (!height || !grad_samples || !grad_height) return fail(PO_ERR_INVALID_ARGUMENT, "null pointer");
+  if (numel < 2 || numelvert < 1) return fail(PO_ERR_INVALID_ARGUMENT, "numel must be >= 2 and numelvert >= 1");
+  if (ring_begin < 0 || ring_end < ring_begin || ring_end >= numel)
+    return fail(PO_ERR_INVALID_ARGUMENT, "ring range must satisfy 0 <= begin <= end < numel");
+  if ((int64_t)numel * numelvert > (int64_t)1 << 30) return fail(PO_ERR_INVALID_ARGUMENT, "height field too large");
+  if (!(unitz > 0) || !std::isfinite(period)) return fail(PO_ERR_INVALID_ARGUMENT, "unitz must be > 0");
+  cudaStream_t st = (cudaStream_t)stream;
+  const int64_t nv = 2 * (int64_t)numel * numelvert;
+  const int64_t n = (int64_t)(ring_end - ring_begin + 1) * numelvert;
+  double *acc = nullptr;
+  PO_CUDA(cudaMallocAsync((void **)&acc, sizeof(double) * nv, st));
+  po_status s = PO_OK;
+  cudaError_t e = cudaMemsetAsync(acc, 0, sizeof(double) * nv, st);
+  if (e != cudaSuccess) s = cuda_fail(e, "cudaMemsetAsync");
+  if (s == PO_OK) {
+    k_height_field_adjoint<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(
+        height, height + (int64_t)numel * numelvert, numel, numelvert, unitz, period * 0.5f, ring_begin, ring_end,
+        grad_samples, n, acc, acc + (int64_t)numel * numelvert);
+    count_launch();
+    k_narrow_f64<<<(unsigned)((nv + 255) / 256), 256, 0, st>>>(acc, grad_height, nv);
+    count_launch();
+    e = cudaGetLastError();
+    if (e != cudaSuccess) s = cuda_fail(e, "height field adjoint launch");
+  }
+  cudaFreeAsync(acc, st);
   return s;
 }

@@ -59,30 +59,22 @@ static float bf16_to_f(uint16_t h) {
 // (mirror) the partner half column rows 0..Rc-1.
 size_t theta_matrix_words(int Rp, int Kp) { return (size_t)((Rp + 15) / 16) * (Kp / 16) * 32 * 8; }
 
-void build_theta_matrix(int Tc, int Tp, int Rc, int Rp, int mirror, int Kp, std::vector<uint32_t> &out) {
-  const int K = mirror ? 2 * Rc : Rc;
-  const int nth_c = Tc / 2;
-  std::vector<double> M((size_t)Rp * Kp, 0.0);
-  for (int r = 0; r < Rp; ++r) {
-    for (int t = 0; t < Rc; ++t) M[(size_t)r * Kp + t] = trig_kernel(Tc, (double)r / Tp - (double)t / Tc);
-    if (mirror)
-      for (int s = 1; s < nth_c; ++s) M[(size_t)r * Kp + Rc + s] = trig_kernel(Tc, (double)r / Tp - (double)(Tc - s) / Tc);
-  }
-  (void)K;
-  const int MT = (Rp + 15) / 16, KS = Kp / 16;
-  out.assign(theta_matrix_words(Rp, Kp), 0u);
+// dense M (rows x Kp, row-major) -> A fragments (split hi + lo bf16)
+static void a_fragments(const std::vector<double> &M, int rows, int Kp, std::vector<uint32_t> &out) {
+  const int MT = (rows + 15) / 16, KS = Kp / 16;
+  out.assign(theta_matrix_words(rows, Kp), 0u);
   for (int mt = 0; mt < MT; ++mt)
     for (int ks = 0; ks < KS; ++ks)
       for (int lane = 0; lane < 32; ++lane) {
         const int g = lane >> 2, tq = lane & 3;
-        const int rows[4] = {mt * 16 + g, mt * 16 + g + 8, mt * 16 + g, mt * 16 + g + 8};
-        const int cols[4] = {ks * 16 + 2 * tq, ks * 16 + 2 * tq, ks * 16 + 2 * tq + 8, ks * 16 + 2 * tq + 8};
+        const int rr[4] = {mt * 16 + g, mt * 16 + g + 8, mt * 16 + g, mt * 16 + g + 8};
+        const int cc[4] = {ks * 16 + 2 * tq, ks * 16 + 2 * tq, ks * 16 + 2 * tq + 8, ks * 16 + 2 * tq + 8};
         uint32_t *dst = &out[(((size_t)mt * KS + ks) * 32 + lane) * 8];
         for (int q = 0; q < 4; ++q) {
           uint16_t h[2], l[2];
           for (int e = 0; e < 2; ++e) {
-            int r = rows[q], c = cols[q] + e;
-            double v = (r < Rp && c < Kp) ? M[(size_t)r * Kp + c] : 0.0;
+            int r = rr[q], c = cc[q] + e;
+            double v = (r < rows && c < Kp) ? M[(size_t)r * Kp + c] : 0.0;
             h[e] = bf16_rne((float)v);
             l[e] = bf16_rne((float)(v - (double)bf16_to_f(h[e])));
           }
@@ -90,6 +82,38 @@ void build_theta_matrix(int Tc, int Tp, int Rc, int Rp, int mirror, int Kp, std:
           dst[4 + q] = (uint32_t)l[0] | ((uint32_t)l[1] << 16);
         }
       }
+}
+
+// theta interpolation of one level: parent row r from the child's own half
+// column (rows t < Rc) and, mirrored, its partner half column (rows s)
+static double theta_own(int Tc, int Tp, int r, int t) { return trig_kernel(Tc, (double)r / Tp - (double)t / Tc); }
+static double theta_partner(int Tc, int Tp, int r, int s) {
+  return trig_kernel(Tc, (double)r / Tp - (double)(Tc - s) / Tc);
+}
+
+void build_theta_matrix(int Tc, int Tp, int Rc, int Rp, int mirror, int Kp, std::vector<uint32_t> &out) {
+  const int nth_c = Tc / 2;
+  std::vector<double> M((size_t)Rp * Kp, 0.0);
+  for (int r = 0; r < Rp; ++r) {
+    for (int t = 0; t < Rc; ++t) M[(size_t)r * Kp + t] = theta_own(Tc, Tp, r, t);
+    if (mirror)
+      for (int s = 1; s < nth_c; ++s) M[(size_t)r * Kp + Rc + s] = theta_partner(Tc, Tp, r, s);
+  }
+  a_fragments(M, Rp, Kp, out);
+}
+
+// Transpose of the mirrored theta map (double cover only): child row t of a
+// half column pair from the parent's own column (K = r < Rp) and its partner
+// (K = Rp + r):  [A_own^T | A_partner^T], rows t < Rc.
+void build_theta_matrix_adj(int Tc, int Tp, int Rc, int Rp, int Kp, std::vector<uint32_t> &out) {
+  const int nth_c = Tc / 2;
+  std::vector<double> M((size_t)Rc * Kp, 0.0);
+  for (int t = 0; t < Rc; ++t)
+    for (int r = 0; r < Rp; ++r) {
+      M[(size_t)t * Kp + r] = theta_own(Tc, Tp, r, t);
+      if (t >= 1 && t < nth_c) M[(size_t)t * Kp + Rp + r] = theta_partner(Tc, Tp, r, t);
+    }
+  a_fragments(M, Rc, Kp, out);
 }
 
 // ---------------------------------------------------------- device side
@@ -248,6 +272,138 @@ po_status launch_interp_cols_mma(const float2 *mid, float2 *parent, const int32_
   return PO_OK;
 }
 
+// ----------------------------------------------- transposed theta pass
+// Adjoint of k_interp_cols_mma for one child: its parent's adjoint pattern
+// times exp(-i k s.(c_child - c_parent)) on the parent grid, then the
+// transposed mirrored theta map [A_own^T | A_partner^T] (rows t < Rc, K over
+// the parent's own and partner half columns).  Every child writes its own
+// output, so there is no reduction.  CTA: one (child, component, slot) and
+// NCC complex columns (NCC/2 mirror pairs), 4 warps over the 16-row tiles.
+template <int NCC>
+__global__ void __launch_bounds__(128) k_interp_cols_adj_mma(
+    const float2 *__restrict__ parent_adj, float2 *__restrict__ mid_adj, const int32_t *__restrict__ child_parent,
+    const uint32_t *__restrict__ child_prefix, int64_t n_parent, int64_t n_child, int phi, int Rc, int Rp, int Kp,
+    const uint4 *__restrict__ Afrag, const float4 *__restrict__ trans, int G) {
+  constexpr int NT = NCC / 4;
+  constexpr int TW = NCC / 2;
+  extern __shared__ uint4 smem_u4[];
+  const int KS = Kp / 16, MT = (Rc + 15) / 16;
+  uint4 *Bf = smem_u4;                                   // [KS][NT][32]
+  float2 *tile = (float2 *)(Bf + (size_t)KS * NT * 32);  // [Rp][NCC]
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, tq = lane & 3;
+  const int span = phi / 2;
+  const int ntile = (span + TW - 1) / TW;
+  const int j0 = (int)(blockIdx.x % ntile) * TW;
+  const int64_t cc = blockIdx.x / ntile;
+  const int64_t c = cc / 6;
+  const int comp = (int)(cc % 6);
+  const int slot = blockIdx.z, lam = slot / G;
+  auto col_of = [&](int q) { return q < TW ? j0 + q : j0 + (q - TW) + phi / 2; };
+  auto ok_of = [&](int q) { return j0 + (q < TW ? q : q - TW) < span; };
+  auto partner_of = [&](int q) { return q < TW ? q + TW : q - TW; };
+  const int64_t p = child_parent[c];
+  const int o = (int)(child_prefix[c] & 7u);
+  const float sgx = (o & 1) ? 1.f : -1.f, sgy = (o & 2) ? -1.f : 1.f, sgz = (o & 4) ? -1.f : 1.f;
+  const float4 *tr = trans + (int64_t)lam * Rp * phi;
+  const float2 *src = parent_adj + (((int64_t)slot * n_parent + p) * 6 + comp) * (int64_t)Rp * phi;
+  for (int e = threadIdx.x; e < Rp * NCC; e += blockDim.x) {
+    const int r = e / NCC, q = e - r * NCC;
+    float2 v = make_float2(0.f, 0.f);
+    if (ok_of(q)) {
+      const int j = col_of(q);
+      const float2 a = src[(int64_t)r * phi + j];
+      const float4 rr = tr[(int64_t)r * phi + j];
+      float sn, cs;
+      sincos_small(fmaf(sgx, rr.x, fmaf(sgy, rr.y, sgz * rr.z)), &sn, &cs);
+      v = make_float2(a.x * cs + a.y * sn, a.y * cs - a.x * sn);  // a * exp(-i ph)
+    }
+    tile[e] = v;
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < KS * NT * 32; e += blockDim.x) {
+    const int ln = e & 31, nt = (e >> 5) % NT, ks = (e >> 5) / NT;
+    const int n = nt * 8 + (ln >> 2), q = n >> 1, part = n & 1;
+    const int kb = ks * 16 + 2 * (ln & 3);
+    float v[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int kk = kb + (u & 1) + (u >> 1) * 8;
+      float2 x = make_float2(0.f, 0.f);
+      if (kk < Rp) x = tile[kk * NCC + q];
+      else if (kk < 2 * Rp) x = tile[(kk - Rp) * NCC + partner_of(q)];
+      v[u] = part ? x.y : x.x;
+    }
+    uint32_t h0, l0, h1, l1;
+    split_bf16x2(v[0], v[1], h0, l0);
+    split_bf16x2(v[2], v[3], h1, l1);
+    Bf[e] = make_uint4(h0, h1, l0, l1);
+  }
+  __syncthreads();
+  float2 *dst = mid_adj + (((int64_t)slot * n_child + c) * 6 + comp) * (int64_t)Rc * phi;
+  for (int mt = warp; mt < MT; mt += 4) {
+    float d[NT][4];
+#pragma unroll
+    for (int nt = 0; nt < NT; ++nt) d[nt][0] = d[nt][1] = d[nt][2] = d[nt][3] = 0.f;
+    const uint4 *ap = Afrag + ((size_t)mt * KS) * 64 + lane * 2;
+    for (int ks = 0; ks < KS; ++ks) {
+      const uint4 ah = __ldg(ap + (size_t)ks * 64), al = __ldg(ap + (size_t)ks * 64 + 1);
+      const uint32_t a_hi[4] = {ah.x, ah.y, ah.z, ah.w}, a_lo[4] = {al.x, al.y, al.z, al.w};
+#pragma unroll
+      for (int nt = 0; nt < NT; ++nt) {
+        const uint4 b = Bf[((size_t)ks * NT + nt) * 32 + lane];
+        const uint32_t b_hi[2] = {b.x, b.y}, b_lo[2] = {b.z, b.w};
+        mma_bf16(d[nt], a_hi, b_hi);
+        mma_bf16(d[nt], a_hi, b_lo);
+        mma_bf16(d[nt], a_lo, b_hi);
+      }
+    }
+#pragma unroll
+    for (int nt = 0; nt < NT; ++nt) {
+      const int q = nt * 4 + tq;
+      if (!ok_of(q)) continue;
+      const int j = col_of(q);
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int t = mt * 16 + g + 8 * h;
+        if (t < Rc) dst[(int64_t)t * phi + j] = make_float2(d[nt][2 * h], d[nt][2 * h + 1]);
+      }
+    }
+  }
+}
+
+static size_t cols_adj_smem(int ncc, int Rp, int Kp) {
+  return sizeof(uint4) * (size_t)(Kp / 16) * (ncc / 4) * 32 + sizeof(float2) * (size_t)Rp * ncc;
+}
+
+po_status launch_interp_cols_adj_mma(const float2 *parent_adj, float2 *mid_adj, const int32_t *child_parent,
+                                     const uint32_t *child_prefix, int64_t n_parent, int64_t n_child, int phi, int Rc,
+                                     int Rp, int Kp, const uint32_t *Afrag, const float4 *trans, int n_slots, int G,
+                                     cudaStream_t st) {
+  if (n_child <= 0 || n_slots <= 0) return PO_OK;
+  if (Kp % 16 || Kp < 2 * Rp) return fail(PO_ERR_INTERNAL, "adjoint theta matrix K padding");
+  if (phi % 2) return fail(PO_ERR_INTERNAL, "mirrored storage needs an even phi grid");
+  int ncc = 16;
+  if (cols_adj_smem(ncc, Rp, Kp) > 100 * 1024 || phi / 2 <= 4) ncc = 8;
+  const size_t smem = cols_adj_smem(ncc, Rp, Kp);
+  if (smem > 227 * 1024) return fail(PO_ERR_UNSUPPORTED, "angular grid too large for the adjoint theta pass");
+  const int TW = ncc / 2;
+  int64_t gx = (int64_t)((phi / 2 + TW - 1) / TW) * n_child * 6;
+  if (gx > 2147483647LL || n_slots > 65535) return fail(PO_ERR_UNSUPPORTED, "too many nodes for one launch");
+  dim3 grid((unsigned)gx, 1u, (unsigned)n_slots);
+  if (ncc == 16) {
+    PO_CUDA(cudaFuncSetAttribute(k_interp_cols_adj_mma<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_interp_cols_adj_mma<16><<<grid, 128, smem, st>>>(parent_adj, mid_adj, child_parent, child_prefix, n_parent,
+                                                       n_child, phi, Rc, Rp, Kp, (const uint4 *)Afrag, trans, G);
+  } else {
+    PO_CUDA(cudaFuncSetAttribute(k_interp_cols_adj_mma<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_interp_cols_adj_mma<8><<<grid, 128, smem, st>>>(parent_adj, mid_adj, child_parent, child_prefix, n_parent,
+                                                      n_child, phi, Rc, Rp, Kp, (const uint4 *)Afrag, trans, G);
+  }
+  count_launch();
+  PO_CUDA(cudaGetLastError());
+  return PO_OK;
+}
+
 // ---------------------------------------------------------------- row pass
 // The phi half of interpFFT (interpolation.h:17-45) is out[r][j'] =
 // sum_j K_{Phi_c}(j'/Phi_p - j/Phi_c) in[r][j] for every stored row r.  As a
@@ -258,9 +414,11 @@ po_status launch_interp_cols_mma(const float2 *mid, float2 *parent, const int32_
 // in fragment order  Bm[ntile][kstep][lane] = {hi0, hi1, lo0, lo1}.
 size_t phi_matrix_words(int Pp, int Kp) { return (size_t)((Pp + 7) / 8) * (Kp / 16) * 32 * 4; }
 
-void build_phi_matrix(int Pc, int Pp, int Kp, std::vector<uint32_t> &out) {
-  const int NTt = (Pp + 7) / 8, KS = Kp / 16;
-  out.assign(phi_matrix_words(Pp, Kp), 0u);
+// B operand of the row kernel for out[n] = sum_k W(n, k) in[k], n < Pout, k < Kin
+template <typename F>
+static void b_fragments(int Pout, int Kin, int Kp, F W, std::vector<uint32_t> &out) {
+  const int NTt = (Pout + 7) / 8, KS = Kp / 16;
+  out.assign(phi_matrix_words(Pout, Kp), 0u);
   for (int nt = 0; nt < NTt; ++nt)
     for (int ks = 0; ks < KS; ++ks)
       for (int lane = 0; lane < 32; ++lane) {
@@ -268,7 +426,7 @@ void build_phi_matrix(int Pc, int Pp, int Kp, std::vector<uint32_t> &out) {
         const int ks4[4] = {kb, kb + 1, kb + 8, kb + 9};
         uint16_t h[4], l[4];
         for (int u = 0; u < 4; ++u) {
-          double v = (n < Pp && ks4[u] < Pc) ? trig_kernel(Pc, (double)n / Pp - (double)ks4[u] / Pc) : 0.0;
+          double v = (n < Pout && ks4[u] < Kin) ? W(n, ks4[u]) : 0.0;
           h[u] = bf16_rne((float)v);
           l[u] = bf16_rne((float)(v - (double)bf16_to_f(h[u])));
         }
@@ -278,6 +436,15 @@ void build_phi_matrix(int Pc, int Pp, int Kp, std::vector<uint32_t> &out) {
         dst[2] = (uint32_t)l[0] | ((uint32_t)l[1] << 16);
         dst[3] = (uint32_t)l[2] | ((uint32_t)l[3] << 16);
       }
+}
+
+void build_phi_matrix(int Pc, int Pp, int Kp, std::vector<uint32_t> &out) {
+  b_fragments(Pp, Pc, Kp, [&](int n, int k) { return trig_kernel(Pc, (double)n / Pp - (double)k / Pc); }, out);
+}
+
+// transpose of the phi map: child column j (< Pc) from parent columns j' (< Pp)
+void build_phi_matrix_adj(int Pc, int Pp, int Kp, std::vector<uint32_t> &out) {
+  b_fragments(Pc, Pp, Kp, [&](int j, int jp) { return trig_kernel(Pc, (double)jp / Pp - (double)j / Pc); }, out);
 }
 
 // One warp per block of 8 rows; n-tiles in groups of kRowNG (accumulators in

@@ -77,6 +77,13 @@ size_t phi_matrix_words(int Pp, int Kp);
 void build_phi_matrix(int Pc, int Pp, int Kp, std::vector<uint32_t> &out);
 po_status launch_interp_rows_mma(const float2 *src, float2 *dst, int64_t nrows, int Pc, int Pp, int Kp,
                                  const uint32_t *Bm, int sm_count, cudaStream_t st);
+// adjoint (transposed) passes, double cover only (po_interp_mma.cu)
+void build_theta_matrix_adj(int Tc, int Tp, int Rc, int Rp, int Kp, std::vector<uint32_t> &out);
+void build_phi_matrix_adj(int Pc, int Pp, int Kp, std::vector<uint32_t> &out);
+po_status launch_interp_cols_adj_mma(const float2 *parent_adj, float2 *mid_adj, const int32_t *child_parent,
+                                     const uint32_t *child_prefix, int64_t n_parent, int64_t n_child, int phi, int Rc,
+                                     int Rp, int Kp, const uint32_t *Afrag, const float4 *trans, int n_slots, int G,
+                                     cudaStream_t st);
 po_status launch_trans_table(const double *k_per_lambda, int n_lambda, int nth, int Rp, int phi, const double a[3],
                              float4 *out, cudaStream_t st);
 
@@ -84,6 +91,22 @@ po_status launch_trans_table(const double *k_per_lambda, int n_lambda, int nth, 
 // out = {x, y, z, nx, ny, nz, area}; err |= 1 on a vertex at the origin (po_geometry.cu)
 po_status launch_height_field(const float *height, int numel, int numelvert, float period, float unitz, int ring_begin,
                               int ring_end, float *const out[7], int *err, cudaStream_t st);
+
+// adjoint of the intensity and of the far-field sums (po_adjoint.cu)
+po_status launch_intensity_adjoint_f32(const float2 *fields, const float *dl_di, int n_slots, int T, int Phi, int nth,
+                                       int nph, int mt, int mp, float2 *G, cudaStream_t st);
+po_status launch_intensity_adjoint_f64(const double2 *fields, const float *dl_di, int n_slots, int nth, int nph,
+                                       double2 *G, cudaStream_t st);
+po_status launch_point_adjoint_f32(const float *const g[7], const int32_t *begin, int64_t n_nodes,
+                                   const double *center, int center_stride, const float2 *G, int64_t node_stride,
+                                   int64_t slot_stride, const float4 *dirs, int ndir, const SlotParams<double> *slots,
+                                   int n_lambda, int Gc, int64_t n, double *grad, cudaStream_t st);
+po_status launch_point_adjoint_f64(const float *const g[7], const int32_t *begin, int64_t n_nodes,
+                                   const double *center, int center_stride, const double2 *G, int64_t node_stride,
+                                   int64_t slot_stride, const double *dirs_d, int ndir, const SlotParams<double> *slots,
+                                   int n_lambda, int Gc, int64_t n, double *grad, cudaStream_t st);
+po_status launch_chunk_begin(int32_t *begin, int64_t n, cudaStream_t st);
+po_status launch_scatter_grad(const double *grad_sorted, const int32_t *perm, int64_t n, float *out, cudaStream_t st);
 
 // intensity: fields [slot][comp][T][Phi] (root, possibly supersampled by
 // (mt, mp)) -> out [slot][nth][nph]

@@ -139,6 +139,11 @@ struct po_ctx {
   size_t bmat_off[PO_MAX_DEPTH] = {};
   int bmat_kp[PO_MAX_DEPTH] = {};
   DevBuf amat, bmat;
+  // transposed level matrices of the adjoint (built on the first po_grad)
+  bool adj_ready = false;
+  size_t amat_adj_off[PO_MAX_DEPTH] = {}, bmat_adj_off[PO_MAX_DEPTH] = {};
+  int amat_adj_kp[PO_MAX_DEPTH] = {}, bmat_adj_kp[PO_MAX_DEPTH] = {};
+  DevBuf amat_adj, bmat_adj, slots64, grad_acc, chunk_begin, center0;
   std::map<int, int> tw_offset;
   DevBuf twiddles;
   DevBuf geom_in, geom_sorted, octree_ws, leaf_ctr, dirs, dirs_d, trans, levelA, levelB, mid, slots, kvals, out,
@@ -369,8 +374,40 @@ static int chunk_slot_count(int64_t budget, double bytes_per_slot, int S) {
   return (int)std::max(1.0, std::min((double)S, c));
 }
 
+// Transposed level matrices for the adjoint aggregation (double cover and
+// tensor-core interpolation only).
+static po_status ensure_adjoint_matrices(po_ctx *c) {
+  if (c->adj_ready) return PO_OK;
+  const int d = c->depth;
+  std::vector<uint32_t> all, one, ball, bone;
+  for (int l = 0; l < d; ++l) {
+    c->amat_adj_kp[l] = (2 * c->R[l] + 15) / 16 * 16;
+    build_theta_matrix_adj(c->T[l + 1], c->T[l], c->R[l + 1], c->R[l], c->amat_adj_kp[l], one);
+    c->amat_adj_off[l] = all.size();
+    all.insert(all.end(), one.begin(), one.end());
+    c->bmat_adj_kp[l] = (c->Phi[l] + 15) / 16 * 16;
+    build_phi_matrix_adj(c->Phi[l + 1], c->Phi[l], c->bmat_adj_kp[l], bone);
+    c->bmat_adj_off[l] = ball.size();
+    ball.insert(ball.end(), bone.begin(), bone.end());
+  }
+  PO_TRY(c->amat_adj.ensure(sizeof(uint32_t) * std::max<size_t>(all.size(), 1)));
+  PO_TRY(c->bmat_adj.ensure(sizeof(uint32_t) * std::max<size_t>(ball.size(), 1)));
+  if (!all.empty()) PO_CUDA(cudaMemcpy(c->amat_adj.p, all.data(), sizeof(uint32_t) * all.size(), cudaMemcpyHostToDevice));
+  if (!ball.empty())
+    PO_CUDA(cudaMemcpy(c->bmat_adj.p, ball.data(), sizeof(uint32_t) * ball.size(), cudaMemcpyHostToDevice));
+  c->adj_ready = true;
+  return PO_OK;
+}
+
+// Adjoint request of po_grad: dL/dI on the output grid and the gradient out
+// (both device arrays; NULL for a plain solve).
+struct AdjointArgs {
+  const float *dl_di = nullptr;  // [S][n_theta][n_phi]
+  float *grad = nullptr;         // [7][n]
+};
+
 static po_status solve_impl(po_ctx *c, const po_geometry *g, const po_illum *il, float *intensity, int out_on_device,
-                            cudaStream_t st, po_report *rep) {
+                            cudaStream_t st, po_report *rep, const AdjointArgs *adj = nullptr) {
   const po_config &cfg = c->cfg;
   const int d = c->depth;
   const int64_t n = g->n;
@@ -408,7 +445,7 @@ static po_status solve_impl(po_ctx *c, const po_geometry *g, const po_illum *il,
 
   // ---- output buffer
   float *out_dev = intensity;
-  if (!out_on_device) {
+  if (!out_on_device || !intensity) {
     PO_TRY(c->out.ensure(sizeof(float) * (size_t)S * nd_out));
     out_dev = c->out.as<float>();
   }
@@ -438,12 +475,27 @@ static po_status solve_impl(po_ctx *c, const po_geometry *g, const po_illum *il,
     PO_CUDA(cudaMemcpyAsync(c->slots.p, sp64.data(), sizeof(SlotParams<double>) * S, cudaMemcpyHostToDevice, st));
   else
     PO_CUDA(cudaMemcpyAsync(c->slots.p, sp32.data(), sizeof(SlotParams<float>) * S, cudaMemcpyHostToDevice, st));
+  const SlotParams<double> *sp64_dev = nullptr;
+  if (adj) {
+    PO_TRY(c->slots64.ensure(sizeof(SlotParams<double>) * S));
+    PO_CUDA(cudaMemcpyAsync(c->slots64.p, sp64.data(), sizeof(SlotParams<double>) * S, cudaMemcpyHostToDevice, st));
+    sp64_dev = c->slots64.as<SlotParams<double>>();
+    PO_TRY(c->grad_acc.ensure(sizeof(double) * 7 * (size_t)std::max<int64_t>(n, 1)));
+    if (n > 0) PO_CUDA(cudaMemsetAsync(c->grad_acc.p, 0, sizeof(double) * 7 * (size_t)n, st));
+    PO_TRY(c->chunk_begin.ensure(sizeof(int32_t) * (size_t)((n + 31) / 32 + 1)));
+    PO_TRY(c->center0.ensure(sizeof(double) * 3));
+  }
   const double *k_lambda = c->kvals.as<double>();
   const double *k_slot = k_lambda + L;
 
   // root centre (tree.h:116-120, float box)
   double c0[3];
   for (int a = 0; a < 3; ++a) c0[a] = (double)(0.5f * (cfg.box_min[a] + cfg.box_max[a]));
+  if (adj) {
+    PO_CUDA(cudaMemcpyAsync(c->center0.p, c0, sizeof(c0), cudaMemcpyHostToDevice, st));
+    if (n > 0) PO_TRY(launch_chunk_begin(c->chunk_begin.as<int32_t>(), n, st));
+  }
+  const int32_t *perm_out = nullptr;  // sorted position -> input index of the gradient
 
   // Accumulates the device times of one chunk (needs its events complete).
   auto chunk_times = [&](bool tree_levels) {
@@ -490,6 +542,14 @@ static po_status solve_impl(po_ctx *c, const po_geometry *g, const po_illum *il,
       PO_CUDA(cudaEventRecord(c->ev[3], st));
       PO_TRY(launch_intensity_f64(c->levelA.as<double2>(), ch.ns, nth_out, nph_out, out_dev + (size_t)ch.s0 * nd_out,
                                   st));
+      if (adj) {
+        double2 *Gd = c->partial.as<double2>();
+        PO_TRY(launch_intensity_adjoint_f64(c->levelA.as<double2>(), adj->dl_di + (size_t)ch.s0 * nd_out, ch.ns,
+                                            nth_out, nph_out, Gd, st));
+        PO_TRY(launch_point_adjoint_f64(gin, c->chunk_begin.as<int32_t>(), (n + 31) / 32, c->center0.as<double>(), 0,
+                                        Gd, 0, 6 * nd_out, c->dirs_d.as<double>(), (int)nd_out, sp64_dev + ch.s0,
+                                        ch.nl, ch.gc, n, c->grad_acc.as<double>(), st));
+      }
       PO_CUDA(cudaEventRecord(c->ev[4], st));
       n_leaf_launches += 3;
       if (rep) {
@@ -535,6 +595,8 @@ static po_status solve_impl(po_ctx *c, const po_geometry *g, const po_illum *il,
       PO_TRY(c->tile_ctr.ensure(sizeof(double) * 3 * (size_t)((n + 127) / 128 + 1)));
       PO_TRY(c->partial.ensure(sizeof(float2) * 6 * (size_t)ns_max * nd_out * nsplit_max));
       PO_TRY(c->levelA.ensure(sizeof(float2) * 6 * (size_t)ns_max * nd_out));
+      if (adj) PO_TRY(c->levelB.ensure(sizeof(float2) * 6 * (size_t)ns_max * nd_out));
+      perm_out = tree.perm;
       for (const SlotChunk &ch : chunks) {
         PO_CUDA(cudaEventRecord(c->kev[0], st));
         PO_TRY(launch_currents_f32(n, gsc, c->slots.as<SlotParams<float>>() + ch.s0, ch.ns, c->cur.as<float>(), st));
@@ -546,6 +608,14 @@ static po_status solve_impl(po_ctx *c, const po_geometry *g, const po_illum *il,
         PO_CUDA(cudaEventRecord(c->ev[3], st));
         PO_TRY(launch_intensity_f32(c->levelA.as<float2>(), ch.ns, nth_out, nph_out, nth_out, nph_out, 1, 1,
                                     out_dev + (size_t)ch.s0 * nd_out, st));
+        if (adj) {
+          float2 *Gf = c->levelB.as<float2>();
+          PO_TRY(launch_intensity_adjoint_f32(c->levelA.as<float2>(), adj->dl_di + (size_t)ch.s0 * nd_out, ch.ns,
+                                              nth_out, nph_out, nth_out, nph_out, 1, 1, Gf, st));
+          PO_TRY(launch_point_adjoint_f32(gsc, c->chunk_begin.as<int32_t>(), (n + 31) / 32, c->center0.as<double>(),
+                                          0, Gf, 0, 6 * nd_out, c->dirs.as<float4>(), (int)nd_out, sp64_dev + ch.s0,
+                                          ch.nl, ch.gc, n, c->grad_acc.as<double>(), st));
+        }
         PO_CUDA(cudaEventRecord(c->ev[4], st));
         n_leaf_launches += 3 + (ch.gc + 3) / 4;
         if (rep) {
@@ -595,6 +665,7 @@ static po_status solve_impl(po_ctx *c, const po_geometry *g, const po_illum *il,
       PO_TRY(c->dirs.ensure(sizeof(float4) * df.size()));
       PO_CUDA(cudaMemcpyAsync(c->dirs.p, df.data(), sizeof(float4) * df.size(), cudaMemcpyHostToDevice, st));
       const int refnq = c->cover == 1 ? 1 : 0;
+      perm_out = tree.perm;
       for (const SlotChunk &ch : chunks) {
         const SlotParams<float> *sp = c->slots.as<SlotParams<float>>() + ch.s0;
         PO_CUDA(cudaEventRecord(c->kev[0], st));
@@ -646,6 +717,28 @@ static po_status solve_impl(po_ctx *c, const po_geometry *g, const po_illum *il,
         PO_CUDA(cudaEventRecord(c->ev[3], st));
         PO_TRY(launch_intensity_f32(cur_lvl, ch.ns, c->R[0], c->Phi[0], nth_out, nph_out, c->mt, c->mp,
                                     out_dev + (size_t)ch.s0 * nd_out, st));
+        if (adj) {
+          // root adjoint, then the transposed aggregation down to the leaves
+          PO_TRY(launch_intensity_adjoint_f32(cur_lvl, adj->dl_di + (size_t)ch.s0 * nd_out, ch.ns, c->R[0], c->Phi[0],
+                                              nth_out, nph_out, c->mt, c->mp, nxt, st));
+          std::swap(cur_lvl, nxt);
+          for (int l = 0; l < d; ++l) {
+            const int64_t np = tree.level[l].count, nc = tree.level[l + 1].count;
+            const float4 *trans = c->trans.as<float4>() + tr_off[l] + (size_t)ch.l0 * c->R[l] * c->Phi[l];
+            PO_TRY(launch_interp_cols_adj_mma(cur_lvl, c->mid.as<float2>(), tree.level[l + 1].parent,
+                                              tree.level[l + 1].prefix, np, nc, c->Phi[l], c->R[l + 1], c->R[l],
+                                              c->amat_adj_kp[l], c->amat_adj.as<uint32_t>() + c->amat_adj_off[l],
+                                              trans, ch.ns, ch.gc, st));
+            PO_TRY(launch_interp_rows_mma(c->mid.as<float2>(), nxt, (int64_t)ch.ns * nc * 6 * c->R[l + 1], c->Phi[l],
+                                          c->Phi[l + 1], c->bmat_adj_kp[l],
+                                          c->bmat_adj.as<uint32_t>() + c->bmat_adj_off[l], c->sm_count, st));
+            std::swap(cur_lvl, nxt);
+          }
+          const int64_t ndl = (int64_t)c->R[d] * c->Phi[d];
+          PO_TRY(launch_point_adjoint_f32(gsc, tree.level[d].begin, nleaf, c->leaf_ctr.as<double>(), 1, cur_lvl,
+                                          6 * ndl, nleaf * 6 * ndl, c->dirs.as<float4>(), (int)ndl, sp64_dev + ch.s0,
+                                          ch.nl, ch.gc, n, c->grad_acc.as<double>(), st));
+        }
         PO_CUDA(cudaEventRecord(c->ev[4], st));
         if (rep) {
           PO_CUDA(cudaEventSynchronize(c->ev[4]));
@@ -655,7 +748,8 @@ static po_status solve_impl(po_ctx *c, const po_geometry *g, const po_illum *il,
       leaf_pd = (double)n * c->R[d] * c->Phi[d] * S;
     }
   }
-  if (!out_on_device)
+  if (adj) PO_TRY(launch_scatter_grad(c->grad_acc.as<double>(), perm_out, n, adj->grad, st));
+  if (intensity && !out_on_device)
     PO_CUDA(cudaMemcpyAsync(intensity, out_dev, sizeof(float) * (size_t)S * nd_out, cudaMemcpyDeviceToHost, st));
   PO_CUDA(cudaEventRecord(c->ev[5], st));
   if (rep || !out_on_device) PO_CUDA(cudaEventSynchronize(c->ev[5]));
@@ -674,7 +768,7 @@ static po_status solve_impl(po_ctx *c, const po_geometry *g, const po_illum *il,
     int64_t ws = 0;
     for (DevBuf *b : {&c->twiddles, &c->geom_in, &c->geom_sorted, &c->octree_ws, &c->leaf_ctr, &c->dirs, &c->dirs_d,
                       &c->trans, &c->levelA, &c->levelB, &c->mid, &c->slots, &c->kvals, &c->out, &c->cur, &c->partial,
-                      &c->tile_ctr})
+                      &c->tile_ctr, &c->slots64, &c->grad_acc, &c->chunk_begin, &c->amat_adj, &c->bmat_adj})
       ws += (int64_t)b->bytes;
     rep->workspace_bytes = ws;
     rep->kernel_launches = g_launch_count - launches0;
@@ -718,6 +812,35 @@ po_status po_solve(po_ctx *c, const po_geometry *g, const po_illum *il, float *i
 }
 
 // ---------------------------------------------------------------- single steps
+po_status po_grad(po_ctx *c, const po_geometry *g, const po_illum *il, const float *dl_di, float *grad,
+                  float *intensity, void *stream, po_report *rep) {
+  if (!c || !g || !il || !dl_di || !grad) return fail(PO_ERR_INVALID_ARGUMENT, "null argument");
+  if (g->n < 0 || g->n > 2000000000LL) return fail(PO_ERR_INVALID_ARGUMENT, "point count out of range");
+  if (g->n > 0 && (!g->x || !g->y || !g->z || !g->nx || !g->ny || !g->nz || !g->area))
+    return fail(PO_ERR_INVALID_ARGUMENT, "null geometry array");
+  if (il->n_lambda <= 0 || !il->lambda_m) return fail(PO_ERR_INVALID_ARGUMENT, "no wavelengths");
+  if (il->n_inc <= 0 || !il->theta_i || !il->phi_i) return fail(PO_ERR_INVALID_ARGUMENT, "no incident directions");
+  if ((il->pol_mask & (PO_POL_TM | PO_POL_TE)) == 0 || (il->pol_mask & ~(PO_POL_TM | PO_POL_TE)))
+    return fail(PO_ERR_INVALID_ARGUMENT, "pol_mask must select TM and/or TE");
+  for (int l = 0; l < il->n_lambda; ++l)
+    if (!(il->lambda_m[l] > 0) || !std::isfinite(il->lambda_m[l]))
+      return fail(PO_ERR_INVALID_ARGUMENT, "wavelengths must be positive");
+  if (!(il->sigma > 0)) return fail(PO_ERR_INVALID_ARGUMENT, "beam sigma must be > 0");
+  const int npol = ((il->pol_mask & PO_POL_TM) ? 1 : 0) + ((il->pol_mask & PO_POL_TE) ? 1 : 0);
+  if ((int64_t)il->n_lambda * il->n_inc * npol > 65535) return fail(PO_ERR_UNSUPPORTED, "too many patterns per call");
+  if (c->depth > 0 && !c->tensor_theta)
+    return fail(PO_ERR_UNSUPPORTED, "the adjoint of a tree solve needs double-cover theta and PO_INTERP_TENSOR");
+  int dev = 0;
+  PO_CUDA(cudaGetDevice(&dev));
+  if (dev != c->device) return fail(PO_ERR_INVALID_ARGUMENT, "context was created on another device");
+  if (c->depth > 0) PO_TRY(ensure_adjoint_matrices(c));
+  if (rep) std::memset(rep, 0, sizeof(*rep));
+  AdjointArgs a;
+  a.dl_di = dl_di;
+  a.grad = grad;
+  return solve_impl(c, g, il, intensity, 1, (cudaStream_t)stream, rep, &a);
+}
+
 po_status po_tangent_plane_currents(int64_t n, const float *x, const float *y, const float *z, const float *nx,
                                     const float *ny, const float *nz, const float *area, double lambda_m,
                                     double theta_i, double phi_i, int pol, double eta_re, double eta_im, double sigma,
