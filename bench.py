@@ -415,6 +415,166 @@ def run_fiber(args, world, rank, local):
     }
 
 
+# ---------------------------------------------------- differentiation workload
+CYL_R, CYL_L, CYL_N, CYL_DEPTH, CYL_INC, CYL_EXTENT = 10e-6, 20e-6, 1_000_000, 6, 8, 26e-6
+CYL_WORKLOAD = ("rough cylinder r=10um L=20um (1.0M points), normal displacement h ~ Gaussian(0.02um, 0.5um), "
+                "25 wavelengths x 8 incidences x TM, depth 6, loss ||I(h) - I(h_target)||^2, gradient dL/dh")
+
+
+def run_cylinder_grad(args, world, rank, local):
+    """Forward + adjoint of the loss ||I(h) - I_t||^2 over the displacement
+    field h of a rough cylinder, through torch.autograd; the gradient is
+    checked against the FP64 reference gradient and central differences."""
+    import torch
+
+    from wavefiber3d_gb300 import api, autograd, geometry
+    import __graft_entry__
+    __graft_entry__.build()
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    st = torch.cuda.current_stream()
+    hf, h = geometry.cylinder_height_field(CYL_R, CYL_L, CYL_N, seed=1)
+    _, h_t = geometry.cylinder_height_field(CYL_R, CYL_L, CYL_N, seed=2)
+    numel, numelvert = hf.numel, hf.numelvert
+    phi = torch.arange(numel, dtype=torch.float64, device=dev) * (2 * math.pi / numel)
+    cs, sn = torch.cos(phi)[:, None], torch.sin(phi)[:, None]
+
+    def xy_of(hh):
+        r = CYL_R + hh
+        return torch.stack([r * cs, r * sn]).float()
+
+    box = [-1.1 * CYL_R, -1.1 * CYL_R, -0.55 * CYL_L]
+    bmax = [-v for v in box]
+    # level grids by the reference rule (ratio 1.2) on a 26 um extent: the rule's 20 um (the cylinder
+    # length) leaves the level-1 cells of the 22 um box (19 um diagonals) under-resolved (forward
+    # rel-L2 7e-4, gradient 5%); 26 um gives 4e-6 and 1e-4 for 1.4x the time
+    cfg = api.Config.reference_rule(CYL_DEPTH, N_THETA, N_PHI, box, bmax, CYL_EXTENT, CYL_EXTENT, 1.2,
+                                    precision=PRECISIONS[args.precision])
+    th = [0.05 * i for i in range(CYL_INC)]  # theta sweep from normal incidence on the axis-normal plane
+    ph = [0.0] * CYL_INC
+    lams = LAMBDAS[: args.cyl_lambdas]
+    illum = api.Illumination(lams, th, ph, api.PO_POL_TM, ETA, 1.0)
+    solver = api.Solver(cfg)
+    h_dev = torch.from_numpy(h).to(dev)
+    with torch.no_grad():
+        s_t = api.height_field_points_tensor(xy_of(torch.from_numpy(h_t).to(dev)), hf.period, hf.unitz, 0, numel - 1)
+        target = solver.solve(tuple(s_t[k] for k in range(7)), illum)
+
+    def step():
+        hh = h_dev.clone().requires_grad_(True)
+        samples = autograd.height_field_samples(xy_of(hh), hf.period, hf.unitz)
+        inten = autograd.far_field_intensity(solver, illum, samples)
+        loss = ((inten - target) ** 2).sum()
+        loss.backward()
+        return loss, hh.grad
+
+    for _ in range(max(1, min(args.warmup, 2))):
+        step()
+    torch.cuda.synchronize()
+    evs = []
+    clocks = ClockSampler(local)
+    for _ in range(args.steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        loss, g_h = step()
+        e1.record(st)
+        evs.append((e0, e1))
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms_step = statistics.mean(a.elapsed_time(b) for a, b in evs)
+    # forward alone, for the adjoint/forward ratio
+    with torch.no_grad():
+        s0 = api.height_field_points_tensor(xy_of(h_dev), hf.period, hf.unitz, 0, numel - 1)
+        out = torch.empty(solver.out_shape(illum), dtype=torch.float32, device=dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        solver.solve(tuple(s0[k] for k in range(7)), illum, out=out)
+        e1.record(st)
+        torch.cuda.synchronize()
+        ms_fwd = e0.elapsed_time(e1)
+        w_full = 2 * (out - target)
+        e0.record(st)
+        solver.grad(s0, illum, w_full)
+        e1.record(st)
+        torch.cuda.synchronize()
+        ms_grad = e0.elapsed_time(e1)
+    grad_report = dict(solver.last_report)
+    solver.close()
+
+    # ---- checks on one pattern (400 nm, first incidence), all points
+    import oracle
+    il1 = api.Illumination(lams[:1], th[:1], ph[:1], api.PO_POL_TM, ETA, 1.0)
+    cfg64 = api.Config(0, [N_THETA], [N_PHI], box, bmax, precision=api.PO_PREC_FP64)
+    with api.Solver(cfg) as s_tree, api.Solver(cfg64) as s64, torch.no_grad():
+        t1 = s64.solve(tuple(s_t[k] for k in range(7)), il1)
+        i64 = s64.solve(tuple(s0[k] for k in range(7)), il1)
+        w1 = 2 * (i64 - t1)
+        t0 = time.perf_counter()
+        g64 = s64.grad(s0, il1, w1).double()
+        torch.cuda.synchronize()
+        s_fp64 = time.perf_counter() - t0
+        g_tree = s_tree.grad(s0, il1, w1).double()
+        ref_err = {grp: float((g_tree[r] - g64[r]).norm() / g64[r].norm())
+                   for grp, r in (("positions", slice(0, 3)), ("normals", slice(3, 6)), ("areas", slice(6, 7)))}
+        gh_tree = api.height_field_adjoint(xy_of(h_dev), hf.period, hf.unitz, 0, numel - 1, g_tree.float())
+        gh_64 = api.height_field_adjoint(xy_of(h_dev), hf.period, hf.unitz, 0, numel - 1, g64.float())
+        dh_tree = (gh_tree[0].double() * cs + gh_tree[1].double() * sn)
+        dh_64 = (gh_64[0].double() * cs + gh_64[1].double() * sn)
+        ref_err_h = float((dh_tree - dh_64).norm() / dh_64.norm())
+        # central differences of the FP64 oracle (host, sampled directions) under a perturbation of
+        # 64 random samples, against the gradients of the same sampled loss
+        rng = np.random.default_rng(64)
+        dirs = np.sort(rng.choice(N_THETA * N_PHI, args.cyl_fd_dirs, replace=False))
+        wv = np.zeros(N_THETA * N_PHI)
+        wv[dirs] = rng.standard_normal(dirs.size)
+        wt = torch.from_numpy(wv.reshape(1, 1, 1, N_THETA, N_PHI)).float().to(dev)
+        gs64 = s64.grad(s0, il1, wt).double().cpu().numpy()
+        gst = s_tree.grad(s0, il1, wt).double().cpu().numpy()
+        sn0 = s0.double().cpu().numpy()
+        pick = rng.choice(sn0.shape[1], 64, replace=False)
+        v = np.zeros_like(sn0)
+        v[:3, pick] = rng.choice([-1.0, 1.0], (3, 64)) * 1e-10
+        v[3:6, pick] = rng.choice([-1.0, 1.0], (3, 64)) * 1e-6
+        v[6, pick] = sn0[6, pick] * 1e-6
+        il_o = oracle.make_illum(lams[0], th[0], ph[0], "M", ETA, 1.0)
+        t0 = time.perf_counter()
+        fd = float(wv[dirs] @ (oracle.solve_sampled_f64(sn0 + v, il_o, N_THETA, N_PHI, dirs) -
+                               oracle.solve_sampled_f64(sn0 - v, il_o, N_THETA, N_PHI, dirs)))
+        s_fd = time.perf_counter() - t0
+        ad64 = float((gs64 * 2 * v).sum())
+        adtree = float((gst * 2 * v).sum())
+    n = numel * numelvert
+    pd = float(n) * N_THETA * N_PHI * illum.n_patterns
+    return {
+        "metric": "gradient evaluations/s of ||I(h) - I_target||^2 w.r.t. the displacement field h (forward + adjoint)",
+        "value": 1000.0 / ms_step, "unit": "gradients/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": max(1, min(args.warmup, 2)), "ms_per_step": ms_step, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "split bf16 hi+lo products, f32 accumulation (f64 phase arguments); f64 currents Jacobian"
+                 if args.precision == "split_bf16" else "f32 (f64 phase arguments); f64 currents Jacobian",
+        "data": "synthetic (seeded displacement fields, target from a second seed)",
+        "config": {"workload": CYL_WORKLOAD, "points": n, "numel": numel, "numelvert": numelvert,
+                   "wavelengths": len(lams), "incidences": CYL_INC, "depth": CYL_DEPTH,
+                   "level_grids": [list(cfg.n_theta), list(cfg.n_phi)], "precision": args.precision},
+        "ms_forward": ms_fwd, "ms_po_grad": ms_grad, "grad_over_forward": ms_grad / ms_fwd,
+        "equivalent_gpoint_dirs_per_s_forward": pd / (ms_fwd * 1e-3) / 1e9,
+        "gradient_check": {
+            "pattern": f"lambda={lams[0] * 1e9:.0f} nm, incidence 0, all {n} points, loss ||I - I_t||^2",
+            "rel_l2_vs_fp64_reference_gradient": ref_err,
+            "rel_l2_vs_fp64_reference_gradient_dL_dh": ref_err_h,
+            "fd_64_samples": {"loss": f"sum of seeded weights x FP64 oracle intensity on {dirs.size} directions",
+                              "steps": "1e-10 m positions, 1e-6 normals, 1e-6 relative areas, random signs",
+                              "central_difference": fd, "adjoint_fp64": ad64, "adjoint_tree": adtree,
+                              "rel_err_fp64": abs(ad64 - fd) / abs(fd), "rel_err_tree": abs(adtree - fd) / abs(fd),
+                              "oracle_s": s_fd},
+            "fp64_reference_gradient_s": s_fp64},
+        "loss": float(loss.detach()), "grad_h_norm": float(g_h.norm()),
+        "gpu_launches": int(grad_report.get("kernel_launches", 0)),
+        "clocks": clk,
+        "report_grad": grad_report,
+    }
+
+
 def run_reference(args, world, rank):
     """CPU implementation of the path (FP64 direct sum restatement), all host cores."""
     if rank != 0:
@@ -456,11 +616,13 @@ def main():
     ap.add_argument("--cpu-dirs", type=int, default=2048, help="directions of the FP64 CPU sample")
     ap.add_argument("--precision", choices=sorted(PRECISIONS), default="fp32")
     ap.add_argument("--interp", choices=sorted(INTERP), default="tensor")
-    ap.add_argument("--workload", choices=["ellipsoid", "fiber"], default="ellipsoid",
+    ap.add_argument("--workload", choices=["ellipsoid", "fiber", "cylinder-grad"], default="ellipsoid",
                     help="ellipsoid: the headline 400k-point depth-5 workload; fiber: the 3.4M-point fiber "
                          "segment (split precision vs plain FP64 on the same GPU)")
     ap.add_argument("--fiber-lambdas", type=int, default=1, help="wavelengths per fiber step (400 nm first)")
     ap.add_argument("--fiber-dirs", type=int, default=512, help="directions of the fiber accuracy sample")
+    ap.add_argument("--cyl-lambdas", type=int, default=25, help="wavelengths of the cylinder gradient step")
+    ap.add_argument("--cyl-fd-dirs", type=int, default=256, help="directions of the cylinder FD check")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "engine":
         args.warmup = 3
@@ -469,6 +631,8 @@ def main():
         res = run_reference(args, world, rank)
     elif args.workload == "fiber":
         res = run_fiber(args, world, rank, local) if rank == 0 else None
+    elif args.workload == "cylinder-grad":
+        res = run_cylinder_grad(args, world, rank, local) if rank == 0 else None
     else:
         res = run_engine(args, world, rank, local)
     if rank == 0 and res is not None:

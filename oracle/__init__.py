@@ -67,6 +67,8 @@ def lib():
         L.po_oracle_height_field.argtypes = [f32p, ctypes.c_int, ctypes.c_int, ctypes.c_float, ctypes.c_float,
                                              ctypes.c_int, ctypes.c_int] + [f32p] * 7
         L.po_oracle_height_field.restype = ctypes.c_int
+        L.po_oracle_solve_sampled_d.argtypes = [ctypes.c_int64] + [f64p] * 7 + [ctypes.POINTER(Illum), ctypes.c_int,
+                                                                               ctypes.c_int, ctypes.c_int64, i64p, f64p]
         L.po_oracle_solve_direct_d.argtypes = [ctypes.c_int64] + [f64p] * 7 + [ctypes.POINTER(Illum), f64p,
                                                                               ctypes.c_int, ctypes.c_int, f64p]
         L.po_oracle_average.argtypes = [f32p, ctypes.c_int, ctypes.c_int, f32p, ctypes.c_int, ctypes.c_int]
@@ -214,4 +216,14 @@ def solve_direct_f64(samples, il: Illum, n_theta: int, n_phi: int, center=(0.0, 
     c = np.ascontiguousarray(center, dtype=np.float64)
     lib().po_oracle_solve_direct_d(a.shape[1], *[np.ascontiguousarray(a[k]) for k in range(7)], ctypes.byref(il),
                                    c, n_theta, n_phi, out)
+    return out
+
+
+def solve_sampled_f64(samples, il: Illum, n_theta: int, n_phi: int, dirs) -> np.ndarray:
+    """FP64 intensity of (7, n) float64 samples at the flat direction indices dirs."""
+    a = np.ascontiguousarray(samples, dtype=np.float64)
+    d = np.ascontiguousarray(dirs, dtype=np.int64)
+    out = np.zeros(d.size, dtype=np.float64)
+    lib().po_oracle_solve_sampled_d(a.shape[1], *[np.ascontiguousarray(a[k]) for k in range(7)], ctypes.byref(il),
+                                    n_theta, n_phi, d.size, d, out)
     return out

@@ -27,6 +27,9 @@
 
 typedef double complex cdbl;
 
+void po_oracle_intensity_sampled(int nth, int nph, int64_t m, const int64_t *dirs, const double *fields,
+                                 double *intensity);
+
 /* util/util.h:16-19 */
 static const double ORC_C0 = 299792458.0;
 static const double ORC_MU0 = 4e-7 * M_PI;
@@ -309,6 +312,45 @@ void po_oracle_solve_direct_d(int64_t n, const double *x, const double *y, const
     }
   }
   po_oracle_intensity(nth, nph, fld, intensity);
+  free(cur);
+  free(fld);
+}
+
+/* po_oracle_solve_direct_d on the listed flat direction indices only
+ * (intensity out: [m]). */
+void po_oracle_solve_sampled_d(int64_t n, const double *x, const double *y, const double *z, const double *nx,
+                               const double *ny, const double *nz, const double *area, const po_oracle_illum *il,
+                               int nth, int nph, int64_t m, const int64_t *dirs, double *intensity) {
+  double wavedir[3], edir[3], hdir[3];
+  po_oracle_incident(il->theta_i, il->phi_i, il->mode_te, wavedir, edir, hdir);
+  double k0 = 2.0 * M_PI / il->lambda_m, z0 = orc_z0();
+  cdbl ef, hf;
+  prefactors(k0, il->dis, &ef, &hf);
+  cdbl eta = il->eta_re + I * il->eta_im;
+  cdbl *cur = (cdbl *)malloc(sizeof(cdbl) * 6 * (size_t)(n > 0 ? n : 1));
+  double *fld = (double *)malloc(sizeof(double) * 12 * (size_t)(m > 0 ? m : 1));
+#pragma omp parallel for schedule(static)
+  for (int64_t p = 0; p < n; ++p) {
+    double src[3] = {x[p], y[p], z[p]}, nrm[3] = {nx[p], ny[p], nz[p]};
+    tangent_plane_point(wavedir, edir, hdir, 1.0, eta, z0, il->sigma, k0, il->mode_te, src, nrm, cur + 6 * p);
+    for (int c = 0; c < 6; ++c) cur[6 * p + c] *= area[p] * (c < 3 ? ef : hf);
+  }
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int64_t j = 0; j < m; ++j) {
+    double s[3];
+    direction((int)(dirs[j] / nph), (int)(dirs[j] % nph), nth, nph, s);
+    cdbl acc[6] = {0, 0, 0, 0, 0, 0};
+    for (int64_t p = 0; p < n; ++p) {
+      double ph = k0 * (x[p] * s[0] + y[p] * s[1] + z[p] * s[2]);
+      cdbl g = cos(ph) + I * sin(ph);
+      for (int k = 0; k < 6; ++k) acc[k] += cur[6 * p + k] * g;
+    }
+    for (int k = 0; k < 6; ++k) {
+      fld[j * 12 + 2 * k] = creal(acc[k]);
+      fld[j * 12 + 2 * k + 1] = cimag(acc[k]);
+    }
+  }
+  po_oracle_intensity_sampled(nth, nph, m, dirs, fld, intensity);
   free(cur);
   free(fld);
 }
