@@ -575,6 +575,136 @@ def run_cylinder_grad(args, world, rank, local):
     }
 
 
+# ------------------------------------------------------------ batch workload
+BATCH_WORKLOAD = ("256 independent solves: spheres and ellipsoids r = 1-10 um, 5k-500k points (log-uniform), "
+                  "random wavelength 400-700 nm and incidence, TM, 180x360, depth / leaf precision / tile by "
+                  "the autotuner, one CUDA graph")
+
+
+def make_batch_items(n_items: int, seed: int = 4):
+    from wavefiber3d_gb300 import geometry
+    rng = np.random.default_rng(seed)
+    items = []
+    for i in range(n_items):
+        r = float(rng.uniform(1e-6, 10e-6))
+        n = int(round(math.exp(rng.uniform(math.log(5e3), math.log(5e5)))))
+        if rng.random() < 0.5:
+            radii = (r, r, r)
+            cloud = geometry.fibonacci_sphere(r, n)
+        else:
+            radii = (r, r * float(rng.uniform(0.5, 1.0)), r * float(rng.uniform(0.5, 1.0)))
+            cloud = geometry.ellipsoid(radii, n)
+        lam = float(rng.uniform(400e-9, 700e-9))
+        th = float(rng.uniform(-math.pi / 2 + 0.05, math.pi / 2 - 0.05))
+        ph = float(rng.uniform(0, 2 * math.pi))
+        items.append((cloud, radii, lam, th, ph))
+    return items
+
+
+def run_batch(args, world, rank, local):
+    """Config 4: many independent solves in one captured CUDA graph."""
+    import torch
+
+    import oracle
+    from wavefiber3d_gb300 import api, autotune
+    import __graft_entry__
+    __graft_entry__.build()
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    st = torch.cuda.current_stream()
+    items = make_batch_items(args.batch_items)
+    tuner = autotune.Autotuner(cache_path=args.tune_cache, reps=2)
+    configs, samples, illums, choices = [], [], [], []
+    t0 = time.perf_counter()
+    for cloud, radii, lam, th, ph in items:
+        r = max(radii)
+        box = [-1.1 * a for a in radii], [1.1 * a for a in radii]
+        g = torch.from_numpy(cloud.soa()).to(dev)
+        il = api.Illumination([lam], [th], [ph], api.PO_POL_TM, ETA, 1.0)
+
+        def make(depth, prec, tile, box=box, r=r):
+            return api.Config.reference_rule(depth, N_THETA, N_PHI, box[0], box[1], 2 * r, 2 * r, 1.3,
+                                             precision=prec, interp_tile=tile)
+        ch = tuner.choose(g, il, make, 2 * r)
+        configs.append(make(ch["depth"], ch["precision"], ch["tile"]))
+        samples.append(g)
+        illums.append(il)
+        choices.append(ch)
+    tune_s = time.perf_counter() - t0
+    tuner.save()
+    batch = api.Batch(configs, n_streams=args.batch_streams)
+    t0 = time.perf_counter()
+    batch.prepare(samples, illums)
+    torch.cuda.synchronize()
+    prepare_s = time.perf_counter() - t0
+    for _ in range(args.warmup):
+        batch.launch()
+    torch.cuda.synchronize()
+    evs = []
+    clocks = ClockSampler(local)
+    for _ in range(args.steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        batch.launch()
+        e1.record(st)
+        evs.append((e0, e1))
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms_graph = statistics.mean(a.elapsed_time(b) for a, b in evs)
+    info = batch.info()
+    # the same solves one by one (po_solve, no graph)
+    solvers = [api.Solver(c) for c in configs]
+    outs = [torch.empty(s.out_shape(il), dtype=torch.float32, device=dev) for s, il in zip(solvers, illums)]
+    for s, g, il, o in zip(solvers, samples, illums, outs):
+        s.solve(tuple(g[k] for k in range(7)), il, out=o)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for s, g, il, o in zip(solvers, samples, illums, outs):
+        s.solve(tuple(g[k] for k in range(7)), il, out=o)
+    e1.record(st)
+    torch.cuda.synchronize()
+    ms_serial = e0.elapsed_time(e1)
+    same = all(torch.equal(a, b) for a, b in zip(outs, batch.outputs))
+    for s in solvers:
+        s.close()
+    # per-solve error against the FP64 oracle on sampled directions
+    rng = np.random.default_rng(7)
+    errs = []
+    t0 = time.perf_counter()
+    for (cloud, radii, lam, th, ph), o in zip(items, batch.outputs):
+        dirs = np.sort(rng.choice(N_THETA * N_PHI, args.batch_dirs, replace=False))
+        il_o = oracle.make_illum(lam, th, ph, "M", ETA, 1.0)
+        ref = oracle.solve_sampled_f64(cloud.soa().astype(np.float64), il_o, N_THETA, N_PHI, dirs)
+        got = o.reshape(-1).cpu().numpy()[dirs].astype(np.float64)
+        errs.append(float(np.linalg.norm(got - ref) / np.linalg.norm(ref)))
+    oracle_s = time.perf_counter() - t0
+    batch.close()
+    npts = sum(int(g.shape[1]) for g in samples)
+    pd = float(npts) * N_THETA * N_PHI
+    depth_hist = {d: sum(1 for c in choices if c["depth"] == d) for d in range(7)}
+    return {
+        "metric": "Gpoint-dirs/s (equivalent depth-0 terms) of a batch of independent solves in one CUDA graph",
+        "value": pd / (ms_graph * 1e-3) / 1e9, "unit": "Gpoint-dirs/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_graph, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 / split bf16 per solve (autotuned), f64 phase arguments",
+        "data": "synthetic (seeded spheres and ellipsoids)",
+        "config": {"workload": BATCH_WORKLOAD, "solves": len(items), "points_total": npts,
+                   "streams": args.batch_streams, "depths": depth_hist,
+                   "split_bf16_solves": sum(1 for c in choices if c["precision"] == api.PO_PREC_SPLIT_BF16),
+                   "tiles": {t: sum(1 for c in choices if c["tile"] == t) for t in (0, 8, 16)}},
+        "solves_per_s": len(items) / (ms_graph * 1e-3),
+        "ms_same_solves_one_by_one": ms_serial, "graph_speedup": ms_serial / ms_graph,
+        "graph_equals_one_by_one": same,
+        "graph_nodes": info["graph_nodes"], "workspace_bytes": info["workspace_bytes"],
+        "prepare_s": prepare_s, "tuning_s": tune_s, "tuning_trials": tuner.trials, "tuned_classes": len(tuner.cache),
+        "per_solve_rel_l2_vs_fp64": {"max": max(errs), "median": float(np.median(errs)),
+                                     "sample": f"{args.batch_dirs} seeded directions per solve, FP64 oracle"},
+        "oracle_s": oracle_s,
+        "clocks": clk,
+    }
+
+
 def run_reference(args, world, rank):
     """CPU implementation of the path (FP64 direct sum restatement), all host cores."""
     if rank != 0:
@@ -616,13 +746,17 @@ def main():
     ap.add_argument("--cpu-dirs", type=int, default=2048, help="directions of the FP64 CPU sample")
     ap.add_argument("--precision", choices=sorted(PRECISIONS), default="fp32")
     ap.add_argument("--interp", choices=sorted(INTERP), default="tensor")
-    ap.add_argument("--workload", choices=["ellipsoid", "fiber", "cylinder-grad"], default="ellipsoid",
+    ap.add_argument("--workload", choices=["ellipsoid", "fiber", "cylinder-grad", "batch"], default="ellipsoid",
                     help="ellipsoid: the headline 400k-point depth-5 workload; fiber: the 3.4M-point fiber "
                          "segment (split precision vs plain FP64 on the same GPU)")
     ap.add_argument("--fiber-lambdas", type=int, default=1, help="wavelengths per fiber step (400 nm first)")
     ap.add_argument("--fiber-dirs", type=int, default=512, help="directions of the fiber accuracy sample")
     ap.add_argument("--cyl-lambdas", type=int, default=25, help="wavelengths of the cylinder gradient step")
     ap.add_argument("--cyl-fd-dirs", type=int, default=256, help="directions of the cylinder FD check")
+    ap.add_argument("--batch-items", type=int, default=256, help="independent solves of the batch workload")
+    ap.add_argument("--batch-streams", type=int, default=16, help="concurrent graph branches of the batch")
+    ap.add_argument("--batch-dirs", type=int, default=64, help="FP64 check directions per batch solve")
+    ap.add_argument("--tune-cache", default=None, help="JSON file of the autotuner's choices (read and written)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "engine":
         args.warmup = 3
@@ -633,6 +767,8 @@ def main():
         res = run_fiber(args, world, rank, local) if rank == 0 else None
     elif args.workload == "cylinder-grad":
         res = run_cylinder_grad(args, world, rank, local) if rank == 0 else None
+    elif args.workload == "batch":
+        res = run_batch(args, world, rank, local) if rank == 0 else None
     else:
         res = run_engine(args, world, rank, local)
     if rank == 0 and res is not None:

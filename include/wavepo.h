@@ -71,6 +71,8 @@ typedef struct po_config {
   int64_t max_workspace_bytes;      /* device workspace cap of one solve; the patterns are
                                        processed in chunks of slots that fit (0 = half of
                                        the device's memory) */
+  int interp_tile;                  /* complex columns per CTA of the tensor-core theta pass:
+                                       0 = chosen by shared memory, 8 or 16 (autotuner knob) */
 } po_config;
 
 /* How the theta interpolation + translation + child sum between tree levels
@@ -164,6 +166,29 @@ po_status po_solve(po_ctx *ctx, const po_geometry *geom, const po_illum *illum, 
  * are held fixed. */
 po_status po_grad(po_ctx *ctx, const po_geometry *geom, const po_illum *illum, const float *dl_di, float *grad,
                   float *intensity, void *stream, po_report *report);
+
+/* ---- batches of independent solves (no counterpart in the reference) ----
+ * Many geometries, each with its own configuration and illumination, run as
+ * one CUDA graph: po_batch_prepare builds every octree and table (host
+ * synchronisations happen here) and captures the pattern computations of all
+ * items into a graph whose branches run concurrently (items spread over
+ * n_streams branches, longest estimated first); po_batch_launch replays it on
+ * a stream.  Items keep their own workspaces, so a replay recomputes every
+ * pattern from the prepared trees (the geometry arrays must not move).
+ * Geometry and intensity pointers are device memory. */
+typedef struct po_batch po_batch;
+typedef struct po_batch_item {
+  po_geometry geom;                 /* on_device must be 1 */
+  po_illum illum;
+  float *intensity;                 /* [n_lambda][n_inc][n_pol][n_theta[0]][n_phi[0]] of its config */
+} po_batch_item;
+po_status po_batch_create(po_batch **batch, int n_items, const po_config *configs, int n_streams);
+po_status po_batch_prepare(po_batch *batch, const po_batch_item *items, void *stream);
+po_status po_batch_launch(po_batch *batch, void *stream);
+/* graph nodes, device workspace of all items, host+device time of the last
+ * prepare (ms); any pointer may be NULL */
+po_status po_batch_info(const po_batch *batch, int64_t *graph_nodes, int64_t *workspace_bytes, double *ms_prepare);
+po_status po_batch_destroy(po_batch *batch);
 
 /* ---- single steps of the path (device pointers) ------------------------ */
 

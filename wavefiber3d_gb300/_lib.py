@@ -36,7 +36,7 @@ class po_config(ctypes.Structure):
                 ("box_min", ctypes.c_float * 3), ("box_max", ctypes.c_float * 3),
                 ("precision", ctypes.c_int), ("theta_mode", ctypes.c_int), ("nyquist_quirk", ctypes.c_int),
                 ("distance", ctypes.c_double), ("interp_method", ctypes.c_int),
-                ("max_workspace_bytes", ctypes.c_int64)]
+                ("max_workspace_bytes", ctypes.c_int64), ("interp_tile", ctypes.c_int)]
 
 
 class po_geometry(ctypes.Structure):
@@ -51,6 +51,10 @@ class po_illum(ctypes.Structure):
                 ("n_inc", ctypes.c_int), ("theta_i", ctypes.c_void_p), ("phi_i", ctypes.c_void_p),
                 ("pol_mask", ctypes.c_int), ("eta_re", ctypes.c_double), ("eta_im", ctypes.c_double),
                 ("sigma", ctypes.c_double)]
+
+
+class po_batch_item(ctypes.Structure):
+    _fields_ = [("geom", po_geometry), ("illum", po_illum), ("intensity", ctypes.c_void_p)]
 
 
 class po_report(ctypes.Structure):
@@ -71,7 +75,8 @@ class po_report(ctypes.Structure):
 EXPORTS = ("po_config_init", "po_status_string", "po_last_error", "po_create", "po_destroy", "po_solve",
            "po_tangent_plane_currents", "po_build_octree", "po_far_field_direct", "po_interp_fft",
            "po_compute_intensity", "po_version", "po_interp_fft_noalloc", "po_height_field_points",
-           "po_average_pattern", "po_grad", "po_height_field_adjoint")
+           "po_average_pattern", "po_grad", "po_height_field_adjoint", "po_batch_create", "po_batch_prepare",
+           "po_batch_launch", "po_batch_info", "po_batch_destroy")
 
 _lib = None
 
@@ -104,6 +109,12 @@ def load():
     L.po_grad.argtypes = [vp, ctypes.POINTER(po_geometry), ctypes.POINTER(po_illum), vp, vp, vp, vp,
                           ctypes.POINTER(po_report)]
     L.po_height_field_adjoint.argtypes = [vp, i32, i32, ctypes.c_float, ctypes.c_float, i32, i32, vp, vp, vp]
+    L.po_batch_create.argtypes = [ctypes.POINTER(vp), i32, ctypes.POINTER(po_config), i32]
+    L.po_batch_prepare.argtypes = [vp, ctypes.POINTER(po_batch_item), vp]
+    L.po_batch_launch.argtypes = [vp, vp]
+    L.po_batch_info.argtypes = [vp, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64),
+                                ctypes.POINTER(ctypes.c_double)]
+    L.po_batch_destroy.argtypes = [vp]
     L.po_average_pattern.argtypes = [vp, i32, i32, vp, i32, i32, i32, vp]
     L.po_height_field_points.argtypes = [vp, i32, i32, ctypes.c_float, ctypes.c_float, i32, i32] + [vp] * 8
     for name in EXPORTS:

@@ -84,6 +84,7 @@ class Config:
     distance: float = 1.0
     interp_method: int = PO_INTERP_TENSOR
     max_workspace_bytes: int = 0
+    interp_tile: int = 0
 
     @classmethod
     def reference_rule(cls, max_depth, n_theta_out, n_phi_out, box_min, box_max, theta_extent, phi_extent,
@@ -111,6 +112,7 @@ class Config:
         c.distance = float(self.distance)
         c.interp_method = int(self.interp_method)
         c.max_workspace_bytes = int(self.max_workspace_bytes)
+        c.interp_tile = int(self.interp_tile)
         return c
 
 
@@ -361,3 +363,71 @@ def height_field_adjoint(xy, period: float, unitz: float, ring_begin: int, ring_
                                               int(ring_begin), int(ring_end), _ptr(g), _ptr(out),
                                               _stream_ptr(stream)))
     return out
+
+
+class Batch:
+    """Independent solves captured in one CUDA graph (po_batch_*).
+
+    ``Batch(configs, n_streams)`` creates one engine context per item;
+    ``prepare(samples, illums)`` builds every octree and table and captures the
+    pattern computations of all items into a graph (items spread over
+    ``n_streams`` concurrent branches); ``launch()`` replays it.  Geometry is a
+    list of (7, n) float32 CUDA tensors; results are CUDA tensors
+    ``self.outputs[i]`` shaped like Solver.solve's."""
+
+    def __init__(self, configs, n_streams: int = 8):
+        self.configs = list(configs)
+        arr = (_lib.po_config * len(self.configs))(*[c.to_c() for c in self.configs])
+        h = ctypes.c_void_p()
+        check(_lib.load().po_batch_create(ctypes.byref(h), len(self.configs), arr, int(n_streams)))
+        self._h = h
+        self._keep = []
+        self.outputs = []
+
+    def prepare(self, samples, illums, stream=None):
+        torch = _torch()
+        if len(samples) != len(self.configs) or len(illums) != len(self.configs):
+            raise ValueError("one geometry and one illumination per configuration")
+        items = (_lib.po_batch_item * len(self.configs))()
+        keep, outs = [], []
+        for i, (s, il, cfg) in enumerate(zip(samples, illums, self.configs)):
+            g7 = s.to(device="cuda", dtype=torch.float32).contiguous()
+            n = g7.shape[1]
+            ilc, ka = il.to_c()
+            npol = (1 if il.pol_mask & PO_POL_TM else 0) + (1 if il.pol_mask & PO_POL_TE else 0)
+            out = torch.empty((len(il.wavelengths_m), len(il.theta_i), npol, int(cfg.n_theta[0]), int(cfg.n_phi[0])),
+                              dtype=torch.float32, device="cuda")
+            items[i].geom = _lib.po_geometry(n, *[g7[k].data_ptr() for k in range(7)], 1)
+            items[i].illum = ilc
+            items[i].intensity = out.data_ptr()
+            keep += [g7, ka]
+            outs.append(out)
+        check(_lib.load().po_batch_prepare(self._h, items, _stream_ptr(stream)))
+        self._keep, self.outputs = keep, outs
+        return outs
+
+    def launch(self, stream=None):
+        check(_lib.load().po_batch_launch(self._h, _stream_ptr(stream)))
+        return self.outputs
+
+    def info(self) -> dict:
+        nodes, ws, ms = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_double()
+        check(_lib.load().po_batch_info(self._h, ctypes.byref(nodes), ctypes.byref(ws), ctypes.byref(ms)))
+        return {"graph_nodes": nodes.value, "workspace_bytes": ws.value, "ms_prepare": ms.value}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib.load().po_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()

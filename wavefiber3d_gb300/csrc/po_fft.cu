@@ -324,7 +324,6 @@ po_status launch_interp_rows(const float2 *src, float2 *dst, int64_t nrows, cons
   while (rows_smem(pin, pout, threads / L) > 72 * 1024 && threads > std::max(32, L)) threads >>= 1;
   const size_t smem = rows_smem(pin, pout, threads / L);
   if (smem > 227 * 1024) return fail(PO_ERR_UNSUPPORTED, "angular grid too large for the shared-memory FFT");
-  PO_CUDA(cudaFuncSetAttribute(k_interp_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const int NG = threads / L;
   int64_t blocks = (nrows + NG - 1) / NG;
   int64_t cap = (int64_t)sm_count * 32;
@@ -472,7 +471,6 @@ po_status launch_interp_cols(const float2 *mid, float2 *parent, const int32_t *c
   if (mirror && NG < 2) return fail(PO_ERR_UNSUPPORTED, "mirrored column pass needs two lane groups per CTA");
   int lg = 0;
   while ((1 << lg) < NG) ++lg;
-  PO_CUDA(cudaFuncSetAttribute(k_interp_cols, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const int TW = mirror ? NG / 2 : NG;
   int64_t gx = (int64_t)((span + TW - 1) / TW) * n_parent * ncomp;
   if (gx > 2147483647LL || n_slots > 65535) return fail(PO_ERR_UNSUPPORTED, "too many nodes for one launch");
@@ -517,6 +515,13 @@ po_status launch_trans_table(const double *k_per_lambda, int n_lambda, int nth, 
   k_trans_table<<<grid, 256, 0, st>>>(k_per_lambda, n_lambda, nth, Rp, phi, a[0], a[1], a[2], out);
   count_launch();
   PO_CUDA(cudaGetLastError());
+  return PO_OK;
+}
+
+// opt-in shared-memory limit of the FFT interpolation kernels, set once per device
+po_status init_fft_attributes(int max_smem) {
+  PO_CUDA(cudaFuncSetAttribute(k_interp_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
+  PO_CUDA(cudaFuncSetAttribute(k_interp_cols, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
   return PO_OK;
 }
 

@@ -27,6 +27,9 @@ po_status cuda_fail(cudaError_t e, const char *what);
     if (_s != PO_OK) return _s;        \
   } while (0)
 
+// opt-in shared-memory attributes of the engine's kernels on a device (once)
+po_status init_device_attributes(int dev);
+
 // counts launches made by the engine (po_report.kernel_launches)
 extern thread_local int64_t g_launch_count;
 inline void count_launch() { ++g_launch_count; }

@@ -246,11 +246,12 @@ static size_t cols_mma_smem(int ncc, int Rc, int Rp, int Kp) {
 
 po_status launch_interp_cols_mma(const float2 *mid, float2 *parent, const int32_t *child_table, int64_t n_parent,
                                  int64_t n_child, int phi, int Rc, int Rp, int Kp, int mirror, const uint32_t *Afrag,
-                                 const float4 *trans, int n_slots, int G, cudaStream_t st) {
+                                 const float4 *trans, int n_slots, int G, int tile, cudaStream_t st) {
   if (n_parent <= 0 || n_slots <= 0) return PO_OK;
   if (Kp % 16 || Kp < (mirror ? 2 * Rc : Rc)) return fail(PO_ERR_INTERNAL, "theta matrix K padding");
   int ncc = 16;
   if (cols_mma_smem(ncc, Rc, Rp, Kp) > 100 * 1024 || (mirror ? phi / 2 : phi) <= 4) ncc = 8;
+  if ((tile == 8 || tile == 16) && cols_mma_smem(tile, Rc, Rp, Kp) <= 227 * 1024) ncc = tile;
   const size_t smem = cols_mma_smem(ncc, Rc, Rp, Kp);
   if (smem > 227 * 1024) return fail(PO_ERR_UNSUPPORTED, "angular grid too large for the tensor-core interpolation");
   const int TW = mirror ? ncc / 2 : ncc;
@@ -259,11 +260,9 @@ po_status launch_interp_cols_mma(const float2 *mid, float2 *parent, const int32_
   if (gx > 2147483647LL || n_slots > 65535) return fail(PO_ERR_UNSUPPORTED, "too many nodes for one launch");
   dim3 grid((unsigned)gx, 1u, (unsigned)n_slots);
   if (ncc == 16) {
-    PO_CUDA(cudaFuncSetAttribute(k_interp_cols_mma<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     k_interp_cols_mma<16><<<grid, 128, smem, st>>>(mid, parent, child_table, n_parent, n_child, phi, Rc, Rp, Kp,
                                                    mirror, (const uint4 *)Afrag, trans, G, 0.f);
   } else {
-    PO_CUDA(cudaFuncSetAttribute(k_interp_cols_mma<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     k_interp_cols_mma<8><<<grid, 128, smem, st>>>(mid, parent, child_table, n_parent, n_child, phi, Rc, Rp, Kp,
                                                   mirror, (const uint4 *)Afrag, trans, G, 0.f);
   }
@@ -391,11 +390,9 @@ po_status launch_interp_cols_adj_mma(const float2 *parent_adj, float2 *mid_adj, 
   if (gx > 2147483647LL || n_slots > 65535) return fail(PO_ERR_UNSUPPORTED, "too many nodes for one launch");
   dim3 grid((unsigned)gx, 1u, (unsigned)n_slots);
   if (ncc == 16) {
-    PO_CUDA(cudaFuncSetAttribute(k_interp_cols_adj_mma<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     k_interp_cols_adj_mma<16><<<grid, 128, smem, st>>>(parent_adj, mid_adj, child_parent, child_prefix, n_parent,
                                                        n_child, phi, Rc, Rp, Kp, (const uint4 *)Afrag, trans, G);
   } else {
-    PO_CUDA(cudaFuncSetAttribute(k_interp_cols_adj_mma<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     k_interp_cols_adj_mma<8><<<grid, 128, smem, st>>>(parent_adj, mid_adj, child_parent, child_prefix, n_parent,
                                                       n_child, phi, Rc, Rp, Kp, (const uint4 *)Afrag, trans, G);
   }
@@ -514,7 +511,6 @@ po_status launch_interp_rows_mma(const float2 *src, float2 *dst, int64_t nrows, 
   const size_t bbytes = sizeof(uint32_t) * phi_matrix_words(Pp, Kp);
   const bool b_smem = bbytes <= 48 * 1024;
   const size_t smem = b_smem ? bbytes : 0;
-  if (smem) PO_CUDA(cudaFuncSetAttribute(k_interp_rows_mma, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int64_t blocks = ((nrows + 7) / 8 + 3) / 4;
   const int64_t cap = (int64_t)sm_count * 16;
   if (blocks > cap) blocks = cap;
@@ -522,6 +518,18 @@ po_status launch_interp_rows_mma(const float2 *src, float2 *dst, int64_t nrows, 
                                                          b_smem ? 1 : 0);
   count_launch();
   PO_CUDA(cudaGetLastError());
+  return PO_OK;
+}
+
+// Opt-in shared-memory limit of every kernel here, set once per device (the
+// launchers pick their shared-memory size at run time and must not change
+// function attributes while a stream is being captured).
+po_status init_interp_mma_attributes(int max_smem) {
+  PO_CUDA(cudaFuncSetAttribute(k_interp_cols_mma<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
+  PO_CUDA(cudaFuncSetAttribute(k_interp_cols_mma<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
+  PO_CUDA(cudaFuncSetAttribute(k_interp_cols_adj_mma<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
+  PO_CUDA(cudaFuncSetAttribute(k_interp_cols_adj_mma<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
+  PO_CUDA(cudaFuncSetAttribute(k_interp_rows_mma, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
   return PO_OK;
 }
 

@@ -71,7 +71,7 @@ size_t theta_matrix_words(int Rp, int Kp);
 void build_theta_matrix(int Tc, int Tp, int Rc, int Rp, int mirror, int Kp, std::vector<uint32_t> &out);
 po_status launch_interp_cols_mma(const float2 *mid, float2 *parent, const int32_t *child_table, int64_t n_parent,
                                  int64_t n_child, int phi, int Rc, int Rp, int Kp, int mirror, const uint32_t *Afrag,
-                                 const float4 *trans, int n_slots, int G, cudaStream_t st);
+                                 const float4 *trans, int n_slots, int G, int tile, cudaStream_t st);
 // tensor-core phi pass (po_interp_mma.cu)
 size_t phi_matrix_words(int Pp, int Kp);
 void build_phi_matrix(int Pc, int Pp, int Kp, std::vector<uint32_t> &out);
@@ -107,6 +107,10 @@ po_status launch_point_adjoint_f64(const float *const g[7], const int32_t *begin
                                    int n_lambda, int Gc, int64_t n, double *grad, cudaStream_t st);
 po_status launch_chunk_begin(int32_t *begin, int64_t n, cudaStream_t st);
 po_status launch_scatter_grad(const double *grad_sorted, const int32_t *perm, int64_t n, float *out, cudaStream_t st);
+
+// once per device: opt-in shared memory of the kernels whose launchers size it at run time
+po_status init_interp_mma_attributes(int max_smem);
+po_status init_fft_attributes(int max_smem);
 
 // intensity: fields [slot][comp][T][Phi] (root, possibly supersampled by
 // (mt, mp)) -> out [slot][nth][nph]

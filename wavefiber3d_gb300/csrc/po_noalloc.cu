@@ -78,6 +78,11 @@ extern "C" po_status po_interp_fft_noalloc(const float *in, int th_c, int ph_c, 
                 "PO_NOALLOC_SCRATCH_BYTES; use po_interp_fft or split the batch");
   if (batch == 0) return PO_OK;
   void *base = nullptr;
+  {
+    int dev = 0;
+    PO_CUDA(cudaGetDevice(&dev));
+    PO_TRY(init_device_attributes(dev));
+  }
   PO_TRY(scratch_address(&base));
   float2 *tw = (float2 *)base;
   float2 *mid = (float2 *)((char *)base + tw_bytes);

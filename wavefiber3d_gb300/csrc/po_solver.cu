@@ -13,10 +13,13 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <mutex>
+#include <set>
 #include <string>
 #include <vector>
 
@@ -116,6 +119,21 @@ int smooth_at_least(int n, bool even) {
 }
 
 }  // namespace
+
+// Kernel attributes are per device; set them before the first launch on a
+// device (and so before any stream capture of engine launches).
+po_status init_device_attributes(int dev) {
+  static std::mutex mu;
+  static std::set<int> done;
+  std::lock_guard<std::mutex> lock(mu);
+  if (done.count(dev)) return PO_OK;
+  int smem = 0;
+  PO_CUDA(cudaDeviceGetAttribute(&smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  PO_TRY(init_interp_mma_attributes(smem));
+  PO_TRY(init_fft_attributes(smem));
+  done.insert(dev);
+  return PO_OK;
+}
 
 }  // namespace wavepo
 
@@ -232,8 +250,11 @@ po_status po_create(po_ctx **out, const po_config *cfg) {
   if (!(cfg->distance > 0)) return fail(PO_ERR_INVALID_ARGUMENT, "distance must be > 0");
   if (cfg->interp_method != PO_INTERP_FFT && cfg->interp_method != PO_INTERP_TENSOR)
     return fail(PO_ERR_INVALID_ARGUMENT, "unknown interpolation method");
+  if (cfg->interp_tile != 0 && cfg->interp_tile != 8 && cfg->interp_tile != 16)
+    return fail(PO_ERR_INVALID_ARGUMENT, "interp_tile must be 0, 8 or 16");
   int dev = 0;
   PO_CUDA(cudaGetDevice(&dev));
+  PO_TRY(init_device_attributes(dev));
   po_ctx *c = new po_ctx();
   c->cfg = *cfg;
   c->device = dev;
@@ -406,8 +427,35 @@ struct AdjointArgs {
   float *grad = nullptr;         // [7][n]
 };
 
-static po_status solve_impl(po_ctx *c, const po_geometry *g, const po_illum *il, float *intensity, int out_on_device,
-                            cudaStream_t st, po_report *rep, const AdjointArgs *adj = nullptr) {
+// Everything a solve needs on the device before its patterns are computed:
+// built by prepare_solve (allocations, uploads, the octree with its count
+// read-back, tables), consumed by enqueue_solve (kernel launches only).
+struct SolvePlan {
+  int L = 0, G = 0, S = 0;
+  int64_t n = 0, nd_out = 0;
+  bool fp64 = false, adj = false;
+  const float *gin[7] = {};   // input order
+  const float *gsc[7] = {};   // octree order
+  OctreeBuffers tree;
+  int64_t nleaf = 0;
+  double c0[3] = {0, 0, 0};
+  std::vector<SlotChunk> chunks;
+  std::vector<size_t> tr_off;
+  int nsplit_max = 1;
+  const double *k_lambda = nullptr, *k_slot = nullptr;
+  const SlotParams<double> *sp64_dev = nullptr;
+  const int32_t *perm_out = nullptr;  // sorted position -> input index of the gradient
+};
+
+// Per-kernel-class device times of a solve (CUDA events; requested by a report).
+struct SolveTimes {
+  double leaf = 0, agg = 0, inten = 0, leafk = 0, rows = 0, cols = 0;
+  int n_leaf = 0, n_row = 0, n_col = 0;
+  double leaf_pd = 0, rows_b = 0, cols_b = 0;
+};
+
+static po_status prepare_solve(po_ctx *c, const po_geometry *g, const po_illum *il, bool adj, cudaStream_t st,
+                               SolvePlan &P) {
   const po_config &cfg = c->cfg;
   const int d = c->depth;
   const int64_t n = g->n;
@@ -415,11 +463,13 @@ static po_status solve_impl(po_ctx *c, const po_geometry *g, const po_illum *il,
   const int L = il->n_lambda, I = il->n_inc, G = I * npol, S = L * G;
   const int nth_out = cfg.n_theta[0], nph_out = cfg.n_phi[0];
   const int64_t nd_out = (int64_t)nth_out * nph_out;
-  const int64_t launches0 = g_launch_count;
-  int n_leaf_launches = 0, n_row_launches = 0, n_col_launches = 0;
-  double leaf_pd = 0, rows_b = 0, cols_b = 0;
-  double t_leaf = 0, t_agg = 0, t_int = 0, t_leafk = 0, t_rows = 0, t_cols = 0;
-  PO_CUDA(cudaEventRecord(c->ev[0], st));
+  P.L = L;
+  P.G = G;
+  P.S = S;
+  P.n = n;
+  P.nd_out = nd_out;
+  P.adj = adj;
+  P.fp64 = cfg.precision == PO_PREC_FP64;
 
   int64_t budget = cfg.max_workspace_bytes;
   if (budget <= 0) {
@@ -429,31 +479,22 @@ static po_status solve_impl(po_ctx *c, const po_geometry *g, const po_illum *il,
   }
 
   // ---- geometry on the device
-  const float *gin[7];
   if (g->on_device) {
     const float *src[7] = {g->x, g->y, g->z, g->nx, g->ny, g->nz, g->area};
-    for (int k = 0; k < 7; ++k) gin[k] = src[k];
+    for (int k = 0; k < 7; ++k) P.gin[k] = src[k];
   } else {
     PO_TRY(c->geom_in.ensure(sizeof(float) * 7 * (size_t)std::max<int64_t>(n, 1)));
     const float *src[7] = {g->x, g->y, g->z, g->nx, g->ny, g->nz, g->area};
     for (int k = 0; k < 7; ++k) {
       float *dst = c->geom_in.as<float>() + (size_t)k * n;
       if (n > 0) PO_CUDA(cudaMemcpyAsync(dst, src[k], sizeof(float) * n, cudaMemcpyHostToDevice, st));
-      gin[k] = dst;
+      P.gin[k] = dst;
     }
-  }
-
-  // ---- output buffer
-  float *out_dev = intensity;
-  if (!out_on_device || !intensity) {
-    PO_TRY(c->out.ensure(sizeof(float) * (size_t)S * nd_out));
-    out_dev = c->out.as<float>();
   }
 
   // per-slot parameters, slot = (lambda, incidence, polarisation)
   std::vector<double> kl(L), ks(S);
   for (int l = 0; l < L; ++l) kl[l] = kTwoPi / il->lambda_m[l];
-  const bool fp64 = cfg.precision == PO_PREC_FP64;
   std::vector<SlotParams<float>> sp32;
   std::vector<SlotParams<double>> sp64;
   for (int l = 0; l < L; ++l)
@@ -469,288 +510,321 @@ static po_status solve_impl(po_ctx *c, const po_geometry *g, const po_illum *il,
       }
   PO_TRY(c->slots.ensure(std::max(sizeof(SlotParams<float>), sizeof(SlotParams<double>)) * S));
   PO_TRY(c->kvals.ensure(sizeof(double) * (L + S)));
+  // the host vectors go out of scope: these copies complete before returning (synchronous)
   PO_CUDA(cudaMemcpyAsync(c->kvals.as<double>(), kl.data(), sizeof(double) * L, cudaMemcpyHostToDevice, st));
   PO_CUDA(cudaMemcpyAsync(c->kvals.as<double>() + L, ks.data(), sizeof(double) * S, cudaMemcpyHostToDevice, st));
-  if (fp64)
+  if (P.fp64)
     PO_CUDA(cudaMemcpyAsync(c->slots.p, sp64.data(), sizeof(SlotParams<double>) * S, cudaMemcpyHostToDevice, st));
   else
     PO_CUDA(cudaMemcpyAsync(c->slots.p, sp32.data(), sizeof(SlotParams<float>) * S, cudaMemcpyHostToDevice, st));
-  const SlotParams<double> *sp64_dev = nullptr;
   if (adj) {
     PO_TRY(c->slots64.ensure(sizeof(SlotParams<double>) * S));
     PO_CUDA(cudaMemcpyAsync(c->slots64.p, sp64.data(), sizeof(SlotParams<double>) * S, cudaMemcpyHostToDevice, st));
-    sp64_dev = c->slots64.as<SlotParams<double>>();
+    P.sp64_dev = c->slots64.as<SlotParams<double>>();
     PO_TRY(c->grad_acc.ensure(sizeof(double) * 7 * (size_t)std::max<int64_t>(n, 1)));
-    if (n > 0) PO_CUDA(cudaMemsetAsync(c->grad_acc.p, 0, sizeof(double) * 7 * (size_t)n, st));
     PO_TRY(c->chunk_begin.ensure(sizeof(int32_t) * (size_t)((n + 31) / 32 + 1)));
     PO_TRY(c->center0.ensure(sizeof(double) * 3));
   }
-  const double *k_lambda = c->kvals.as<double>();
-  const double *k_slot = k_lambda + L;
+  P.k_lambda = c->kvals.as<double>();
+  P.k_slot = P.k_lambda + L;
 
   // root centre (tree.h:116-120, float box)
-  double c0[3];
-  for (int a = 0; a < 3; ++a) c0[a] = (double)(0.5f * (cfg.box_min[a] + cfg.box_max[a]));
+  for (int a = 0; a < 3; ++a) P.c0[a] = (double)(0.5f * (cfg.box_min[a] + cfg.box_max[a]));
   if (adj) {
-    PO_CUDA(cudaMemcpyAsync(c->center0.p, c0, sizeof(c0), cudaMemcpyHostToDevice, st));
+    PO_CUDA(cudaMemcpyAsync(c->center0.p, P.c0, sizeof(P.c0), cudaMemcpyHostToDevice, st));
     if (n > 0) PO_TRY(launch_chunk_begin(c->chunk_begin.as<int32_t>(), n, st));
   }
-  const int32_t *perm_out = nullptr;  // sorted position -> input index of the gradient
 
-  // Accumulates the device times of one chunk (needs its events complete).
-  auto chunk_times = [&](bool tree_levels) {
-    float t = 0;
-    if (cudaEventElapsedTime(&t, c->kev[0], c->kev[1]) == cudaSuccess) { t_leafk += t; t_leaf += t; }
-    if (cudaEventElapsedTime(&t, c->kev[1], c->ev[3]) == cudaSuccess) t_agg += t;
-    if (cudaEventElapsedTime(&t, c->ev[3], c->ev[4]) == cudaSuccess) t_int += t;
-    if (tree_levels)
-      for (int l = 0; l < d; ++l) {
-        if (cudaEventElapsedTime(&t, c->kev[2 + 4 * l], c->kev[3 + 4 * l]) == cudaSuccess) t_rows += t;
-        if (cudaEventElapsedTime(&t, c->kev[4 + 4 * l], c->kev[5 + 4 * l]) == cudaSuccess) t_cols += t;
-      }
-    cudaGetLastError();
-  };
-  std::vector<SlotChunk> chunks;
-
-  if (fp64) {
+  if (P.fp64) {
     // ---- plain FP64 direct sum (the "plain method"): no tree, no sort
-    PO_CUDA(cudaEventRecord(c->ev[1], st));
-    PO_CUDA(cudaEventRecord(c->ev[2], st));
     auto splits = [&](int ns) {
       int64_t tiles = (int64_t)ns * ceil_div((int)nd_out, 128);
-      int s = (int)std::max<int64_t>(1, std::min<int64_t>(64, (c->sm_count * 8 + tiles - 1) / std::max<int64_t>(1, tiles)));
+      int s = (int)std::max<int64_t>(
+          1, std::min<int64_t>(64, (c->sm_count * 8 + tiles - 1) / std::max<int64_t>(1, tiles)));
       return (int)std::min<int64_t>(s, std::max<int64_t>(1, n));
     };
     int cs = chunk_slot_count(budget, 96.0 * (double)(n + nd_out * (1 + splits(1))), S);
     cs = chunk_slot_count(budget, 96.0 * (double)(n + nd_out * (1 + splits(cs))), S);
-    chunks = plan_chunks(L, G, cs);
-    const int ns_max = chunks.front().ns, nsplit_max = splits(std::min(ns_max, chunks.back().ns));
+    P.chunks = plan_chunks(L, G, cs);
+    const int ns_max = P.chunks.front().ns;
+    P.nsplit_max = splits(std::min(ns_max, P.chunks.back().ns));
     PO_TRY(c->cur.ensure(sizeof(double2) * 6 * (size_t)ns_max * std::max<int64_t>(n, 1)));
     std::vector<double> dd = host_dirs_d(nth_out, nph_out, nth_out);
     PO_TRY(c->dirs_d.ensure(sizeof(double) * dd.size()));
     PO_CUDA(cudaMemcpyAsync(c->dirs_d.p, dd.data(), sizeof(double) * dd.size(), cudaMemcpyHostToDevice, st));
-    PO_TRY(c->partial.ensure(sizeof(double2) * 6 * (size_t)ns_max * nd_out * nsplit_max));
+    PO_TRY(c->partial.ensure(sizeof(double2) * 6 * (size_t)ns_max * nd_out * P.nsplit_max));
     PO_TRY(c->levelA.ensure(sizeof(double2) * 6 * (size_t)ns_max * nd_out));
-    for (const SlotChunk &ch : chunks) {
-      PO_CUDA(cudaEventRecord(c->kev[0], st));
-      PO_TRY(launch_currents_f64(n, gin, c->slots.as<SlotParams<double>>() + ch.s0, ch.ns, c->cur.as<double>(), st));
-      const int nsplit = std::min(splits(ch.ns), nsplit_max);
-      PO_TRY(launch_direct_f64(n, gin[0], gin[1], gin[2], c->cur.as<double2>(), k_slot + ch.s0, ch.ns, c0,
+    P.perm_out = nullptr;
+    PO_CUDA(cudaStreamSynchronize(st));  // host tables above are released on return
+    return PO_OK;
+  }
+
+  // ---- octree (depth 0 still sorts the points so that direct-sum tiles are compact)
+  const int tdepth = d > 0 ? d : 6;
+  size_t wsb = octree_workspace_bytes(n, tdepth);
+  PO_TRY(c->octree_ws.ensure(wsb));
+  PO_TRY(build_octree(P.gin[0], P.gin[1], P.gin[2], n, cfg.box_min, cfg.box_max, tdepth, c->octree_ws.p, wsb, &P.tree,
+                      st));
+  PO_TRY(c->geom_sorted.ensure(sizeof(float) * 7 * (size_t)std::max<int64_t>(n, 1)));
+  float *gs[7];
+  for (int k = 0; k < 7; ++k) gs[k] = c->geom_sorted.as<float>() + (size_t)k * n;
+  PO_TRY(gather_points(n, P.tree.perm, P.gin, gs, st));
+  for (int k = 0; k < 7; ++k) P.gsc[k] = gs[k];
+  P.perm_out = P.tree.perm;
+  if (d == 0) {
+    std::vector<float4> df = host_dirs_f4(nth_out, nph_out, nth_out);
+    std::vector<double> dd = host_dirs_d(nth_out, nph_out, nth_out);
+    PO_TRY(c->dirs.ensure(sizeof(float4) * df.size()));
+    PO_TRY(c->dirs_d.ensure(sizeof(double) * dd.size()));
+    PO_CUDA(cudaMemcpyAsync(c->dirs.p, df.data(), sizeof(float4) * df.size(), cudaMemcpyHostToDevice, st));
+    PO_CUDA(cudaMemcpyAsync(c->dirs_d.p, dd.data(), sizeof(double) * dd.size(), cudaMemcpyHostToDevice, st));
+    int cs = chunk_slot_count(
+        budget, 48.0 * (double)(n + nd_out * (1 + direct_splits(n, (int)nd_out, 1, c->sm_count))), S);
+    P.chunks = plan_chunks(L, G, cs);
+    const int ns_max = P.chunks.front().ns;
+    P.nsplit_max = 1;
+    for (const SlotChunk &ch : P.chunks)
+      P.nsplit_max = std::max(P.nsplit_max, direct_splits(n, (int)nd_out, ch.nl, c->sm_count));
+    PO_TRY(c->cur.ensure(sizeof(float2) * 6 * (size_t)ns_max * std::max<int64_t>(n, 1)));
+    PO_TRY(c->tile_ctr.ensure(sizeof(double) * 3 * (size_t)((n + 127) / 128 + 1)));
+    PO_TRY(c->partial.ensure(sizeof(float2) * 6 * (size_t)ns_max * nd_out * P.nsplit_max));
+    PO_TRY(c->levelA.ensure(sizeof(float2) * 6 * (size_t)ns_max * nd_out));
+    if (adj) PO_TRY(c->levelB.ensure(sizeof(float2) * 6 * (size_t)ns_max * nd_out));
+    PO_CUDA(cudaStreamSynchronize(st));
+    return PO_OK;
+  }
+
+  // ---- hierarchical solve
+  P.nleaf = P.tree.level[d].count;
+  PO_TRY(c->leaf_ctr.ensure(sizeof(double) * 3 * (size_t)std::max<int64_t>(P.nleaf, 1)));
+  double3 lo = make_double3(cfg.box_min[0], cfg.box_min[1], cfg.box_min[2]);
+  double3 hi = make_double3(cfg.box_max[0], cfg.box_max[1], cfg.box_max[2]);
+  if (P.nleaf > 0) {
+    k_leaf_centers<<<(unsigned)((P.nleaf + 255) / 256), 256, 0, st>>>(P.tree.level[d].prefix, P.nleaf, d, lo, hi,
+                                                                       c->leaf_ctr.as<double>());
+    count_launch();
+  }
+  // pattern buffers per slot: two level buffers + the row-pass output
+  size_t lvl_max = 0, mid_max = 0;
+  for (int l = 0; l <= d; ++l)
+    lvl_max = std::max(lvl_max, (size_t)P.tree.level[l].count * 6 * (size_t)c->R[l] * c->Phi[l]);
+  for (int l = 0; l < d; ++l)
+    mid_max = std::max(mid_max, (size_t)P.tree.level[l + 1].count * 6 * (size_t)c->R[l + 1] * c->Phi[l]);
+  P.chunks = plan_chunks(L, G, chunk_slot_count(budget, 8.0 * (2.0 * lvl_max + mid_max), S));
+  const int ns_max = P.chunks.front().ns;
+  PO_TRY(c->levelA.ensure(sizeof(float2) * lvl_max * ns_max));
+  PO_TRY(c->levelB.ensure(sizeof(float2) * lvl_max * ns_max));
+  PO_TRY(c->mid.ensure(sizeof(float2) * std::max<size_t>(mid_max * ns_max, 1)));
+  // translation tables (per level, per wavelength)
+  size_t tr_total = 0;
+  P.tr_off.assign(d, 0);
+  for (int l = 0; l < d; ++l) {
+    P.tr_off[l] = tr_total;
+    tr_total += (size_t)L * c->R[l] * c->Phi[l];
+  }
+  PO_TRY(c->trans.ensure(sizeof(float4) * std::max<size_t>(tr_total, 1)));
+  for (int l = 0; l < d; ++l) {
+    double a[3];
+    for (int q = 0; q < 3; ++q) a[q] = ((double)cfg.box_max[q] - (double)cfg.box_min[q]) / std::ldexp(1.0, l + 2);
+    PO_TRY(launch_trans_table(P.k_lambda, L, c->nth[l], c->R[l], c->Phi[l], a, c->trans.as<float4>() + P.tr_off[l],
+                              st));
+  }
+  // leaf directions
+  std::vector<float4> df = host_dirs_f4(c->R[d], c->Phi[d], c->nth[d]);
+  PO_TRY(c->dirs.ensure(sizeof(float4) * df.size()));
+  PO_CUDA(cudaMemcpyAsync(c->dirs.p, df.data(), sizeof(float4) * df.size(), cudaMemcpyHostToDevice, st));
+  PO_CUDA(cudaStreamSynchronize(st));
+  return PO_OK;
+}
+
+// Kernel launches of a prepared solve: per slot chunk the leaf (or depth-0)
+// sums, the level passes, the intensity into out_dev and, for po_grad, the
+// adjoint.  No allocation and no host synchronisation unless `times` asks for
+// per-chunk event timing, so this runs inside a stream capture.
+static po_status enqueue_solve(po_ctx *c, const SolvePlan &P, float *out_dev, const AdjointArgs *adj,
+                               cudaStream_t st, SolveTimes *times) {
+  const po_config &cfg = c->cfg;
+  const int d = c->depth;
+  const int64_t n = P.n, nd_out = P.nd_out;
+  const int nth_out = cfg.n_theta[0], nph_out = cfg.n_phi[0];
+  auto rec = [&](cudaEvent_t e) -> po_status {
+    if (times) PO_CUDA(cudaEventRecord(e, st));
+    return PO_OK;
+  };
+  auto chunk_done = [&](bool tree_levels) -> po_status {
+    if (!times) return PO_OK;
+    PO_CUDA(cudaEventSynchronize(c->ev[4]));
+    float t = 0;
+    if (cudaEventElapsedTime(&t, c->kev[0], c->kev[1]) == cudaSuccess) { times->leafk += t; times->leaf += t; }
+    if (cudaEventElapsedTime(&t, c->kev[1], c->ev[3]) == cudaSuccess) times->agg += t;
+    if (cudaEventElapsedTime(&t, c->ev[3], c->ev[4]) == cudaSuccess) times->inten += t;
+    if (tree_levels)
+      for (int l = 0; l < d; ++l) {
+        if (cudaEventElapsedTime(&t, c->kev[2 + 4 * l], c->kev[3 + 4 * l]) == cudaSuccess) times->rows += t;
+        if (cudaEventElapsedTime(&t, c->kev[4 + 4 * l], c->kev[5 + 4 * l]) == cudaSuccess) times->cols += t;
+      }
+    cudaGetLastError();
+    return PO_OK;
+  };
+  SolveTimes dummy;
+  SolveTimes &T = times ? *times : dummy;
+  if (adj && n > 0) PO_CUDA(cudaMemsetAsync(c->grad_acc.p, 0, sizeof(double) * 7 * (size_t)n, st));
+
+  if (P.fp64) {
+    for (const SlotChunk &ch : P.chunks) {
+      PO_TRY(rec(c->kev[0]));
+      PO_TRY(launch_currents_f64(n, P.gin, c->slots.as<SlotParams<double>>() + ch.s0, ch.ns, c->cur.as<double>(), st));
+      int64_t tiles = (int64_t)ch.ns * ceil_div((int)nd_out, 128);
+      int nsplit = (int)std::max<int64_t>(
+          1, std::min<int64_t>(64, (c->sm_count * 8 + tiles - 1) / std::max<int64_t>(1, tiles)));
+      nsplit = (int)std::min<int64_t>(std::min(nsplit, P.nsplit_max), std::max<int64_t>(1, n));
+      PO_TRY(launch_direct_f64(n, P.gin[0], P.gin[1], P.gin[2], c->cur.as<double2>(), P.k_slot + ch.s0, ch.ns, P.c0,
                                c->dirs_d.as<double>(), (int)nd_out, nsplit, c->partial.as<double2>(),
                                c->levelA.as<double2>(), st));
-      PO_CUDA(cudaEventRecord(c->kev[1], st));
-      PO_CUDA(cudaEventRecord(c->ev[3], st));
+      PO_TRY(rec(c->kev[1]));
+      PO_TRY(rec(c->ev[3]));
       PO_TRY(launch_intensity_f64(c->levelA.as<double2>(), ch.ns, nth_out, nph_out, out_dev + (size_t)ch.s0 * nd_out,
                                   st));
       if (adj) {
         double2 *Gd = c->partial.as<double2>();
         PO_TRY(launch_intensity_adjoint_f64(c->levelA.as<double2>(), adj->dl_di + (size_t)ch.s0 * nd_out, ch.ns,
                                             nth_out, nph_out, Gd, st));
-        PO_TRY(launch_point_adjoint_f64(gin, c->chunk_begin.as<int32_t>(), (n + 31) / 32, c->center0.as<double>(), 0,
-                                        Gd, 0, 6 * nd_out, c->dirs_d.as<double>(), (int)nd_out, sp64_dev + ch.s0,
+        PO_TRY(launch_point_adjoint_f64(P.gin, c->chunk_begin.as<int32_t>(), (n + 31) / 32, c->center0.as<double>(),
+                                        0, Gd, 0, 6 * nd_out, c->dirs_d.as<double>(), (int)nd_out,
+                                        P.sp64_dev + ch.s0, ch.nl, ch.gc, n, c->grad_acc.as<double>(), st));
+      }
+      PO_TRY(rec(c->ev[4]));
+      T.n_leaf += 3;
+      PO_TRY(chunk_done(false));
+    }
+    T.leaf_pd = (double)n * nd_out * P.S;
+  } else if (d == 0) {
+    for (const SlotChunk &ch : P.chunks) {
+      PO_TRY(rec(c->kev[0]));
+      PO_TRY(launch_currents_f32(n, P.gsc, c->slots.as<SlotParams<float>>() + ch.s0, ch.ns, c->cur.as<float>(), st));
+      int nsplit = direct_splits(n, (int)nd_out, ch.nl, c->sm_count);
+      PO_TRY(launch_direct_f32(n, P.gsc[0], P.gsc[1], P.gsc[2], c->cur.as<float2>(), c->tile_ctr.as<double>(),
+                               P.k_lambda + ch.l0, ch.nl, ch.gc, P.c0, c->dirs.as<float4>(), c->dirs_d.as<double>(),
+                               (int)nd_out, nsplit, c->partial.as<float2>(), c->levelA.as<float2>(), st));
+      PO_TRY(rec(c->kev[1]));
+      PO_TRY(rec(c->ev[3]));
+      PO_TRY(launch_intensity_f32(c->levelA.as<float2>(), ch.ns, nth_out, nph_out, nth_out, nph_out, 1, 1,
+                                  out_dev + (size_t)ch.s0 * nd_out, st));
+      if (adj) {
+        float2 *Gf = c->levelB.as<float2>();
+        PO_TRY(launch_intensity_adjoint_f32(c->levelA.as<float2>(), adj->dl_di + (size_t)ch.s0 * nd_out, ch.ns,
+                                            nth_out, nph_out, nth_out, nph_out, 1, 1, Gf, st));
+        PO_TRY(launch_point_adjoint_f32(P.gsc, c->chunk_begin.as<int32_t>(), (n + 31) / 32, c->center0.as<double>(), 0,
+                                        Gf, 0, 6 * nd_out, c->dirs.as<float4>(), (int)nd_out, P.sp64_dev + ch.s0,
                                         ch.nl, ch.gc, n, c->grad_acc.as<double>(), st));
       }
-      PO_CUDA(cudaEventRecord(c->ev[4], st));
-      n_leaf_launches += 3;
-      if (rep) {
-        PO_CUDA(cudaEventSynchronize(c->ev[4]));
-        chunk_times(false);
-      }
+      PO_TRY(rec(c->ev[4]));
+      T.n_leaf += 3 + (ch.gc + 3) / 4;
+      PO_TRY(chunk_done(false));
     }
-    leaf_pd = (double)n * nd_out * S;
+    T.leaf_pd = (double)n * nd_out * P.S;
   } else {
-    // ---- octree (depth 0 still sorts the points so that direct-sum tiles are compact)
-    PO_CUDA(cudaEventRecord(c->ev[1], st));
-    const int tdepth = d > 0 ? d : 6;
-    size_t wsb = octree_workspace_bytes(n, tdepth);
-    PO_TRY(c->octree_ws.ensure(wsb));
-    OctreeBuffers tree;
-    PO_TRY(build_octree(gin[0], gin[1], gin[2], n, cfg.box_min, cfg.box_max, tdepth, c->octree_ws.p, wsb, &tree, st));
-    PO_TRY(c->geom_sorted.ensure(sizeof(float) * 7 * (size_t)std::max<int64_t>(n, 1)));
-    float *gs[7];
-    for (int k = 0; k < 7; ++k) gs[k] = c->geom_sorted.as<float>() + (size_t)k * n;
-    PO_TRY(gather_points(n, tree.perm, gin, gs, st));
-    const float *gsc[7] = {gs[0], gs[1], gs[2], gs[3], gs[4], gs[5], gs[6]};
-    PO_CUDA(cudaEventRecord(c->ev[2], st));
-    if (rep) {
-      rep->n_leaves = tree.level[tdepth].count;
-      int64_t tot = 0;
-      for (int l = 0; l <= tdepth; ++l) tot += tree.level[l].count;
-      rep->n_nodes_total = tot;
-    }
-    if (d == 0) {
-      std::vector<float4> df = host_dirs_f4(nth_out, nph_out, nth_out);
-      std::vector<double> dd = host_dirs_d(nth_out, nph_out, nth_out);
-      PO_TRY(c->dirs.ensure(sizeof(float4) * df.size()));
-      PO_TRY(c->dirs_d.ensure(sizeof(double) * dd.size()));
-      PO_CUDA(cudaMemcpyAsync(c->dirs.p, df.data(), sizeof(float4) * df.size(), cudaMemcpyHostToDevice, st));
-      PO_CUDA(cudaMemcpyAsync(c->dirs_d.p, dd.data(), sizeof(double) * dd.size(), cudaMemcpyHostToDevice, st));
-      int cs = chunk_slot_count(budget, 48.0 * (double)(n + nd_out * (1 + direct_splits(n, (int)nd_out, 1, c->sm_count))), S);
-      chunks = plan_chunks(L, G, cs);
-      const int ns_max = chunks.front().ns;
-      int nsplit_max = 1;
-      for (const SlotChunk &ch : chunks)
-        nsplit_max = std::max(nsplit_max, direct_splits(n, (int)nd_out, ch.nl, c->sm_count));
-      PO_TRY(c->cur.ensure(sizeof(float2) * 6 * (size_t)ns_max * std::max<int64_t>(n, 1)));
-      PO_TRY(c->tile_ctr.ensure(sizeof(double) * 3 * (size_t)((n + 127) / 128 + 1)));
-      PO_TRY(c->partial.ensure(sizeof(float2) * 6 * (size_t)ns_max * nd_out * nsplit_max));
-      PO_TRY(c->levelA.ensure(sizeof(float2) * 6 * (size_t)ns_max * nd_out));
-      if (adj) PO_TRY(c->levelB.ensure(sizeof(float2) * 6 * (size_t)ns_max * nd_out));
-      perm_out = tree.perm;
-      for (const SlotChunk &ch : chunks) {
-        PO_CUDA(cudaEventRecord(c->kev[0], st));
-        PO_TRY(launch_currents_f32(n, gsc, c->slots.as<SlotParams<float>>() + ch.s0, ch.ns, c->cur.as<float>(), st));
-        int nsplit = direct_splits(n, (int)nd_out, ch.nl, c->sm_count);
-        PO_TRY(launch_direct_f32(n, gs[0], gs[1], gs[2], c->cur.as<float2>(), c->tile_ctr.as<double>(),
-                                 k_lambda + ch.l0, ch.nl, ch.gc, c0, c->dirs.as<float4>(), c->dirs_d.as<double>(),
-                                 (int)nd_out, nsplit, c->partial.as<float2>(), c->levelA.as<float2>(), st));
-        PO_CUDA(cudaEventRecord(c->kev[1], st));
-        PO_CUDA(cudaEventRecord(c->ev[3], st));
-        PO_TRY(launch_intensity_f32(c->levelA.as<float2>(), ch.ns, nth_out, nph_out, nth_out, nph_out, 1, 1,
-                                    out_dev + (size_t)ch.s0 * nd_out, st));
-        if (adj) {
-          float2 *Gf = c->levelB.as<float2>();
-          PO_TRY(launch_intensity_adjoint_f32(c->levelA.as<float2>(), adj->dl_di + (size_t)ch.s0 * nd_out, ch.ns,
-                                              nth_out, nph_out, nth_out, nph_out, 1, 1, Gf, st));
-          PO_TRY(launch_point_adjoint_f32(gsc, c->chunk_begin.as<int32_t>(), (n + 31) / 32, c->center0.as<double>(),
-                                          0, Gf, 0, 6 * nd_out, c->dirs.as<float4>(), (int)nd_out, sp64_dev + ch.s0,
-                                          ch.nl, ch.gc, n, c->grad_acc.as<double>(), st));
+    const int refnq = c->cover == 1 ? 1 : 0;
+    for (const SlotChunk &ch : P.chunks) {
+      const SlotParams<float> *sp = c->slots.as<SlotParams<float>>() + ch.s0;
+      PO_TRY(rec(c->kev[0]));
+      if (cfg.precision == PO_PREC_SPLIT_BF16)
+        PO_TRY(launch_leaf_mma(P.gsc, P.tree.level[d].begin, c->leaf_ctr.as<double>(), P.nleaf, sp, ch.nl, ch.gc,
+                               c->dirs.as<float4>(), c->R[d] * c->Phi[d], c->levelA.as<float2>(), st));
+      else
+        PO_TRY(launch_leaf(P.gsc, P.tree.level[d].begin, c->leaf_ctr.as<double>(), P.nleaf, sp, ch.nl, ch.gc,
+                           c->dirs.as<float4>(), c->R[d] * c->Phi[d], c->levelA.as<float2>(), st));
+      PO_TRY(rec(c->kev[1]));
+      T.n_leaf += P.nleaf > 0 ? (ch.gc + 3) / 4 : 0;
+      float2 *cur_lvl = c->levelA.as<float2>(), *nxt = c->levelB.as<float2>();
+      for (int l = d - 1; l >= 0; --l) {
+        const int64_t nc = P.tree.level[l + 1].count, np = P.tree.level[l].count;
+        const float4 *trans = c->trans.as<float4>() + P.tr_off[l] + (size_t)ch.l0 * c->R[l] * c->Phi[l];
+        int64_t nrows = (int64_t)ch.ns * nc * 6 * c->R[l + 1];
+        PO_TRY(rec(c->kev[2 + 4 * l]));
+        if (c->tensor_theta) {
+          PO_TRY(launch_interp_rows_mma(cur_lvl, c->mid.as<float2>(), nrows, c->Phi[l + 1], c->Phi[l], c->bmat_kp[l],
+                                        c->bmat.as<uint32_t>() + c->bmat_off[l], c->sm_count, st));
+        } else {
+          FftPlan prow_in = make_plan(c->Phi[l + 1], c->tw_offset[c->Phi[l + 1]]);
+          FftPlan prow_out = make_plan(c->Phi[l], c->tw_offset[c->Phi[l]]);
+          PO_TRY(launch_interp_rows(cur_lvl, c->mid.as<float2>(), nrows, prow_in, prow_out, c->twiddles.as<float2>(),
+                                    1.0f / (float)c->Phi[l + 1], c->sm_count, refnq, st));
         }
-        PO_CUDA(cudaEventRecord(c->ev[4], st));
-        n_leaf_launches += 3 + (ch.gc + 3) / 4;
-        if (rep) {
-          PO_CUDA(cudaEventSynchronize(c->ev[4]));
-          chunk_times(false);
+        PO_TRY(rec(c->kev[3 + 4 * l]));
+        T.rows_b += 8.0 * nrows * (c->Phi[l + 1] + c->Phi[l]);
+        T.cols_b += 8.0 * ch.ns * 6 * ((double)nc * c->R[l + 1] * c->Phi[l] + (double)np * c->R[l] * c->Phi[l]);
+        if (nrows > 0) ++T.n_row;
+        if (np > 0) ++T.n_col;
+        PO_TRY(rec(c->kev[4 + 4 * l]));
+        if (c->tensor_theta) {
+          PO_TRY(launch_interp_cols_mma(c->mid.as<float2>(), nxt, P.tree.level[l].child, np, nc, c->Phi[l],
+                                        c->R[l + 1], c->R[l], c->amat_kp[l], c->mirror,
+                                        c->amat.as<uint32_t>() + c->amat_off[l], trans, ch.ns, ch.gc, cfg.interp_tile,
+                                        st));
+        } else {
+          FftPlan pcol_in = make_plan(c->T[l + 1], c->tw_offset[c->T[l + 1]]);
+          FftPlan pcol_out = make_plan(c->T[l], c->tw_offset[c->T[l]]);
+          int reach = 0x7fffffff;
+          if (c->cover == 1 && cfg.nyquist_quirk) reach = 256 * (c->T[l + 1] / 256 + 1);
+          PO_TRY(launch_interp_cols(c->mid.as<float2>(), nxt, P.tree.level[l].child, np, nc, c->Phi[l], c->R[l + 1],
+                                    c->R[l], pcol_in, pcol_out, c->twiddles.as<float2>(), trans, ch.ns, ch.gc, reach,
+                                    1.0f / (float)c->T[l + 1], 6, c->mirror, refnq, st));
         }
+        PO_TRY(rec(c->kev[5 + 4 * l]));
+        std::swap(cur_lvl, nxt);
       }
-      leaf_pd = (double)n * nd_out * S;
-    } else {
-      // ---- hierarchical solve
-      const int64_t nleaf = tree.level[d].count;
-      PO_TRY(c->leaf_ctr.ensure(sizeof(double) * 3 * (size_t)std::max<int64_t>(nleaf, 1)));
-      double3 lo = make_double3(cfg.box_min[0], cfg.box_min[1], cfg.box_min[2]);
-      double3 hi = make_double3(cfg.box_max[0], cfg.box_max[1], cfg.box_max[2]);
-      if (nleaf > 0) {
-        k_leaf_centers<<<(unsigned)((nleaf + 255) / 256), 256, 0, st>>>(tree.level[d].prefix, nleaf, d, lo, hi,
-                                                                         c->leaf_ctr.as<double>());
-        count_launch();
-      }
-      // pattern buffers per slot: two level buffers + the row-pass output
-      size_t lvl_max = 0, mid_max = 0;
-      for (int l = 0; l <= d; ++l)
-        lvl_max = std::max(lvl_max, (size_t)tree.level[l].count * 6 * (size_t)c->R[l] * c->Phi[l]);
-      for (int l = 0; l < d; ++l)
-        mid_max = std::max(mid_max, (size_t)tree.level[l + 1].count * 6 * (size_t)c->R[l + 1] * c->Phi[l]);
-      chunks = plan_chunks(L, G, chunk_slot_count(budget, 8.0 * (2.0 * lvl_max + mid_max), S));
-      const int ns_max = chunks.front().ns;
-      PO_TRY(c->levelA.ensure(sizeof(float2) * lvl_max * ns_max));
-      PO_TRY(c->levelB.ensure(sizeof(float2) * lvl_max * ns_max));
-      PO_TRY(c->mid.ensure(sizeof(float2) * std::max<size_t>(mid_max * ns_max, 1)));
-      // translation tables (per level, per wavelength)
-      size_t tr_total = 0;
-      std::vector<size_t> tr_off(d);
-      for (int l = 0; l < d; ++l) {
-        tr_off[l] = tr_total;
-        tr_total += (size_t)L * c->R[l] * c->Phi[l];
-      }
-      PO_TRY(c->trans.ensure(sizeof(float4) * std::max<size_t>(tr_total, 1)));
-      for (int l = 0; l < d; ++l) {
-        double a[3];
-        for (int q = 0; q < 3; ++q) a[q] = ((double)cfg.box_max[q] - (double)cfg.box_min[q]) / std::ldexp(1.0, l + 2);
-        PO_TRY(launch_trans_table(k_lambda, L, c->nth[l], c->R[l], c->Phi[l], a, c->trans.as<float4>() + tr_off[l],
-                                  st));
-      }
-      // leaf directions
-      std::vector<float4> df = host_dirs_f4(c->R[d], c->Phi[d], c->nth[d]);
-      PO_TRY(c->dirs.ensure(sizeof(float4) * df.size()));
-      PO_CUDA(cudaMemcpyAsync(c->dirs.p, df.data(), sizeof(float4) * df.size(), cudaMemcpyHostToDevice, st));
-      const int refnq = c->cover == 1 ? 1 : 0;
-      perm_out = tree.perm;
-      for (const SlotChunk &ch : chunks) {
-        const SlotParams<float> *sp = c->slots.as<SlotParams<float>>() + ch.s0;
-        PO_CUDA(cudaEventRecord(c->kev[0], st));
-        if (cfg.precision == PO_PREC_SPLIT_BF16)
-          PO_TRY(launch_leaf_mma(gsc, tree.level[d].begin, c->leaf_ctr.as<double>(), nleaf, sp, ch.nl, ch.gc,
-                                 c->dirs.as<float4>(), c->R[d] * c->Phi[d], c->levelA.as<float2>(), st));
-        else
-          PO_TRY(launch_leaf(gsc, tree.level[d].begin, c->leaf_ctr.as<double>(), nleaf, sp, ch.nl, ch.gc,
-                             c->dirs.as<float4>(), c->R[d] * c->Phi[d], c->levelA.as<float2>(), st));
-        PO_CUDA(cudaEventRecord(c->kev[1], st));
-        n_leaf_launches += nleaf > 0 ? (ch.gc + 3) / 4 : 0;
-        float2 *cur_lvl = c->levelA.as<float2>(), *nxt = c->levelB.as<float2>();
-        for (int l = d - 1; l >= 0; --l) {
-          const int64_t nc = tree.level[l + 1].count, np = tree.level[l].count;
-          const float4 *trans = c->trans.as<float4>() + tr_off[l] + (size_t)ch.l0 * c->R[l] * c->Phi[l];
-          int64_t nrows = (int64_t)ch.ns * nc * 6 * c->R[l + 1];
-          PO_CUDA(cudaEventRecord(c->kev[2 + 4 * l], st));
-          if (c->tensor_theta) {
-            PO_TRY(launch_interp_rows_mma(cur_lvl, c->mid.as<float2>(), nrows, c->Phi[l + 1], c->Phi[l],
-                                          c->bmat_kp[l], c->bmat.as<uint32_t>() + c->bmat_off[l], c->sm_count, st));
-          } else {
-            FftPlan prow_in = make_plan(c->Phi[l + 1], c->tw_offset[c->Phi[l + 1]]);
-            FftPlan prow_out = make_plan(c->Phi[l], c->tw_offset[c->Phi[l]]);
-            PO_TRY(launch_interp_rows(cur_lvl, c->mid.as<float2>(), nrows, prow_in, prow_out,
-                                      c->twiddles.as<float2>(), 1.0f / (float)c->Phi[l + 1], c->sm_count, refnq, st));
-          }
-          PO_CUDA(cudaEventRecord(c->kev[3 + 4 * l], st));
-          rows_b += 8.0 * nrows * (c->Phi[l + 1] + c->Phi[l]);
-          cols_b += 8.0 * ch.ns * 6 * ((double)nc * c->R[l + 1] * c->Phi[l] + (double)np * c->R[l] * c->Phi[l]);
-          if (nrows > 0) ++n_row_launches;
-          if (np > 0) ++n_col_launches;
-          PO_CUDA(cudaEventRecord(c->kev[4 + 4 * l], st));
-          if (c->tensor_theta) {
-            PO_TRY(launch_interp_cols_mma(c->mid.as<float2>(), nxt, tree.level[l].child, np, nc, c->Phi[l],
-                                          c->R[l + 1], c->R[l], c->amat_kp[l], c->mirror,
-                                          c->amat.as<uint32_t>() + c->amat_off[l], trans, ch.ns, ch.gc, st));
-          } else {
-            FftPlan pcol_in = make_plan(c->T[l + 1], c->tw_offset[c->T[l + 1]]);
-            FftPlan pcol_out = make_plan(c->T[l], c->tw_offset[c->T[l]]);
-            int reach = 0x7fffffff;
-            if (c->cover == 1 && cfg.nyquist_quirk) reach = 256 * (c->T[l + 1] / 256 + 1);
-            PO_TRY(launch_interp_cols(c->mid.as<float2>(), nxt, tree.level[l].child, np, nc, c->Phi[l],
-                                      c->R[l + 1], c->R[l], pcol_in, pcol_out, c->twiddles.as<float2>(), trans,
-                                      ch.ns, ch.gc, reach, 1.0f / (float)c->T[l + 1], 6, c->mirror, refnq, st));
-          }
-          PO_CUDA(cudaEventRecord(c->kev[5 + 4 * l], st));
+      PO_TRY(rec(c->ev[3]));
+      PO_TRY(launch_intensity_f32(cur_lvl, ch.ns, c->R[0], c->Phi[0], nth_out, nph_out, c->mt, c->mp,
+                                  out_dev + (size_t)ch.s0 * nd_out, st));
+      if (adj) {
+        // root adjoint, then the transposed aggregation down to the leaves
+        PO_TRY(launch_intensity_adjoint_f32(cur_lvl, adj->dl_di + (size_t)ch.s0 * nd_out, ch.ns, c->R[0], c->Phi[0],
+                                            nth_out, nph_out, c->mt, c->mp, nxt, st));
+        std::swap(cur_lvl, nxt);
+        for (int l = 0; l < d; ++l) {
+          const int64_t np = P.tree.level[l].count, nc = P.tree.level[l + 1].count;
+          const float4 *trans = c->trans.as<float4>() + P.tr_off[l] + (size_t)ch.l0 * c->R[l] * c->Phi[l];
+          PO_TRY(launch_interp_cols_adj_mma(cur_lvl, c->mid.as<float2>(), P.tree.level[l + 1].parent,
+                                            P.tree.level[l + 1].prefix, np, nc, c->Phi[l], c->R[l + 1], c->R[l],
+                                            c->amat_adj_kp[l], c->amat_adj.as<uint32_t>() + c->amat_adj_off[l], trans,
+                                            ch.ns, ch.gc, st));
+          PO_TRY(launch_interp_rows_mma(c->mid.as<float2>(), nxt, (int64_t)ch.ns * nc * 6 * c->R[l + 1], c->Phi[l],
+                                        c->Phi[l + 1], c->bmat_adj_kp[l],
+                                        c->bmat_adj.as<uint32_t>() + c->bmat_adj_off[l], c->sm_count, st));
           std::swap(cur_lvl, nxt);
         }
-        PO_CUDA(cudaEventRecord(c->ev[3], st));
-        PO_TRY(launch_intensity_f32(cur_lvl, ch.ns, c->R[0], c->Phi[0], nth_out, nph_out, c->mt, c->mp,
-                                    out_dev + (size_t)ch.s0 * nd_out, st));
-        if (adj) {
-          // root adjoint, then the transposed aggregation down to the leaves
-          PO_TRY(launch_intensity_adjoint_f32(cur_lvl, adj->dl_di + (size_t)ch.s0 * nd_out, ch.ns, c->R[0], c->Phi[0],
-                                              nth_out, nph_out, c->mt, c->mp, nxt, st));
-          std::swap(cur_lvl, nxt);
-          for (int l = 0; l < d; ++l) {
-            const int64_t np = tree.level[l].count, nc = tree.level[l + 1].count;
-            const float4 *trans = c->trans.as<float4>() + tr_off[l] + (size_t)ch.l0 * c->R[l] * c->Phi[l];
-            PO_TRY(launch_interp_cols_adj_mma(cur_lvl, c->mid.as<float2>(), tree.level[l + 1].parent,
-                                              tree.level[l + 1].prefix, np, nc, c->Phi[l], c->R[l + 1], c->R[l],
-                                              c->amat_adj_kp[l], c->amat_adj.as<uint32_t>() + c->amat_adj_off[l],
-                                              trans, ch.ns, ch.gc, st));
-            PO_TRY(launch_interp_rows_mma(c->mid.as<float2>(), nxt, (int64_t)ch.ns * nc * 6 * c->R[l + 1], c->Phi[l],
-                                          c->Phi[l + 1], c->bmat_adj_kp[l],
-                                          c->bmat_adj.as<uint32_t>() + c->bmat_adj_off[l], c->sm_count, st));
-            std::swap(cur_lvl, nxt);
-          }
-          const int64_t ndl = (int64_t)c->R[d] * c->Phi[d];
-          PO_TRY(launch_point_adjoint_f32(gsc, tree.level[d].begin, nleaf, c->leaf_ctr.as<double>(), 1, cur_lvl,
-                                          6 * ndl, nleaf * 6 * ndl, c->dirs.as<float4>(), (int)ndl, sp64_dev + ch.s0,
-                                          ch.nl, ch.gc, n, c->grad_acc.as<double>(), st));
-        }
-        PO_CUDA(cudaEventRecord(c->ev[4], st));
-        if (rep) {
-          PO_CUDA(cudaEventSynchronize(c->ev[4]));
-          chunk_times(true);
-        }
+        const int64_t ndl = (int64_t)c->R[d] * c->Phi[d];
+        PO_TRY(launch_point_adjoint_f32(P.gsc, P.tree.level[d].begin, P.nleaf, c->leaf_ctr.as<double>(), 1, cur_lvl,
+                                        6 * ndl, P.nleaf * 6 * ndl, c->dirs.as<float4>(), (int)ndl, P.sp64_dev + ch.s0,
+                                        ch.nl, ch.gc, n, c->grad_acc.as<double>(), st));
       }
-      leaf_pd = (double)n * c->R[d] * c->Phi[d] * S;
+      PO_TRY(rec(c->ev[4]));
+      PO_TRY(chunk_done(true));
     }
+    T.leaf_pd = (double)n * c->R[d] * c->Phi[d] * P.S;
   }
-  if (adj) PO_TRY(launch_scatter_grad(c->grad_acc.as<double>(), perm_out, n, adj->grad, st));
+  if (adj) PO_TRY(launch_scatter_grad(c->grad_acc.as<double>(), P.perm_out, n, adj->grad, st));
+  return PO_OK;
+}
+
+static po_status solve_impl(po_ctx *c, const po_geometry *g, const po_illum *il, float *intensity, int out_on_device,
+                            cudaStream_t st, po_report *rep, const AdjointArgs *adj = nullptr) {
+  const int64_t launches0 = g_launch_count;
+  PO_CUDA(cudaEventRecord(c->ev[0], st));
+  SolvePlan P;
+  PO_CUDA(cudaEventRecord(c->ev[1], st));
+  PO_TRY(prepare_solve(c, g, il, adj != nullptr, st, P));
+  PO_CUDA(cudaEventRecord(c->ev[2], st));
+  float *out_dev = intensity;
+  if (!out_on_device || !intensity) {
+    PO_TRY(c->out.ensure(sizeof(float) * (size_t)P.S * P.nd_out));
+    out_dev = c->out.as<float>();
+  }
+  SolveTimes T;
+  PO_TRY(enqueue_solve(c, P, out_dev, adj, st, rep ? &T : nullptr));
   if (intensity && !out_on_device)
-    PO_CUDA(cudaMemcpyAsync(intensity, out_dev, sizeof(float) * (size_t)S * nd_out, cudaMemcpyDeviceToHost, st));
+    PO_CUDA(cudaMemcpyAsync(intensity, out_dev, sizeof(float) * (size_t)P.S * P.nd_out, cudaMemcpyDeviceToHost, st));
   PO_CUDA(cudaEventRecord(c->ev[5], st));
   if (rep || !out_on_device) PO_CUDA(cudaEventSynchronize(c->ev[5]));
   PO_CUDA(cudaGetLastError());
@@ -760,11 +834,18 @@ static po_status solve_impl(po_ctx *c, const po_geometry *g, const po_illum *il,
     cudaEventElapsedTime(&t[1], c->ev[1], c->ev[2]);
     rep->ms_total = t[0];
     rep->ms_build = t[1];
-    rep->ms_leaf = t_leaf;
-    rep->ms_aggregate = t_agg;
-    rep->ms_intensity = t_int;
+    rep->ms_leaf = T.leaf;
+    rep->ms_aggregate = T.agg;
+    rep->ms_intensity = T.inten;
     rep->root_theta = c->nth[0];
     rep->root_phi = c->Phi[0];
+    if (!P.fp64) {
+      const int tdepth = c->depth > 0 ? c->depth : 6;
+      rep->n_leaves = P.tree.level[tdepth].count;
+      int64_t tot = 0;
+      for (int l = 0; l <= tdepth; ++l) tot += P.tree.level[l].count;
+      rep->n_nodes_total = tot;
+    }
     int64_t ws = 0;
     for (DevBuf *b : {&c->twiddles, &c->geom_in, &c->geom_sorted, &c->octree_ws, &c->leaf_ctr, &c->dirs, &c->dirs_d,
                       &c->trans, &c->levelA, &c->levelB, &c->mid, &c->slots, &c->kvals, &c->out, &c->cur, &c->partial,
@@ -772,17 +853,17 @@ static po_status solve_impl(po_ctx *c, const po_geometry *g, const po_illum *il,
       ws += (int64_t)b->bytes;
     rep->workspace_bytes = ws;
     rep->kernel_launches = g_launch_count - launches0;
-    rep->n_leaf_launches = n_leaf_launches;
-    rep->n_row_launches = n_row_launches;
-    rep->n_col_launches = n_col_launches;
-    rep->n_chunks = (int)chunks.size();
-    rep->chunk_slots = chunks.empty() ? 0 : chunks.front().ns;
-    rep->leaf_point_dirs = leaf_pd;
-    rep->rows_bytes = rows_b;
-    rep->cols_bytes = cols_b;
-    rep->ms_leaf_kernel = t_leafk;
-    rep->ms_rows = t_rows;
-    rep->ms_cols = t_cols;
+    rep->n_leaf_launches = T.n_leaf;
+    rep->n_row_launches = T.n_row;
+    rep->n_col_launches = T.n_col;
+    rep->n_chunks = (int)P.chunks.size();
+    rep->chunk_slots = P.chunks.empty() ? 0 : P.chunks.front().ns;
+    rep->leaf_point_dirs = T.leaf_pd;
+    rep->rows_bytes = T.rows_b;
+    rep->cols_bytes = T.cols_b;
+    rep->ms_leaf_kernel = T.leafk;
+    rep->ms_rows = T.rows;
+    rep->ms_cols = T.cols;
     cudaGetLastError();
   }
   return PO_OK;
@@ -946,6 +1027,11 @@ po_status po_interp_fft(const float *in, int th_c, int ph_c, float *out, int th_
   if (theta_mode != PO_THETA_DOUBLE_COVER && theta_mode != PO_THETA_REFERENCE)
     return fail(PO_ERR_INVALID_ARGUMENT, "unknown theta mode");
   if (batch == 0) return PO_OK;
+  {
+    int dev = 0;
+    PO_CUDA(cudaGetDevice(&dev));
+    PO_TRY(init_device_attributes(dev));
+  }
   cudaStream_t st = (cudaStream_t)stream;
   std::vector<int> lens = {ph_c, ph_p, th_c, th_p};
   std::sort(lens.begin(), lens.end());
@@ -982,6 +1068,205 @@ po_status po_compute_intensity(const float *fields, int n_theta, int n_phi, floa
   if (!fields || !intensity || n_theta <= 0 || n_phi <= 0) return fail(PO_ERR_INVALID_ARGUMENT, "invalid argument");
   return launch_intensity_f32((const float2 *)fields, 1, n_theta, n_phi, n_theta, n_phi, 1, 1, intensity,
                               (cudaStream_t)stream);
+}
+
+
+// ------------------------------------------------------------------ batches
+struct po_batch {
+  std::vector<po_ctx *> ctx;
+  std::vector<SolvePlan> plans;
+  std::vector<int> branch;  // stream branch of each item
+  int n_streams = 1;
+  std::vector<cudaStream_t> streams;
+  std::vector<cudaEvent_t> joins;
+  cudaEvent_t fork = nullptr;
+  cudaStream_t cap = nullptr;  // capture origin (the caller's stream may be the legacy default stream)
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  int64_t nodes = 0;
+  double ms_prepare = 0;
+  int device = 0;
+};
+
+static void batch_release_graph(po_batch *b) {
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  if (b->graph) cudaGraphDestroy(b->graph);
+  b->exec = nullptr;
+  b->graph = nullptr;
+  b->nodes = 0;
+}
+
+po_status po_batch_destroy(po_batch *b) {
+  if (!b) return PO_OK;
+  batch_release_graph(b);
+  for (po_ctx *c : b->ctx) po_destroy(c);
+  for (cudaStream_t s : b->streams)
+    if (s) cudaStreamDestroy(s);
+  for (cudaEvent_t e : b->joins)
+    if (e) cudaEventDestroy(e);
+  if (b->fork) cudaEventDestroy(b->fork);
+  if (b->cap) cudaStreamDestroy(b->cap);
+  delete b;
+  return PO_OK;
+}
+
+po_status po_batch_create(po_batch **out, int n_items, const po_config *configs, int n_streams) {
+  if (!out || !configs || n_items <= 0) return fail(PO_ERR_INVALID_ARGUMENT, "null argument or empty batch");
+  if (n_streams < 1 || n_streams > 64) return fail(PO_ERR_INVALID_ARGUMENT, "n_streams must be in [1, 64]");
+  *out = nullptr;
+  po_batch *b = new po_batch();
+  b->n_streams = n_streams;
+  cudaGetDevice(&b->device);
+  for (int i = 0; i < n_items; ++i) {
+    if (configs[i].precision == PO_PREC_FP64) {
+      po_batch_destroy(b);
+      return fail(PO_ERR_UNSUPPORTED, "batches run the FP32 / split-BF16 engine (no PO_PREC_FP64 items)");
+    }
+    po_ctx *c = nullptr;
+    po_status s = po_create(&c, &configs[i]);
+    if (s != PO_OK) {
+      po_batch_destroy(b);
+      return s;
+    }
+    b->ctx.push_back(c);
+  }
+  b->streams.assign(n_streams, nullptr);
+  b->joins.assign(n_streams, nullptr);
+  for (int k = 0; k < n_streams; ++k) {
+    if (cudaStreamCreateWithFlags(&b->streams[k], cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->joins[k], cudaEventDisableTiming) != cudaSuccess) {
+      po_batch_destroy(b);
+      return fail(PO_ERR_CUDA, "stream / event creation failed");
+    }
+  }
+  if (cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&b->cap, cudaStreamNonBlocking) != cudaSuccess) {
+    po_batch_destroy(b);
+    return fail(PO_ERR_CUDA, "event / stream creation failed");
+  }
+  *out = b;
+  return PO_OK;
+}
+
+// Estimated device work of a prepared item (multiply-adds of its leaf sums
+// and level GEMMs), for the branch assignment.
+static double plan_cost(const po_ctx *c, const SolvePlan &P) {
+  const int d = c->depth;
+  if (d == 0) return (double)P.S * (double)P.n * (double)P.nd_out;
+  double w = (double)P.n * c->R[d] * c->Phi[d];
+  for (int l = 0; l < d; ++l)
+    w += (double)P.tree.level[l + 1].count * 6.0 * c->R[l + 1] * (double)c->Phi[l] * (c->Phi[l + 1] + 2.0 * c->R[l]);
+  return (double)P.S * w;
+}
+
+po_status po_batch_prepare(po_batch *b, const po_batch_item *items, void *stream) {
+  if (!b || !items) return fail(PO_ERR_INVALID_ARGUMENT, "null argument");
+  int dev = 0;
+  PO_CUDA(cudaGetDevice(&dev));
+  if (dev != b->device) return fail(PO_ERR_INVALID_ARGUMENT, "batch was created on another device");
+  const int n = (int)b->ctx.size();
+  for (int i = 0; i < n; ++i) {
+    const po_batch_item &it = items[i];
+    if (!it.geom.on_device) return fail(PO_ERR_INVALID_ARGUMENT, "batch geometry must be device memory");
+    if (!it.intensity) return fail(PO_ERR_INVALID_ARGUMENT, "null intensity of a batch item");
+    if (it.geom.n < 0 || (it.geom.n > 0 && (!it.geom.x || !it.geom.y || !it.geom.z || !it.geom.nx || !it.geom.ny ||
+                                             !it.geom.nz || !it.geom.area)))
+      return fail(PO_ERR_INVALID_ARGUMENT, "null geometry array in a batch item");
+    const po_illum &il = it.illum;
+    if (il.n_lambda <= 0 || !il.lambda_m || il.n_inc <= 0 || !il.theta_i || !il.phi_i || !(il.sigma > 0) ||
+        (il.pol_mask & (PO_POL_TM | PO_POL_TE)) == 0 || (il.pol_mask & ~(PO_POL_TM | PO_POL_TE)))
+      return fail(PO_ERR_INVALID_ARGUMENT, "invalid illumination in a batch item");
+    for (int l = 0; l < il.n_lambda; ++l)
+      if (!(il.lambda_m[l] > 0) || !std::isfinite(il.lambda_m[l]))
+        return fail(PO_ERR_INVALID_ARGUMENT, "wavelengths must be positive");
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  batch_release_graph(b);
+  const auto t0 = std::chrono::steady_clock::now();
+  b->plans.assign(n, SolvePlan());
+  for (int i = 0; i < n; ++i) PO_TRY(prepare_solve(b->ctx[i], &items[i].geom, &items[i].illum, false, st, b->plans[i]));
+  // branch assignment: longest estimated item first onto the least loaded branch
+  std::vector<int> order(n);
+  std::vector<double> cost(n);
+  for (int i = 0; i < n; ++i) {
+    order[i] = i;
+    cost[i] = plan_cost(b->ctx[i], b->plans[i]);
+  }
+  std::sort(order.begin(), order.end(), [&](int a, int c) { return cost[a] > cost[c]; });
+  std::vector<double> load(b->n_streams, 0.0);
+  b->branch.assign(n, 0);
+  std::vector<std::vector<int>> per(b->n_streams);
+  for (int i : order) {
+    int k = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+    b->branch[i] = k;
+    load[k] += cost[i];
+    per[k].push_back(i);
+  }
+  // capture on the batch's own stream: fork onto the branches, enqueue, join
+  PO_CUDA(cudaStreamSynchronize(st));
+  const cudaStream_t cap = b->cap;
+  PO_CUDA(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
+  po_status s = PO_OK;
+  cudaError_t e = cudaEventRecord(b->fork, cap);
+  if (e != cudaSuccess) s = cuda_fail(e, "cudaEventRecord(fork)");
+  for (int k = 0; k < b->n_streams && s == PO_OK; ++k) {
+    e = cudaStreamWaitEvent(b->streams[k], b->fork, 0);
+    if (e != cudaSuccess) s = cuda_fail(e, "cudaStreamWaitEvent(fork)");
+    for (int i : per[k]) {
+      if (s != PO_OK) break;
+      s = enqueue_solve(b->ctx[i], b->plans[i], items[i].intensity, nullptr, b->streams[k], nullptr);
+    }
+    if (s == PO_OK) {
+      e = cudaEventRecord(b->joins[k], b->streams[k]);
+      if (e != cudaSuccess) s = cuda_fail(e, "cudaEventRecord(join)");
+    }
+    if (s == PO_OK) {
+      e = cudaStreamWaitEvent(cap, b->joins[k], 0);
+      if (e != cudaSuccess) s = cuda_fail(e, "cudaStreamWaitEvent(join)");
+    }
+  }
+  cudaGraph_t g = nullptr;
+  e = cudaStreamEndCapture(cap, &g);
+  if (s != PO_OK) {
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();
+    return s;
+  }
+  if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+  b->graph = g;
+  e = cudaGraphInstantiate(&b->exec, g, 0);
+  if (e != cudaSuccess) {
+    batch_release_graph(b);
+    return cuda_fail(e, "cudaGraphInstantiate");
+  }
+  size_t nn = 0;
+  if (cudaGraphGetNodes(g, nullptr, &nn) == cudaSuccess) b->nodes = (int64_t)nn;
+  PO_CUDA(cudaStreamSynchronize(st));
+  b->ms_prepare = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  return PO_OK;
+}
+
+po_status po_batch_launch(po_batch *b, void *stream) {
+  if (!b) return fail(PO_ERR_INVALID_ARGUMENT, "null batch");
+  if (!b->exec) return fail(PO_ERR_INVALID_ARGUMENT, "po_batch_prepare has not captured a graph");
+  PO_CUDA(cudaGraphLaunch(b->exec, (cudaStream_t)stream));
+  return PO_OK;
+}
+
+po_status po_batch_info(const po_batch *b, int64_t *graph_nodes, int64_t *workspace_bytes, double *ms_prepare) {
+  if (!b) return fail(PO_ERR_INVALID_ARGUMENT, "null batch");
+  if (graph_nodes) *graph_nodes = b->nodes;
+  if (ms_prepare) *ms_prepare = b->ms_prepare;
+  if (workspace_bytes) {
+    int64_t ws = 0;
+    for (const po_ctx *c : b->ctx)
+      for (const DevBuf *d : {&c->twiddles, &c->geom_in, &c->geom_sorted, &c->octree_ws, &c->leaf_ctr, &c->dirs,
+                              &c->dirs_d, &c->trans, &c->levelA, &c->levelB, &c->mid, &c->slots, &c->kvals, &c->out,
+                              &c->cur, &c->partial, &c->tile_ctr, &c->amat, &c->bmat})
+        ws += (int64_t)d->bytes;
+    *workspace_bytes = ws;
+  }
+  return PO_OK;
 }
 
 }  // extern "C"
