@@ -52,14 +52,15 @@ PRECISIONS = {"fp32": 0, "split_bf16": 2}
 INTERP = {"fft": 0, "tensor": 1}
 
 
-def make_workload(precision: str = "fp32", interp: str = "tensor"):
+def make_workload(precision: str = "fp32", interp: str = "tensor", tile: int = 0, n_lambda: int = 25):
     from wavefiber3d_gb300 import api, geometry
     cloud = geometry.ellipsoid(RADII, N_POINTS)
     bmin = [-1.1 * r for r in RADII]
     bmax = [1.1 * r for r in RADII]
     cfg = api.Config.reference_rule(DEPTH, N_THETA, N_PHI, bmin, bmax, 16e-6, 16e-6, 1.3,
-                                    precision=PRECISIONS[precision], interp_method=INTERP[interp])
-    illum = api.Illumination(LAMBDAS, [0.0], [0.0], api.PO_POL_TM, ETA, SIGMA)
+                                    precision=PRECISIONS[precision], interp_method=INTERP[interp],
+                                    interp_tile=tile)
+    illum = api.Illumination(LAMBDAS[:n_lambda], [0.0], [0.0], api.PO_POL_TM, ETA, SIGMA)
     return cloud, cfg, illum
 
 
@@ -170,7 +171,7 @@ def run_engine(args, world, rank, local):
     bf16_peak = peaks.get("bf16_tflops", 1900.0)
     peak_src = "measured" if peaks else "fallback"
 
-    cloud, cfg, illum = make_workload(args.precision, args.interp)
+    cloud, cfg, illum = make_workload(args.precision, args.interp, args.interp_tile, args.lambdas)
     pd_step = point_dirs_per_step(illum)
     st = torch.cuda.current_stream()
     g_dev = torch.from_numpy(cloud.soa()).to(dev)
@@ -268,9 +269,10 @@ def run_engine(args, world, rank, local):
                      "split bf16 hi+lo leaf products, f32 accumulation (f64 phase arguments)",
             "data": "synthetic (seeded ellipsoid, analytic normals)",
             "config": {"workload": WORKLOAD, "points": N_POINTS, "directions": N_THETA * N_PHI,
-                       "wavelengths": len(LAMBDAS), "incidences": 1, "polarisations": 1, "depth": DEPTH,
+                       "wavelengths": len(illum.wavelengths_m), "incidences": 1, "polarisations": 1, "depth": DEPTH,
                        "level_grids": [list(cfg.n_theta), list(cfg.n_phi)], "theta_mode": "double cover",
                        "precision": args.precision, "theta_interpolation": args.interp,
+                       "theta_tile": args.interp_tile,
                        "l2": "flushed between steps (256 MiB write, outside the timed events)",
                        "parallelism": f"replicas x{world}"},
             "patterns_per_s": illum.n_patterns * world / (ms_step_max * 1e-3),
@@ -746,6 +748,10 @@ def main():
     ap.add_argument("--cpu-dirs", type=int, default=2048, help="directions of the FP64 CPU sample")
     ap.add_argument("--precision", choices=sorted(PRECISIONS), default="fp32")
     ap.add_argument("--interp", choices=sorted(INTERP), default="tensor")
+    ap.add_argument("--interp-tile", type=int, choices=[0, 8, 16], default=0,
+                    help="complex columns per CTA of the tensor-core theta pass (0: automatic)")
+    ap.add_argument("--lambdas", type=int, default=25,
+                    help="wavelengths of the ellipsoid workload (25 = the headline; fewer for profiling runs)")
     ap.add_argument("--workload", choices=["ellipsoid", "fiber", "cylinder-grad", "batch"], default="ellipsoid",
                     help="ellipsoid: the headline 400k-point depth-5 workload; fiber: the 3.4M-point fiber "
                          "segment (split precision vs plain FP64 on the same GPU)")

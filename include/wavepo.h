@@ -71,8 +71,8 @@ typedef struct po_config {
   int64_t max_workspace_bytes;      /* device workspace cap of one solve; the patterns are
                                        processed in chunks of slots that fit (0 = half of
                                        the device's memory) */
-  int interp_tile;                  /* complex columns per CTA of the tensor-core theta pass:
-                                       0 = chosen by shared memory, 8 or 16 (autotuner knob) */
+  int interp_tile;                  /* complex columns per CTA of the tensor-core theta pass
+                                       (autotuner knob): 0 = automatic, 8 or 16 */
 } po_config;
 
 /* How the theta interpolation + translation + child sum between tree levels

@@ -143,11 +143,12 @@ __global__ void __launch_bounds__(128) k_interp_cols_mma(
     int64_t n_parent, int64_t n_child, int phi, int Rc, int Rp, int Kp, int mirror,
     const uint4 *__restrict__ Afrag, const float4 *__restrict__ trans, int G, float scale_unused) {
   constexpr int NT = NCC / 4;  // n-tiles of 8 (re, im interleaved)
+  constexpr int NP = NCC + 1;  // padded row stride of the staged tiles (no bank conflicts)
   extern __shared__ uint4 smem_u4[];
   const int KS = Kp / 16, MT = (Rp + 15) / 16;
   uint4 *Bf = smem_u4;                                       // [KS][NT][32]
-  float2 *tile = (float2 *)(Bf + (size_t)KS * NT * 32);      // [Rc][NCC]
-  float2 *acc = tile + (size_t)Rc * NCC;                     // [Rp][NCC]
+  float2 *tile = (float2 *)(Bf + (size_t)KS * NT * 32);      // [Rc][NP]
+  float2 *acc = tile + (size_t)Rc * NP;                      // [Rp][NP]
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, tq = lane & 3;
   const int TW = mirror ? NCC / 2 : NCC;
   const int span = mirror ? phi / 2 : phi;
@@ -160,7 +161,7 @@ __global__ void __launch_bounds__(128) k_interp_cols_mma(
   auto col_of = [&](int q) { return mirror ? (q < TW ? j0 + q : j0 + (q - TW) + phi / 2) : j0 + q; };
   auto ok_of = [&](int q) { return (mirror ? j0 + (q < TW ? q : q - TW) : j0 + q) < span; };
   auto partner_of = [&](int q) { return mirror ? (q < TW ? q + TW : q - TW) : q; };
-  for (int e = threadIdx.x; e < Rp * NCC; e += blockDim.x) acc[e] = make_float2(0.f, 0.f);
+  for (int e = threadIdx.x; e < Rp * NCC; e += blockDim.x) acc[(e / NCC) * NP + e % NCC] = make_float2(0.f, 0.f);
   const float4 *tr = trans + (int64_t)lam * Rp * phi;
   for (int o = 0; o < 8; ++o) {
     const int32_t c = child_table[p * 8 + o];
@@ -169,7 +170,7 @@ __global__ void __launch_bounds__(128) k_interp_cols_mma(
     const float2 *m = mid + (((int64_t)slot * n_child + c) * 6 + comp) * (int64_t)Rc * phi;
     for (int e = threadIdx.x; e < Rc * NCC; e += blockDim.x) {
       int t = e / NCC, q = e - t * NCC;
-      tile[e] = ok_of(q) ? m[(int64_t)t * phi + col_of(q)] : make_float2(0.f, 0.f);
+      tile[t * NP + q] = ok_of(q) ? m[(int64_t)t * phi + col_of(q)] : make_float2(0.f, 0.f);
     }
     __syncthreads();
     // B fragments: rows kk of the stacked operand [own half; partner half]
@@ -182,8 +183,8 @@ __global__ void __launch_bounds__(128) k_interp_cols_mma(
       for (int u = 0; u < 4; ++u) {
         const int kk = kb + (u & 1) + (u >> 1) * 8;
         float2 x = make_float2(0.f, 0.f);
-        if (kk < Rc) x = tile[kk * NCC + q];
-        else if (mirror && kk < 2 * Rc) x = tile[(kk - Rc) * NCC + partner_of(q)];
+        if (kk < Rc) x = tile[kk * NP + q];
+        else if (mirror && kk < 2 * Rc) x = tile[(kk - Rc) * NP + partner_of(q)];
         v[u] = part ? x.y : x.x;
       }
       uint32_t h0, l0, h1, l1;
@@ -198,8 +199,13 @@ __global__ void __launch_bounds__(128) k_interp_cols_mma(
 #pragma unroll
       for (int nt = 0; nt < NT; ++nt) d[nt][0] = d[nt][1] = d[nt][2] = d[nt][3] = 0.f;
       const uint4 *ap = Afrag + ((size_t)mt * KS) * 64 + lane * 2;
+      uint4 nh = __ldg(ap), nl = __ldg(ap + 1);  // A fragments of the next k-step in flight
       for (int ks = 0; ks < KS; ++ks) {
-        const uint4 ah = __ldg(ap + (size_t)ks * 64), al = __ldg(ap + (size_t)ks * 64 + 1);
+        const uint4 ah = nh, al = nl;
+        if (ks + 1 < KS) {
+          nh = __ldg(ap + (size_t)(ks + 1) * 64);
+          nl = __ldg(ap + (size_t)(ks + 1) * 64 + 1);
+        }
         const uint32_t a_hi[4] = {ah.x, ah.y, ah.z, ah.w}, a_lo[4] = {al.x, al.y, al.z, al.w};
 #pragma unroll
         for (int nt = 0; nt < NT; ++nt) {
@@ -224,10 +230,10 @@ __global__ void __launch_bounds__(128) k_interp_cols_mma(
           float sn, cs;
           sincos_small(fmaf(sgx, rr.x, fmaf(sgy, rr.y, sgz * rr.z)), &sn, &cs);
           const float vr = d[nt][2 * h], vi = d[nt][2 * h + 1];
-          float2 a = acc[r * NCC + q];
+          float2 a = acc[r * NP + q];
           a.x += vr * cs - vi * sn;
           a.y += vr * sn + vi * cs;
-          acc[r * NCC + q] = a;
+          acc[r * NP + q] = a;
         }
       }
     }
@@ -236,12 +242,162 @@ __global__ void __launch_bounds__(128) k_interp_cols_mma(
   float2 *out = parent + (((int64_t)slot * n_parent + p) * 6 + comp) * (int64_t)Rp * phi;
   for (int e = threadIdx.x; e < Rp * NCC; e += blockDim.x) {
     int t = e / NCC, q = e - t * NCC;
-    if (ok_of(q)) out[(int64_t)t * phi + col_of(q)] = acc[e];
+    if (ok_of(q)) out[(int64_t)t * phi + col_of(q)] = acc[t * NP + q];
   }
 }
 
+// Register-accumulator variant (double cover): CTA of W warps, warp w owns
+// the 16-row tiles w, w+W, ... (at most MTPW of them) and keeps its part of
+// the parent tile in registers across the children, so shared memory holds
+// only the staged child tile and its B fragments.  That leaves room for 16
+// columns per CTA (half the A traffic of 8) at the upper levels.
+template <int NCC, int MTPW>
+__global__ void __launch_bounds__(256) k_interp_cols_reg(
+    const float2 *__restrict__ mid, float2 *__restrict__ parent, const int32_t *__restrict__ child_table,
+    int64_t n_parent, int64_t n_child, int phi, int Rc, int Rp, int Kp, const uint4 *__restrict__ Afrag,
+    const float4 *__restrict__ trans, int G) {
+  constexpr int NT = NCC / 4;
+  constexpr int NP = NCC + 1;
+  constexpr int TW = NCC / 2;
+  extern __shared__ uint4 smem_u4[];
+  const int KS = Kp / 16, MT = (Rp + 15) / 16;
+  const int W = blockDim.x >> 5;
+  uint4 *Bf = smem_u4;                                   // [KS][NT][32]
+  float2 *tile = (float2 *)(Bf + (size_t)KS * NT * 32);  // [Rc][NP]
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, tq = lane & 3;
+  const int span = phi / 2;
+  const int ntile = (span + TW - 1) / TW;
+  const int j0 = (int)(blockIdx.x % ntile) * TW;
+  const int64_t pc = blockIdx.x / ntile;
+  const int64_t p = pc / 6;
+  const int comp = (int)(pc % 6);
+  const int slot = blockIdx.z, lam = slot / G;
+  auto col_of = [&](int q) { return q < TW ? j0 + q : j0 + (q - TW) + span; };
+  auto ok_of = [&](int q) { return j0 + (q < TW ? q : q - TW) < span; };
+  auto partner_of = [&](int q) { return q < TW ? q + TW : q - TW; };
+  float acc[MTPW][NT][4];
+#pragma unroll
+  for (int i = 0; i < MTPW; ++i)
+#pragma unroll
+    for (int nt = 0; nt < NT; ++nt) acc[i][nt][0] = acc[i][nt][1] = acc[i][nt][2] = acc[i][nt][3] = 0.f;
+  const float4 *tr = trans + (int64_t)lam * Rp * phi;
+  for (int o = 0; o < 8; ++o) {
+    const int32_t c = child_table[p * 8 + o];
+    if (c < 0) continue;
+    __syncthreads();
+    const float2 *m = mid + (((int64_t)slot * n_child + c) * 6 + comp) * (int64_t)Rc * phi;
+    for (int e = threadIdx.x; e < Rc * NCC; e += blockDim.x) {
+      const int t = e / NCC, q = e - t * NCC;
+      tile[t * NP + q] = ok_of(q) ? m[(int64_t)t * phi + col_of(q)] : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < KS * NT * 32; e += blockDim.x) {
+      const int ln = e & 31, nt = (e >> 5) % NT, ks = (e >> 5) / NT;
+      const int n = nt * 8 + (ln >> 2), q = n >> 1, part = n & 1;
+      const int kb = ks * 16 + 2 * (ln & 3);
+      float v[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int kk = kb + (u & 1) + (u >> 1) * 8;
+        float2 x = make_float2(0.f, 0.f);
+        if (kk < Rc) x = tile[kk * NP + q];
+        else if (kk < 2 * Rc) x = tile[(kk - Rc) * NP + partner_of(q)];
+        v[u] = part ? x.y : x.x;
+      }
+      uint32_t h0, l0, h1, l1;
+      split_bf16x2(v[0], v[1], h0, l0);
+      split_bf16x2(v[2], v[3], h1, l1);
+      Bf[e] = make_uint4(h0, h1, l0, l1);
+    }
+    __syncthreads();
+    const float sgx = (o & 1) ? 1.f : -1.f, sgy = (o & 2) ? -1.f : 1.f, sgz = (o & 4) ? -1.f : 1.f;
+#pragma unroll
+    for (int i = 0; i < MTPW; ++i) {
+      const int mt = warp + i * W;
+      if (mt >= MT) break;
+      float d[NT][4];
+#pragma unroll
+      for (int nt = 0; nt < NT; ++nt) d[nt][0] = d[nt][1] = d[nt][2] = d[nt][3] = 0.f;
+      const uint4 *ap = Afrag + ((size_t)mt * KS) * 64 + lane * 2;
+      uint4 nh = __ldg(ap), nl = __ldg(ap + 1);
+      for (int ks = 0; ks < KS; ++ks) {
+        const uint4 ah = nh, al = nl;
+        if (ks + 1 < KS) {
+          nh = __ldg(ap + (size_t)(ks + 1) * 64);
+          nl = __ldg(ap + (size_t)(ks + 1) * 64 + 1);
+        }
+        const uint32_t a_hi[4] = {ah.x, ah.y, ah.z, ah.w}, a_lo[4] = {al.x, al.y, al.z, al.w};
+#pragma unroll
+        for (int nt = 0; nt < NT; ++nt) {
+          const uint4 b = Bf[((size_t)ks * NT + nt) * 32 + lane];
+          const uint32_t b_hi[2] = {b.x, b.y}, b_lo[2] = {b.z, b.w};
+          mma_bf16(d[nt], a_hi, b_hi);
+          mma_bf16(d[nt], a_hi, b_lo);
+          mma_bf16(d[nt], a_lo, b_hi);
+        }
+      }
+#pragma unroll
+      for (int nt = 0; nt < NT; ++nt) {
+        const int q = nt * 4 + tq;
+        if (!ok_of(q)) continue;
+        const int j = col_of(q);
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const int r = mt * 16 + g + 8 * h;
+          if (r >= Rp) continue;
+          const float4 rr = __ldg(tr + (int64_t)r * phi + j);
+          float sn, cs;
+          sincos_small(fmaf(sgx, rr.x, fmaf(sgy, rr.y, sgz * rr.z)), &sn, &cs);
+          const float vr = d[nt][2 * h], vi = d[nt][2 * h + 1];
+          acc[i][nt][2 * h] += vr * cs - vi * sn;
+          acc[i][nt][2 * h + 1] += vr * sn + vi * cs;
+        }
+      }
+    }
+  }
+  float2 *out = parent + (((int64_t)slot * n_parent + p) * 6 + comp) * (int64_t)Rp * phi;
+#pragma unroll
+  for (int i = 0; i < MTPW; ++i) {
+    const int mt = warp + i * W;
+    if (mt >= MT) break;
+#pragma unroll
+    for (int nt = 0; nt < NT; ++nt) {
+      const int q = nt * 4 + tq;
+      if (!ok_of(q)) continue;
+      const int j = col_of(q);
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int r = mt * 16 + g + 8 * h;
+        if (r < Rp) out[(int64_t)r * phi + j] = make_float2(acc[i][nt][2 * h], acc[i][nt][2 * h + 1]);
+      }
+    }
+  }
+}
+
+static size_t cols_reg_smem(int ncc, int Rc, int Kp) {
+  return sizeof(uint4) * (size_t)(Kp / 16) * (ncc / 4) * 32 + sizeof(float2) * (size_t)Rc * (ncc + 1);
+}
+
+template <int NCC>
+static po_status launch_cols_reg(dim3 grid, int W, int mtpw, size_t smem, const float2 *mid, float2 *parent,
+                                 const int32_t *child_table, int64_t n_parent, int64_t n_child, int phi, int Rc,
+                                 int Rp, int Kp, const uint4 *A, const float4 *trans, int G, cudaStream_t st) {
+  switch (mtpw) {
+#define PO_REG(M)                                                                                               \
+  case M:                                                                                                      \
+    k_interp_cols_reg<NCC, M><<<grid, 32 * W, smem, st>>>(mid, parent, child_table, n_parent, n_child, phi, Rc, \
+                                                          Rp, Kp, A, trans, G);                                 \
+    break;
+    PO_REG(1) PO_REG(2) PO_REG(3) PO_REG(4) PO_REG(5) PO_REG(6)
+#undef PO_REG
+    default: return fail(PO_ERR_UNSUPPORTED, "angular grid too large for the register theta pass");
+  }
+  return PO_OK;
+}
+
 static size_t cols_mma_smem(int ncc, int Rc, int Rp, int Kp) {
-  return sizeof(uint4) * (size_t)(Kp / 16) * (ncc / 4) * 32 + sizeof(float2) * ((size_t)Rc * ncc + (size_t)Rp * ncc);
+  return sizeof(uint4) * (size_t)(Kp / 16) * (ncc / 4) * 32 +
+         sizeof(float2) * ((size_t)Rc * (ncc + 1) + (size_t)Rp * (ncc + 1));
 }
 
 po_status launch_interp_cols_mma(const float2 *mid, float2 *parent, const int32_t *child_table, int64_t n_parent,
@@ -249,9 +405,35 @@ po_status launch_interp_cols_mma(const float2 *mid, float2 *parent, const int32_
                                  const float4 *trans, int n_slots, int G, int tile, cudaStream_t st) {
   if (n_parent <= 0 || n_slots <= 0) return PO_OK;
   if (Kp % 16 || Kp < (mirror ? 2 * Rc : Rc)) return fail(PO_ERR_INTERNAL, "theta matrix K padding");
-  int ncc = 16;
-  if (cols_mma_smem(ncc, Rc, Rp, Kp) > 100 * 1024 || (mirror ? phi / 2 : phi) <= 4) ncc = 8;
-  if ((tile == 8 || tile == 16) && cols_mma_smem(tile, Rc, Rp, Kp) <= 227 * 1024) ncc = tile;
+  // large parent grids (the root): register accumulators and 16 columns per CTA
+  // (half the A traffic); smaller grids: the shared-memory kernel with 8 columns
+  // (per-level launch lists of the headline workload: 3.4 vs 5.5 ms at the root,
+  // 4.8-9.0 vs 7.1-13.7 ms below it)
+  if (mirror && phi % 2 == 0 && tile == 0 && (Rp + 15) / 16 >= 16) {
+    const int MT = (Rp + 15) / 16;
+    const int mtpw = (MT + 7) / 8;
+    const int W = (MT + mtpw - 1) / mtpw;
+    int ncc = (phi / 2 > 4 && cols_reg_smem(16, Rc, Kp) <= 96 * 1024) ? 16 : 8;
+    const size_t smem = cols_reg_smem(ncc, Rc, Kp);
+    if (mtpw <= 6 && smem <= 227 * 1024) {
+      const int TW = ncc / 2;
+      const int64_t gx = (int64_t)((phi / 2 + TW - 1) / TW) * n_parent * 6;
+      if (gx > 2147483647LL || n_slots > 65535) return fail(PO_ERR_UNSUPPORTED, "too many nodes for one launch");
+      dim3 grid((unsigned)gx, 1u, (unsigned)n_slots);
+      const uint4 *A = (const uint4 *)Afrag;
+      if (ncc == 16)
+        PO_TRY(launch_cols_reg<16>(grid, W, mtpw, smem, mid, parent, child_table, n_parent, n_child, phi, Rc, Rp, Kp,
+                                   A, trans, G, st));
+      else
+        PO_TRY(launch_cols_reg<8>(grid, W, mtpw, smem, mid, parent, child_table, n_parent, n_child, phi, Rc, Rp, Kp, A,
+                                  trans, G, st));
+      count_launch();
+      PO_CUDA(cudaGetLastError());
+      return PO_OK;
+    }
+  }
+  int ncc = 8;
+  if (tile == 16 && cols_mma_smem(16, Rc, Rp, Kp) <= 227 * 1024 && (mirror ? phi / 2 : phi) > 4) ncc = 16;
   const size_t smem = cols_mma_smem(ncc, Rc, Rp, Kp);
   if (smem > 227 * 1024) return fail(PO_ERR_UNSUPPORTED, "angular grid too large for the tensor-core interpolation");
   const int TW = mirror ? ncc / 2 : ncc;
@@ -285,10 +467,11 @@ __global__ void __launch_bounds__(128) k_interp_cols_adj_mma(
     const uint4 *__restrict__ Afrag, const float4 *__restrict__ trans, int G) {
   constexpr int NT = NCC / 4;
   constexpr int TW = NCC / 2;
+  constexpr int NP = NCC + 1;  // padded row stride of the staged tile
   extern __shared__ uint4 smem_u4[];
   const int KS = Kp / 16, MT = (Rc + 15) / 16;
   uint4 *Bf = smem_u4;                                   // [KS][NT][32]
-  float2 *tile = (float2 *)(Bf + (size_t)KS * NT * 32);  // [Rp][NCC]
+  float2 *tile = (float2 *)(Bf + (size_t)KS * NT * 32);  // [Rp][NP]
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, tq = lane & 3;
   const int span = phi / 2;
   const int ntile = (span + TW - 1) / TW;
@@ -316,7 +499,7 @@ __global__ void __launch_bounds__(128) k_interp_cols_adj_mma(
       sincos_small(fmaf(sgx, rr.x, fmaf(sgy, rr.y, sgz * rr.z)), &sn, &cs);
       v = make_float2(a.x * cs + a.y * sn, a.y * cs - a.x * sn);  // a * exp(-i ph)
     }
-    tile[e] = v;
+    tile[r * NP + q] = v;
   }
   __syncthreads();
   for (int e = threadIdx.x; e < KS * NT * 32; e += blockDim.x) {
@@ -328,8 +511,8 @@ __global__ void __launch_bounds__(128) k_interp_cols_adj_mma(
     for (int u = 0; u < 4; ++u) {
       const int kk = kb + (u & 1) + (u >> 1) * 8;
       float2 x = make_float2(0.f, 0.f);
-      if (kk < Rp) x = tile[kk * NCC + q];
-      else if (kk < 2 * Rp) x = tile[(kk - Rp) * NCC + partner_of(q)];
+      if (kk < Rp) x = tile[kk * NP + q];
+      else if (kk < 2 * Rp) x = tile[(kk - Rp) * NP + partner_of(q)];
       v[u] = part ? x.y : x.x;
     }
     uint32_t h0, l0, h1, l1;
@@ -344,8 +527,13 @@ __global__ void __launch_bounds__(128) k_interp_cols_adj_mma(
 #pragma unroll
     for (int nt = 0; nt < NT; ++nt) d[nt][0] = d[nt][1] = d[nt][2] = d[nt][3] = 0.f;
     const uint4 *ap = Afrag + ((size_t)mt * KS) * 64 + lane * 2;
+    uint4 nh = __ldg(ap), nl = __ldg(ap + 1);
     for (int ks = 0; ks < KS; ++ks) {
-      const uint4 ah = __ldg(ap + (size_t)ks * 64), al = __ldg(ap + (size_t)ks * 64 + 1);
+      const uint4 ah = nh, al = nl;
+      if (ks + 1 < KS) {
+        nh = __ldg(ap + (size_t)(ks + 1) * 64);
+        nl = __ldg(ap + (size_t)(ks + 1) * 64 + 1);
+      }
       const uint32_t a_hi[4] = {ah.x, ah.y, ah.z, ah.w}, a_lo[4] = {al.x, al.y, al.z, al.w};
 #pragma unroll
       for (int nt = 0; nt < NT; ++nt) {
@@ -371,7 +559,7 @@ __global__ void __launch_bounds__(128) k_interp_cols_adj_mma(
 }
 
 static size_t cols_adj_smem(int ncc, int Rp, int Kp) {
-  return sizeof(uint4) * (size_t)(Kp / 16) * (ncc / 4) * 32 + sizeof(float2) * (size_t)Rp * ncc;
+  return sizeof(uint4) * (size_t)(Kp / 16) * (ncc / 4) * 32 + sizeof(float2) * (size_t)Rp * (ncc + 1);
 }
 
 po_status launch_interp_cols_adj_mma(const float2 *parent_adj, float2 *mid_adj, const int32_t *child_parent,
@@ -530,6 +718,11 @@ po_status init_interp_mma_attributes(int max_smem) {
   PO_CUDA(cudaFuncSetAttribute(k_interp_cols_adj_mma<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
   PO_CUDA(cudaFuncSetAttribute(k_interp_cols_adj_mma<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
   PO_CUDA(cudaFuncSetAttribute(k_interp_rows_mma, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
+#define PO_REG_ATTR(N, M) \
+  PO_CUDA(cudaFuncSetAttribute(k_interp_cols_reg<N, M>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
+  PO_REG_ATTR(8, 1) PO_REG_ATTR(8, 2) PO_REG_ATTR(8, 3) PO_REG_ATTR(8, 4) PO_REG_ATTR(8, 5) PO_REG_ATTR(8, 6)
+  PO_REG_ATTR(16, 1) PO_REG_ATTR(16, 2) PO_REG_ATTR(16, 3) PO_REG_ATTR(16, 4) PO_REG_ATTR(16, 5) PO_REG_ATTR(16, 6)
+#undef PO_REG_ATTR
   return PO_OK;
 }
 
