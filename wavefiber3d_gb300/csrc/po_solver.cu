@@ -352,7 +352,8 @@ po_status po_destroy(po_ctx *c) {
   if (!c) return PO_OK;
   for (DevBuf *b : {&c->twiddles, &c->geom_in, &c->geom_sorted, &c->octree_ws, &c->leaf_ctr, &c->dirs, &c->dirs_d,
                     &c->trans, &c->levelA, &c->levelB, &c->mid, &c->slots, &c->kvals, &c->out, &c->cur, &c->partial,
-                    &c->tile_ctr, &c->amat, &c->bmat})
+                    &c->tile_ctr, &c->amat, &c->bmat, &c->amat_adj, &c->bmat_adj, &c->slots64, &c->grad_acc,
+                    &c->chunk_begin, &c->center0})
     b->release();
   for (auto &e : c->ev)
     if (e) cudaEventDestroy(e);
