@@ -15,8 +15,9 @@
 // and
 //   dL/dx_p,a += -2 k Im(A_p^a^H C_p)          (phase of the far-field sum)
 //   dL/dq     += 2 Re(A_p^H dC_p/dq)            (q in x, y, z, n, area)
-// The Jacobian dC_p/dq of the tangent-plane model is taken in FP64 forward
-// mode (dual numbers with 7 tangents), per point and pattern.  Only the root
+// The Jacobian dC_p/dq of the tangent-plane model is taken in forward mode
+// (dual numbers with 7 tangents) per point and pattern, in the precision of
+// the back-projection (FP32, or FP64 for the FP64 chain).  Only the root
 // fields of the forward pass are kept; nothing of the intermediate levels is
 // stored, because the transposed aggregation is linear.
 #include <cuda_runtime.h>
@@ -27,185 +28,224 @@
 
 namespace wavepo {
 
-// ------------------------------------------------ FP64 forward-mode duals
+// ------------------------------------------- forward-mode duals (FP32 / FP64)
 constexpr int kNT = 7;  // tangents: x, y, z, nx, ny, nz, area
 
-struct D7 {
-  double v;
-  double d[kNT];
+template <typename T>
+struct Dual {
+  T v;
+  T d[kNT];
 };
 
-__device__ __forceinline__ D7 dconst(double v) {
-  D7 r;
+template <typename T>
+__device__ __forceinline__ Dual<T> dconst(T v) {
+  Dual<T> r;
   r.v = v;
 #pragma unroll
-  for (int i = 0; i < kNT; ++i) r.d[i] = 0.0;
+  for (int i = 0; i < kNT; ++i) r.d[i] = (T)0;
   return r;
 }
-__device__ __forceinline__ D7 dvar(double v, int i) {
-  D7 r = dconst(v);
-  r.d[i] = 1.0;
+template <typename T>
+__device__ __forceinline__ Dual<T> dvar(T v, int i) {
+  Dual<T> r = dconst<T>(v);
+  r.d[i] = (T)1;
   return r;
 }
 // f(u) with f(u.v) = fv and f'(u.v) = fp
-__device__ __forceinline__ D7 dchain(const D7 &u, double fv, double fp) {
-  D7 r;
+template <typename T>
+__device__ __forceinline__ Dual<T> dchain(const Dual<T> &u, T fv, T fp) {
+  Dual<T> r;
   r.v = fv;
 #pragma unroll
   for (int i = 0; i < kNT; ++i) r.d[i] = fp * u.d[i];
   return r;
 }
-__device__ __forceinline__ D7 operator+(const D7 &a, const D7 &b) {
-  D7 r;
+template <typename T>
+__device__ __forceinline__ Dual<T> operator+(const Dual<T> &a, const Dual<T> &b) {
+  Dual<T> r;
   r.v = a.v + b.v;
 #pragma unroll
   for (int i = 0; i < kNT; ++i) r.d[i] = a.d[i] + b.d[i];
   return r;
 }
-__device__ __forceinline__ D7 operator-(const D7 &a, const D7 &b) {
-  D7 r;
+template <typename T>
+__device__ __forceinline__ Dual<T> operator-(const Dual<T> &a, const Dual<T> &b) {
+  Dual<T> r;
   r.v = a.v - b.v;
 #pragma unroll
   for (int i = 0; i < kNT; ++i) r.d[i] = a.d[i] - b.d[i];
   return r;
 }
-__device__ __forceinline__ D7 operator-(const D7 &a) { return dchain(a, -a.v, -1.0); }
-__device__ __forceinline__ D7 operator*(const D7 &a, const D7 &b) {
-  D7 r;
+template <typename T>
+__device__ __forceinline__ Dual<T> operator-(const Dual<T> &a) { return dchain(a, -a.v, (T)-1); }
+template <typename T>
+__device__ __forceinline__ Dual<T> operator*(const Dual<T> &a, const Dual<T> &b) {
+  Dual<T> r;
   r.v = a.v * b.v;
 #pragma unroll
   for (int i = 0; i < kNT; ++i) r.d[i] = a.d[i] * b.v + a.v * b.d[i];
   return r;
 }
-__device__ __forceinline__ D7 operator*(const D7 &a, double s) { return dchain(a, a.v * s, s); }
-__device__ __forceinline__ D7 operator*(double s, const D7 &a) { return dchain(a, a.v * s, s); }
-__device__ __forceinline__ D7 operator/(const D7 &a, const D7 &b) {
-  D7 r;
-  const double ib = 1.0 / b.v;
+template <typename T>
+__device__ __forceinline__ Dual<T> operator*(const Dual<T> &a, T s) { return dchain(a, a.v * s, s); }
+template <typename T>
+__device__ __forceinline__ Dual<T> operator/(const Dual<T> &a, const Dual<T> &b) {
+  Dual<T> r;
+  const T ib = (T)1 / b.v;
   r.v = a.v * ib;
 #pragma unroll
   for (int i = 0; i < kNT; ++i) r.d[i] = (a.d[i] - r.v * b.d[i]) * ib;
   return r;
 }
-__device__ __forceinline__ D7 dsqrt(const D7 &a) {
-  const double s = sqrt(a.v);
-  return dchain(a, s, s > 0 ? 0.5 / s : 0.0);
+template <typename T>
+__device__ __forceinline__ Dual<T> dsqrt(const Dual<T> &a) {
+  const T s = sqrt(a.v);
+  return dchain(a, s, s > (T)0 ? (T)0.5 / s : (T)0);
 }
-__device__ __forceinline__ D7 dexp(const D7 &a) {
-  const double e = exp(a.v);
+template <typename T>
+__device__ __forceinline__ Dual<T> dexp(const Dual<T> &a) {
+  const T e = exp(a.v);
   return dchain(a, e, e);
 }
-__device__ __forceinline__ D7 dacos(const D7 &a) {
-  const double q = 1.0 - a.v * a.v;
-  return dchain(a, acos(a.v), q > 0 ? -1.0 / sqrt(q) : 0.0);
+template <typename T>
+__device__ __forceinline__ Dual<T> dacos(const Dual<T> &a) {
+  const T q = (T)1 - a.v * a.v;
+  return dchain(a, acos(a.v), q > (T)0 ? (T)-1 / sqrt(q) : (T)0);
 }
-__device__ __forceinline__ D7 dabs(const D7 &a) { return a.v < 0 ? -a : a; }
-__device__ __forceinline__ D7 dsin(const D7 &a) { return dchain(a, sin(a.v), cos(a.v)); }
+template <typename T>
+__device__ __forceinline__ Dual<T> dabs(const Dual<T> &a) { return a.v < (T)0 ? -a : a; }
+template <typename T>
+__device__ __forceinline__ Dual<T> dsin(const Dual<T> &a) { return dchain(a, sin(a.v), cos(a.v)); }
 
-using CD = cx<D7>;
-__device__ __forceinline__ CD cd(double re, double im) { return {dconst(re), dconst(im)}; }
-__device__ __forceinline__ CD operator*(const CD &a, const CD &b) {
+template <typename T>
+using CDual = cx<Dual<T>>;
+template <typename T>
+__device__ __forceinline__ CDual<T> cd(T re, T im) { return {dconst<T>(re), dconst<T>(im)}; }
+template <typename T>
+__device__ __forceinline__ CDual<T> operator*(const CDual<T> &a, const CDual<T> &b) {
   return {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re};
 }
-__device__ __forceinline__ CD operator*(const CD &a, const D7 &s) { return {a.re * s, a.im * s}; }
-__device__ __forceinline__ CD operator*(const CD &a, double s) { return {a.re * s, a.im * s}; }
-__device__ __forceinline__ CD operator+(const CD &a, const CD &b) { return {a.re + b.re, a.im + b.im}; }
-__device__ __forceinline__ CD operator-(const CD &a, const CD &b) { return {a.re - b.re, a.im - b.im}; }
-__device__ __forceinline__ CD cddiv(const CD &a, const CD &b) {
-  D7 d = b.re * b.re + b.im * b.im;
+template <typename T>
+__device__ __forceinline__ CDual<T> operator*(const CDual<T> &a, const Dual<T> &s) { return {a.re * s, a.im * s}; }
+template <typename T>
+__device__ __forceinline__ CDual<T> operator*(const CDual<T> &a, T s) { return {a.re * s, a.im * s}; }
+template <typename T>
+__device__ __forceinline__ CDual<T> operator+(const CDual<T> &a, const CDual<T> &b) {
+  return {a.re + b.re, a.im + b.im};
+}
+template <typename T>
+__device__ __forceinline__ CDual<T> operator-(const CDual<T> &a, const CDual<T> &b) {
+  return {a.re - b.re, a.im - b.im};
+}
+template <typename T>
+__device__ __forceinline__ CDual<T> cddiv(const CDual<T> &a, const CDual<T> &b) {
+  Dual<T> d = b.re * b.re + b.im * b.im;
   return {(a.re * b.re + a.im * b.im) / d, (a.im * b.re - a.re * b.im) / d};
 }
 // principal square root (as csqrt_ of po_common.cuh)
-__device__ __forceinline__ CD cdsqrt(const CD &z) {
-  const D7 r = dsqrt(z.re * z.re + z.im * z.im);
-  const D7 ha = (r + z.re) * 0.5, hb = (r - z.re) * 0.5;
-  const D7 a = ha.v > 0 ? dsqrt(ha) : dconst(0.0);
-  const D7 b = hb.v > 0 ? dsqrt(hb) : dconst(0.0);
-  return {a, z.im.v < 0 ? -b : b};
+template <typename T>
+__device__ __forceinline__ CDual<T> cdsqrt(const CDual<T> &z) {
+  const Dual<T> r = dsqrt(z.re * z.re + z.im * z.im);
+  const Dual<T> ha = (r + z.re) * (T)0.5, hb = (r - z.re) * (T)0.5;
+  const Dual<T> a = ha.v > (T)0 ? dsqrt(ha) : dconst<T>(0);
+  const Dual<T> b = hb.v > (T)0 ? dsqrt(hb) : dconst<T>(0);
+  return {a, z.im.v < (T)0 ? -b : b};
 }
 // util/util.h:365-382 with a dual angle and constant indices
-__device__ __forceinline__ CD d_cos_internal(const CD &n, const D7 &theta) {
-  D7 s = dsin(theta);
-  CD q = cddiv({s, dconst(0.0)}, n);
+template <typename T>
+__device__ __forceinline__ CDual<T> d_cos_internal(const CDual<T> &n, const Dual<T> &theta) {
+  Dual<T> s = dsin(theta);
+  CDual<T> q = cddiv(CDual<T>{s, dconst<T>(0)}, n);
   q = cddiv(q * s, n);
-  return cdsqrt({dconst(1.0) - q.re, -q.im});
+  return cdsqrt(CDual<T>{dconst<T>(1) - q.re, -q.im});
 }
-__device__ __forceinline__ CD d_rs(const D7 &theta, const CD &n0, const CD &nt) {
-  CD p0 = n0 * d_cos_internal(n0, theta);
-  CD pt = nt * d_cos_internal(cddiv(nt, n0), theta);
+template <typename T>
+__device__ __forceinline__ CDual<T> d_rs(const Dual<T> &theta, const CDual<T> &n0, const CDual<T> &nt) {
+  CDual<T> p0 = n0 * d_cos_internal(n0, theta);
+  CDual<T> pt = nt * d_cos_internal(cddiv(nt, n0), theta);
   return cddiv(p0 - pt, p0 + pt);
 }
-__device__ __forceinline__ CD d_rp(const D7 &theta, const CD &n0, const CD &nt) {
-  CD q0 = cddiv(d_cos_internal(n0, theta), n0);
-  CD qt = cddiv(d_cos_internal(nt, theta), nt);
+template <typename T>
+__device__ __forceinline__ CDual<T> d_rp(const Dual<T> &theta, const CDual<T> &n0, const CDual<T> &nt) {
+  CDual<T> q0 = cddiv(d_cos_internal(n0, theta), n0);
+  CDual<T> qt = cddiv(d_cos_internal(nt, theta), nt);
   return cddiv(q0 - qt, q0 + qt);
 }
 
-// The tangent-plane model of tangent_plane() (po_common.cuh) in FP64 on dual
-// inputs: the same branches (taken on the float-rounded values, as the
-// forward kernels take them), differentiated.  out[0..2] = J, out[3..5] = M.
+// The tangent-plane model of tangent_plane() (po_common.cuh) on dual inputs
+// in precision T: the same branches (taken on the float-rounded values, as
+// the forward kernels take them), differentiated.  The incident phase value
+// k0 w.x is formed and reduced in FP64 whatever T is; its derivative is
+// -k0 w.  out[0..2] = J, out[3..5] = M.
+template <typename T>
 __device__ void tangent_plane_jvp(const SlotParams<double> &P, float px, float py, float pz, float qx, float qy,
-                                  float qz, float area, CD out[6]) {
-  const D7 X = dvar(px, 0), Y = dvar(py, 1), Z = dvar(pz, 2);
-  const D7 nr[3] = {dvar(qx, 3), dvar(qy, 4), dvar(qz, 5)};
-  const D7 Ar = dvar(area, 6);
-  const double kd[3] = {P.wavedir[0], P.wavedir[1], P.wavedir[2]};
-  const D7 dotvalue = nr[0] * kd[0] + nr[1] * kd[1] + nr[2] * kd[2];
-  CD Ei[3] = {cd(0, 0), cd(0, 0), cd(0, 0)}, Hi[3] = {cd(0, 0), cd(0, 0), cd(0, 0)};
-  CD Es[3] = {cd(0, 0), cd(0, 0), cd(0, 0)}, Hs[3] = {cd(0, 0), cd(0, 0), cd(0, 0)};
-  const float dot_f = (float)(kd[0] * qx + kd[1] * qy + kd[2] * qz);
+                                  float qz, float area, CDual<T> out[6]) {
+  const Dual<T> Z = dvar<T>(pz, 2);
+  const Dual<T> nr[3] = {dvar<T>(qx, 3), dvar<T>(qy, 4), dvar<T>(qz, 5)};
+  const Dual<T> Ar = dvar<T>(area, 6);
+  const T kd[3] = {(T)P.wavedir[0], (T)P.wavedir[1], (T)P.wavedir[2]};
+  const Dual<T> dotvalue = nr[0] * kd[0] + nr[1] * kd[1] + nr[2] * kd[2];
+  const CDual<T> zero = cd<T>(0, 0);
+  CDual<T> Ei[3] = {zero, zero, zero}, Hi[3] = {zero, zero, zero};
+  CDual<T> Es[3] = {zero, zero, zero}, Hs[3] = {zero, zero, zero};
+  const float dot_f = (float)(P.wavedir[0] * qx + P.wavedir[1] * qy + P.wavedir[2] * qz);
   if (dot_f <= 0.0f) {
     // incident phase exp(-i k0 w.x) and beam exp(-z^2 / (2 sigma^2))
-    const D7 arg = (X * P.wd[0] + Y * P.wd[1] + Z * P.wd[2]) * (-P.k0d);
-    double sn, cs;
-    sincos(arg.v, &sn, &cs);
-    const CD e = {dchain(arg, cs, -sn), dchain(arg, sn, cs)};
-    const D7 beam = dexp(-(Z * Z) * P.inv_two_sigma2);
-    const CD Ei0 = e * beam;
-    const CD Hi0 = Ei0 * (1.0 / P.z0);
+    const double argd = -P.k0d * (P.wd[0] * (double)px + P.wd[1] * (double)py + P.wd[2] * (double)pz);
+    const double rd = argd - kTwoPi * rint(argd * (1.0 / kTwoPi));
+    double snd, csd;
+    sincos(rd, &snd, &csd);
+    Dual<T> arg = dconst<T>((T)rd);
+#pragma unroll
+    for (int a = 0; a < 3; ++a) arg.d[a] = (T)(-P.k0d * P.wd[a]);
+    const CDual<T> e = {dchain(arg, (T)csd, (T)-snd), dchain(arg, (T)snd, (T)csd)};
+    const Dual<T> beam = dexp(-(Z * Z) * (T)P.inv_two_sigma2);
+    const CDual<T> Ei0 = e * beam;
+    const CDual<T> Hi0 = Ei0 * (T)(1.0 / P.z0);
     for (int c = 0; c < 3; ++c) {
-      Ei[c] = Ei0 * P.edir[c];
-      Hi[c] = Hi0 * P.hdir[c];
+      Ei[c] = Ei0 * (T)P.edir[c];
+      Hi[c] = Hi0 * (T)P.hdir[c];
     }
-    const CD eta_in = cd(1, 0), eta_out = cd(P.eta_re, P.eta_im);
+    const CDual<T> eta_in = cd<T>(1, 0), eta_out = cd<T>((T)P.eta_re, (T)P.eta_im);
     if (fabsf(fabsf(dot_f) - 1.0f) < 1e-10f) {  // tangentplane.h:39-49
-      const CD R = P.te ? cddiv(eta_out - eta_in, eta_in + eta_out) : cddiv(eta_in - eta_out, eta_in + eta_out);
+      const CDual<T> R =
+          P.te ? cddiv(eta_out - eta_in, eta_in + eta_out) : cddiv(eta_in - eta_out, eta_in + eta_out);
       for (int c = 0; c < 3; ++c) {
         Es[c] = Ei[c] * R;
         Hs[c] = Hi[c] * R;
       }
     } else {  // tangentplane.h:51-62
-      D7 rp[3] = {nr[2] * kd[1] - nr[1] * kd[2], nr[0] * kd[2] - nr[2] * kd[0], nr[1] * kd[0] - nr[0] * kd[1]};
-      const D7 inv = dconst(1.0) / dsqrt(rp[0] * rp[0] + rp[1] * rp[1] + rp[2] * rp[2]);
+      Dual<T> rp[3] = {nr[2] * kd[1] - nr[1] * kd[2], nr[0] * kd[2] - nr[2] * kd[0], nr[1] * kd[0] - nr[0] * kd[1]};
+      const Dual<T> inv = dconst<T>(1) / dsqrt(rp[0] * rp[0] + rp[1] * rp[1] + rp[2] * rp[2]);
       for (int c = 0; c < 3; ++c) rp[c] = rp[c] * inv;
-      const CD f = Ei[0] * rp[0] + Ei[1] * rp[1] + Ei[2] * rp[2];
-      CD Eperp[3], Epar[3], Hpar[3], Hperp[3];
+      const CDual<T> f = Ei[0] * rp[0] + Ei[1] * rp[1] + Ei[2] * rp[2];
+      CDual<T> Eperp[3], Epar[3], Hpar[3], Hperp[3];
       for (int c = 0; c < 3; ++c) {
         Eperp[c] = f * rp[c];
         Epar[c] = Ei[c] - Eperp[c];
       }
-      const double iz = 1.0 / P.z0;
+      const T iz = (T)(1.0 / P.z0);
       Hpar[0] = (Epar[2] * kd[1] - Epar[1] * kd[2]) * iz;
       Hpar[1] = (Epar[0] * kd[2] - Epar[2] * kd[0]) * iz;
       Hpar[2] = (Epar[1] * kd[0] - Epar[0] * kd[1]) * iz;
       for (int c = 0; c < 3; ++c) Hperp[c] = Hi[c] - Hpar[c];
-      const D7 lphi = dacos(dabs(dotvalue));
-      const CD Rs = d_rs(lphi, eta_in, eta_out);
-      const CD Rp = d_rp(lphi, eta_in, eta_out);
+      const Dual<T> lphi = dacos(dabs(dotvalue));
+      const CDual<T> Rs = d_rs(lphi, eta_in, eta_out);
+      const CDual<T> Rp = d_rp(lphi, eta_in, eta_out);
       for (int c = 0; c < 3; ++c) {
         Es[c] = Eperp[c] * Rs - Epar[c] * Rp;
         Hs[c] = Hpar[c] * Rp - Hperp[c] * Rs;
       }
     }
   }
-  CD Et[3], Ht[3];
+  CDual<T> Et[3], Ht[3];
   for (int c = 0; c < 3; ++c) {
     Et[c] = Ei[c] + Es[c];
     Ht[c] = Hi[c] + Hs[c];
   }
-  const CD M[3] = {Et[1] * nr[2] - Et[2] * nr[1], Et[2] * nr[0] - Et[0] * nr[2], Et[0] * nr[1] - Et[1] * nr[0]};
-  const CD J[3] = {Ht[2] * nr[1] - Ht[1] * nr[2], Ht[0] * nr[2] - Ht[2] * nr[0], Ht[1] * nr[0] - Ht[0] * nr[1]};
-  const CD ef = {Ar * P.ef_re, Ar * P.ef_im}, hf = {Ar * P.hf_re, Ar * P.hf_im};
+  const CDual<T> M[3] = {Et[1] * nr[2] - Et[2] * nr[1], Et[2] * nr[0] - Et[0] * nr[2], Et[0] * nr[1] - Et[1] * nr[0]};
+  const CDual<T> J[3] = {Ht[2] * nr[1] - Ht[1] * nr[2], Ht[0] * nr[2] - Ht[2] * nr[0], Ht[1] * nr[0] - Ht[0] * nr[1]};
+  const CDual<T> ef = {Ar * (T)P.ef_re, Ar * (T)P.ef_im}, hf = {Ar * (T)P.hf_re, Ar * (T)P.hf_im};
   for (int c = 0; c < 3; ++c) {
     out[c] = J[c] * ef;
     out[3 + c] = M[c] * hf;
@@ -387,8 +427,8 @@ __global__ void __launch_bounds__(32 * kAdjWarps) k_point_adjoint(
           }
         }
         if (!ok) continue;
-        CD C[6];
-        tangent_plane_jvp(slots[slot], px, py, pz, nx[p], ny[p], nz[p], area[p], C);
+        CDual<R> C[6];
+        tangent_plane_jvp<R>(slots[slot], px, py, pz, nx[p], ny[p], nz[p], area[p], C);
 #pragma unroll
         for (int i = 0; i < kNT; ++i) {
           double s = 0.0;
