@@ -287,6 +287,25 @@ po_status po_height_field_adjoint(const float *height, int numel, int numelvert,
 po_status po_average_pattern(const float *in, int nth_in, int nph_in, float *out, int nth_out, int nph_out,
                              int n_patterns, void *stream);
 
+/* fitting/fittingutil.py:22-33 (ForwardFFT_shifted, inverse = 0): for each
+ * of `batch` complex64 arrays [n_theta][n_phi] (device), roll by floor(n/2)
+ * along both axes, unnormalised forward 2-D DFT (FFTW / numpy sign
+ * convention), roll back by -floor(n/2).  inverse = 1 is InverseFFT_shifted
+ * (fittingutil.py:35-46): roll by -floor(n/2), unnormalised backward DFT
+ * (FFTW_BACKWARD, no 1/n), roll by +floor(n/2).  out may equal in.  FP32
+ * accumulation, twiddles exact to FP32 rounding.  Scratch from the
+ * stream-ordered allocator. */
+po_status po_shifted_fft2(const float *in, float *out, int batch, int n_theta, int n_phi, int inverse,
+                          void *stream);
+
+/* fitting/fittingutil.py:67-74 (ACFfromFT) with the mean of :55-65
+ * (weightedsum): patterns = n_inst real float32 arrays [n_theta][n_phi]
+ * (device, instance-major); outputs (device, [n_theta][n_phi]): the mean over
+ * the instances, spectrum = mean_i |ForwardFFT_shifted(pattern_i - mean)| and
+ * acf = Re ForwardFFT_shifted(spectrum^2). */
+po_status po_acf_from_patterns(const float *patterns, int n_inst, int n_theta, int n_phi, float *mean,
+                               float *spectrum, float *acf, void *stream);
+
 /* Library build identification (sm arch, version). */
 const char *po_version(void);
 

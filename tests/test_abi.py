@@ -91,3 +91,10 @@ def test_single_step_argument_checks(lib):
     assert lib.po_height_field_points(fake, 8, 4, 1e-6, 2.5e-7, 5, 4, *([fake] * 7), None) == 1
     assert lib.po_height_field_points(fake, 8, 4, 1e-6, 2.5e-7, 0, 8, *([fake] * 7), None) == 1
     assert lib.po_height_field_points(fake, 8, 4, 1e-6, 0.0, 0, 7, *([fake] * 7), None) == 1
+    # pattern statistics: null arrays and bad sizes
+    assert lib.po_shifted_fft2(None, fake, 1, 8, 8, 0, None) == 1
+    assert lib.po_shifted_fft2(fake, fake, 1, 0, 8, 0, None) == 1
+    assert lib.po_shifted_fft2(fake, fake, -1, 8, 8, 0, None) == 1
+    assert lib.po_shifted_fft2(fake, fake, 1, 8, 8, 2, None) == 1
+    assert lib.po_acf_from_patterns(fake, 0, 8, 8, fake, fake, fake, None) == 1
+    assert lib.po_acf_from_patterns(fake, 4, 8, 8, None, fake, fake, None) == 1

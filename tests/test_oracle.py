@@ -300,3 +300,32 @@ def test_average_oracle_uses_leading_samples_only():
     q = np.arange(45 * 88, dtype=np.float32).reshape(45, 88)
     want = q[:36, :72].reshape(18, 2, 36, 2).mean(axis=(1, 3))
     assert np.allclose(oracle.average(q, 18, 36), want, rtol=1e-6)
+
+
+# ------------------------------------- pattern statistics (fittingutil.py)
+def test_acf_oracle_shifted_fft_matches_definition():
+    """numpy stands in for FFTW in the restatement of ForwardFFT_shifted; pin it
+    to the transform's definition (odd and even sizes)."""
+    from oracle import acf
+    rng = np.random.default_rng(3)
+    for shape in ((6, 10), (7, 9), (5, 8)):
+        a = rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
+        assert np.allclose(acf.forward_fft_shifted(a), acf.shifted_dft_direct(a), rtol=1e-12, atol=1e-12)
+        assert np.allclose(acf.inverse_fft_shifted(a), acf.shifted_idft_direct(a), rtol=1e-12, atol=1e-12)
+        # unnormalised pair: inverse(forward(a)) = N a when both sizes are even
+        # (for an odd size the two rolls differ by one sample, as in the reference)
+        n = shape[0] * shape[1]
+        if shape[0] % 2 == 0 and shape[1] % 2 == 0:
+            assert np.allclose(acf.inverse_fft_shifted(acf.forward_fft_shifted(a)), n * a, rtol=1e-10,
+                               atol=1e-10)
+
+
+def test_acf_oracle_pipeline_properties():
+    """The ACF of the mean spectrum peaks at the shifted origin and is symmetric."""
+    from oracle import acf
+    rng = np.random.default_rng(4)
+    raw = rng.standard_normal((16, 20, 12, 3))
+    noisemat, mean = acf.weightedsum(raw, [0.5, 1.0, 2.0])
+    f, a = acf.acf_from_ft(noisemat, mean)
+    assert a.shape == (16, 20) and np.argmax(a) == np.ravel_multi_index((8, 10), (16, 20))
+    assert np.allclose(a[1:, 1:], a[1:, 1:][::-1, ::-1], rtol=1e-9, atol=1e-9 * np.abs(a).max())
