@@ -65,11 +65,14 @@ po_status launch_currents_f64(int64_t n, const float *const g[7], const SlotPara
 // ------------------------------------------------------------- leaf sums
 // One CTA per (leaf, wavelength).  G slots (incidences x polarisations)
 // share the phase of a wavelength.  Output: P[slot][leaf][comp][dir] complex.
-constexpr int kLeafThreads = 128;
+// The block holds ceil(ndir / DPT) threads rounded up to a warp (at most
+// kLeafMaxThreads; more directions take balanced passes), so no pass runs
+// mostly empty direction slots.
+constexpr int kLeafMaxThreads = 256;
 constexpr int kLeafChunk = 256;
 
 template <int G, int DPT>
-__global__ void __launch_bounds__(kLeafThreads) k_leaf(
+__global__ void __launch_bounds__(kLeafMaxThreads) k_leaf(
     const float *__restrict__ x, const float *__restrict__ y, const float *__restrict__ z,
     const float *__restrict__ nx, const float *__restrict__ ny, const float *__restrict__ nz,
     const float *__restrict__ area, const int32_t *__restrict__ leaf_begin, const double *__restrict__ leaf_center,
@@ -85,11 +88,12 @@ __global__ void __launch_bounds__(kLeafThreads) k_leaf(
   const double k0 = sl[0].k0d;
   const int64_t slot_stride = n_leaves * 6 * (int64_t)ndir;
   float2 *obase = out + ((int64_t)lam * Gtot + g0) * slot_stride + leaf * 6 * (int64_t)ndir;
-  const int per_pass = kLeafThreads * DPT;
+  const int nthr = blockDim.x;
+  const int per_pass = nthr * DPT;
   for (int c0 = b; c0 < e; c0 += kLeafChunk) {
     const int cnt = min(kLeafChunk, e - c0);
     __syncthreads();
-    for (int q = threadIdx.x; q < cnt; q += kLeafThreads) {
+    for (int q = threadIdx.x; q < cnt; q += nthr) {
       int p = c0 + q;
       float px = x[p], py = y[p], pz = z[p];
       s_u[q] = make_float4((float)(k0 * ((double)px - cxd)), (float)(k0 * ((double)py - cyd)),
@@ -110,7 +114,7 @@ __global__ void __launch_bounds__(kLeafThreads) k_leaf(
       float ar_[DPT][G * 6], ai_[DPT][G * 6];
 #pragma unroll
       for (int q = 0; q < DPT; ++q) {
-        int d = base + q * kLeafThreads + threadIdx.x;
+        int d = base + q * nthr + threadIdx.x;
         float4 sv = d < ndir ? dirs[d] : make_float4(0.f, 0.f, 0.f, 0.f);
         sx[q] = sv.x; sy[q] = sv.y; sz[q] = sv.z;
 #pragma unroll
@@ -133,7 +137,7 @@ __global__ void __launch_bounds__(kLeafThreads) k_leaf(
       }
 #pragma unroll
       for (int q = 0; q < DPT; ++q) {
-        int d = base + q * kLeafThreads + threadIdx.x;
+        int d = base + q * nthr + threadIdx.x;
         if (d >= ndir) continue;
 #pragma unroll
         for (int g = 0; g < G; ++g) {
@@ -149,7 +153,7 @@ __global__ void __launch_bounds__(kLeafThreads) k_leaf(
     }
   }
   if (b == e) {  // an empty node (only the root of an empty cloud) has a zero pattern
-    for (int d = threadIdx.x; d < ndir; d += kLeafThreads)
+    for (int d = threadIdx.x; d < ndir; d += nthr)
       for (int g = 0; g < G; ++g)
         for (int k = 0; k < 6; ++k) obase[g * slot_stride + (int64_t)k * ndir + d] = make_float2(0.f, 0.f);
   }
@@ -165,9 +169,13 @@ po_status launch_leaf(const float *const g[7], const int32_t *leaf_begin, const 
   // chunks of at most 4 (register budget of the accumulators)
   for (int g0 = 0; g0 < G; g0 += 4) {
     const int gc = std::min(4, G - g0);
-#define PO_LEAF(GG, DD)                                                                                     \
-  k_leaf<GG, DD><<<grid, kLeafThreads, 0, st>>>(g[0], g[1], g[2], g[3], g[4], g[5], g[6], leaf_begin,      \
-                                               leaf_center, slots_dev, dirs, ndir, n_leaves, G, g0, out)
+    const int dpt = gc == 1 ? 4 : gc == 2 ? 2 : 1;
+    const int passes = (ndir + kLeafMaxThreads * dpt - 1) / (kLeafMaxThreads * dpt);
+    const int per_pass = (ndir + passes - 1) / passes;
+    const int threads = std::max(64, (per_pass + dpt - 1) / dpt + 31) / 32 * 32;
+#define PO_LEAF(GG, DD)                                                                                   \
+  k_leaf<GG, DD><<<grid, threads, 0, st>>>(g[0], g[1], g[2], g[3], g[4], g[5], g[6], leaf_begin,         \
+                                          leaf_center, slots_dev, dirs, ndir, n_leaves, G, g0, out)
     switch (gc) {
       case 1: PO_LEAF(1, 4); break;
       case 2: PO_LEAF(2, 2); break;

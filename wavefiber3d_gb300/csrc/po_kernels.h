@@ -66,17 +66,22 @@ po_status launch_interp_cols(const float2 *mid, float2 *parent, const int32_t *c
                              int64_t n_child, int phi, int Rc, int Rp, const FftPlan &pin, const FftPlan &pout,
                              const float2 *twiddles, const float4 *trans, int n_slots, int G, int quirk_reach,
                              float scale, int ncomp, int mirror, int ref_nyquist, cudaStream_t st);
-// tensor-core theta pass (po_interp_mma.cu)
+// tensor-core theta pass, double cover (po_interp_mma.cu).  mid: the packed
+// output of launch_interp_rows_packed; Kp = Rc rounded up to even, then to 16.
 size_t theta_matrix_words(int Rp, int Kp);
-void build_theta_matrix(int Tc, int Tp, int Rc, int Rp, int mirror, int Kp, std::vector<uint32_t> &out);
-po_status launch_interp_cols_mma(const float2 *mid, float2 *parent, const int32_t *child_table, int64_t n_parent,
-                                 int64_t n_child, int phi, int Rc, int Rp, int Kp, int mirror, const uint32_t *Afrag,
+size_t theta_pair_words(int Rp, int Kp);
+void build_theta_matrix(int Tc, int Tp, int Rc, int Rp, int Kp, std::vector<uint32_t> &out);
+po_status launch_interp_cols_mma(const uint2 *mid, float2 *parent, const int32_t *child_table, int64_t n_parent,
+                                 int64_t n_child, int phi, int Rc, int Rp, int Kp, const uint32_t *Afrag,
                                  const float4 *trans, int n_slots, int G, int tile, cudaStream_t st);
-// tensor-core phi pass (po_interp_mma.cu)
+// tensor-core phi pass (po_interp_mma.cu): float2 rows -> float2 rows, or
+// (packed) n_patterns x Rc rows -> split-bf16 row pairs for the theta pass
 size_t phi_matrix_words(int Pp, int Kp);
 void build_phi_matrix(int Pc, int Pp, int Kp, std::vector<uint32_t> &out);
 po_status launch_interp_rows_mma(const float2 *src, float2 *dst, int64_t nrows, int Pc, int Pp, int Kp,
                                  const uint32_t *Bm, int sm_count, cudaStream_t st);
+po_status launch_interp_rows_packed(const float2 *src, uint2 *dst, int64_t n_patterns, int Rc, int Pc, int Pp,
+                                    int Kp, const uint32_t *Bm, int sm_count, cudaStream_t st);
 // adjoint (transposed) passes, double cover only (po_interp_mma.cu)
 void build_theta_matrix_adj(int Tc, int Tp, int Rc, int Rp, int Kp, std::vector<uint32_t> &out);
 void build_phi_matrix_adj(int Pc, int Pp, int Kp, std::vector<uint32_t> &out);

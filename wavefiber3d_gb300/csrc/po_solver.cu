@@ -318,9 +318,9 @@ po_status po_create(po_ctx **out, const po_config *cfg) {
   if (c->tensor_theta) {
     std::vector<uint32_t> all, one;
     for (int l = 0; l < d; ++l) {
-      const int K = c->mirror ? 2 * c->R[l + 1] : c->R[l + 1];
-      c->amat_kp[l] = (K + 15) / 16 * 16;
-      build_theta_matrix(c->T[l + 1], c->T[l], c->R[l + 1], c->R[l], c->mirror, c->amat_kp[l], one);
+      const int Rc2 = c->R[l + 1] + (c->R[l + 1] & 1);
+      c->amat_kp[l] = (Rc2 + 15) / 16 * 16;
+      build_theta_matrix(c->T[l + 1], c->T[l], c->R[l + 1], c->R[l], c->amat_kp[l], one);
       c->amat_off[l] = all.size();
       all.insert(all.end(), one.begin(), one.end());
     }
@@ -605,12 +605,13 @@ static po_status prepare_solve(po_ctx *c, const po_geometry *g, const po_illum *
                                                                        c->leaf_ctr.as<double>());
     count_launch();
   }
-  // pattern buffers per slot: two level buffers + the row-pass output
+  // pattern buffers per slot: two level buffers + the row-pass output (R + 1
+  // rows: the packed tensor-core row pass pads odd row counts to even)
   size_t lvl_max = 0, mid_max = 0;
   for (int l = 0; l <= d; ++l)
     lvl_max = std::max(lvl_max, (size_t)P.tree.level[l].count * 6 * (size_t)c->R[l] * c->Phi[l]);
   for (int l = 0; l < d; ++l)
-    mid_max = std::max(mid_max, (size_t)P.tree.level[l + 1].count * 6 * (size_t)c->R[l + 1] * c->Phi[l]);
+    mid_max = std::max(mid_max, (size_t)P.tree.level[l + 1].count * 6 * (size_t)(c->R[l + 1] + 1) * c->Phi[l]);
   P.chunks = plan_chunks(L, G, chunk_slot_count(budget, 8.0 * (2.0 * lvl_max + mid_max), S));
   const int ns_max = P.chunks.front().ns;
   PO_TRY(c->levelA.ensure(sizeof(float2) * lvl_max * ns_max));
@@ -744,8 +745,9 @@ static po_status enqueue_solve(po_ctx *c, const SolvePlan &P, float *out_dev, co
         int64_t nrows = (int64_t)ch.ns * nc * 6 * c->R[l + 1];
         PO_TRY(rec(c->kev[2 + 4 * l]));
         if (c->tensor_theta) {
-          PO_TRY(launch_interp_rows_mma(cur_lvl, c->mid.as<float2>(), nrows, c->Phi[l + 1], c->Phi[l], c->bmat_kp[l],
-                                        c->bmat.as<uint32_t>() + c->bmat_off[l], c->sm_count, st));
+          PO_TRY(launch_interp_rows_packed(cur_lvl, c->mid.as<uint2>(), (int64_t)ch.ns * nc * 6, c->R[l + 1],
+                                           c->Phi[l + 1], c->Phi[l], c->bmat_kp[l],
+                                           c->bmat.as<uint32_t>() + c->bmat_off[l], c->sm_count, st));
         } else {
           FftPlan prow_in = make_plan(c->Phi[l + 1], c->tw_offset[c->Phi[l + 1]]);
           FftPlan prow_out = make_plan(c->Phi[l], c->tw_offset[c->Phi[l]]);
@@ -759,10 +761,9 @@ static po_status enqueue_solve(po_ctx *c, const SolvePlan &P, float *out_dev, co
         if (np > 0) ++T.n_col;
         PO_TRY(rec(c->kev[4 + 4 * l]));
         if (c->tensor_theta) {
-          PO_TRY(launch_interp_cols_mma(c->mid.as<float2>(), nxt, P.tree.level[l].child, np, nc, c->Phi[l],
-                                        c->R[l + 1], c->R[l], c->amat_kp[l], c->mirror,
-                                        c->amat.as<uint32_t>() + c->amat_off[l], trans, ch.ns, ch.gc, cfg.interp_tile,
-                                        st));
+          PO_TRY(launch_interp_cols_mma(c->mid.as<uint2>(), nxt, P.tree.level[l].child, np, nc, c->Phi[l],
+                                        c->R[l + 1], c->R[l], c->amat_kp[l], c->amat.as<uint32_t>() + c->amat_off[l],
+                                        trans, ch.ns, ch.gc, cfg.interp_tile, st));
         } else {
           FftPlan pcol_in = make_plan(c->T[l + 1], c->tw_offset[c->T[l + 1]]);
           FftPlan pcol_out = make_plan(c->T[l], c->tw_offset[c->T[l]]);
