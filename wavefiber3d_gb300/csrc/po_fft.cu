@@ -484,17 +484,41 @@ po_status launch_interp_cols(const float2 *mid, float2 *parent, const int32_t *c
 }
 
 // ----------------------------------------------------- translation table
+// Direction factors of one level's grid (the terms of grid_direction):
+// trig[it] = (cos th, sin th) for rows it < R, trig[R + ip] = (cos ph, sin ph).
+// Built once per context, so the per-solve table below needs no FP64 trig.
+__global__ void k_dir_trig(int nth, int R, int phi, double2 *__restrict__ trig) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < R) {
+    const double th = -kPi / 2 + kThetaOffset + kPi / nth * e;
+    trig[e] = make_double2(cos(th), sin(th));
+  } else if (e < R + phi) {
+    const double ph = kTwoPi / phi * (e - R);
+    trig[e] = make_double2(cos(ph), sin(ph));
+  }
+}
+
+po_status launch_dir_trig(int nth, int R, int phi, double2 *trig, cudaStream_t st) {
+  if (R + phi <= 0) return PO_OK;
+  k_dir_trig<<<(unsigned)((R + phi + 255) / 256), 256, 0, st>>>(nth, R, phi, trig);
+  count_launch();
+  PO_CUDA(cudaGetLastError());
+  return PO_OK;
+}
+
 // r_a = (k * a_a * s_a) mod 2pi for a = x, y, z and every direction of a
-// Tp x Phi grid (theta rows may run into the second cover), per wavelength.
-__global__ void k_trans_table(const double *__restrict__ k_per_lambda, int n_lambda, int nth, int Rp, int phi,
-                              double ax, double ay, double az, float4 *__restrict__ out) {
+// Tp x Phi grid (theta rows may run into the second cover), per wavelength;
+// s = (cos th cos ph, cos th sin ph, sin th) from the level's trig table.
+__global__ void k_trans_table(const double *__restrict__ k_per_lambda, int n_lambda, int Rp, int phi,
+                              const double2 *__restrict__ trig, double ax, double ay, double az,
+                              float4 *__restrict__ out) {
   int64_t d = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   int lam = blockIdx.y;
   int64_t nd = (int64_t)Rp * phi;
   if (d >= nd || lam >= n_lambda) return;
   int it = (int)(d / phi), ip = (int)(d % phi);
-  double s[3];
-  grid_direction(it, ip, nth, phi, s);
+  const double2 th = trig[it], ph = trig[Rp + ip];
+  const double s[3] = {th.x * ph.x, th.x * ph.y, th.y};
   double k = k_per_lambda[lam];
   const double inv2pi = 0.15915494309189533577, p_hi = 6.28318530717958623200, p_lo = 2.44929359829470635445e-16;
   double a[3] = {k * ax * s[0], k * ay * s[1], k * az * s[2]};
@@ -507,12 +531,12 @@ __global__ void k_trans_table(const double *__restrict__ k_per_lambda, int n_lam
   out[(int64_t)lam * nd + d] = make_float4(r[0], r[1], r[2], 0.f);
 }
 
-po_status launch_trans_table(const double *k_per_lambda, int n_lambda, int nth, int Rp, int phi, const double a[3],
-                             float4 *out, cudaStream_t st) {
+po_status launch_trans_table(const double *k_per_lambda, int n_lambda, int Rp, int phi, const double2 *trig,
+                             const double a[3], float4 *out, cudaStream_t st) {
   int64_t nd = (int64_t)Rp * phi;
   if (nd <= 0 || n_lambda <= 0) return PO_OK;
   dim3 grid((unsigned)((nd + 255) / 256), (unsigned)n_lambda);
-  k_trans_table<<<grid, 256, 0, st>>>(k_per_lambda, n_lambda, nth, Rp, phi, a[0], a[1], a[2], out);
+  k_trans_table<<<grid, 256, 0, st>>>(k_per_lambda, n_lambda, Rp, phi, trig, a[0], a[1], a[2], out);
   count_launch();
   PO_CUDA(cudaGetLastError());
   return PO_OK;

@@ -8,13 +8,16 @@
 //   K_n(v) = (1/n) [1 + 2 sum_{k=1}^{n/2-1} cos(2 pi k v) + cos(pi n v)]   (n even)
 //   K_n(v) = (1/n) sin(pi n v) / sin(pi v)                                 (n odd).
 // With the double cover stored as rows 0..n_theta (see k_interp_cols), a
-// parent column j is A_own h_j + A_partner h_{j+Phi/2} and column j+Phi/2 is
-// A_own h_{j+Phi/2} + A_partner h_j: two GEMMs with K = Rc over the child's
-// stored half columns.  Operands are split into bf16 hi + lo parts and
-// multiplied as hi*hi + hi*lo + lo*hi with FP32 accumulation (mma.sync
-// m16n8k16), which keeps ~16 bits of every operand.  The row (phi) pass writes
-// its output already split, in row pairs, so the theta pass loads B fragments
-// straight from global memory.  The epilogue multiplies each child's result by
+// parent column j is A_own h_j + A_partner h_j' and its mirror j' = j + Phi/2
+// is A_own h_j' + A_partner h_j.  In sums and differences S = h_j + h_j',
+// D = h_j - h_j' this is two GEMMs with K = Rc instead of four:
+//   U = A_plus S,  V = A_minus D,  A_plus/minus = (A_own +- A_partner) / 2,
+//   Y_j = U + V,  Y_j' = U - V.
+// The row (phi) pass orders its output columns as (j, j') pairs and writes S
+// and D, already split into bf16 hi + lo parts in row pairs, so the theta pass
+// loads B fragments straight from global memory.  Products are hi*hi + hi*lo
+// + lo*hi with FP32 accumulation (mma.sync m16n8k16), which keeps ~16 bits of
+// every operand.  The epilogue multiplies each child's result by
 // exp(i k s.(c_child - c_parent)) and sums the children in registers.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -93,30 +96,33 @@ static double theta_partner(int Tc, int Tp, int r, int s) {
 }
 
 // Forward theta matrices of one level (double cover), K = rows t < Rc of one
-// half column, padded to 16:  A_own[r][t] and A_partner[r][s] (s >= 1).
-// Layout [mtile][kstep][u][lane] uint4 with u = own hi, own lo, partner hi,
-// partner lo (a lane's four a-registers), so a warp's shared-memory reads of
-// one u are 512 contiguous bytes.
+// half column, padded to 16:  A_plus/minus[r][t] = (A_own[r][t] +- A_partner[r][t]) / 2
+// with A_partner[r][s] nonzero for 1 <= s < Tc/2.  Layout [mtile][kstep][u][lane]
+// uint4 with u = plus hi, plus lo, minus hi, minus lo (a lane's four a-registers),
+// so a warp's shared-memory reads of one u are 512 contiguous bytes.
 size_t theta_pair_words(int Rp, int Kp) { return (size_t)((Rp + 15) / 16) * (Kp / 16) * 4 * 32 * 4; }
 
 void build_theta_matrix(int Tc, int Tp, int Rc, int Rp, int Kp, std::vector<uint32_t> &out) {
   const int nth_c = Tc / 2;
-  std::vector<double> Mo((size_t)Rp * Kp, 0.0), Mp((size_t)Rp * Kp, 0.0);
-  for (int r = 0; r < Rp; ++r) {
-    for (int t = 0; t < Rc; ++t) Mo[(size_t)r * Kp + t] = theta_own(Tc, Tp, r, t);
-    for (int s = 1; s < nth_c; ++s) Mp[(size_t)r * Kp + s] = theta_partner(Tc, Tp, r, s);
-  }
-  std::vector<uint32_t> fo, fp;
-  a_fragments(Mo, Rp, Kp, fo);
-  a_fragments(Mp, Rp, Kp, fp);
+  std::vector<double> Mplus((size_t)Rp * Kp, 0.0), Mminus((size_t)Rp * Kp, 0.0);
+  for (int r = 0; r < Rp; ++r)
+    for (int t = 0; t < Rc; ++t) {
+      const double own = theta_own(Tc, Tp, r, t);
+      const double partner = (t >= 1 && t < nth_c) ? theta_partner(Tc, Tp, r, t) : 0.0;
+      Mplus[(size_t)r * Kp + t] = 0.5 * (own + partner);
+      Mminus[(size_t)r * Kp + t] = 0.5 * (own - partner);
+    }
+  std::vector<uint32_t> fp, fm;
+  a_fragments(Mplus, Rp, Kp, fp);
+  a_fragments(Mminus, Rp, Kp, fm);
   const int MT = (Rp + 15) / 16, KS = Kp / 16;
   out.assign(theta_pair_words(Rp, Kp), 0u);
   for (int mt = 0; mt < MT; ++mt)
     for (int ks = 0; ks < KS; ++ks)
       for (int lane = 0; lane < 32; ++lane) {
-        const uint32_t *so = &fo[(((size_t)mt * KS + ks) * 32 + lane) * 8];
         const uint32_t *sp = &fp[(((size_t)mt * KS + ks) * 32 + lane) * 8];
-        const uint32_t *src[4] = {so, so + 4, sp, sp + 4};
+        const uint32_t *sm = &fm[(((size_t)mt * KS + ks) * 32 + lane) * 8];
+        const uint32_t *src[4] = {sp, sp + 4, sm, sm + 4};
         for (int u = 0; u < 4; ++u)
           std::memcpy(&out[((((size_t)mt * KS + ks) * 4 + u) * 32 + lane) * 4], src[u], 16);
       }
@@ -156,22 +162,23 @@ __device__ __forceinline__ void split_bf16x2(float x0, float x1, uint32_t &hi, u
 }
 
 // Theta pass as warp tasks (double cover).  A warp owns one (slot, parent,
-// component) and TW = 2 NT own columns j0.. with their partners j0+Phi/2..,
-// for the CTA's 16-row tiles mt0 .. mt0+MTW-1 (blockIdx.y selects them).
-// mid (from k_interp_rows_mma<true>): per (slot, child, component) rows in
-// pairs, [Rc2/2][phi] x {re, im} x {hi pair, lo pair} -- exactly a lane's B
-// registers.  The CTA stages its slice of the theta matrices in shared memory
-// once; after that warps run independently: B fragments of the next k-step
-// (or next child) are loaded while the current one multiplies, and the
-// parent tile accumulates in registers across the children.
-template <int NT, int MTW>
-__global__ void __launch_bounds__(256, 2) k_theta_warp(const uint2 *__restrict__ mid, float2 *__restrict__ parent,
-                                                    const int32_t *__restrict__ child_table, int64_t n_parent,
-                                                    int64_t n_child, int phi, int Rch, int Rp, int KS, int MT,
-                                                    const uint4 *__restrict__ Afrag, const float4 *__restrict__ trans,
-                                                    int G, int n_ct, int64_t n_task) {
-  constexpr int NO = NT / 2;  // own n-tiles; n-tile NO + i holds the partners of n-tile i
-  constexpr int TW = 4 * NO;  // own complex columns per warp
+// component) and TW = 4 NPT column pairs (j, j + Phi/2), j = j0.., for the
+// CTA's 16-row tiles mt0 .. mt0+MTW-1 (blockIdx.y selects them).
+// mid (from k_interp_rows_mma<true>): per (slot, child, component)
+// [Rc2/2][Phi/2][re, im] uint4 {S hi pair, S lo pair, D hi pair, D lo pair} --
+// a lane's B registers for the S and the D n-tile in one 16-byte load.  The
+// CTA stages its slice of the theta matrices in shared memory once; after
+// that warps run independently: B fragments of the next k-step (or next
+// child) are loaded while the current one multiplies, and the parent tile
+// accumulates in registers across the children.
+template <int NPT, int MTW>
+__global__ void __launch_bounds__(256, 2) k_theta_warp(const uint4 *__restrict__ mid, float2 *__restrict__ parent,
+                                                       const int32_t *__restrict__ child_table, int64_t n_parent,
+                                                       int64_t n_child, int phi, int Rch, int Rp, int KS, int MT,
+                                                       const uint4 *__restrict__ Afrag,
+                                                       const float4 *__restrict__ trans, int G, int n_ct,
+                                                       int64_t n_task) {
+  constexpr int TW = 4 * NPT;    // column pairs per warp
   extern __shared__ uint4 sA[];  // [MTW][KS][4][32]
   const int mt0 = blockIdx.y * MTW;
   const int nmt = MT - mt0 < MTW ? MT - mt0 : MTW;
@@ -193,107 +200,109 @@ __global__ void __launch_bounds__(256, 2) k_theta_warp(const uint2 *__restrict__
   const int64_t p = rest % n_parent;
   const int slot = (int)(rest / n_parent), lam = slot / G;
   const int span = phi / 2, j0 = ct * TW, part = g & 1;
-  const int64_t pat = (int64_t)Rch * phi * 2;  // uint2 words of one child pattern component
-  const uint2 *mbase = mid + ((int64_t)slot * n_child * 6 + comp) * pat;
+  const int64_t pat = (int64_t)Rch * span * 2;  // uint4 words of one child pattern component
+  const uint4 *mbase = mid + ((int64_t)slot * n_child * 6 + comp) * pat;
   const int32_t cl = lane < 8 ? child_table[p * 8 + lane] : -1;
   unsigned rem = __ballot_sync(0xffffffffu, cl >= 0);  // children present (bits 0..7)
-  // B operand of k-step ks of one child: n-tile nt, k rows 2 tq, 2 tq + 1 (pair tq) and + 8 (pair tq + 4)
-  auto load_b = [&](const uint2 *m, int ks, uint32_t (&h)[NT][2], uint32_t (&l)[NT][2]) {
+  // B operand of k-step ks of one child: pair tile pt, k rows 2 tq, 2 tq + 1 (pair tq) and + 8 (pair tq + 4)
+  auto load_b = [&](const uint4 *m, int ks, uint4 (&b)[NPT][2]) {
 #pragma unroll
-    for (int nt = 0; nt < NT; ++nt) {
-      const int q = (nt % NO) * 4 + (g >> 1);
-      const bool ok = j0 + q < span;
-      const int col = j0 + q + (nt < NO ? 0 : span);
+    for (int pt = 0; pt < NPT; ++pt) {
+      const int col = j0 + pt * 4 + (g >> 1);
 #pragma unroll
       for (int hh = 0; hh < 2; ++hh) {
         const int tp = ks * 8 + tq + 4 * hh;
-        uint2 u = make_uint2(0u, 0u);
-        if (ok && tp < Rch) u = __ldg(m + ((int64_t)tp * phi + col) * 2 + part);
-        h[nt][hh] = u.x;
-        l[nt][hh] = u.y;
+        uint4 u = make_uint4(0u, 0u, 0u, 0u);
+        if (col < span && tp < Rch) u = __ldg(m + ((int64_t)tp * span + col) * 2 + part);
+        b[pt][hh] = u;
       }
     }
   };
   auto child_ptr = [&](int o) { return mbase + (int64_t)__shfl_sync(0xffffffffu, cl, o) * 6 * pat; };
-  float acc[MTW][NT][4];
+  float acc[MTW][NPT][2][4];  // [..][j / j'][re, im of rows g and g + 8]
 #pragma unroll
   for (int i = 0; i < MTW; ++i)
 #pragma unroll
-    for (int nt = 0; nt < NT; ++nt) acc[i][nt][0] = acc[i][nt][1] = acc[i][nt][2] = acc[i][nt][3] = 0.f;
+    for (int pt = 0; pt < NPT; ++pt)
+#pragma unroll
+      for (int w = 0; w < 2; ++w) acc[i][pt][w][0] = acc[i][pt][w][1] = acc[i][pt][w][2] = acc[i][pt][w][3] = 0.f;
   const float4 *tr = trans + (int64_t)lam * Rp * phi;
   bool more = rem != 0;
   int o = more ? __ffs(rem) - 1 : 0;
   rem &= rem - 1;
-  const uint2 *m = child_ptr(o);
-  uint32_t nh[NT][2] = {}, nl[NT][2] = {};
-  if (more) load_b(m, 0, nh, nl);
+  const uint4 *m = child_ptr(o);
+  uint4 nb[NPT][2] = {};
+  if (more) load_b(m, 0, nb);
   while (more) {
-    float d[MTW][NT][4];
+    float d[MTW][NPT][2][4];  // [..][U, V][..]
 #pragma unroll
     for (int i = 0; i < MTW; ++i)
 #pragma unroll
-      for (int nt = 0; nt < NT; ++nt) d[i][nt][0] = d[i][nt][1] = d[i][nt][2] = d[i][nt][3] = 0.f;
-    int o_next = o;
-    const uint2 *m_next = m;
-    for (int ks = 0; ks < KS; ++ks) {
-      uint32_t bh[NT][2], bl[NT][2];
+      for (int pt = 0; pt < NPT; ++pt)
 #pragma unroll
-      for (int nt = 0; nt < NT; ++nt) {
-        bh[nt][0] = nh[nt][0];
-        bh[nt][1] = nh[nt][1];
-        bl[nt][0] = nl[nt][0];
-        bl[nt][1] = nl[nt][1];
+        for (int w = 0; w < 2; ++w) d[i][pt][w][0] = d[i][pt][w][1] = d[i][pt][w][2] = d[i][pt][w][3] = 0.f;
+    int o_next = o;
+    const uint4 *m_next = m;
+    for (int ks = 0; ks < KS; ++ks) {
+      uint4 b[NPT][2];
+#pragma unroll
+      for (int pt = 0; pt < NPT; ++pt) {
+        b[pt][0] = nb[pt][0];
+        b[pt][1] = nb[pt][1];
       }
       if (ks + 1 < KS) {
-        load_b(m, ks + 1, nh, nl);
+        load_b(m, ks + 1, nb);
       } else if (rem) {
         o_next = __ffs(rem) - 1;
         m_next = child_ptr(o_next);
-        load_b(m_next, 0, nh, nl);
+        load_b(m_next, 0, nb);
       }
-      // one basic block: MTW x NT independent accumulators, each product
-      // term issued across all of them before the next
+      // one basic block: MTW x NPT x 2 independent accumulators
 #pragma unroll
       for (int i = 0; i < MTW; ++i) {
         const uint4 *a = sA + (size_t)(i * KS + ks) * 128 + lane;
-        const uint4 oh = a[0], ol = a[32], ph = a[64], pl = a[96];
-        const uint32_t aoh[4] = {oh.x, oh.y, oh.z, oh.w}, aol[4] = {ol.x, ol.y, ol.z, ol.w};
+        const uint4 ph = a[0], pl = a[32], mh = a[64], ml = a[96];
         const uint32_t aph[4] = {ph.x, ph.y, ph.z, ph.w}, apl[4] = {pl.x, pl.y, pl.z, pl.w};
+        const uint32_t amh[4] = {mh.x, mh.y, mh.z, mh.w}, aml[4] = {ml.x, ml.y, ml.z, ml.w};
 #pragma unroll
-        for (int nt = 0; nt < NT; ++nt) {
-          const int nx = nt < NO ? nt + NO : nt - NO;  // partner n-tile
-          const uint32_t bsh[2] = {bh[nt][0], bh[nt][1]}, bsl[2] = {bl[nt][0], bl[nt][1]};
-          const uint32_t bxh[2] = {bh[nx][0], bh[nx][1]}, bxl[2] = {bl[nx][0], bl[nx][1]};
-          mma_bf16(d[i][nt], aoh, bsh);
-          mma_bf16(d[i][nt], aph, bxh);
-          mma_bf16(d[i][nt], aoh, bsl);
-          mma_bf16(d[i][nt], aph, bxl);
-          mma_bf16(d[i][nt], aol, bsh);
-          mma_bf16(d[i][nt], apl, bxh);
+        for (int pt = 0; pt < NPT; ++pt) {
+          const uint32_t sh[2] = {b[pt][0].x, b[pt][1].x}, sl[2] = {b[pt][0].y, b[pt][1].y};
+          const uint32_t dh[2] = {b[pt][0].z, b[pt][1].z}, dl[2] = {b[pt][0].w, b[pt][1].w};
+          mma_bf16(d[i][pt][0], aph, sh);
+          mma_bf16(d[i][pt][1], amh, dh);
+          mma_bf16(d[i][pt][0], aph, sl);
+          mma_bf16(d[i][pt][1], amh, dl);
+          mma_bf16(d[i][pt][0], apl, sh);
+          mma_bf16(d[i][pt][1], aml, dh);
         }
       }
     }
-    // translation of child octant o and the child sum.  Rows >= Rp (zero
-    // rows of A) and columns past the half span (zero B) hold exact zeros, so
-    // every element runs unguarded with its table index clamped in range:
-    // one basic block of independent chains.
+    // Y_j = U + V, Y_j' = U - V; translation of child octant o and the child
+    // sum.  Rows >= Rp (zero rows of A) and columns past the half span (zero
+    // B) hold exact zeros, so every element runs unguarded with its table
+    // index clamped in range: one basic block of independent chains.
     const float sgx = (o & 1) ? 1.f : -1.f, sgy = (o & 2) ? -1.f : 1.f, sgz = (o & 4) ? -1.f : 1.f;
 #pragma unroll
     for (int i = 0; i < MTW; ++i) {
 #pragma unroll
-      for (int nt = 0; nt < NT; ++nt) {
-        const int q = (nt % NO) * 4 + tq;
-        const int j = (j0 + q < span ? j0 + q : span - 1) + (nt < NO ? 0 : span);
+      for (int pt = 0; pt < NPT; ++pt) {
+        const int jq = j0 + pt * 4 + tq;
+        const int jc = jq < span ? jq : span - 1;
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
           const int r0 = (mt0 + i) * 16 + g + 8 * h;
           const int r = r0 < Rp ? r0 : Rp - 1;
-          const float4 rr = __ldg(tr + (int64_t)r * phi + j);
-          float sn, cs;
-          sincos_small(fmaf(sgx, rr.x, fmaf(sgy, rr.y, sgz * rr.z)), &sn, &cs);
-          const float vr = d[i][nt][2 * h], vi = d[i][nt][2 * h + 1];
-          acc[i][nt][2 * h] += vr * cs - vi * sn;
-          acc[i][nt][2 * h + 1] += vr * sn + vi * cs;
+          const float ur = d[i][pt][0][2 * h], ui = d[i][pt][0][2 * h + 1];
+          const float vr = d[i][pt][1][2 * h], vi = d[i][pt][1][2 * h + 1];
+#pragma unroll
+          for (int w = 0; w < 2; ++w) {
+            const float4 rr = __ldg(tr + (int64_t)r * phi + jc + w * span);
+            float sn, cs;
+            sincos_small(fmaf(sgx, rr.x, fmaf(sgy, rr.y, sgz * rr.z)), &sn, &cs);
+            const float yr = w ? ur - vr : ur + vr, yi = w ? ui - vi : ui + vi;
+            acc[i][pt][w][2 * h] += yr * cs - yi * sn;
+            acc[i][pt][w][2 * h + 1] += yr * sn + yi * cs;
+          }
         }
       }
     }
@@ -309,28 +318,30 @@ __global__ void __launch_bounds__(256, 2) k_theta_warp(const uint2 *__restrict__
   for (int i = 0; i < MTW; ++i) {
     if (i >= nmt) break;
 #pragma unroll
-    for (int nt = 0; nt < NT; ++nt) {
-      const int q = (nt % NO) * 4 + tq;
-      if (j0 + q >= span) continue;
-      const int j = j0 + q + (nt < NO ? 0 : span);
+    for (int pt = 0; pt < NPT; ++pt) {
+      const int jq = j0 + pt * 4 + tq;
+      if (jq >= span) continue;
 #pragma unroll
       for (int h = 0; h < 2; ++h) {
         const int r = (mt0 + i) * 16 + g + 8 * h;
-        if (r < Rp) out[(int64_t)r * phi + j] = make_float2(acc[i][nt][2 * h], acc[i][nt][2 * h + 1]);
+        if (r >= Rp) continue;
+#pragma unroll
+        for (int w = 0; w < 2; ++w)
+          out[(int64_t)r * phi + jq + w * span] = make_float2(acc[i][pt][w][2 * h], acc[i][pt][w][2 * h + 1]);
       }
     }
   }
 }
 
-template <int NT, int MTW>
-static void launch_theta_warp(dim3 grid, size_t smem, const uint2 *mid, float2 *parent, const int32_t *child_table,
+template <int NPT, int MTW>
+static void launch_theta_warp(dim3 grid, size_t smem, const uint4 *mid, float2 *parent, const int32_t *child_table,
                               int64_t n_parent, int64_t n_child, int phi, int Rch, int Rp, int KS, int MT,
                               const uint4 *A, const float4 *trans, int G, int n_ct, int64_t n_task, cudaStream_t st) {
-  k_theta_warp<NT, MTW><<<grid, 256, smem, st>>>(mid, parent, child_table, n_parent, n_child, phi, Rch, Rp, KS, MT, A,
-                                                 trans, G, n_ct, n_task);
+  k_theta_warp<NPT, MTW><<<grid, 256, smem, st>>>(mid, parent, child_table, n_parent, n_child, phi, Rch, Rp, KS, MT,
+                                                  A, trans, G, n_ct, n_task);
 }
 
-po_status launch_interp_cols_mma(const uint2 *mid, float2 *parent, const int32_t *child_table, int64_t n_parent,
+po_status launch_interp_cols_mma(const uint4 *mid, float2 *parent, const int32_t *child_table, int64_t n_parent,
                                  int64_t n_child, int phi, int Rc, int Rp, int Kp, const uint32_t *Afrag,
                                  const float4 *trans, int n_slots, int G, int tile, cudaStream_t st) {
   if (n_parent <= 0 || n_slots <= 0) return PO_OK;
@@ -338,15 +349,14 @@ po_status launch_interp_cols_mma(const uint2 *mid, float2 *parent, const int32_t
   if (Kp % 16 || Kp < Rc2) return fail(PO_ERR_INTERNAL, "theta matrix K padding");
   if (phi % 2) return fail(PO_ERR_INTERNAL, "mirrored storage needs an even phi grid");
   const int KS = Kp / 16, MT = (Rp + 15) / 16;
-  const int NT = tile == 16 ? 4 : 2;
-  // 16-row tiles per warp: up to 4 (measured on the headline workload: caps of
-  // 1 / 2 / 4 tiles gave 23.5 / 18.4 / 15.1 ms for the theta passes of a solve)
-  const int cap = NT == 4 ? 2 : 4;
+  const int NPT = tile == 16 ? 2 : 1;
+  // 16-row tiles per warp: up to 4 (register budget of the accumulators)
+  const int cap = NPT == 2 ? 2 : 4;
   const int nmg = (MT + cap - 1) / cap;
   const int MTW = (MT + nmg - 1) / nmg;
   const size_t smem = sizeof(uint4) * (size_t)MTW * KS * 128;
   if (smem > 227 * 1024) return fail(PO_ERR_UNSUPPORTED, "angular grid too large for the tensor-core interpolation");
-  const int TW = 2 * NT;
+  const int TW = 4 * NPT;
   const int n_ct = (phi / 2 + TW - 1) / TW;
   const int64_t n_task = (int64_t)n_slots * n_parent * 6 * n_ct;
   const int64_t gx = (n_task + 7) / 8;
@@ -354,11 +364,11 @@ po_status launch_interp_cols_mma(const uint2 *mid, float2 *parent, const int32_t
   dim3 grid((unsigned)gx, (unsigned)nmg, 1u);
   const uint4 *A = (const uint4 *)Afrag;
 #define PO_TW(N, M)                                                                                                 \
-  if (NT == N && MTW == M) {                                                                                       \
+  if (NPT == N && MTW == M) {                                                                                      \
     launch_theta_warp<N, M>(grid, smem, mid, parent, child_table, n_parent, n_child, phi, Rc2 / 2, Rp, KS, MT, A, \
                             trans, G, n_ct, n_task, st);                                                            \
   } else
-  PO_TW(2, 1) PO_TW(2, 2) PO_TW(2, 3) PO_TW(2, 4) PO_TW(4, 1) PO_TW(4, 2) {
+  PO_TW(1, 1) PO_TW(1, 2) PO_TW(1, 3) PO_TW(1, 4) PO_TW(2, 1) PO_TW(2, 2) {
     return fail(PO_ERR_INTERNAL, "theta pass variant");
   }
 #undef PO_TW
@@ -537,8 +547,18 @@ static void b_fragments(int Pout, int Kin, int Kp, F W, std::vector<uint32_t> &o
       }
 }
 
+// Forward phi matrix in mirror-pair column order (the packed row pass):
+// n-tile nt, slot 2q + w holds parent column nt*4 + q + w Pp/2, so a lane's
+// D fragment holds a column and its mirror for two rows.
 void build_phi_matrix(int Pc, int Pp, int Kp, std::vector<uint32_t> &out) {
-  b_fragments(Pp, Pc, Kp, [&](int n, int k) { return trig_kernel(Pc, (double)n / Pp - (double)k / Pc); }, out);
+  const int half = Pp / 2, NTt = (half + 3) / 4;
+  b_fragments(NTt * 8, Pc, Kp,
+              [&](int n, int k) {
+                const int j = (n >> 3) * 4 + ((n & 7) >> 1);
+                if (j >= half) return 0.0;
+                return trig_kernel(Pc, (double)(j + (n & 1) * half) / Pp - (double)k / Pc);
+              },
+              out);
 }
 
 // transpose of the phi map: child column j (< Pc) from parent columns j' (< Pp)
@@ -548,27 +568,35 @@ void build_phi_matrix_adj(int Pc, int Pp, int Kp, std::vector<uint32_t> &out) {
 
 // One warp per block of 8 rows; n-tiles in groups of kRowNG (accumulators in
 // registers); the B fragments come from shared memory when they fit.
-// PACK (forward pass feeding k_theta_warp): rows are indexed over patterns of
-// Rc2 = Rc rounded up to even rows (row Rc of an odd Rc is a zero row), and the
-// output is split into bf16 hi + lo and stored in row pairs: per pattern
-// [Rc2/2][Pp] uint4 {re hi pair, re lo pair, im hi pair, im lo pair}, each pair
-// holding rows 2 tp (low half) and 2 tp + 1.  Lane g and lane g^1 (4 apart)
-// hold the two rows of a pair and swap one column each, so every lane stores
-// one 16-byte word.
+// PACK (forward pass feeding k_theta_warp): the phi matrix is in mirror-pair
+// column order (build_phi_matrix), rows are indexed over patterns of Rc2 = Rc
+// rounded up to even rows (row Rc of an odd Rc is a zero row), and the output
+// is S = h_j + h_j', D = h_j - h_j' (j' = j + Pp/2) split into bf16 hi + lo in
+// row pairs: per pattern [Rc2/2][Pp/2][re, im] uint4 {S hi pair, S lo pair,
+// D hi pair, D lo pair}, each pair holding rows 2 tp (low half) and 2 tp + 1.
+// Lane g and lane g^1 (4 apart) hold the two rows of a pair; the even lane
+// stores the real parts, the odd lane the imaginary parts.
 constexpr int kRowNG = 8;
+// blockIdx.y selects a group of kRowNG n-tiles (output columns); its slice of
+// the phi matrix is staged in shared memory when it fits (b_in_smem), and
+// every warp runs over blocks of 8 rows with the next k-step's input loads in
+// flight while the current one multiplies.
 template <bool PACK>
 __global__ void __launch_bounds__(128) k_interp_rows_mma(const float2 *__restrict__ src, void *__restrict__ dst_,
                                                          int64_t nrows, int Rc, int Pc, int Pp, int Kp,
                                                          const uint4 *__restrict__ Bm, int b_in_smem) {
   extern __shared__ uint4 bsm[];
-  const int KS = Kp / 16, NTt = (Pp + 7) / 8;
+  const int KS = Kp / 16, NTt = PACK ? (Pp / 2 + 3) / 4 : (Pp + 7) / 8;
+  const int ng = blockIdx.y * kRowNG;
+  const int nq = NTt - ng < kRowNG ? NTt - ng : kRowNG;  // n-tiles in this group
+  const uint4 *Bg = Bm + (size_t)ng * KS * 32;
   if (b_in_smem) {
-    for (int e = threadIdx.x; e < NTt * KS * 32; e += blockDim.x) bsm[e] = Bm[e];
+    for (int e = threadIdx.x; e < nq * KS * 32; e += blockDim.x) bsm[e] = Bg[e];
     __syncthreads();
   }
-  const uint4 *B = b_in_smem ? bsm : Bm;
+  const uint4 *B = b_in_smem ? bsm : Bg;
   const int lane = threadIdx.x & 31, g = lane >> 2, tq = lane & 3;
-  const int Rc2 = Rc + (Rc & 1);
+  const int Rc2 = Rc + (Rc & 1), half = Pp / 2;
   const int64_t nblk = (nrows + 7) / 8;
   for (int64_t blk = (int64_t)blockIdx.x * 4 + (threadIdx.x >> 5); blk < nblk; blk += (int64_t)gridDim.x * 4) {
     const int64_t r = blk * 8 + g;
@@ -582,81 +610,86 @@ __global__ void __launch_bounds__(128) k_interp_rows_mma(const float2 *__restric
       in_ok = rok && t < Rc;
     }
     const float2 *in = src + (in_ok ? srow : 0) * (int64_t)Pc;
-    for (int ng = 0; ng < NTt; ng += kRowNG) {
-      float acc[kRowNG][4];
+    auto load_in = [&](int ks, float2 (&v)[4]) {
+      const int k0 = ks * 16 + 2 * tq;
 #pragma unroll
-      for (int q = 0; q < kRowNG; ++q) acc[q][0] = acc[q][1] = acc[q][2] = acc[q][3] = 0.f;
-      for (int ks = 0; ks < KS; ++ks) {
-        const int k0 = ks * 16 + 2 * tq;
-        float2 v[4];
+      for (int u = 0; u < 4; ++u) {
+        const int k = k0 + (u & 1) + (u >> 1) * 8;
+        v[u] = (in_ok && k < Pc) ? in[k] : make_float2(0.f, 0.f);
+      }
+    };
+    float acc[kRowNG][4];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          const int k = k0 + (u & 1) + (u >> 1) * 8;
-          v[u] = (in_ok && k < Pc) ? in[k] : make_float2(0.f, 0.f);
+    for (int q = 0; q < kRowNG; ++q) acc[q][0] = acc[q][1] = acc[q][2] = acc[q][3] = 0.f;
+    float2 vn[4];
+    load_in(0, vn);
+    for (int ks = 0; ks < KS; ++ks) {
+      const float2 v[4] = {vn[0], vn[1], vn[2], vn[3]};
+      if (ks + 1 < KS) load_in(ks + 1, vn);
+      uint32_t ahi[4], alo[4];
+      split_bf16x2(v[0].x, v[1].x, ahi[0], alo[0]);  // row g (real parts), k0, k0+1
+      split_bf16x2(v[0].y, v[1].y, ahi[1], alo[1]);  // row g+8 (imaginary parts)
+      split_bf16x2(v[2].x, v[3].x, ahi[2], alo[2]);  // row g, k0+8, k0+9
+      split_bf16x2(v[2].y, v[3].y, ahi[3], alo[3]);
+      if (nq == kRowNG) {  // full group: one basic block, 8 independent accumulators
+        uint4 bv[kRowNG];
+#pragma unroll
+        for (int q = 0; q < kRowNG; ++q) bv[q] = B[((size_t)q * KS + ks) * 32 + lane];
+#pragma unroll
+        for (int q = 0; q < kRowNG; ++q) {
+          const uint32_t bhi[2] = {bv[q].x, bv[q].y};
+          mma_bf16(acc[q], ahi, bhi);
         }
-        uint32_t ahi[4], alo[4];
-        split_bf16x2(v[0].x, v[1].x, ahi[0], alo[0]);  // row g (real parts), k0, k0+1
-        split_bf16x2(v[0].y, v[1].y, ahi[1], alo[1]);  // row g+8 (imaginary parts)
-        split_bf16x2(v[2].x, v[3].x, ahi[2], alo[2]);  // row g, k0+8, k0+9
-        split_bf16x2(v[2].y, v[3].y, ahi[3], alo[3]);
-        if (ng + kRowNG <= NTt) {  // full group: one basic block, 8 independent accumulators
-          uint4 bv[kRowNG];
 #pragma unroll
-          for (int q = 0; q < kRowNG; ++q) bv[q] = B[((size_t)(ng + q) * KS + ks) * 32 + lane];
+        for (int q = 0; q < kRowNG; ++q) {
+          const uint32_t blo[2] = {bv[q].z, bv[q].w};
+          mma_bf16(acc[q], ahi, blo);
+        }
 #pragma unroll
-          for (int q = 0; q < kRowNG; ++q) {
-            const uint32_t bhi[2] = {bv[q].x, bv[q].y};
-            mma_bf16(acc[q], ahi, bhi);
-          }
+        for (int q = 0; q < kRowNG; ++q) {
+          const uint32_t bhi[2] = {bv[q].x, bv[q].y};
+          mma_bf16(acc[q], alo, bhi);
+        }
+      } else {
 #pragma unroll
-          for (int q = 0; q < kRowNG; ++q) {
-            const uint32_t blo[2] = {bv[q].z, bv[q].w};
-            mma_bf16(acc[q], ahi, blo);
-          }
-#pragma unroll
-          for (int q = 0; q < kRowNG; ++q) {
-            const uint32_t bhi[2] = {bv[q].x, bv[q].y};
-            mma_bf16(acc[q], alo, bhi);
-          }
-        } else {
-#pragma unroll
-          for (int q = 0; q < kRowNG; ++q) {
-            const int nt = ng + q;
-            if (nt >= NTt) break;
-            const uint4 bv = B[((size_t)nt * KS + ks) * 32 + lane];
-            const uint32_t bhi[2] = {bv.x, bv.y}, blo[2] = {bv.z, bv.w};
-            mma_bf16(acc[q], ahi, bhi);
-            mma_bf16(acc[q], ahi, blo);
-            mma_bf16(acc[q], alo, bhi);
-          }
+        for (int q = 0; q < kRowNG; ++q) {
+          if (q >= nq) break;
+          const uint4 bv = B[((size_t)q * KS + ks) * 32 + lane];
+          const uint32_t bhi[2] = {bv.x, bv.y}, blo[2] = {bv.z, bv.w};
+          mma_bf16(acc[q], ahi, bhi);
+          mma_bf16(acc[q], ahi, blo);
+          mma_bf16(acc[q], alo, bhi);
         }
       }
-      if (PACK) {
-        uint4 *dst = (uint4 *)dst_;
-        const bool odd = g & 1;
-        const int64_t pair_row = r >> 1;  // = pattern * Rc2/2 + t/2, Rc2 even
+    }
+    if (PACK) {
+      uint4 *dst = (uint4 *)dst_;
+      const bool odd = g & 1;
+      const int64_t pair_row = r >> 1;  // = pattern * Rc2/2 + t/2, Rc2 even
 #pragma unroll
-        for (int q = 0; q < kRowNG; ++q) {
-          if (ng + q >= NTt) break;
-          // even g keeps column j (rows t, t+1 from the neighbour), odd g keeps j+1
-          const float sr = odd ? acc[q][0] : acc[q][1], si = odd ? acc[q][2] : acc[q][3];
-          const float rr = __shfl_xor_sync(0xffffffffu, sr, 4), ri = __shfl_xor_sync(0xffffffffu, si, 4);
-          const float r0 = odd ? rr : acc[q][0], i0 = odd ? ri : acc[q][2];  // row t (even)
-          const float r1 = odd ? acc[q][1] : rr, i1 = odd ? acc[q][3] : ri;  // row t+1
-          const int j = (ng + q) * 8 + 2 * tq + (odd ? 1 : 0);
-          uint32_t hr, lr, hi, li;
-          split_bf16x2(r0, r1, hr, lr);
-          split_bf16x2(i0, i1, hi, li);
-          if (rok && j < Pp) dst[pair_row * Pp + j] = make_uint4(hr, lr, hi, li);
-        }
-      } else if (rok) {
-        float2 *out = (float2 *)dst_ + r * (int64_t)Pp;
+      for (int q = 0; q < kRowNG; ++q) {
+        if (q >= nq) break;
+        // acc: {re j, re j', im j, im j'} of this lane's row
+        const float sr = acc[q][0] + acc[q][1], dr = acc[q][0] - acc[q][1];
+        const float si = acc[q][2] + acc[q][3], di = acc[q][2] - acc[q][3];
+        // even lane (row t) keeps the real parts and sends its imaginary ones
+        const float xs = __shfl_xor_sync(0xffffffffu, odd ? sr : si, 4);
+        const float xd = __shfl_xor_sync(0xffffffffu, odd ? dr : di, 4);
+        const float s0 = odd ? xs : sr, s1 = odd ? si : xs;  // rows t, t+1 of this lane's part
+        const float d0 = odd ? xd : dr, d1 = odd ? di : xd;
+        const int j = (ng + q) * 4 + tq;
+        uint32_t sh, sl, dh, dl;
+        split_bf16x2(s0, s1, sh, sl);
+        split_bf16x2(d0, d1, dh, dl);
+        if (rok && j < half) dst[(pair_row * half + j) * 2 + (odd ? 1 : 0)] = make_uint4(sh, sl, dh, dl);
+      }
+    } else if (rok) {
+      float2 *out = (float2 *)dst_ + r * (int64_t)Pp;
 #pragma unroll
-        for (int q = 0; q < kRowNG; ++q) {
-          const int j = (ng + q) * 8 + 2 * tq;
-          if (j < Pp) out[j] = make_float2(acc[q][0], acc[q][2]);
-          if (j + 1 < Pp) out[j + 1] = make_float2(acc[q][1], acc[q][3]);
-        }
+      for (int q = 0; q < kRowNG; ++q) {
+        const int j = (ng + q) * 8 + 2 * tq;
+        if (j < Pp) out[j] = make_float2(acc[q][0], acc[q][2]);
+        if (j + 1 < Pp) out[j + 1] = make_float2(acc[q][1], acc[q][3]);
       }
     }
   }
@@ -666,18 +699,22 @@ static po_status launch_rows(bool pack, const float2 *src, void *dst, int64_t nr
                              const uint32_t *Bm, int sm_count, cudaStream_t st) {
   if (nrows <= 0) return PO_OK;
   if (Kp % 16 || Kp < Pc) return fail(PO_ERR_INTERNAL, "phi matrix K padding");
-  const size_t bbytes = sizeof(uint32_t) * phi_matrix_words(Pp, Kp);
-  const bool b_smem = bbytes <= 48 * 1024;
+  const int NTt = pack ? (Pp / 2 + 3) / 4 : (Pp + 7) / 8;
+  const int ngroups = (NTt + kRowNG - 1) / kRowNG;
+  const size_t bbytes = sizeof(uint4) * (size_t)kRowNG * (Kp / 16) * 32;
+  const bool b_smem = bbytes <= 128 * 1024;
   const size_t smem = b_smem ? bbytes : 0;
   int64_t blocks = ((nrows + 7) / 8 + 3) / 4;
-  const int64_t cap = (int64_t)sm_count * 16;
+  const int64_t cap = (int64_t)sm_count * 16 / ngroups + 1;
   if (blocks > cap) blocks = cap;
+  if (ngroups > 65535) return fail(PO_ERR_UNSUPPORTED, "angular grid too large for the row pass");
+  dim3 grid((unsigned)blocks, (unsigned)ngroups);
   if (pack)
-    k_interp_rows_mma<true><<<(unsigned)blocks, 128, smem, st>>>(src, dst, nrows, Rc, Pc, Pp, Kp, (const uint4 *)Bm,
-                                                                 b_smem ? 1 : 0);
+    k_interp_rows_mma<true><<<grid, 128, smem, st>>>(src, dst, nrows, Rc, Pc, Pp, Kp, (const uint4 *)Bm,
+                                                     b_smem ? 1 : 0);
   else
-    k_interp_rows_mma<false><<<(unsigned)blocks, 128, smem, st>>>(src, dst, nrows, Rc, Pc, Pp, Kp,
-                                                                  (const uint4 *)Bm, b_smem ? 1 : 0);
+    k_interp_rows_mma<false><<<grid, 128, smem, st>>>(src, dst, nrows, Rc, Pc, Pp, Kp, (const uint4 *)Bm,
+                                                      b_smem ? 1 : 0);
   count_launch();
   PO_CUDA(cudaGetLastError());
   return PO_OK;
@@ -688,7 +725,7 @@ po_status launch_interp_rows_mma(const float2 *src, float2 *dst, int64_t nrows, 
   return launch_rows(false, src, dst, nrows, 0, Pc, Pp, Kp, Bm, sm_count, st);
 }
 
-po_status launch_interp_rows_packed(const float2 *src, uint2 *dst, int64_t n_patterns, int Rc, int Pc, int Pp,
+po_status launch_interp_rows_packed(const float2 *src, uint4 *dst, int64_t n_patterns, int Rc, int Pc, int Pp,
                                     int Kp, const uint32_t *Bm, int sm_count, cudaStream_t st) {
   const int64_t nrows = n_patterns * (int64_t)(Rc + (Rc & 1));
   return launch_rows(true, src, dst, nrows, Rc, Pc, Pp, Kp, Bm, sm_count, st);
@@ -704,8 +741,7 @@ po_status init_interp_mma_attributes(int max_smem) {
   PO_CUDA(cudaFuncSetAttribute(k_interp_rows_mma<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
 #define PO_TW_ATTR(N, M) \
   PO_CUDA(cudaFuncSetAttribute(k_theta_warp<N, M>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
-  PO_TW_ATTR(2, 1) PO_TW_ATTR(2, 2) PO_TW_ATTR(2, 3) PO_TW_ATTR(2, 4)
-  PO_TW_ATTR(4, 1) PO_TW_ATTR(4, 2)
+  PO_TW_ATTR(1, 1) PO_TW_ATTR(1, 2) PO_TW_ATTR(1, 3) PO_TW_ATTR(1, 4) PO_TW_ATTR(2, 1) PO_TW_ATTR(2, 2)
 #undef PO_TW_ATTR
   return PO_OK;
 }

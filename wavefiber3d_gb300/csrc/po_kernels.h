@@ -71,16 +71,17 @@ po_status launch_interp_cols(const float2 *mid, float2 *parent, const int32_t *c
 size_t theta_matrix_words(int Rp, int Kp);
 size_t theta_pair_words(int Rp, int Kp);
 void build_theta_matrix(int Tc, int Tp, int Rc, int Rp, int Kp, std::vector<uint32_t> &out);
-po_status launch_interp_cols_mma(const uint2 *mid, float2 *parent, const int32_t *child_table, int64_t n_parent,
+po_status launch_interp_cols_mma(const uint4 *mid, float2 *parent, const int32_t *child_table, int64_t n_parent,
                                  int64_t n_child, int phi, int Rc, int Rp, int Kp, const uint32_t *Afrag,
                                  const float4 *trans, int n_slots, int G, int tile, cudaStream_t st);
 // tensor-core phi pass (po_interp_mma.cu): float2 rows -> float2 rows, or
-// (packed) n_patterns x Rc rows -> split-bf16 row pairs for the theta pass
+// (packed) n_patterns x Rc rows -> mirror-pair sums / differences in split-bf16
+// row pairs for the theta pass
 size_t phi_matrix_words(int Pp, int Kp);
 void build_phi_matrix(int Pc, int Pp, int Kp, std::vector<uint32_t> &out);
 po_status launch_interp_rows_mma(const float2 *src, float2 *dst, int64_t nrows, int Pc, int Pp, int Kp,
                                  const uint32_t *Bm, int sm_count, cudaStream_t st);
-po_status launch_interp_rows_packed(const float2 *src, uint2 *dst, int64_t n_patterns, int Rc, int Pc, int Pp,
+po_status launch_interp_rows_packed(const float2 *src, uint4 *dst, int64_t n_patterns, int Rc, int Pc, int Pp,
                                     int Kp, const uint32_t *Bm, int sm_count, cudaStream_t st);
 // adjoint (transposed) passes, double cover only (po_interp_mma.cu)
 void build_theta_matrix_adj(int Tc, int Tp, int Rc, int Rp, int Kp, std::vector<uint32_t> &out);
@@ -89,8 +90,11 @@ po_status launch_interp_cols_adj_mma(const float2 *parent_adj, float2 *mid_adj, 
                                      const uint32_t *child_prefix, int64_t n_parent, int64_t n_child, int phi, int Rc,
                                      int Rp, int Kp, const uint32_t *Afrag, const float4 *trans, int n_slots, int G,
                                      cudaStream_t st);
-po_status launch_trans_table(const double *k_per_lambda, int n_lambda, int nth, int Rp, int phi, const double a[3],
-                             float4 *out, cudaStream_t st);
+// direction factors of a level grid (once per context) and the per-solve
+// translation phases built from them (po_fft.cu)
+po_status launch_dir_trig(int nth, int R, int phi, double2 *trig, cudaStream_t st);
+po_status launch_trans_table(const double *k_per_lambda, int n_lambda, int Rp, int phi, const double2 *trig,
+                             const double a[3], float4 *out, cudaStream_t st);
 
 // height field [2][numel][numelvert] -> samples of quads (i, j in [ring_begin, ring_end]);
 // out = {x, y, z, nx, ny, nz, area}; err |= 1 on a vertex at the origin (po_geometry.cu)

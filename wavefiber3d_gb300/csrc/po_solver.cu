@@ -157,6 +157,8 @@ struct po_ctx {
   size_t bmat_off[PO_MAX_DEPTH] = {};
   int bmat_kp[PO_MAX_DEPTH] = {};
   DevBuf amat, bmat;
+  DevBuf dir_trig;  // per level: (cos, sin) of the grid's theta rows, then of its phi columns
+  size_t trig_off[PO_MAX_DEPTH] = {};
   // transposed level matrices of the adjoint (built on the first po_grad)
   bool adj_ready = false;
   size_t amat_adj_off[PO_MAX_DEPTH] = {}, bmat_adj_off[PO_MAX_DEPTH] = {};
@@ -302,16 +304,28 @@ po_status po_create(po_ctx **out, const po_config *cfg) {
     total += n;
   }
   po_status s = c->twiddles.ensure(sizeof(float2) * (size_t)std::max(total, 1));
-  if (s != PO_OK) { delete c; return s; }
+  if (s != PO_OK) { po_destroy(c); return s; }
   for (int n : lens) {
     s = launch_twiddles(n, c->twiddles.as<float2>() + c->tw_offset[n], 0);
-    if (s != PO_OK) { delete c; return s; }
+    if (s != PO_OK) { po_destroy(c); return s; }
+  }
+  // direction factors of every parent level (translation tables)
+  {
+    size_t n_trig = 0;
+    for (int l = 0; l < d; ++l) {
+      c->trig_off[l] = n_trig;
+      n_trig += (size_t)c->R[l] + c->Phi[l];
+    }
+    s = c->dir_trig.ensure(sizeof(double2) * std::max<size_t>(n_trig, 1));
+    for (int l = 0; l < d && s == PO_OK; ++l)
+      s = launch_dir_trig(c->nth[l], c->R[l], c->Phi[l], c->dir_trig.as<double2>() + c->trig_off[l], 0);
+    if (s != PO_OK) { po_destroy(c); return s; }
   }
   for (auto &e : c->ev) {
-    if (cudaEventCreate(&e) != cudaSuccess) { delete c; return fail(PO_ERR_CUDA, "cudaEventCreate"); }
+    if (cudaEventCreate(&e) != cudaSuccess) { po_destroy(c); return fail(PO_ERR_CUDA, "cudaEventCreate"); }
   }
   for (auto &e : c->kev) {
-    if (cudaEventCreate(&e) != cudaSuccess) { delete c; return fail(PO_ERR_CUDA, "cudaEventCreate"); }
+    if (cudaEventCreate(&e) != cudaSuccess) { po_destroy(c); return fail(PO_ERR_CUDA, "cudaEventCreate"); }
   }
   // constant theta-interpolation matrices of every level (tensor-core path)
   c->tensor_theta = cfg->interp_method == PO_INTERP_TENSOR && c->mirror;
@@ -343,7 +357,7 @@ po_status po_create(po_ctx **out, const po_config *cfg) {
       s = fail(PO_ERR_CUDA, "upload of the interpolation matrices");
     if (s != PO_OK) { po_destroy(c); return s; }
   }
-  if (cudaDeviceSynchronize() != cudaSuccess) { delete c; return fail(PO_ERR_CUDA, "twiddle set-up failed"); }
+  if (cudaDeviceSynchronize() != cudaSuccess) { po_destroy(c); return fail(PO_ERR_CUDA, "set-up kernels failed"); }
   *out = c;
   return PO_OK;
 }
@@ -353,7 +367,7 @@ po_status po_destroy(po_ctx *c) {
   for (DevBuf *b : {&c->twiddles, &c->geom_in, &c->geom_sorted, &c->octree_ws, &c->leaf_ctr, &c->dirs, &c->dirs_d,
                     &c->trans, &c->levelA, &c->levelB, &c->mid, &c->slots, &c->kvals, &c->out, &c->cur, &c->partial,
                     &c->tile_ctr, &c->amat, &c->bmat, &c->amat_adj, &c->bmat_adj, &c->slots64, &c->grad_acc,
-                    &c->chunk_begin, &c->center0})
+                    &c->chunk_begin, &c->center0, &c->dir_trig})
     b->release();
   for (auto &e : c->ev)
     if (e) cudaEventDestroy(e);
@@ -628,8 +642,8 @@ static po_status prepare_solve(po_ctx *c, const po_geometry *g, const po_illum *
   for (int l = 0; l < d; ++l) {
     double a[3];
     for (int q = 0; q < 3; ++q) a[q] = ((double)cfg.box_max[q] - (double)cfg.box_min[q]) / std::ldexp(1.0, l + 2);
-    PO_TRY(launch_trans_table(P.k_lambda, L, c->nth[l], c->R[l], c->Phi[l], a, c->trans.as<float4>() + P.tr_off[l],
-                              st));
+    PO_TRY(launch_trans_table(P.k_lambda, L, c->R[l], c->Phi[l], c->dir_trig.as<double2>() + c->trig_off[l], a,
+                              c->trans.as<float4>() + P.tr_off[l], st));
   }
   // leaf directions
   std::vector<float4> df = host_dirs_f4(c->R[d], c->Phi[d], c->nth[d]);
@@ -745,7 +759,7 @@ static po_status enqueue_solve(po_ctx *c, const SolvePlan &P, float *out_dev, co
         int64_t nrows = (int64_t)ch.ns * nc * 6 * c->R[l + 1];
         PO_TRY(rec(c->kev[2 + 4 * l]));
         if (c->tensor_theta) {
-          PO_TRY(launch_interp_rows_packed(cur_lvl, c->mid.as<uint2>(), (int64_t)ch.ns * nc * 6, c->R[l + 1],
+          PO_TRY(launch_interp_rows_packed(cur_lvl, c->mid.as<uint4>(), (int64_t)ch.ns * nc * 6, c->R[l + 1],
                                            c->Phi[l + 1], c->Phi[l], c->bmat_kp[l],
                                            c->bmat.as<uint32_t>() + c->bmat_off[l], c->sm_count, st));
         } else {
@@ -761,7 +775,7 @@ static po_status enqueue_solve(po_ctx *c, const SolvePlan &P, float *out_dev, co
         if (np > 0) ++T.n_col;
         PO_TRY(rec(c->kev[4 + 4 * l]));
         if (c->tensor_theta) {
-          PO_TRY(launch_interp_cols_mma(c->mid.as<uint2>(), nxt, P.tree.level[l].child, np, nc, c->Phi[l],
+          PO_TRY(launch_interp_cols_mma(c->mid.as<uint4>(), nxt, P.tree.level[l].child, np, nc, c->Phi[l],
                                         c->R[l + 1], c->R[l], c->amat_kp[l], c->amat.as<uint32_t>() + c->amat_off[l],
                                         trans, ch.ns, ch.gc, cfg.interp_tile, st));
         } else {
