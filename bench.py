@@ -746,7 +746,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["engine", "reference"], default="engine")
     ap.add_argument("--cpu-dirs", type=int, default=2048, help="directions of the FP64 CPU sample")
-    ap.add_argument("--precision", choices=sorted(PRECISIONS), default="fp32")
+    ap.add_argument("--precision", choices=sorted(PRECISIONS), default=None,
+                    help="leaf precision (default: split_bf16 for the ellipsoid and the fiber -- the faster one at "
+                         "the same accuracy on GB300 -- and fp32 for the cylinder gradient)")
     ap.add_argument("--interp", choices=sorted(INTERP), default="tensor")
     ap.add_argument("--interp-tile", type=int, choices=[0, 8, 16], default=0,
                     help="complex columns per CTA of the tensor-core theta pass (0: automatic)")
@@ -764,6 +766,8 @@ def main():
     ap.add_argument("--batch-dirs", type=int, default=64, help="FP64 check directions per batch solve")
     ap.add_argument("--tune-cache", default=None, help="JSON file of the autotuner's choices (read and written)")
     args = ap.parse_args()
+    if args.precision is None:
+        args.precision = "fp32" if args.workload == "cylinder-grad" else "split_bf16"
     if args.warmup < 3 and args.impl == "engine":
         args.warmup = 3
     world, rank, local = dist_setup(args)

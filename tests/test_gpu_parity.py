@@ -316,3 +316,17 @@ def test_chunked_solve_matches_single_pass(depth, prec):
         seen.add((r["n_chunks"], r["chunk_slots"]))
         assert np.array_equal(out, full), (k, r["n_chunks"], r["chunk_slots"])
     assert len(seen) >= 2, seen
+
+
+@pytest.mark.parametrize("prec", [api.PO_PREC_FP32, api.PO_PREC_SPLIT_BF16])
+def test_large_level_grids_vs_fp64_direct(prec):
+    """The fiber preset's upper level grids (616 x 518 and 323 x 273 under the
+    180 x 360 output): theta matrices with 40 k-steps and phi matrices too large
+    to stage in shared memory take the reduced-tile paths."""
+    cloud = geometry.fibonacci_sphere(1.0e-6, 2000)
+    box = [-1.1e-6] * 3 + [1.1e-6] * 3
+    cfg = api.Config(2, [180, 616, 323], [360, 518, 273], box[:3], box[3:], precision=prec)
+    il = api.Illumination([500e-9], [0.3], [0.7], api.PO_POL_TM, 1.55 + 0.1j, 2e-6)
+    out, rep = _solve(cloud, cfg, il)
+    o = oracle.solve_direct(cloud, oracle.make_illum(500e-9, 0.3, 0.7, "M", 1.55 + 0.1j, 2e-6), 180, 360)
+    assert rel(out.reshape(o.shape), o) < TOL_TREE, rep

@@ -1,6 +1,7 @@
 // po_common.cuh -- shared device/host helpers of the PO engine.
 #pragma once
 
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -88,6 +89,29 @@ __device__ __forceinline__ void sincos_small(float ph, float *s, float *c) {
   float r = fmaf(-n, 6.28318548202514648f, ph);
   r = fmaf(-n, -1.74845553e-7f, r);
   __sincosf(r, s, c);
+}
+
+// ------------------------------------------------ split-bf16 tensor products
+// mma.sync m16n8k16, bf16 operands, FP32 accumulation.  Not volatile: a pure
+// function of its operands, so the scheduler may interleave independent
+// accumulators.
+__device__ __forceinline__ void mma_bf16(float *d, const uint32_t *a, const uint32_t *b) {
+  asm("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+// (x0, x1) -> bf16x2 hi = rn(x), lo = rn(x - hi), x0 in the low half (fragment
+// order): two packed conversions, the hi parts widened back by shifts.
+__device__ __forceinline__ void split_bf16x2(float x0, float x1, uint32_t &hi, uint32_t &lo) {
+  const __nv_bfloat162 h = __floats2bfloat162_rn(x0, x1);
+  uint32_t hu;
+  memcpy(&hu, &h, 4);
+  const float h0 = __uint_as_float(hu << 16), h1 = __uint_as_float(hu & 0xffff0000u);
+  const __nv_bfloat162 l = __floats2bfloat162_rn(x0 - h0, x1 - h1);
+  hi = hu;
+  memcpy(&lo, &l, 4);
 }
 
 // ------------------------------------------------------------------ vectors

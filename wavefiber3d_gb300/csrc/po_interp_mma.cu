@@ -143,24 +143,6 @@ void build_theta_matrix_adj(int Tc, int Tp, int Rc, int Rp, int Kp, std::vector<
 }
 
 // ---------------------------------------------------------- device side
-// (not volatile: a pure function of its operands, so the scheduler may
-// interleave independent accumulators)
-__device__ __forceinline__ void mma_bf16(float *d, const uint32_t *a, const uint32_t *b) {
-  asm(
-      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-      "{%0,%1,%2,%3};\n"
-      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
-}
-
-__device__ __forceinline__ void split_bf16x2(float x0, float x1, uint32_t &hi, uint32_t &lo) {
-  __nv_bfloat16 h0 = __float2bfloat16_rn(x0), h1 = __float2bfloat16_rn(x1);
-  __nv_bfloat16 l0 = __float2bfloat16_rn(x0 - __bfloat162float(h0));
-  __nv_bfloat16 l1 = __float2bfloat16_rn(x1 - __bfloat162float(h1));
-  hi = (uint32_t)__bfloat16_as_ushort(h0) | ((uint32_t)__bfloat16_as_ushort(h1) << 16);
-  lo = (uint32_t)__bfloat16_as_ushort(l0) | ((uint32_t)__bfloat16_as_ushort(l1) << 16);
-}
-
 // Theta pass as warp tasks (double cover).  A warp owns one (slot, parent,
 // component) and TW = 4 NPT column pairs (j, j + Phi/2), j = j0.., for the
 // CTA's 16-row tiles mt0 .. mt0+MTW-1 (blockIdx.y selects them).
@@ -294,11 +276,14 @@ __global__ void __launch_bounds__(256, 2) k_theta_warp(const uint4 *__restrict__
           const int r = r0 < Rp ? r0 : Rp - 1;
           const float ur = d[i][pt][0][2 * h], ui = d[i][pt][0][2 * h + 1];
           const float vr = d[i][pt][1][2 * h], vi = d[i][pt][1][2 * h + 1];
+          // phi_{j+Phi/2} = phi_j + pi: the mirror column's x and y phases are
+          // the negatives of column j's, so one table entry serves both
+          const float4 rr = __ldg(tr + (int64_t)r * phi + jc);
+          const float pxy = fmaf(sgx, rr.x, sgy * rr.y), pz = sgz * rr.z;
 #pragma unroll
           for (int w = 0; w < 2; ++w) {
-            const float4 rr = __ldg(tr + (int64_t)r * phi + jc + w * span);
             float sn, cs;
-            sincos_small(fmaf(sgx, rr.x, fmaf(sgy, rr.y, sgz * rr.z)), &sn, &cs);
+            sincos_small(w ? pz - pxy : pz + pxy, &sn, &cs);
             const float yr = w ? ur - vr : ur + vr, yi = w ? ui - vi : ui + vi;
             acc[i][pt][w][2 * h] += yr * cs - yi * sn;
             acc[i][pt][w][2 * h + 1] += yr * sn + yi * cs;
@@ -350,12 +335,17 @@ po_status launch_interp_cols_mma(const uint4 *mid, float2 *parent, const int32_t
   if (phi % 2) return fail(PO_ERR_INTERNAL, "mirrored storage needs an even phi grid");
   const int KS = Kp / 16, MT = (Rp + 15) / 16;
   const int NPT = tile == 16 ? 2 : 1;
-  // 16-row tiles per warp: up to 4 (register budget of the accumulators)
-  const int cap = NPT == 2 ? 2 : 4;
+  // 16-row tiles per warp: up to 4 (register budget of the accumulators), and
+  // few enough that the CTA's matrix slice (2 KB per tile and k-step) leaves
+  // room for two CTAs per SM; a single tile may use the whole opt-in limit
+  const size_t tile_bytes = sizeof(uint4) * (size_t)KS * 128;
+  int cap = NPT == 2 ? 2 : 4;
+  while (cap > 1 && (size_t)cap * tile_bytes > 113 * 1024) --cap;
+  if (tile_bytes > 227 * 1024)
+    return fail(PO_ERR_UNSUPPORTED, "angular grid too large for the tensor-core interpolation");
   const int nmg = (MT + cap - 1) / cap;
   const int MTW = (MT + nmg - 1) / nmg;
-  const size_t smem = sizeof(uint4) * (size_t)MTW * KS * 128;
-  if (smem > 227 * 1024) return fail(PO_ERR_UNSUPPORTED, "angular grid too large for the tensor-core interpolation");
+  const size_t smem = (size_t)MTW * tile_bytes;
   const int TW = 4 * NPT;
   const int n_ct = (phi / 2 + TW - 1) / TW;
   const int64_t n_task = (int64_t)n_slots * n_parent * 6 * n_ct;

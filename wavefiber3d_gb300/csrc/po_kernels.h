@@ -38,6 +38,7 @@ po_status launch_leaf(const float *const g[7], const int32_t *leaf_begin, const 
                       const float4 *dirs, int ndir, float2 *out, cudaStream_t st);
 
 // split hi+lo BF16 tensor-core leaf sums (po_leaf_mma.cu); same layout as launch_leaf
+po_status init_leaf_mma_attributes();
 po_status launch_leaf_mma(const float *const g[7], const int32_t *leaf_begin, const double *leaf_center,
                           int64_t n_leaves, const SlotParams<float> *slots_dev, int n_lambda, int G,
                           const float4 *dirs, int ndir, float2 *out, cudaStream_t st);

@@ -28,149 +28,157 @@ namespace wavepo {
 
 namespace {
 
-__device__ __forceinline__ void mma_bf16_16816(float *d, const uint32_t *a, const uint32_t *b) {
-  asm volatile(
-      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-      "{%0,%1,%2,%3};\n"
-      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
-}
-
-__device__ __forceinline__ void split2(float x0, float x1, uint32_t &hi, uint32_t &lo) {
-  __nv_bfloat16 h0 = __float2bfloat16_rn(x0), h1 = __float2bfloat16_rn(x1);
-  __nv_bfloat16 l0 = __float2bfloat16_rn(x0 - __bfloat162float(h0));
-  __nv_bfloat16 l1 = __float2bfloat16_rn(x1 - __bfloat162float(h1));
-  hi = (uint32_t)__bfloat16_as_ushort(h0) | ((uint32_t)__bfloat16_as_ushort(h1) << 16);
-  lo = (uint32_t)__bfloat16_as_ushort(l0) | ((uint32_t)__bfloat16_as_ushort(l1) << 16);
-}
-
 // (cos, sin) of the phase of direction s and point u, split into hi/lo pairs
 __device__ __forceinline__ void phase_frag(float sx, float sy, float sz, float4 u, uint32_t &hi, uint32_t &lo) {
   float sn, cs;
   sincos_small(fmaf(sx, u.x, fmaf(sy, u.y, sz * u.z)), &sn, &cs);
-  split2(cs, sn, hi, lo);
+  split_bf16x2(cs, sn, hi, lo);
 }
 
-constexpr int kPC = 64;         // points per chunk (8 k-steps of 16 = 8 points x cos/sin)
-constexpr int kSlotsGroup = 4;  // slots per N-group: 4 x 6 complex = 48 real columns = 6 n-tiles
-constexpr int kMaxNT = 6;
+constexpr int kPC = 128;  // points per chunk (16 k-steps of 16 = 8 points x cos/sin)
 
 }  // namespace
 
-// CTA: one (leaf, wavelength), 4 warps.  Slots of the wavelength go in groups
-// of up to 4; warps share the 16-direction row tiles.
+// CTA: one (leaf, wavelength) and GC slots g0.. of the wavelength (NT n-tiles
+// of 8 real columns = 2 x 6 GC), 4 warps over the 16-direction row tiles.
+// Dynamic shared memory: s_u[kPC] float4, s_cur[kPC][6 GC] float2,
+// s_b[kPC/8][NT][32] uint4 (B fragments {hi0, hi1, lo0, lo1}).
+template <int GC>
 __global__ void __launch_bounds__(128) k_leaf_mma(
     const float *__restrict__ x, const float *__restrict__ y, const float *__restrict__ z,
     const float *__restrict__ nx, const float *__restrict__ ny, const float *__restrict__ nz,
     const float *__restrict__ area, const int32_t *__restrict__ leaf_begin, const double *__restrict__ leaf_center,
     const SlotParams<float> *__restrict__ slots, const float4 *__restrict__ dirs, int ndir, int64_t n_leaves,
-    int Gtot, float2 *__restrict__ out) {
-  __shared__ float4 s_u[kPC];
-  __shared__ float2 s_cur[kPC][kSlotsGroup * 6];
-  __shared__ uint4 s_b[kPC / 8][kMaxNT][32];  // B fragments {hi0, hi1, lo0, lo1} per (k-step, n-tile, lane)
+    int Gtot, int g0, float2 *__restrict__ out) {
+  constexpr int NC = 6 * GC;            // complex columns
+  constexpr int NT = (2 * NC + 7) / 8;  // n-tiles of 8 real columns
+  extern __shared__ uint4 smem_leaf[];
+  uint4 *s_b = smem_leaf;                                        // [kPC/8][NT][32]
+  float4 *s_u = (float4 *)(s_b + (kPC / 8) * NT * 32);           // [kPC]
+  float2 *s_cur = (float2 *)(s_u + kPC);                         // [kPC][NC]
   const int64_t leaf = blockIdx.x;
   const int lam = blockIdx.y;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, tq = lane & 3;
   const int b = leaf_begin[leaf], e = leaf_begin[leaf + 1];
   const double cxd = leaf_center[3 * leaf], cyd = leaf_center[3 * leaf + 1], czd = leaf_center[3 * leaf + 2];
-  const SlotParams<float> *sl = slots + (int64_t)lam * Gtot;
+  const SlotParams<float> *sl = slots + (int64_t)lam * Gtot + g0;
   const double k0 = sl[0].k0d;
   const int64_t slot_stride = n_leaves * 6 * (int64_t)ndir;
-  float2 *obase = out + (int64_t)lam * Gtot * slot_stride + leaf * 6 * (int64_t)ndir;
+  float2 *obase = out + ((int64_t)lam * Gtot + g0) * slot_stride + leaf * 6 * (int64_t)ndir;
   const int MT = (ndir + 15) / 16;
-  for (int g0 = 0; g0 < Gtot; g0 += kSlotsGroup) {
-    const int gc = min(kSlotsGroup, Gtot - g0);
-    const int ncols = gc * 6;            // complex columns of this group
-    const int NT = (2 * ncols + 7) / 8;  // n-tiles of 8 real columns
-    for (int c0 = b; c0 < e || (c0 == b && b == e); c0 += kPC) {
-      const int cnt = max(0, min(kPC, e - c0));
-      const bool first = (c0 == b);
-      __syncthreads();
-      for (int q = threadIdx.x; q < kPC; q += blockDim.x) {
-        if (q < cnt) {
-          const int p = c0 + q;
-          const float px = x[p], py = y[p], pz = z[p];
-          s_u[q] = make_float4((float)(k0 * ((double)px - cxd)), (float)(k0 * ((double)py - cyd)),
-                               (float)(k0 * ((double)pz - czd)), 0.f);
-          const float qx = nx[p], qy = ny[p], qz = nz[p], ar = area[p];
-          for (int s = 0; s < gc; ++s) {
-            cx<float> c[6];
-            tangent_plane<float>(sl[g0 + s], px, py, pz, qx, qy, qz, ar, c);
-            for (int k = 0; k < 6; ++k) s_cur[q][s * 6 + k] = make_float2(c[k].re, c[k].im);
-          }
-        } else {
-          s_u[q] = make_float4(0.f, 0.f, 0.f, 0.f);
-          for (int k = 0; k < kSlotsGroup * 6; ++k) s_cur[q][k] = make_float2(0.f, 0.f);
+  for (int c0 = b; c0 < e || (c0 == b && b == e); c0 += kPC) {
+    const int cnt = max(0, min(kPC, e - c0));
+    const bool first = (c0 == b);
+    __syncthreads();
+    for (int q = threadIdx.x; q < kPC; q += blockDim.x) {
+      if (q < cnt) {
+        const int p = c0 + q;
+        const float px = x[p], py = y[p], pz = z[p];
+        s_u[q] = make_float4((float)(k0 * ((double)px - cxd)), (float)(k0 * ((double)py - cyd)),
+                             (float)(k0 * ((double)pz - czd)), 0.f);
+        const float qx = nx[p], qy = ny[p], qz = nz[p], ar = area[p];
+#pragma unroll
+        for (int s2 = 0; s2 < GC; ++s2) {
+          cx<float> c[6];
+          tangent_plane<float>(sl[s2], px, py, pz, qx, qy, qz, ar, c);
+#pragma unroll
+          for (int k = 0; k < 6; ++k) s_cur[q * NC + s2 * 6 + k] = make_float2(c[k].re, c[k].im);
+        }
+      } else {
+        s_u[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for (int k = 0; k < NC; ++k) s_cur[q * NC + k] = make_float2(0.f, 0.f);
+      }
+    }
+    __syncthreads();
+    const int ksteps = (cnt + 7) / 8;
+    // B fragments: lane ln of n-tile nt holds rows k = 2tq', 2tq'+1 (point tq') and
+    // 2tq'+8, 2tq'+9 (point tq'+4) of real column n = nt*8 + g'
+    for (int idx = threadIdx.x; idx < ksteps * NT * 32; idx += blockDim.x) {
+      const int ln = idx & 31, nt = (idx >> 5) % NT, ks = (idx >> 5) / NT;
+      const int n = nt * 8 + (ln >> 2), j = n >> 1, part = n & 1;
+      const int p0 = ks * 8 + (ln & 3);
+      float v[4];
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const float2 cv = j < NC ? s_cur[(p0 + 4 * h) * NC + j] : make_float2(0.f, 0.f);
+        v[2 * h] = part ? cv.y : cv.x;       // cos row
+        v[2 * h + 1] = part ? cv.x : -cv.y;  // sin row
+      }
+      uint32_t h0, l0, h1, l1;
+      split_bf16x2(v[0], v[1], h0, l0);
+      split_bf16x2(v[2], v[3], h1, l1);
+      s_b[idx] = make_uint4(h0, h1, l0, l1);
+    }
+    __syncthreads();
+    for (int mt = warp; mt < MT; mt += 4) {
+      const int d0 = mt * 16 + g, d1 = d0 + 8;
+      const float4 s0 = __ldg(dirs + min(d0, ndir - 1)), s1 = __ldg(dirs + min(d1, ndir - 1));
+      float acc[NT][4];
+#pragma unroll
+      for (int nt = 0; nt < NT; ++nt) acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.f;
+      for (int ks = 0; ks < ksteps; ++ks) {
+        const float4 ua = s_u[ks * 8 + tq], ub = s_u[ks * 8 + tq + 4];
+        uint32_t ahi[4], alo[4];
+        phase_frag(s0.x, s0.y, s0.z, ua, ahi[0], alo[0]);
+        phase_frag(s1.x, s1.y, s1.z, ua, ahi[1], alo[1]);
+        phase_frag(s0.x, s0.y, s0.z, ub, ahi[2], alo[2]);
+        phase_frag(s1.x, s1.y, s1.z, ub, ahi[3], alo[3]);
+        uint4 bv[NT];
+#pragma unroll
+        for (int nt = 0; nt < NT; ++nt) bv[nt] = s_b[(ks * NT + nt) * 32 + lane];
+#pragma unroll
+        for (int nt = 0; nt < NT; ++nt) {
+          const uint32_t bhi[2] = {bv[nt].x, bv[nt].y};
+          mma_bf16(acc[nt], ahi, bhi);
+        }
+#pragma unroll
+        for (int nt = 0; nt < NT; ++nt) {
+          const uint32_t blo[2] = {bv[nt].z, bv[nt].w};
+          mma_bf16(acc[nt], ahi, blo);
+        }
+#pragma unroll
+        for (int nt = 0; nt < NT; ++nt) {
+          const uint32_t bhi[2] = {bv[nt].x, bv[nt].y};
+          mma_bf16(acc[nt], alo, bhi);
         }
       }
-      __syncthreads();
-      // B fragments: lane ln of n-tile nt holds rows k = 2tq', 2tq'+1 (point tq') and
-      // 2tq'+8, 2tq'+9 (point tq'+4) of real column n = nt*8 + g'
-      for (int idx = threadIdx.x; idx < (kPC / 8) * NT * 32; idx += blockDim.x) {
-        const int ln = idx & 31, nt = (idx >> 5) % NT, ks = (idx >> 5) / NT;
-        const int n = nt * 8 + (ln >> 2), j = n >> 1, part = n & 1;
-        const int p0 = ks * 8 + (ln & 3);
-        float v[4];
+      // D fragment: (d0, d1) = Re/Im of complex column nt*4+tq at direction d0; (d2, d3) at d1
+#pragma unroll
+      for (int nt = 0; nt < NT; ++nt) {
+        const int j = nt * 4 + tq;
+        if (j >= NC) continue;
+        float2 *o = obase + (int64_t)(j / 6) * slot_stride + (int64_t)(j % 6) * ndir;
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
-          const float2 cv = j < ncols ? s_cur[p0 + 4 * h][j] : make_float2(0.f, 0.f);
-          v[2 * h] = part ? cv.y : cv.x;        // cos row
-          v[2 * h + 1] = part ? cv.x : -cv.y;   // sin row
-        }
-        uint32_t h0, l0, h1, l1;
-        split2(v[0], v[1], h0, l0);
-        split2(v[2], v[3], h1, l1);
-        s_b[ks][nt][ln] = make_uint4(h0, h1, l0, l1);
-      }
-      __syncthreads();
-      const int ksteps = (cnt + 7) / 8;
-      for (int mt = warp; mt < MT; mt += 4) {
-        const int d0 = mt * 16 + g, d1 = d0 + 8;
-        const float4 s0 = dirs[min(d0, ndir - 1)], s1 = dirs[min(d1, ndir - 1)];
-        float acc[kMaxNT][4];
-#pragma unroll
-        for (int nt = 0; nt < kMaxNT; ++nt) acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.f;
-        for (int ks = 0; ks < ksteps; ++ks) {
-          const float4 ua = s_u[ks * 8 + tq], ub = s_u[ks * 8 + tq + 4];
-          uint32_t ahi[4], alo[4];
-          phase_frag(s0.x, s0.y, s0.z, ua, ahi[0], alo[0]);
-          phase_frag(s1.x, s1.y, s1.z, ua, ahi[1], alo[1]);
-          phase_frag(s0.x, s0.y, s0.z, ub, ahi[2], alo[2]);
-          phase_frag(s1.x, s1.y, s1.z, ub, ahi[3], alo[3]);
-#pragma unroll
-          for (int nt = 0; nt < kMaxNT; ++nt) {
-            if (nt >= NT) break;
-            const uint4 bv = s_b[ks][nt][lane];
-            const uint32_t bhi[2] = {bv.x, bv.y}, blo[2] = {bv.z, bv.w};
-            mma_bf16_16816(acc[nt], ahi, bhi);
-            mma_bf16_16816(acc[nt], ahi, blo);
-            mma_bf16_16816(acc[nt], alo, bhi);
+          const int d = h ? d1 : d0;
+          if (d >= ndir) continue;
+          float2 v = make_float2(acc[nt][2 * h], acc[nt][2 * h + 1]);
+          if (!first) {
+            const float2 w = o[d];
+            v.x += w.x;
+            v.y += w.y;
           }
-        }
-        // D fragment: (d0, d1) = Re/Im of complex column nt*4+tq at direction d0; (d2, d3) at d1
-#pragma unroll
-        for (int nt = 0; nt < kMaxNT; ++nt) {
-          if (nt >= NT) break;
-          const int j = nt * 4 + tq;
-          if (j >= ncols) continue;
-          float2 *o = obase + (int64_t)(g0 + j / 6) * slot_stride + (int64_t)(j % 6) * ndir;
-#pragma unroll
-          for (int h = 0; h < 2; ++h) {
-            const int d = h ? d1 : d0;
-            if (d >= ndir) continue;
-            float2 v = make_float2(acc[nt][2 * h], acc[nt][2 * h + 1]);
-            if (!first) {
-              const float2 w = o[d];
-              v.x += w.x;
-              v.y += w.y;
-            }
-            o[d] = v;
-          }
+          o[d] = v;
         }
       }
-      if (cnt == 0) break;  // an empty leaf (root of an empty cloud) was written as zeros
     }
+    if (cnt == 0) break;  // an empty leaf (root of an empty cloud) was written as zeros
   }
+}
+
+template <int GC>
+static size_t leaf_mma_smem() {
+  constexpr int NT = (12 * GC + 7) / 8;
+  return sizeof(uint4) * (kPC / 8) * NT * 32 + sizeof(float4) * kPC + sizeof(float2) * kPC * 6 * GC;
+}
+
+po_status init_leaf_mma_attributes() {
+  PO_CUDA(cudaFuncSetAttribute(k_leaf_mma<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)leaf_mma_smem<1>()));
+  PO_CUDA(cudaFuncSetAttribute(k_leaf_mma<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)leaf_mma_smem<2>()));
+  PO_CUDA(cudaFuncSetAttribute(k_leaf_mma<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)leaf_mma_smem<3>()));
+  PO_CUDA(cudaFuncSetAttribute(k_leaf_mma<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)leaf_mma_smem<4>()));
+  return PO_OK;
 }
 
 po_status launch_leaf_mma(const float *const g[7], const int32_t *leaf_begin, const double *leaf_center,
@@ -179,9 +187,21 @@ po_status launch_leaf_mma(const float *const g[7], const int32_t *leaf_begin, co
   if (n_leaves <= 0 || n_lambda <= 0) return PO_OK;
   if (n_lambda > 65535) return fail(PO_ERR_UNSUPPORTED, "too many wavelengths for one launch");
   dim3 grid((unsigned)n_leaves, (unsigned)n_lambda);
-  k_leaf_mma<<<grid, 128, 0, st>>>(g[0], g[1], g[2], g[3], g[4], g[5], g[6], leaf_begin, leaf_center, slots_dev, dirs,
-                                   ndir, n_leaves, G, out);
-  count_launch();
+  // slots of a wavelength share its phases; groups of up to 4 per launch
+  for (int g0 = 0; g0 < G; g0 += 4) {
+    const int gc = std::min(4, G - g0);
+#define PO_LEAF_MMA(GG)                                                                                          \
+  k_leaf_mma<GG><<<grid, 128, leaf_mma_smem<GG>(), st>>>(g[0], g[1], g[2], g[3], g[4], g[5], g[6], leaf_begin, \
+                                                        leaf_center, slots_dev, dirs, ndir, n_leaves, G, g0, out)
+    switch (gc) {
+      case 1: PO_LEAF_MMA(1); break;
+      case 2: PO_LEAF_MMA(2); break;
+      case 3: PO_LEAF_MMA(3); break;
+      default: PO_LEAF_MMA(4); break;
+    }
+#undef PO_LEAF_MMA
+    count_launch();
+  }
   PO_CUDA(cudaGetLastError());
   return PO_OK;
 }

@@ -131,6 +131,7 @@ po_status init_device_attributes(int dev) {
   PO_CUDA(cudaDeviceGetAttribute(&smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
   PO_TRY(init_interp_mma_attributes(smem));
   PO_TRY(init_fft_attributes(smem));
+  PO_TRY(init_leaf_mma_attributes());
   done.insert(dev);
   return PO_OK;
 }
