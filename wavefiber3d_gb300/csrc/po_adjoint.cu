@@ -23,234 +23,13 @@
 #include <cuda_runtime.h>
 
 #include "po_common.cuh"
+#include "po_dual.cuh"
 #include "po_internal.h"
 #include "po_kernels.h"
 
 namespace wavepo {
 
-// ------------------------------------------- forward-mode duals (FP32 / FP64)
-constexpr int kNT = 7;  // tangents: x, y, z, nx, ny, nz, area
-
-template <typename T>
-struct Dual {
-  T v;
-  T d[kNT];
-};
-
-template <typename T>
-__device__ __forceinline__ Dual<T> dconst(T v) {
-  Dual<T> r;
-  r.v = v;
-#pragma unroll
-  for (int i = 0; i < kNT; ++i) r.d[i] = (T)0;
-  return r;
-}
-template <typename T>
-__device__ __forceinline__ Dual<T> dvar(T v, int i) {
-  Dual<T> r = dconst<T>(v);
-  r.d[i] = (T)1;
-  return r;
-}
-// f(u) with f(u.v) = fv and f'(u.v) = fp
-template <typename T>
-__device__ __forceinline__ Dual<T> dchain(const Dual<T> &u, T fv, T fp) {
-  Dual<T> r;
-  r.v = fv;
-#pragma unroll
-  for (int i = 0; i < kNT; ++i) r.d[i] = fp * u.d[i];
-  return r;
-}
-template <typename T>
-__device__ __forceinline__ Dual<T> operator+(const Dual<T> &a, const Dual<T> &b) {
-  Dual<T> r;
-  r.v = a.v + b.v;
-#pragma unroll
-  for (int i = 0; i < kNT; ++i) r.d[i] = a.d[i] + b.d[i];
-  return r;
-}
-template <typename T>
-__device__ __forceinline__ Dual<T> operator-(const Dual<T> &a, const Dual<T> &b) {
-  Dual<T> r;
-  r.v = a.v - b.v;
-#pragma unroll
-  for (int i = 0; i < kNT; ++i) r.d[i] = a.d[i] - b.d[i];
-  return r;
-}
-template <typename T>
-__device__ __forceinline__ Dual<T> operator-(const Dual<T> &a) { return dchain(a, -a.v, (T)-1); }
-template <typename T>
-__device__ __forceinline__ Dual<T> operator*(const Dual<T> &a, const Dual<T> &b) {
-  Dual<T> r;
-  r.v = a.v * b.v;
-#pragma unroll
-  for (int i = 0; i < kNT; ++i) r.d[i] = a.d[i] * b.v + a.v * b.d[i];
-  return r;
-}
-template <typename T>
-__device__ __forceinline__ Dual<T> operator*(const Dual<T> &a, T s) { return dchain(a, a.v * s, s); }
-template <typename T>
-__device__ __forceinline__ Dual<T> operator/(const Dual<T> &a, const Dual<T> &b) {
-  Dual<T> r;
-  const T ib = (T)1 / b.v;
-  r.v = a.v * ib;
-#pragma unroll
-  for (int i = 0; i < kNT; ++i) r.d[i] = (a.d[i] - r.v * b.d[i]) * ib;
-  return r;
-}
-template <typename T>
-__device__ __forceinline__ Dual<T> dsqrt(const Dual<T> &a) {
-  const T s = sqrt(a.v);
-  return dchain(a, s, s > (T)0 ? (T)0.5 / s : (T)0);
-}
-template <typename T>
-__device__ __forceinline__ Dual<T> dexp(const Dual<T> &a) {
-  const T e = exp(a.v);
-  return dchain(a, e, e);
-}
-template <typename T>
-__device__ __forceinline__ Dual<T> dacos(const Dual<T> &a) {
-  const T q = (T)1 - a.v * a.v;
-  return dchain(a, acos(a.v), q > (T)0 ? (T)-1 / sqrt(q) : (T)0);
-}
-template <typename T>
-__device__ __forceinline__ Dual<T> dabs(const Dual<T> &a) { return a.v < (T)0 ? -a : a; }
-template <typename T>
-__device__ __forceinline__ Dual<T> dsin(const Dual<T> &a) { return dchain(a, sin(a.v), cos(a.v)); }
-
-template <typename T>
-using CDual = cx<Dual<T>>;
-template <typename T>
-__device__ __forceinline__ CDual<T> cd(T re, T im) { return {dconst<T>(re), dconst<T>(im)}; }
-template <typename T>
-__device__ __forceinline__ CDual<T> operator*(const CDual<T> &a, const CDual<T> &b) {
-  return {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re};
-}
-template <typename T>
-__device__ __forceinline__ CDual<T> operator*(const CDual<T> &a, const Dual<T> &s) { return {a.re * s, a.im * s}; }
-template <typename T>
-__device__ __forceinline__ CDual<T> operator*(const CDual<T> &a, T s) { return {a.re * s, a.im * s}; }
-template <typename T>
-__device__ __forceinline__ CDual<T> operator+(const CDual<T> &a, const CDual<T> &b) {
-  return {a.re + b.re, a.im + b.im};
-}
-template <typename T>
-__device__ __forceinline__ CDual<T> operator-(const CDual<T> &a, const CDual<T> &b) {
-  return {a.re - b.re, a.im - b.im};
-}
-template <typename T>
-__device__ __forceinline__ CDual<T> cddiv(const CDual<T> &a, const CDual<T> &b) {
-  Dual<T> d = b.re * b.re + b.im * b.im;
-  return {(a.re * b.re + a.im * b.im) / d, (a.im * b.re - a.re * b.im) / d};
-}
-// principal square root (as csqrt_ of po_common.cuh)
-template <typename T>
-__device__ __forceinline__ CDual<T> cdsqrt(const CDual<T> &z) {
-  const Dual<T> r = dsqrt(z.re * z.re + z.im * z.im);
-  const Dual<T> ha = (r + z.re) * (T)0.5, hb = (r - z.re) * (T)0.5;
-  const Dual<T> a = ha.v > (T)0 ? dsqrt(ha) : dconst<T>(0);
-  const Dual<T> b = hb.v > (T)0 ? dsqrt(hb) : dconst<T>(0);
-  return {a, z.im.v < (T)0 ? -b : b};
-}
-// util/util.h:365-382 with a dual angle and constant indices
-template <typename T>
-__device__ __forceinline__ CDual<T> d_cos_internal(const CDual<T> &n, const Dual<T> &theta) {
-  Dual<T> s = dsin(theta);
-  CDual<T> q = cddiv(CDual<T>{s, dconst<T>(0)}, n);
-  q = cddiv(q * s, n);
-  return cdsqrt(CDual<T>{dconst<T>(1) - q.re, -q.im});
-}
-template <typename T>
-__device__ __forceinline__ CDual<T> d_rs(const Dual<T> &theta, const CDual<T> &n0, const CDual<T> &nt) {
-  CDual<T> p0 = n0 * d_cos_internal(n0, theta);
-  CDual<T> pt = nt * d_cos_internal(cddiv(nt, n0), theta);
-  return cddiv(p0 - pt, p0 + pt);
-}
-template <typename T>
-__device__ __forceinline__ CDual<T> d_rp(const Dual<T> &theta, const CDual<T> &n0, const CDual<T> &nt) {
-  CDual<T> q0 = cddiv(d_cos_internal(n0, theta), n0);
-  CDual<T> qt = cddiv(d_cos_internal(nt, theta), nt);
-  return cddiv(q0 - qt, q0 + qt);
-}
-
-// The tangent-plane model of tangent_plane() (po_common.cuh) on dual inputs
-// in precision T: the same branches (taken on the float-rounded values, as
-// the forward kernels take them), differentiated.  The incident phase value
-// k0 w.x is formed and reduced in FP64 whatever T is; its derivative is
-// -k0 w.  out[0..2] = J, out[3..5] = M.
-template <typename T>
-__device__ void tangent_plane_jvp(const SlotParams<double> &P, float px, float py, float pz, float qx, float qy,
-                                  float qz, float area, CDual<T> out[6]) {
-  const Dual<T> Z = dvar<T>(pz, 2);
-  const Dual<T> nr[3] = {dvar<T>(qx, 3), dvar<T>(qy, 4), dvar<T>(qz, 5)};
-  const Dual<T> Ar = dvar<T>(area, 6);
-  const T kd[3] = {(T)P.wavedir[0], (T)P.wavedir[1], (T)P.wavedir[2]};
-  const Dual<T> dotvalue = nr[0] * kd[0] + nr[1] * kd[1] + nr[2] * kd[2];
-  const CDual<T> zero = cd<T>(0, 0);
-  CDual<T> Ei[3] = {zero, zero, zero}, Hi[3] = {zero, zero, zero};
-  CDual<T> Es[3] = {zero, zero, zero}, Hs[3] = {zero, zero, zero};
-  const float dot_f = (float)(P.wavedir[0] * qx + P.wavedir[1] * qy + P.wavedir[2] * qz);
-  if (dot_f <= 0.0f) {
-    // incident phase exp(-i k0 w.x) and beam exp(-z^2 / (2 sigma^2))
-    const double argd = -P.k0d * (P.wd[0] * (double)px + P.wd[1] * (double)py + P.wd[2] * (double)pz);
-    const double rd = argd - kTwoPi * rint(argd * (1.0 / kTwoPi));
-    double snd, csd;
-    sincos(rd, &snd, &csd);
-    Dual<T> arg = dconst<T>((T)rd);
-#pragma unroll
-    for (int a = 0; a < 3; ++a) arg.d[a] = (T)(-P.k0d * P.wd[a]);
-    const CDual<T> e = {dchain(arg, (T)csd, (T)-snd), dchain(arg, (T)snd, (T)csd)};
-    const Dual<T> beam = dexp(-(Z * Z) * (T)P.inv_two_sigma2);
-    const CDual<T> Ei0 = e * beam;
-    const CDual<T> Hi0 = Ei0 * (T)(1.0 / P.z0);
-    for (int c = 0; c < 3; ++c) {
-      Ei[c] = Ei0 * (T)P.edir[c];
-      Hi[c] = Hi0 * (T)P.hdir[c];
-    }
-    const CDual<T> eta_in = cd<T>(1, 0), eta_out = cd<T>((T)P.eta_re, (T)P.eta_im);
-    if (fabsf(fabsf(dot_f) - 1.0f) < 1e-10f) {  // tangentplane.h:39-49
-      const CDual<T> R =
-          P.te ? cddiv(eta_out - eta_in, eta_in + eta_out) : cddiv(eta_in - eta_out, eta_in + eta_out);
-      for (int c = 0; c < 3; ++c) {
-        Es[c] = Ei[c] * R;
-        Hs[c] = Hi[c] * R;
-      }
-    } else {  // tangentplane.h:51-62
-      Dual<T> rp[3] = {nr[2] * kd[1] - nr[1] * kd[2], nr[0] * kd[2] - nr[2] * kd[0], nr[1] * kd[0] - nr[0] * kd[1]};
-      const Dual<T> inv = dconst<T>(1) / dsqrt(rp[0] * rp[0] + rp[1] * rp[1] + rp[2] * rp[2]);
-      for (int c = 0; c < 3; ++c) rp[c] = rp[c] * inv;
-      const CDual<T> f = Ei[0] * rp[0] + Ei[1] * rp[1] + Ei[2] * rp[2];
-      CDual<T> Eperp[3], Epar[3], Hpar[3], Hperp[3];
-      for (int c = 0; c < 3; ++c) {
-        Eperp[c] = f * rp[c];
-        Epar[c] = Ei[c] - Eperp[c];
-      }
-      const T iz = (T)(1.0 / P.z0);
-      Hpar[0] = (Epar[2] * kd[1] - Epar[1] * kd[2]) * iz;
-      Hpar[1] = (Epar[0] * kd[2] - Epar[2] * kd[0]) * iz;
-      Hpar[2] = (Epar[1] * kd[0] - Epar[0] * kd[1]) * iz;
-      for (int c = 0; c < 3; ++c) Hperp[c] = Hi[c] - Hpar[c];
-      const Dual<T> lphi = dacos(dabs(dotvalue));
-      const CDual<T> Rs = d_rs(lphi, eta_in, eta_out);
-      const CDual<T> Rp = d_rp(lphi, eta_in, eta_out);
-      for (int c = 0; c < 3; ++c) {
-        Es[c] = Eperp[c] * Rs - Epar[c] * Rp;
-        Hs[c] = Hpar[c] * Rp - Hperp[c] * Rs;
-      }
-    }
-  }
-  CDual<T> Et[3], Ht[3];
-  for (int c = 0; c < 3; ++c) {
-    Et[c] = Ei[c] + Es[c];
-    Ht[c] = Hi[c] + Hs[c];
-  }
-  const CDual<T> M[3] = {Et[1] * nr[2] - Et[2] * nr[1], Et[2] * nr[0] - Et[0] * nr[2], Et[0] * nr[1] - Et[1] * nr[0]};
-  const CDual<T> J[3] = {Ht[2] * nr[1] - Ht[1] * nr[2], Ht[0] * nr[2] - Ht[2] * nr[0], Ht[1] * nr[0] - Ht[0] * nr[1]};
-  const CDual<T> ef = {Ar * (T)P.ef_re, Ar * (T)P.ef_im}, hf = {Ar * (T)P.hf_re, Ar * (T)P.hf_im};
-  for (int c = 0; c < 3; ++c) {
-    out[c] = J[c] * ef;
-    out[3 + c] = M[c] * hf;
-  }
-}
+// Per-point Jacobians: forward-mode duals (po_dual.cuh), all 7 tangents.
 
 // ------------------------------------------------------------ root adjoint
 // G at the sampled root points (output sample (i, k) = root (mt*i, mp*k));
@@ -427,8 +206,9 @@ __global__ void __launch_bounds__(32 * kAdjWarps) k_point_adjoint(
           }
         }
         if (!ok) continue;
+        const int sel[kNT] = {0, 1, 2, 3, 4, 5, 6};
         CDual<R> C[6];
-        tangent_plane_jvp<R>(slots[slot], px, py, pz, nx[p], ny[p], nz[p], area[p], C);
+        tangent_plane_jvp<R, kNT>(slots[slot], px, py, pz, nx[p], ny[p], nz[p], area[p], sel, C);
 #pragma unroll
         for (int i = 0; i < kNT; ++i) {
           double s = 0.0;

@@ -128,18 +128,34 @@ void build_theta_matrix(int Tc, int Tp, int Rc, int Rp, int Kp, std::vector<uint
       }
 }
 
-// Transpose of the mirrored theta map (double cover only): child row t of a
-// half column pair from the parent's own column (K = r < Rp) and its partner
-// (K = Rp + r):  [A_own^T | A_partner^T], rows t < Rc.
+// Transposed theta matrices of one level (double cover), rows t < Rc of the
+// child, K = parent rows r < Rp padded to 16:  A_plus/minus^T[t][r] =
+// (A_own[r][t] +- A_partner[r][t]) / 2, in the layout of build_theta_matrix
+// ([mtile][kstep][u][lane] uint4, u = plus hi, plus lo, minus hi, minus lo).
 void build_theta_matrix_adj(int Tc, int Tp, int Rc, int Rp, int Kp, std::vector<uint32_t> &out) {
   const int nth_c = Tc / 2;
-  std::vector<double> M((size_t)Rc * Kp, 0.0);
+  std::vector<double> Mplus((size_t)Rc * Kp, 0.0), Mminus((size_t)Rc * Kp, 0.0);
   for (int t = 0; t < Rc; ++t)
     for (int r = 0; r < Rp; ++r) {
-      M[(size_t)t * Kp + r] = theta_own(Tc, Tp, r, t);
-      if (t >= 1 && t < nth_c) M[(size_t)t * Kp + Rp + r] = theta_partner(Tc, Tp, r, t);
+      const double own = theta_own(Tc, Tp, r, t);
+      const double partner = (t >= 1 && t < nth_c) ? theta_partner(Tc, Tp, r, t) : 0.0;
+      Mplus[(size_t)t * Kp + r] = 0.5 * (own + partner);
+      Mminus[(size_t)t * Kp + r] = 0.5 * (own - partner);
     }
-  a_fragments(M, Rc, Kp, out);
+  std::vector<uint32_t> fp, fm;
+  a_fragments(Mplus, Rc, Kp, fp);
+  a_fragments(Mminus, Rc, Kp, fm);
+  const int MT = (Rc + 15) / 16, KS = Kp / 16;
+  out.assign(theta_pair_words(Rc, Kp), 0u);
+  for (int mt = 0; mt < MT; ++mt)
+    for (int ks = 0; ks < KS; ++ks)
+      for (int lane = 0; lane < 32; ++lane) {
+        const uint32_t *sp = &fp[(((size_t)mt * KS + ks) * 32 + lane) * 8];
+        const uint32_t *sm = &fm[(((size_t)mt * KS + ks) * 32 + lane) * 8];
+        const uint32_t *src[4] = {sp, sp + 4, sm, sm + 4};
+        for (int u = 0; u < 4; ++u)
+          std::memcpy(&out[((((size_t)mt * KS + ks) * 4 + u) * 32 + lane) * 4], src[u], 16);
+      }
 }
 
 // ---------------------------------------------------------- device side
@@ -368,135 +384,156 @@ po_status launch_interp_cols_mma(const uint4 *mid, float2 *parent, const int32_t
 }
 
 // ----------------------------------------------- transposed theta pass
-// Adjoint of k_interp_cols_mma for one child: its parent's adjoint pattern
-// times exp(-i k s.(c_child - c_parent)) on the parent grid, then the
-// transposed mirrored theta map [A_own^T | A_partner^T] (rows t < Rc, K over
-// the parent's own and partner half columns).  Every child writes its own
-// output, so there is no reduction.  CTA: one (child, component, slot) and
-// NCC complex columns (NCC/2 mirror pairs), 4 warps over the 16-row tiles.
-template <int NCC>
-__global__ void __launch_bounds__(128) k_interp_cols_adj_mma(
-    const float2 *__restrict__ parent_adj, float2 *__restrict__ mid_adj, const int32_t *__restrict__ child_parent,
-    const uint32_t *__restrict__ child_prefix, int64_t n_parent, int64_t n_child, int phi, int Rc, int Rp, int Kp,
-    const uint4 *__restrict__ Afrag, const float4 *__restrict__ trans, int G) {
-  constexpr int NT = NCC / 4;
-  constexpr int TW = NCC / 2;
-  constexpr int NP = NCC + 1;  // padded row stride of the staged tile
-  extern __shared__ uint4 smem_u4[];
-  const int KS = Kp / 16, MT = (Rc + 15) / 16;
-  uint4 *Bf = smem_u4;                                   // [KS][NT][32]
-  float2 *tile = (float2 *)(Bf + (size_t)KS * NT * 32);  // [Rp][NP]
+// Adjoint of k_theta_warp for the children of one parent.  With
+// X_j = P_j exp(-i k s.(c_child - c_parent)) on the parent grid (P: the
+// parent's adjoint pattern) and S' = X_j + X_j', D' = X_j - X_j':
+//   U' = A_plus^T S',  V' = A_minus^T D',  mid_j = U' + V',  mid_j' = U' - V'.
+// A warp owns one (slot, parent, component) and 4 column pairs j = j0.., for
+// the CTA's 16-row tiles of the children (blockIdx.y), and writes every child
+// of the parent in turn: the parent's pattern and translation entries are
+// read from L2 for the first child and from L1 after it.  The CTA stages its
+// slice of the transposed matrices in shared memory.  B fragments (K = parent
+// rows) are generated in registers: the lanes of a column's real and
+// imaginary parts (g even / odd) each rotate two of the four rows and swap
+// halves, so every phasor is evaluated once per child.
+template <int MTW>
+__global__ void __launch_bounds__(256, 2) k_theta_adj_warp(
+    const float2 *__restrict__ parent_adj, float2 *__restrict__ mid_adj, const int32_t *__restrict__ child_table,
+    int64_t n_parent, int64_t n_child, int phi, int Rc, int Rp, int KS, int MT, const uint4 *__restrict__ Afrag,
+    const float4 *__restrict__ trans, int G, int n_ct, int64_t n_task) {
+  extern __shared__ uint4 sA[];  // [MTW][KS][4][32]
+  const int mt0 = blockIdx.y * MTW;
+  const int nmt = MT - mt0 < MTW ? MT - mt0 : MTW;
+  {
+    const uint4 *src = Afrag + (size_t)mt0 * KS * 128;
+    const int n = nmt * KS * 128;
+    for (int e = threadIdx.x; e < MTW * KS * 128; e += blockDim.x)
+      sA[e] = e < n ? __ldg(src + e) : make_uint4(0u, 0u, 0u, 0u);
+  }
+  __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, tq = lane & 3;
-  const int span = phi / 2;
-  const int ntile = (span + TW - 1) / TW;
-  const int j0 = (int)(blockIdx.x % ntile) * TW;
-  const int64_t cc = blockIdx.x / ntile;
-  const int64_t c = cc / 6;
-  const int comp = (int)(cc % 6);
-  const int slot = blockIdx.z, lam = slot / G;
-  auto col_of = [&](int q) { return q < TW ? j0 + q : j0 + (q - TW) + phi / 2; };
-  auto ok_of = [&](int q) { return j0 + (q < TW ? q : q - TW) < span; };
-  auto partner_of = [&](int q) { return q < TW ? q + TW : q - TW; };
-  const int64_t p = child_parent[c];
-  const int o = (int)(child_prefix[c] & 7u);
-  const float sgx = (o & 1) ? 1.f : -1.f, sgy = (o & 2) ? -1.f : 1.f, sgz = (o & 4) ? -1.f : 1.f;
+  const int64_t task = (int64_t)blockIdx.x * (blockDim.x >> 5) + warp;
+  if (task >= n_task) return;
+  const int ct = (int)(task % n_ct);
+  int64_t rest = task / n_ct;
+  const int comp = (int)(rest % 6);
+  rest /= 6;
+  const int64_t p = rest % n_parent;
+  const int slot = (int)(rest / n_parent), lam = slot / G;
+  const int span = phi / 2, j0 = ct * 4;
+  const bool odd = g & 1;
   const float4 *tr = trans + (int64_t)lam * Rp * phi;
   const float2 *src = parent_adj + (((int64_t)slot * n_parent + p) * 6 + comp) * (int64_t)Rp * phi;
-  for (int e = threadIdx.x; e < Rp * NCC; e += blockDim.x) {
-    const int r = e / NCC, q = e - r * NCC;
-    float2 v = make_float2(0.f, 0.f);
-    if (ok_of(q)) {
-      const int j = col_of(q);
-      const float2 a = src[(int64_t)r * phi + j];
-      const float4 rr = tr[(int64_t)r * phi + j];
-      float sn, cs;
-      sincos_small(fmaf(sgx, rr.x, fmaf(sgy, rr.y, sgz * rr.z)), &sn, &cs);
-      v = make_float2(a.x * cs + a.y * sn, a.y * cs - a.x * sn);  // a * exp(-i ph)
-    }
-    tile[r * NP + q] = v;
-  }
-  __syncthreads();
-  for (int e = threadIdx.x; e < KS * NT * 32; e += blockDim.x) {
-    const int ln = e & 31, nt = (e >> 5) % NT, ks = (e >> 5) / NT;
-    const int n = nt * 8 + (ln >> 2), q = n >> 1, part = n & 1;
-    const int kb = ks * 16 + 2 * (ln & 3);
-    float v[4];
+  const int jq = j0 + (g >> 1);  // this lane's column pair (B n-index g)
+  const bool jok = jq < span;
+  const int jo = j0 + tq;  // the D fragment's column pair
+  const int32_t cl = lane < 8 ? child_table[p * 8 + lane] : -1;
+  unsigned rem = __ballot_sync(0xffffffffu, cl >= 0);  // children present (bits 0..7)
+  while (rem) {
+    const int o = __ffs(rem) - 1;
+    rem &= rem - 1;
+    const int64_t c = __shfl_sync(0xffffffffu, cl, o);
+    const float sgx = (o & 1) ? 1.f : -1.f, sgy = (o & 2) ? -1.f : 1.f, sgz = (o & 4) ? -1.f : 1.f;
+    // S', D' of parent row r for column pair jq (zero outside the grid)
+    auto rotated = [&](int r, float2 &S, float2 &D) {
+      S = D = make_float2(0.f, 0.f);
+      if (!jok || r >= Rp) return;
+      const float2 a = src[(int64_t)r * phi + jq], b = src[(int64_t)r * phi + jq + span];
+      const float4 rr = __ldg(tr + (int64_t)r * phi + jq);
+      const float pxy = fmaf(sgx, rr.x, sgy * rr.y), pz = sgz * rr.z;
+      float s1, c1, s2, c2;
+      sincos_small(pz + pxy, &s1, &c1);  // column j
+      sincos_small(pz - pxy, &s2, &c2);  // its mirror (x and y phases negated)
+      const float xr = a.x * c1 + a.y * s1, xi = a.y * c1 - a.x * s1;  // a exp(-i ph_j)
+      const float yr = b.x * c2 + b.y * s2, yi = b.y * c2 - b.x * s2;
+      S = make_float2(xr + yr, xi + yi);
+      D = make_float2(xr - yr, xi - yi);
+    };
+    float d[MTW][2][4];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      const int kk = kb + (u & 1) + (u >> 1) * 8;
-      float2 x = make_float2(0.f, 0.f);
-      if (kk < Rp) x = tile[kk * NP + q];
-      else if (kk < 2 * Rp) x = tile[(kk - Rp) * NP + partner_of(q)];
-      v[u] = part ? x.y : x.x;
-    }
-    uint32_t h0, l0, h1, l1;
-    split_bf16x2(v[0], v[1], h0, l0);
-    split_bf16x2(v[2], v[3], h1, l1);
-    Bf[e] = make_uint4(h0, h1, l0, l1);
-  }
-  __syncthreads();
-  float2 *dst = mid_adj + (((int64_t)slot * n_child + c) * 6 + comp) * (int64_t)Rc * phi;
-  for (int mt = warp; mt < MT; mt += 4) {
-    float d[NT][4];
+    for (int i = 0; i < MTW; ++i)
 #pragma unroll
-    for (int nt = 0; nt < NT; ++nt) d[nt][0] = d[nt][1] = d[nt][2] = d[nt][3] = 0.f;
-    const uint4 *ap = Afrag + ((size_t)mt * KS) * 64 + lane * 2;
-    uint4 nh = __ldg(ap), nl = __ldg(ap + 1);
+      for (int w = 0; w < 2; ++w) d[i][w][0] = d[i][w][1] = d[i][w][2] = d[i][w][3] = 0.f;
     for (int ks = 0; ks < KS; ++ks) {
-      const uint4 ah = nh, al = nl;
-      if (ks + 1 < KS) {
-        nh = __ldg(ap + (size_t)(ks + 1) * 64);
-        nl = __ldg(ap + (size_t)(ks + 1) * 64 + 1);
-      }
-      const uint32_t a_hi[4] = {ah.x, ah.y, ah.z, ah.w}, a_lo[4] = {al.x, al.y, al.z, al.w};
+      // even lane: rows 2tq, 2tq+8 (keeps real parts); odd lane: rows 2tq+1, 2tq+9 (imaginary)
+      const int r0 = ks * 16 + 2 * tq + (odd ? 1 : 0);
+      float2 S0, D0, S1, D1;
+      rotated(r0, S0, D0);
+      rotated(r0 + 8, S1, D1);
+      const float xs0 = __shfl_xor_sync(0xffffffffu, odd ? S0.x : S0.y, 4);
+      const float xd0 = __shfl_xor_sync(0xffffffffu, odd ? D0.x : D0.y, 4);
+      const float xs1 = __shfl_xor_sync(0xffffffffu, odd ? S1.x : S1.y, 4);
+      const float xd1 = __shfl_xor_sync(0xffffffffu, odd ? D1.x : D1.y, 4);
+      // pairs (row 2tq, row 2tq+1) and (2tq+8, 2tq+9) of this lane's part
+      const float sa = odd ? xs0 : S0.x, sb = odd ? S0.y : xs0, sc = odd ? xs1 : S1.x, sd = odd ? S1.y : xs1;
+      const float da = odd ? xd0 : D0.x, db = odd ? D0.y : xd0, dc = odd ? xd1 : D1.x, dd = odd ? D1.y : xd1;
+      uint32_t sh[2], sl[2], dh[2], dl[2];
+      split_bf16x2(sa, sb, sh[0], sl[0]);
+      split_bf16x2(sc, sd, sh[1], sl[1]);
+      split_bf16x2(da, db, dh[0], dl[0]);
+      split_bf16x2(dc, dd, dh[1], dl[1]);
 #pragma unroll
-      for (int nt = 0; nt < NT; ++nt) {
-        const uint4 b = Bf[((size_t)ks * NT + nt) * 32 + lane];
-        const uint32_t b_hi[2] = {b.x, b.y}, b_lo[2] = {b.z, b.w};
-        mma_bf16(d[nt], a_hi, b_hi);
-        mma_bf16(d[nt], a_hi, b_lo);
-        mma_bf16(d[nt], a_lo, b_hi);
+      for (int i = 0; i < MTW; ++i) {
+        const uint4 *a = sA + (size_t)(i * KS + ks) * 128 + lane;
+        const uint4 ph = a[0], pl = a[32], mh = a[64], ml = a[96];
+        const uint32_t aph[4] = {ph.x, ph.y, ph.z, ph.w}, apl[4] = {pl.x, pl.y, pl.z, pl.w};
+        const uint32_t amh[4] = {mh.x, mh.y, mh.z, mh.w}, aml[4] = {ml.x, ml.y, ml.z, ml.w};
+        mma_bf16(d[i][0], aph, sh);
+        mma_bf16(d[i][1], amh, dh);
+        mma_bf16(d[i][0], aph, sl);
+        mma_bf16(d[i][1], amh, dl);
+        mma_bf16(d[i][0], apl, sh);
+        mma_bf16(d[i][1], aml, dh);
       }
     }
+    // D fragment: rows t = tile*16 + g (+8), complex column pair j0 + tq
+    if (jo >= span) continue;
+    float2 *dst = mid_adj + (((int64_t)slot * n_child + c) * 6 + comp) * (int64_t)Rc * phi;
 #pragma unroll
-    for (int nt = 0; nt < NT; ++nt) {
-      const int q = nt * 4 + tq;
-      if (!ok_of(q)) continue;
-      const int j = col_of(q);
+    for (int i = 0; i < MTW; ++i) {
+      if (i >= nmt) break;
 #pragma unroll
       for (int h = 0; h < 2; ++h) {
-        const int t = mt * 16 + g + 8 * h;
-        if (t < Rc) dst[(int64_t)t * phi + j] = make_float2(d[nt][2 * h], d[nt][2 * h + 1]);
+        const int t = (mt0 + i) * 16 + g + 8 * h;
+        if (t >= Rc) continue;
+        const float ur = d[i][0][2 * h], ui = d[i][0][2 * h + 1], vr = d[i][1][2 * h], vi = d[i][1][2 * h + 1];
+        dst[(int64_t)t * phi + jo] = make_float2(ur + vr, ui + vi);
+        dst[(int64_t)t * phi + jo + span] = make_float2(ur - vr, ui - vi);
       }
     }
   }
 }
 
-static size_t cols_adj_smem(int ncc, int Rp, int Kp) {
-  return sizeof(uint4) * (size_t)(Kp / 16) * (ncc / 4) * 32 + sizeof(float2) * (size_t)Rp * (ncc + 1);
-}
-
-po_status launch_interp_cols_adj_mma(const float2 *parent_adj, float2 *mid_adj, const int32_t *child_parent,
-                                     const uint32_t *child_prefix, int64_t n_parent, int64_t n_child, int phi, int Rc,
-                                     int Rp, int Kp, const uint32_t *Afrag, const float4 *trans, int n_slots, int G,
+po_status launch_interp_cols_adj_mma(const float2 *parent_adj, float2 *mid_adj, const int32_t *child_table,
+                                     int64_t n_parent, int64_t n_child, int phi, int Rc, int Rp, int Kp,
+                                     const uint32_t *Afrag, const float4 *trans, int n_slots, int G,
                                      cudaStream_t st) {
-  if (n_child <= 0 || n_slots <= 0) return PO_OK;
-  if (Kp % 16 || Kp < 2 * Rp) return fail(PO_ERR_INTERNAL, "adjoint theta matrix K padding");
+  if (n_parent <= 0 || n_slots <= 0) return PO_OK;
+  if (Kp % 16 || Kp < Rp) return fail(PO_ERR_INTERNAL, "adjoint theta matrix K padding");
   if (phi % 2) return fail(PO_ERR_INTERNAL, "mirrored storage needs an even phi grid");
-  int ncc = 16;
-  if (cols_adj_smem(ncc, Rp, Kp) > 100 * 1024 || phi / 2 <= 4) ncc = 8;
-  const size_t smem = cols_adj_smem(ncc, Rp, Kp);
-  if (smem > 227 * 1024) return fail(PO_ERR_UNSUPPORTED, "angular grid too large for the adjoint theta pass");
-  const int TW = ncc / 2;
-  int64_t gx = (int64_t)((phi / 2 + TW - 1) / TW) * n_child * 6;
-  if (gx > 2147483647LL || n_slots > 65535) return fail(PO_ERR_UNSUPPORTED, "too many nodes for one launch");
-  dim3 grid((unsigned)gx, 1u, (unsigned)n_slots);
-  if (ncc == 16) {
-    k_interp_cols_adj_mma<16><<<grid, 128, smem, st>>>(parent_adj, mid_adj, child_parent, child_prefix, n_parent,
-                                                       n_child, phi, Rc, Rp, Kp, (const uint4 *)Afrag, trans, G);
-  } else {
-    k_interp_cols_adj_mma<8><<<grid, 128, smem, st>>>(parent_adj, mid_adj, child_parent, child_prefix, n_parent,
-                                                      n_child, phi, Rc, Rp, Kp, (const uint4 *)Afrag, trans, G);
+  const int KS = Kp / 16, MT = (Rc + 15) / 16;
+  const size_t tile_bytes = sizeof(uint4) * (size_t)KS * 128;
+  int cap = 4;
+  while (cap > 1 && (size_t)cap * tile_bytes > 113 * 1024) --cap;
+  if (tile_bytes > 227 * 1024) return fail(PO_ERR_UNSUPPORTED, "angular grid too large for the adjoint theta pass");
+  const int nmg = (MT + cap - 1) / cap;
+  const int MTW = (MT + nmg - 1) / nmg;
+  const size_t smem = (size_t)MTW * tile_bytes;
+  const int n_ct = (phi / 2 + 3) / 4;
+  const int64_t n_task = (int64_t)n_slots * n_parent * 6 * n_ct;
+  const int64_t gx = (n_task + 7) / 8;
+  if (gx > 2147483647LL || nmg > 65535) return fail(PO_ERR_UNSUPPORTED, "too many nodes for one launch");
+  dim3 grid((unsigned)gx, (unsigned)nmg, 1u);
+  const uint4 *A = (const uint4 *)Afrag;
+  switch (MTW) {
+#define PO_TA(M)                                                                                          \
+  case M:                                                                                                \
+    k_theta_adj_warp<M><<<grid, 256, smem, st>>>(parent_adj, mid_adj, child_table, n_parent, n_child,   \
+                                                 phi, Rc, Rp, KS, MT, A, trans, G, n_ct, n_task);      \
+    break;
+    PO_TA(1) PO_TA(2) PO_TA(3) PO_TA(4)
+#undef PO_TA
+    default: return fail(PO_ERR_INTERNAL, "adjoint theta pass variant");
   }
   count_launch();
   PO_CUDA(cudaGetLastError());
@@ -725,8 +762,10 @@ po_status launch_interp_rows_packed(const float2 *src, uint4 *dst, int64_t n_pat
 // launchers pick their shared-memory size at run time and must not change
 // function attributes while a stream is being captured).
 po_status init_interp_mma_attributes(int max_smem) {
-  PO_CUDA(cudaFuncSetAttribute(k_interp_cols_adj_mma<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
-  PO_CUDA(cudaFuncSetAttribute(k_interp_cols_adj_mma<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
+  PO_CUDA(cudaFuncSetAttribute(k_theta_adj_warp<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
+  PO_CUDA(cudaFuncSetAttribute(k_theta_adj_warp<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
+  PO_CUDA(cudaFuncSetAttribute(k_theta_adj_warp<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
+  PO_CUDA(cudaFuncSetAttribute(k_theta_adj_warp<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
   PO_CUDA(cudaFuncSetAttribute(k_interp_rows_mma<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
   PO_CUDA(cudaFuncSetAttribute(k_interp_rows_mma<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
 #define PO_TW_ATTR(N, M) \

@@ -87,9 +87,9 @@ po_status launch_interp_rows_packed(const float2 *src, uint4 *dst, int64_t n_pat
 // adjoint (transposed) passes, double cover only (po_interp_mma.cu)
 void build_theta_matrix_adj(int Tc, int Tp, int Rc, int Rp, int Kp, std::vector<uint32_t> &out);
 void build_phi_matrix_adj(int Pc, int Pp, int Kp, std::vector<uint32_t> &out);
-po_status launch_interp_cols_adj_mma(const float2 *parent_adj, float2 *mid_adj, const int32_t *child_parent,
-                                     const uint32_t *child_prefix, int64_t n_parent, int64_t n_child, int phi, int Rc,
-                                     int Rp, int Kp, const uint32_t *Afrag, const float4 *trans, int n_slots, int G,
+po_status launch_interp_cols_adj_mma(const float2 *parent_adj, float2 *mid_adj, const int32_t *child_table,
+                                     int64_t n_parent, int64_t n_child, int phi, int Rc, int Rp, int Kp,
+                                     const uint32_t *Afrag, const float4 *trans, int n_slots, int G,
                                      cudaStream_t st);
 // direction factors of a level grid (once per context) and the per-solve
 // translation phases built from them (po_fft.cu)
@@ -107,6 +107,13 @@ po_status launch_intensity_adjoint_f32(const float2 *fields, const float *dl_di,
                                        int nph, int mt, int mp, float2 *G, cudaStream_t st);
 po_status launch_intensity_adjoint_f64(const double2 *fields, const float *dl_di, int n_slots, int nth, int nph,
                                        double2 *G, cudaStream_t st);
+// tensor-core back-projection of the leaf adjoint patterns, FP32 chain (po_adjoint_mma.cu)
+po_status init_point_adjoint_mma_attributes();
+po_status launch_point_adjoint_mma(const float *const g[7], const int32_t *begin, int64_t n_nodes,
+                                   const double *center, int center_stride, const float2 *G, int64_t node_stride,
+                                   int64_t slot_stride, const float4 *dirs, int ndir,
+                                   const SlotParams<double> *slots, int n_lambda, int Gc, int64_t n, double *grad,
+                                   cudaStream_t st);
 po_status launch_point_adjoint_f32(const float *const g[7], const int32_t *begin, int64_t n_nodes,
                                    const double *center, int center_stride, const float2 *G, int64_t node_stride,
                                    int64_t slot_stride, const float4 *dirs, int ndir, const SlotParams<double> *slots,

@@ -132,6 +132,7 @@ po_status init_device_attributes(int dev) {
   PO_TRY(init_interp_mma_attributes(smem));
   PO_TRY(init_fft_attributes(smem));
   PO_TRY(init_leaf_mma_attributes());
+  PO_TRY(init_point_adjoint_mma_attributes());
   done.insert(dev);
   return PO_OK;
 }
@@ -418,7 +419,7 @@ static po_status ensure_adjoint_matrices(po_ctx *c) {
   const int d = c->depth;
   std::vector<uint32_t> all, one, ball, bone;
   for (int l = 0; l < d; ++l) {
-    c->amat_adj_kp[l] = (2 * c->R[l] + 15) / 16 * 16;
+    c->amat_adj_kp[l] = (c->R[l] + 15) / 16 * 16;
     build_theta_matrix_adj(c->T[l + 1], c->T[l], c->R[l + 1], c->R[l], c->amat_adj_kp[l], one);
     c->amat_adj_off[l] = all.size();
     all.insert(all.end(), one.begin(), one.end());
@@ -802,17 +803,16 @@ static po_status enqueue_solve(po_ctx *c, const SolvePlan &P, float *out_dev, co
         for (int l = 0; l < d; ++l) {
           const int64_t np = P.tree.level[l].count, nc = P.tree.level[l + 1].count;
           const float4 *trans = c->trans.as<float4>() + P.tr_off[l] + (size_t)ch.l0 * c->R[l] * c->Phi[l];
-          PO_TRY(launch_interp_cols_adj_mma(cur_lvl, c->mid.as<float2>(), P.tree.level[l + 1].parent,
-                                            P.tree.level[l + 1].prefix, np, nc, c->Phi[l], c->R[l + 1], c->R[l],
-                                            c->amat_adj_kp[l], c->amat_adj.as<uint32_t>() + c->amat_adj_off[l], trans,
-                                            ch.ns, ch.gc, st));
+          PO_TRY(launch_interp_cols_adj_mma(cur_lvl, c->mid.as<float2>(), P.tree.level[l].child, np, nc, c->Phi[l],
+                                            c->R[l + 1], c->R[l], c->amat_adj_kp[l],
+                                            c->amat_adj.as<uint32_t>() + c->amat_adj_off[l], trans, ch.ns, ch.gc, st));
           PO_TRY(launch_interp_rows_mma(c->mid.as<float2>(), nxt, (int64_t)ch.ns * nc * 6 * c->R[l + 1], c->Phi[l],
                                         c->Phi[l + 1], c->bmat_adj_kp[l],
                                         c->bmat_adj.as<uint32_t>() + c->bmat_adj_off[l], c->sm_count, st));
           std::swap(cur_lvl, nxt);
         }
         const int64_t ndl = (int64_t)c->R[d] * c->Phi[d];
-        PO_TRY(launch_point_adjoint_f32(P.gsc, P.tree.level[d].begin, P.nleaf, c->leaf_ctr.as<double>(), 1, cur_lvl,
+        PO_TRY(launch_point_adjoint_mma(P.gsc, P.tree.level[d].begin, P.nleaf, c->leaf_ctr.as<double>(), 1, cur_lvl,
                                         6 * ndl, P.nleaf * 6 * ndl, c->dirs.as<float4>(), (int)ndl, P.sp64_dev + ch.s0,
                                         ch.nl, ch.gc, n, c->grad_acc.as<double>(), st));
       }
