@@ -112,6 +112,8 @@ po_status launch_intensity_adjoint_f64(const double2 *fields, const float *dl_di
 }
 
 // ------------------------------------------------------- point adjoint
+// CUDA-core back-projection of the FP64 chain (the FP32 chain runs the
+// tensor-core kernel of po_adjoint_mma.cu).
 // One warp per (node, 32-point chunk); 4 warps per CTA.  A node's points are
 // [begin[node], begin[node+1]); its adjoint pattern is
 // G[slot][node * node_stride][6][ndir] about centre[3 * node * center_stride]
@@ -249,14 +251,6 @@ static po_status launch_point_adjoint_t(const float *const g[7], const int32_t *
   return PO_OK;
 }
 
-po_status launch_point_adjoint_f32(const float *const g[7], const int32_t *begin, int64_t n_nodes,
-                                   const double *center, int center_stride, const float2 *G, int64_t node_stride,
-                                   int64_t slot_stride, const float4 *dirs, int ndir, const SlotParams<double> *slots,
-                                   int n_lambda, int Gc, int64_t n, double *grad, cudaStream_t st) {
-  return launch_point_adjoint_t<float>(g, begin, n_nodes, center, center_stride, G, node_stride, slot_stride, dirs,
-                                       nullptr, ndir, slots, n_lambda, Gc, n, grad, st);
-}
-
 po_status launch_point_adjoint_f64(const float *const g[7], const int32_t *begin, int64_t n_nodes,
                                    const double *center, int center_stride, const double2 *G, int64_t node_stride,
                                    int64_t slot_stride, const double *dirs_d, int ndir, const SlotParams<double> *slots,
@@ -265,15 +259,16 @@ po_status launch_point_adjoint_f64(const float *const g[7], const int32_t *begin
                                         nullptr, dirs_d, ndir, slots, n_lambda, Gc, n, grad, st);
 }
 
-// chunk starts 0, 32, 64, ... n (the depth-0 adjoint treats every 32 points as a node)
-__global__ void k_chunk_begin(int32_t *begin, int64_t nchunk, int64_t n) {
+// chunk starts 0, chunk, 2 chunk, ... n (the depth-0 adjoint treats every
+// chunk of points as a node)
+__global__ void k_chunk_begin(int32_t *begin, int64_t nchunk, int64_t n, int chunk) {
   int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i <= nchunk) begin[i] = (int32_t)(i * 32 < n ? i * 32 : n);
+  if (i <= nchunk) begin[i] = (int32_t)(i * chunk < n ? i * chunk : n);
 }
 
-po_status launch_chunk_begin(int32_t *begin, int64_t n, cudaStream_t st) {
-  const int64_t nchunk = (n + 31) / 32;
-  k_chunk_begin<<<(unsigned)((nchunk + 256) / 256), 256, 0, st>>>(begin, nchunk, n);
+po_status launch_chunk_begin(int32_t *begin, int64_t n, int chunk, cudaStream_t st) {
+  const int64_t nchunk = (n + chunk - 1) / chunk;
+  k_chunk_begin<<<(unsigned)((nchunk + 256) / 256), 256, 0, st>>>(begin, nchunk, n, chunk);
   count_launch();
   PO_CUDA(cudaGetLastError());
   return PO_OK;

@@ -114,15 +114,11 @@ po_status launch_point_adjoint_mma(const float *const g[7], const int32_t *begin
                                    int64_t slot_stride, const float4 *dirs, int ndir,
                                    const SlotParams<double> *slots, int n_lambda, int Gc, int64_t n, double *grad,
                                    cudaStream_t st);
-po_status launch_point_adjoint_f32(const float *const g[7], const int32_t *begin, int64_t n_nodes,
-                                   const double *center, int center_stride, const float2 *G, int64_t node_stride,
-                                   int64_t slot_stride, const float4 *dirs, int ndir, const SlotParams<double> *slots,
-                                   int n_lambda, int Gc, int64_t n, double *grad, cudaStream_t st);
 po_status launch_point_adjoint_f64(const float *const g[7], const int32_t *begin, int64_t n_nodes,
                                    const double *center, int center_stride, const double2 *G, int64_t node_stride,
                                    int64_t slot_stride, const double *dirs_d, int ndir, const SlotParams<double> *slots,
                                    int n_lambda, int Gc, int64_t n, double *grad, cudaStream_t st);
-po_status launch_chunk_begin(int32_t *begin, int64_t n, cudaStream_t st);
+po_status launch_chunk_begin(int32_t *begin, int64_t n, int chunk, cudaStream_t st);
 po_status launch_scatter_grad(const double *grad_sorted, const int32_t *perm, int64_t n, float *out, cudaStream_t st);
 
 // once per device: opt-in shared memory of the kernels whose launchers size it at run time

@@ -549,7 +549,9 @@ static po_status prepare_solve(po_ctx *c, const po_geometry *g, const po_illum *
   for (int a = 0; a < 3; ++a) P.c0[a] = (double)(0.5f * (cfg.box_min[a] + cfg.box_max[a]));
   if (adj) {
     PO_CUDA(cudaMemcpyAsync(c->center0.p, P.c0, sizeof(P.c0), cudaMemcpyHostToDevice, st));
-    if (n > 0) PO_TRY(launch_chunk_begin(c->chunk_begin.as<int32_t>(), n, st));
+    // depth-0 point adjoint: the points in chunks (32 for the FP64 chain, 128 =
+    // one pass of the tensor-core kernel for the FP32 chain) sharing one pattern
+    if (n > 0) PO_TRY(launch_chunk_begin(c->chunk_begin.as<int32_t>(), n, P.fp64 ? 32 : 128, st));
   }
 
   if (P.fp64) {
@@ -732,8 +734,8 @@ static po_status enqueue_solve(po_ctx *c, const SolvePlan &P, float *out_dev, co
         float2 *Gf = c->levelB.as<float2>();
         PO_TRY(launch_intensity_adjoint_f32(c->levelA.as<float2>(), adj->dl_di + (size_t)ch.s0 * nd_out, ch.ns,
                                             nth_out, nph_out, nth_out, nph_out, 1, 1, Gf, st));
-        PO_TRY(launch_point_adjoint_f32(P.gsc, c->chunk_begin.as<int32_t>(), (n + 31) / 32, c->center0.as<double>(), 0,
-                                        Gf, 0, 6 * nd_out, c->dirs.as<float4>(), (int)nd_out, P.sp64_dev + ch.s0,
+        PO_TRY(launch_point_adjoint_mma(P.gsc, c->chunk_begin.as<int32_t>(), (n + 127) / 128, c->center0.as<double>(),
+                                        0, Gf, 0, 6 * nd_out, c->dirs.as<float4>(), (int)nd_out, P.sp64_dev + ch.s0,
                                         ch.nl, ch.gc, n, c->grad_acc.as<double>(), st));
       }
       PO_TRY(rec(c->ev[4]));
