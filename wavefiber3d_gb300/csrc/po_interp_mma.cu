@@ -170,7 +170,7 @@ void build_theta_matrix_adj(int Tc, int Tp, int Rc, int Rp, int Kp, std::vector<
 // child) are loaded while the current one multiplies, and the parent tile
 // accumulates in registers across the children.
 template <int NPT, int MTW>
-__global__ void __launch_bounds__(256, 2) k_theta_warp(const uint4 *__restrict__ mid, float2 *__restrict__ parent,
+__global__ void __launch_bounds__(256, MTW <= 2 ? 3 : 2) k_theta_warp(const uint4 *__restrict__ mid, float2 *__restrict__ parent,
                                                        const int32_t *__restrict__ child_table, int64_t n_parent,
                                                        int64_t n_child, int phi, int Rch, int Rp, int KS, int MT,
                                                        const uint4 *__restrict__ Afrag,
@@ -609,7 +609,7 @@ constexpr int kRowNG = 8;
 // every warp runs over blocks of 8 rows with the next k-step's input loads in
 // flight while the current one multiplies.
 template <bool PACK>
-__global__ void __launch_bounds__(128) k_interp_rows_mma(const float2 *__restrict__ src, void *__restrict__ dst_,
+__global__ void __launch_bounds__(128, 6) k_interp_rows_mma(const float2 *__restrict__ src, void *__restrict__ dst_,
                                                          int64_t nrows, int Rc, int Pc, int Pp, int Kp,
                                                          const uint4 *__restrict__ Bm, int b_in_smem) {
   extern __shared__ uint4 bsm[];
@@ -658,24 +658,17 @@ __global__ void __launch_bounds__(128) k_interp_rows_mma(const float2 *__restric
       split_bf16x2(v[0].y, v[1].y, ahi[1], alo[1]);  // row g+8 (imaginary parts)
       split_bf16x2(v[2].x, v[3].x, ahi[2], alo[2]);  // row g, k0+8, k0+9
       split_bf16x2(v[2].y, v[3].y, ahi[3], alo[3]);
-      if (nq == kRowNG) {  // full group: one basic block, 8 independent accumulators
-        uint4 bv[kRowNG];
+      if (nq == kRowNG) {  // full group: n-tiles in pairs, two independent accumulators per product
 #pragma unroll
-        for (int q = 0; q < kRowNG; ++q) bv[q] = B[((size_t)q * KS + ks) * 32 + lane];
-#pragma unroll
-        for (int q = 0; q < kRowNG; ++q) {
-          const uint32_t bhi[2] = {bv[q].x, bv[q].y};
-          mma_bf16(acc[q], ahi, bhi);
-        }
-#pragma unroll
-        for (int q = 0; q < kRowNG; ++q) {
-          const uint32_t blo[2] = {bv[q].z, bv[q].w};
-          mma_bf16(acc[q], ahi, blo);
-        }
-#pragma unroll
-        for (int q = 0; q < kRowNG; ++q) {
-          const uint32_t bhi[2] = {bv[q].x, bv[q].y};
-          mma_bf16(acc[q], alo, bhi);
+        for (int q = 0; q < kRowNG; q += 2) {
+          const uint4 b0 = B[((size_t)q * KS + ks) * 32 + lane], b1 = B[((size_t)(q + 1) * KS + ks) * 32 + lane];
+          const uint32_t h0[2] = {b0.x, b0.y}, l0[2] = {b0.z, b0.w}, h1[2] = {b1.x, b1.y}, l1[2] = {b1.z, b1.w};
+          mma_bf16(acc[q], ahi, h0);
+          mma_bf16(acc[q + 1], ahi, h1);
+          mma_bf16(acc[q], ahi, l0);
+          mma_bf16(acc[q + 1], ahi, l1);
+          mma_bf16(acc[q], alo, h0);
+          mma_bf16(acc[q + 1], alo, h1);
         }
       } else {
 #pragma unroll
