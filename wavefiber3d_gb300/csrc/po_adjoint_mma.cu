@@ -38,10 +38,19 @@ constexpr int kPaNT = 6;                    // n-tiles: 6 components x 4 weights
 constexpr size_t kPaSmem = sizeof(uint4) * (kPaDirs / 8) * kPaNT * 32 + sizeof(float2) * 6 * kPaDirs +
                            sizeof(float4) * kPaDirs;
 
-// (cos, sin) of -s.u split into hi / lo bf16 pairs (an A-fragment register)
+// (cos, sin) of -s.u split into hi / lo bf16 pairs (an A-fragment register).
+// REDUCE: Cody-Waite reduction to [-pi, pi] first; without it the hardware
+// sine / cosine take the argument directly, which the kernel allows only when
+// every |u| of the warp is <= kAdjFastPhase (absolute error <= ~2e-6 there).
+constexpr float kAdjFastPhase = 16.f;
+template <bool REDUCE>
 __device__ __forceinline__ void adj_phase_frag(float4 s, float ux, float uy, float uz, uint32_t &hi, uint32_t &lo) {
   float sn, cs;
-  sincos_small(-fmaf(s.x, ux, fmaf(s.y, uy, s.z * uz)), &sn, &cs);
+  const float ph = -fmaf(s.x, ux, fmaf(s.y, uy, s.z * uz));
+  if (REDUCE)
+    sincos_small(ph, &sn, &cs);
+  else
+    __sincosf(ph, &sn, &cs);
   split_bf16x2(cs, sn, hi, lo);
 }
 
@@ -93,12 +102,15 @@ __global__ void __launch_bounds__(32 * kPaWarps, 2) k_point_adjoint_mma(
     for (int lam = 0; lam < n_lambda; ++lam) {
       const double k0 = slots[lam * Gc].k0d;
       float ux[2], uy[2], uz[2];
+      bool big = false;
 #pragma unroll
       for (int h = 0; h < 2; ++h) {
         ux[h] = (float)(k0 * ((double)px[h] - cx_));
         uy[h] = (float)(k0 * ((double)py[h] - cy_));
         uz[h] = (float)(k0 * ((double)pz[h] - cz_));
+        big |= ok[h] && !(ux[h] * ux[h] + uy[h] * uy[h] + uz[h] * uz[h] <= kAdjFastPhase * kAdjFastPhase);
       }
+      const bool reduce = __any_sync(0xffffffffu, big);
       for (int gs = 0; gs < Gc; ++gs) {
         const int slot = lam * Gc + gs;
         const float2 *gp = G + slot * slot_stride + node * node_stride;
@@ -142,10 +154,17 @@ __global__ void __launch_bounds__(32 * kPaWarps, 2) k_point_adjoint_mma(
           for (int ks = 0; ks < ksn; ++ks) {
             const float4 sa = s_s[ks * 8 + tq], sb = s_s[ks * 8 + tq + 4];
             uint32_t ahi[4], alo[4];
-            adj_phase_frag(sa, ux[0], uy[0], uz[0], ahi[0], alo[0]);  // row g, direction tq
-            adj_phase_frag(sa, ux[1], uy[1], uz[1], ahi[1], alo[1]);  // row g + 8
-            adj_phase_frag(sb, ux[0], uy[0], uz[0], ahi[2], alo[2]);  // row g, direction tq + 4
-            adj_phase_frag(sb, ux[1], uy[1], uz[1], ahi[3], alo[3]);
+            if (reduce) {
+              adj_phase_frag<true>(sa, ux[0], uy[0], uz[0], ahi[0], alo[0]);  // row g, direction tq
+              adj_phase_frag<true>(sa, ux[1], uy[1], uz[1], ahi[1], alo[1]);  // row g + 8
+              adj_phase_frag<true>(sb, ux[0], uy[0], uz[0], ahi[2], alo[2]);  // row g, direction tq + 4
+              adj_phase_frag<true>(sb, ux[1], uy[1], uz[1], ahi[3], alo[3]);
+            } else {
+              adj_phase_frag<false>(sa, ux[0], uy[0], uz[0], ahi[0], alo[0]);
+              adj_phase_frag<false>(sa, ux[1], uy[1], uz[1], ahi[1], alo[1]);
+              adj_phase_frag<false>(sb, ux[0], uy[0], uz[0], ahi[2], alo[2]);
+              adj_phase_frag<false>(sb, ux[1], uy[1], uz[1], ahi[3], alo[3]);
+            }
             uint4 bv[kPaNT];
 #pragma unroll
             for (int nt = 0; nt < kPaNT; ++nt) bv[nt] = s_b[(ks * kPaNT + nt) * 32 + lane];

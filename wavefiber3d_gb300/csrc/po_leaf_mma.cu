@@ -28,10 +28,20 @@ namespace wavepo {
 
 namespace {
 
-// (cos, sin) of the phase of direction s and point u, split into hi/lo pairs
+// (cos, sin) of the phase of direction s and point u, split into hi/lo pairs.
+// REDUCE: Cody-Waite reduction to [-pi, pi] first; without it the hardware
+// sine / cosine take the argument directly, which the caller allows only for
+// |phase| <= kLeafFastPhase (absolute error <= ~2e-6 there, below the ~1.5e-5
+// of the split operands).
+constexpr float kLeafFastPhase = 16.f;
+template <bool REDUCE>
 __device__ __forceinline__ void phase_frag(float sx, float sy, float sz, float4 u, uint32_t &hi, uint32_t &lo) {
   float sn, cs;
-  sincos_small(fmaf(sx, u.x, fmaf(sy, u.y, sz * u.z)), &sn, &cs);
+  const float ph = fmaf(sx, u.x, fmaf(sy, u.y, sz * u.z));
+  if (REDUCE)
+    sincos_small(ph, &sn, &cs);
+  else
+    __sincosf(ph, &sn, &cs);
   split_bf16x2(cs, sn, hi, lo);
 }
 
@@ -70,12 +80,15 @@ __global__ void __launch_bounds__(128) k_leaf_mma(
     const int cnt = max(0, min(kPC, e - c0));
     const bool first = (c0 == b);
     __syncthreads();
+    bool big = false;  // a phase |s.u| <= |u| of this chunk may exceed kLeafFastPhase
     for (int q = threadIdx.x; q < kPC; q += blockDim.x) {
       if (q < cnt) {
         const int p = c0 + q;
         const float px = x[p], py = y[p], pz = z[p];
-        s_u[q] = make_float4((float)(k0 * ((double)px - cxd)), (float)(k0 * ((double)py - cyd)),
-                             (float)(k0 * ((double)pz - czd)), 0.f);
+        const float4 u = make_float4((float)(k0 * ((double)px - cxd)), (float)(k0 * ((double)py - cyd)),
+                                     (float)(k0 * ((double)pz - czd)), 0.f);
+        s_u[q] = u;
+        big |= !(u.x * u.x + u.y * u.y + u.z * u.z <= kLeafFastPhase * kLeafFastPhase);
         const float qx = nx[p], qy = ny[p], qz = nz[p], ar = area[p];
 #pragma unroll
         for (int s2 = 0; s2 < GC; ++s2) {
@@ -90,7 +103,7 @@ __global__ void __launch_bounds__(128) k_leaf_mma(
         for (int k = 0; k < NC; ++k) s_cur[q * NC + k] = make_float2(0.f, 0.f);
       }
     }
-    __syncthreads();
+    const bool reduce = __syncthreads_or(big) != 0;
     const int ksteps = (cnt + 7) / 8;
     // B fragments: lane ln of n-tile nt holds rows k = 2tq', 2tq'+1 (point tq') and
     // 2tq'+8, 2tq'+9 (point tq'+4) of real column n = nt*8 + g'
@@ -120,10 +133,17 @@ __global__ void __launch_bounds__(128) k_leaf_mma(
       for (int ks = 0; ks < ksteps; ++ks) {
         const float4 ua = s_u[ks * 8 + tq], ub = s_u[ks * 8 + tq + 4];
         uint32_t ahi[4], alo[4];
-        phase_frag(s0.x, s0.y, s0.z, ua, ahi[0], alo[0]);
-        phase_frag(s1.x, s1.y, s1.z, ua, ahi[1], alo[1]);
-        phase_frag(s0.x, s0.y, s0.z, ub, ahi[2], alo[2]);
-        phase_frag(s1.x, s1.y, s1.z, ub, ahi[3], alo[3]);
+        if (reduce) {
+          phase_frag<true>(s0.x, s0.y, s0.z, ua, ahi[0], alo[0]);
+          phase_frag<true>(s1.x, s1.y, s1.z, ua, ahi[1], alo[1]);
+          phase_frag<true>(s0.x, s0.y, s0.z, ub, ahi[2], alo[2]);
+          phase_frag<true>(s1.x, s1.y, s1.z, ub, ahi[3], alo[3]);
+        } else {
+          phase_frag<false>(s0.x, s0.y, s0.z, ua, ahi[0], alo[0]);
+          phase_frag<false>(s1.x, s1.y, s1.z, ua, ahi[1], alo[1]);
+          phase_frag<false>(s0.x, s0.y, s0.z, ub, ahi[2], alo[2]);
+          phase_frag<false>(s1.x, s1.y, s1.z, ub, ahi[3], alo[3]);
+        }
         uint4 bv[NT];
 #pragma unroll
         for (int nt = 0; nt < NT; ++nt) bv[nt] = s_b[(ks * NT + nt) * 32 + lane];
