@@ -298,8 +298,10 @@ __global__ void __launch_bounds__(256, MTW <= 2 ? 3 : 2) k_theta_warp(const uint
           const float pxy = fmaf(sgx, rr.x, sgy * rr.y), pz = sgz * rr.z;
 #pragma unroll
           for (int w = 0; w < 2; ++w) {
+            // each table phase is reduced to [-pi, pi], so |pz +- pxy| <= 3 pi:
+            // the hardware sine / cosine need no further reduction (abs. error ~1e-6)
             float sn, cs;
-            sincos_small(w ? pz - pxy : pz + pxy, &sn, &cs);
+            __sincosf(w ? pz - pxy : pz + pxy, &sn, &cs);
             const float yr = w ? ur - vr : ur + vr, yi = w ? ui - vi : ui + vi;
             acc[i][pt][w][2 * h] += yr * cs - yi * sn;
             acc[i][pt][w][2 * h + 1] += yr * sn + yi * cs;
@@ -441,9 +443,9 @@ __global__ void __launch_bounds__(256, 2) k_theta_adj_warp(
       const float2 a = src[(int64_t)r * phi + jq], b = src[(int64_t)r * phi + jq + span];
       const float4 rr = __ldg(tr + (int64_t)r * phi + jq);
       const float pxy = fmaf(sgx, rr.x, sgy * rr.y), pz = sgz * rr.z;
-      float s1, c1, s2, c2;
-      sincos_small(pz + pxy, &s1, &c1);  // column j
-      sincos_small(pz - pxy, &s2, &c2);  // its mirror (x and y phases negated)
+      float s1, c1, s2, c2;  // |pz +- pxy| <= 3 pi (table phases reduced to [-pi, pi])
+      __sincosf(pz + pxy, &s1, &c1);  // column j
+      __sincosf(pz - pxy, &s2, &c2);  // its mirror (x and y phases negated)
       const float xr = a.x * c1 + a.y * s1, xi = a.y * c1 - a.x * s1;  // a exp(-i ph_j)
       const float yr = b.x * c2 + b.y * s2, yi = b.y * c2 - b.x * s2;
       S = make_float2(xr + yr, xi + yi);
