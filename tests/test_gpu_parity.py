@@ -330,3 +330,17 @@ def test_large_level_grids_vs_fp64_direct(prec):
     out, rep = _solve(cloud, cfg, il)
     o = oracle.solve_direct(cloud, oracle.make_illum(500e-9, 0.3, 0.7, "M", 1.55 + 0.1j, 2e-6), 180, 360)
     assert rel(out.reshape(o.shape), o) < TOL_TREE, rep
+
+
+@pytest.mark.parametrize("prec", [api.PO_PREC_FP32, api.PO_PREC_SPLIT_BF16])
+def test_large_leaf_phases_vs_fp64_direct(prec):
+    """Leaves of 8.8 um at 500 nm: leaf-local phases reach ~100 rad, so the
+    leaf kernels take their range-reduced phasor path (the fast path covers
+    |phase| <= 16 rad only)."""
+    cloud = geometry.fibonacci_sphere(8.0e-6, 4000)
+    box = [-8.8e-6] * 3 + [8.8e-6] * 3
+    cfg = api.Config.reference_rule(1, 24, 48, box[:3], box[3:], 17.6e-6, 17.6e-6, 1.2, precision=prec)
+    il = api.Illumination([500e-9], [0.3], [0.7], api.PO_POL_TM, 1.55 + 0.1j, 2e-5)
+    out, rep = _solve(cloud, cfg, il)
+    o = oracle.solve_direct(cloud, oracle.make_illum(500e-9, 0.3, 0.7, "M", 1.55 + 0.1j, 2e-5), 24, 48)
+    assert rel(out.reshape(o.shape), o) < TOL_TREE, rep

@@ -170,7 +170,7 @@ void build_theta_matrix_adj(int Tc, int Tp, int Rc, int Rp, int Kp, std::vector<
 // child) are loaded while the current one multiplies, and the parent tile
 // accumulates in registers across the children.
 template <int NPT, int MTW>
-__global__ void __launch_bounds__(256, MTW <= 2 ? 3 : 2) k_theta_warp(const uint4 *__restrict__ mid, float2 *__restrict__ parent,
+__global__ void __launch_bounds__(256, (NPT == 1 && MTW <= 2) ? 3 : 2) k_theta_warp(const uint4 *__restrict__ mid, float2 *__restrict__ parent,
                                                        const int32_t *__restrict__ child_table, int64_t n_parent,
                                                        int64_t n_child, int phi, int Rch, int Rp, int KS, int MT,
                                                        const uint4 *__restrict__ Afrag,
