@@ -175,10 +175,12 @@ class Solver:
         return (len(illum.wavelengths_m), len(illum.theta_i), npol, int(self.config.n_theta[0]),
                 int(self.config.n_phi[0]))
 
-    def solve(self, cloud, illum: Illumination, out=None, stream=None):
+    def solve(self, cloud, illum: Illumination, out=None, stream=None, report: bool = True):
         """cloud: PointCloud (host numpy) or a (7, n) float32 CUDA tensor / tuple of 7 CUDA tensors.
         Returns intensity [L][I][P][n_theta][n_phi] float32 (numpy for host geometry without `out`,
-        else the CUDA tensor `out` or a new CUDA tensor)."""
+        else the CUDA tensor `out` or a new CUDA tensor).  report=True fills `last_report` (per-kernel
+        times: the call then waits for the solve to finish); report=False leaves a device-output solve
+        asynchronous on the stream and sets `last_report` to None."""
         torch = _torch()
         il, keep = illum.to_c()
         host = hasattr(cloud, "soa")
@@ -197,18 +199,19 @@ class Solver:
             n = arrs[0].numel()
             g = _lib.po_geometry(n, *[a.data_ptr() for a in arrs], 1 if on_dev else 0)
         rep = _lib.po_report()
+        rep_ref = ctypes.byref(rep) if report else None
         shape = self.out_shape(illum)
         if out is None and host:
             res = np.empty(shape, dtype=np.float32)
             check(_lib.load().po_solve(self._h, ctypes.byref(g), ctypes.byref(il), res.ctypes.data, 0,
-                                       _stream_ptr(stream), ctypes.byref(rep)))
+                                       _stream_ptr(stream), rep_ref))
         else:
             res = out if out is not None else torch.empty(shape, dtype=torch.float32, device="cuda")
             if not (res.is_contiguous() and res.dtype == torch.float32 and res.numel() == int(np.prod(shape))):
                 raise ValueError(f"out must be a contiguous float32 tensor with {int(np.prod(shape))} elements")
             check(_lib.load().po_solve(self._h, ctypes.byref(g), ctypes.byref(il), ctypes.c_void_p(res.data_ptr()),
-                                       1 if res.is_cuda else 0, _stream_ptr(stream), ctypes.byref(rep)))
-        self.last_report = rep.as_dict()
+                                       1 if res.is_cuda else 0, _stream_ptr(stream), rep_ref))
+        self.last_report = rep.as_dict() if report else None
         del keep
         return res
 

@@ -36,7 +36,8 @@ namespace wavepo {
 // every other root sample gets 0.  fields/G: [slot][6][T][Phi].
 template <typename V, typename R>
 __global__ void k_intensity_adjoint(const V *__restrict__ fields, const float *__restrict__ dl_di, int T, int Phi,
-                                    int nth, int nph, int mt, int mp, R z0, V *__restrict__ G) {
+                                    int nth, int nph, int mt, int mp, const float4 *__restrict__ dirs, R z0,
+                                    V *__restrict__ G) {
   const int64_t cstride = (int64_t)T * Phi;
   const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const int slot = blockIdx.y;
@@ -51,8 +52,15 @@ __global__ void k_intensity_adjoint(const V *__restrict__ fields, const float *_
     return;
   }
   const int i = it / mt, k = ip / mp;
+  // FP32 chain: the context's output-direction table (grid_direction rounded to
+  // float); FP64 chain (dirs == nullptr): the directions in FP64
   double sd[3];
-  grid_direction(i, k, nth, nph, sd);
+  if (dirs) {
+    const float4 sv = __ldg(dirs + (int64_t)i * nph + k);
+    sd[0] = sv.x, sd[1] = sv.y, sd[2] = sv.z;
+  } else {
+    grid_direction(i, k, nth, nph, sd);
+  }
   const R s[3] = {(R)sd[0], (R)sd[1], (R)sd[2]};
   V E[3], H[3];
 #pragma unroll
@@ -89,12 +97,12 @@ __global__ void k_intensity_adjoint(const V *__restrict__ fields, const float *_
 }
 
 po_status launch_intensity_adjoint_f32(const float2 *fields, const float *dl_di, int n_slots, int T, int Phi, int nth,
-                                       int nph, int mt, int mp, float2 *G, cudaStream_t st) {
+                                       int nph, int mt, int mp, const float4 *dirs, float2 *G, cudaStream_t st) {
   const int64_t cs = (int64_t)T * Phi;
   if (cs <= 0 || n_slots <= 0) return PO_OK;
   dim3 grid((unsigned)((cs + 255) / 256), (unsigned)n_slots);
-  k_intensity_adjoint<float2, float><<<grid, 256, 0, st>>>(fields, dl_di, T, Phi, nth, nph, mt, mp, (float)z0_host(),
-                                                          G);
+  k_intensity_adjoint<float2, float><<<grid, 256, 0, st>>>(fields, dl_di, T, Phi, nth, nph, mt, mp, dirs,
+                                                          (float)z0_host(), G);
   count_launch();
   PO_CUDA(cudaGetLastError());
   return PO_OK;
@@ -105,7 +113,8 @@ po_status launch_intensity_adjoint_f64(const double2 *fields, const float *dl_di
   const int64_t cs = (int64_t)nth * nph;
   if (cs <= 0 || n_slots <= 0) return PO_OK;
   dim3 grid((unsigned)((cs + 255) / 256), (unsigned)n_slots);
-  k_intensity_adjoint<double2, double><<<grid, 256, 0, st>>>(fields, dl_di, nth, nph, nth, nph, 1, 1, z0_host(), G);
+  k_intensity_adjoint<double2, double><<<grid, 256, 0, st>>>(fields, dl_di, nth, nph, nth, nph, 1, 1, nullptr,
+                                                            z0_host(), G);
   count_launch();
   PO_CUDA(cudaGetLastError());
   return PO_OK;

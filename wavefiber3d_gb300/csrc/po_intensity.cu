@@ -41,15 +41,39 @@ __device__ __forceinline__ float intensity_at(const V *f, int64_t cstride, int64
   return (float)(xr * xr + xi * xi + yr * yr + yi * yi + zr * zr + zi * zi);
 }
 
+// Output directions of an n_theta x n_phi grid (grid_direction rounded to float),
+// built once per context: dirs[d] = (s_x, s_y, s_z, 0).
+__global__ void k_out_dirs(int nth, int nph, float4 *__restrict__ dirs) {
+  const int64_t d = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (d >= (int64_t)nth * nph) return;
+  double s[3];
+  grid_direction((int)(d / nph), (int)(d % nph), nth, nph, s);
+  dirs[d] = make_float4((float)s[0], (float)s[1], (float)s[2], 0.f);
+}
+
+po_status launch_out_dirs(int nth, int nph, float4 *dirs, cudaStream_t st) {
+  const int64_t nd = (int64_t)nth * nph;
+  if (nd <= 0) return PO_OK;
+  k_out_dirs<<<(unsigned)((nd + 255) / 256), 256, 0, st>>>(nth, nph, dirs);
+  count_launch();
+  PO_CUDA(cudaGetLastError());
+  return PO_OK;
+}
+
 __global__ void k_intensity_f32(const float2 *__restrict__ fields, int n_slots, int T, int Phi, int nth, int nph,
-                                int mt, int mp, float z0, float *__restrict__ out) {
+                                int mt, int mp, const float4 *__restrict__ dirs, float z0, float *__restrict__ out) {
   int64_t d = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   int slot = blockIdx.y;
   int64_t nd = (int64_t)nth * nph;
   if (d >= nd) return;
   int it = (int)(d / nph), ip = (int)(d % nph);
-  double s[3];
-  grid_direction(it, ip, nth, nph, s);
+  double s[3];  // the context's direction table, or (no table) grid_direction itself
+  if (dirs) {
+    const float4 sv = __ldg(dirs + d);
+    s[0] = sv.x, s[1] = sv.y, s[2] = sv.z;
+  } else {
+    grid_direction(it, ip, nth, nph, s);
+  }
   int64_t cstride = (int64_t)T * Phi;
   const float2 *f = fields + (int64_t)slot * 6 * cstride;
   int64_t idx = (int64_t)(it * mt) * Phi + (int64_t)ip * mp;
@@ -69,11 +93,11 @@ __global__ void k_intensity_f64(const double2 *__restrict__ fields, int n_slots,
 }
 
 po_status launch_intensity_f32(const float2 *fields, int n_slots, int T, int Phi, int nth, int nph, int mt, int mp,
-                               float *out, cudaStream_t st) {
+                               const float4 *dirs, float *out, cudaStream_t st) {
   int64_t nd = (int64_t)nth * nph;
   if (nd <= 0 || n_slots <= 0) return PO_OK;
   dim3 grid((unsigned)((nd + 255) / 256), (unsigned)n_slots);
-  k_intensity_f32<<<grid, 256, 0, st>>>(fields, n_slots, T, Phi, nth, nph, mt, mp, (float)z0_host(), out);
+  k_intensity_f32<<<grid, 256, 0, st>>>(fields, n_slots, T, Phi, nth, nph, mt, mp, dirs, (float)z0_host(), out);
   count_launch();
   PO_CUDA(cudaGetLastError());
   return PO_OK;

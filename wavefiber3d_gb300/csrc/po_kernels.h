@@ -104,7 +104,7 @@ po_status launch_height_field(const float *height, int numel, int numelvert, flo
 
 // adjoint of the intensity and of the far-field sums (po_adjoint.cu)
 po_status launch_intensity_adjoint_f32(const float2 *fields, const float *dl_di, int n_slots, int T, int Phi, int nth,
-                                       int nph, int mt, int mp, float2 *G, cudaStream_t st);
+                                       int nph, int mt, int mp, const float4 *dirs, float2 *G, cudaStream_t st);
 po_status launch_intensity_adjoint_f64(const double2 *fields, const float *dl_di, int n_slots, int nth, int nph,
                                        double2 *G, cudaStream_t st);
 // tensor-core back-projection of the leaf adjoint patterns, FP32 chain (po_adjoint_mma.cu)
@@ -127,8 +127,10 @@ po_status init_fft_attributes(int max_smem);
 
 // intensity: fields [slot][comp][T][Phi] (root, possibly supersampled by
 // (mt, mp)) -> out [slot][nth][nph]
+// out_dirs: the context's output-direction table (launch_out_dirs)
+po_status launch_out_dirs(int nth, int nph, float4 *dirs, cudaStream_t st);
 po_status launch_intensity_f32(const float2 *fields, int n_slots, int T, int Phi, int nth, int nph, int mt, int mp,
-                               float *out, cudaStream_t st);
+                               const float4 *dirs, float *out, cudaStream_t st);
 po_status launch_intensity_f64(const double2 *fields, int n_slots, int nth, int nph, float *out, cudaStream_t st);
 
 }  // namespace wavepo

@@ -160,6 +160,7 @@ struct po_ctx {
   int bmat_kp[PO_MAX_DEPTH] = {};
   DevBuf amat, bmat;
   DevBuf dir_trig;  // per level: (cos, sin) of the grid's theta rows, then of its phi columns
+  DevBuf out_dirs;  // output grid directions (float4), for the intensity and its adjoint
   size_t trig_off[PO_MAX_DEPTH] = {};
   // transposed level matrices of the adjoint (built on the first po_grad)
   bool adj_ready = false;
@@ -311,6 +312,10 @@ po_status po_create(po_ctx **out, const po_config *cfg) {
     s = launch_twiddles(n, c->twiddles.as<float2>() + c->tw_offset[n], 0);
     if (s != PO_OK) { po_destroy(c); return s; }
   }
+  // output-grid directions
+  s = c->out_dirs.ensure(sizeof(float4) * std::max<size_t>((size_t)cfg->n_theta[0] * cfg->n_phi[0], 1));
+  if (s == PO_OK) s = launch_out_dirs(cfg->n_theta[0], cfg->n_phi[0], c->out_dirs.as<float4>(), 0);
+  if (s != PO_OK) { po_destroy(c); return s; }
   // direction factors of every parent level (translation tables)
   {
     size_t n_trig = 0;
@@ -369,7 +374,7 @@ po_status po_destroy(po_ctx *c) {
   for (DevBuf *b : {&c->twiddles, &c->geom_in, &c->geom_sorted, &c->octree_ws, &c->leaf_ctr, &c->dirs, &c->dirs_d,
                     &c->trans, &c->levelA, &c->levelB, &c->mid, &c->slots, &c->kvals, &c->out, &c->cur, &c->partial,
                     &c->tile_ctr, &c->amat, &c->bmat, &c->amat_adj, &c->bmat_adj, &c->slots64, &c->grad_acc,
-                    &c->chunk_begin, &c->center0, &c->dir_trig})
+                    &c->chunk_begin, &c->center0, &c->dir_trig, &c->out_dirs})
     b->release();
   for (auto &e : c->ev)
     if (e) cudaEventDestroy(e);
@@ -729,11 +734,12 @@ static po_status enqueue_solve(po_ctx *c, const SolvePlan &P, float *out_dev, co
       PO_TRY(rec(c->kev[1]));
       PO_TRY(rec(c->ev[3]));
       PO_TRY(launch_intensity_f32(c->levelA.as<float2>(), ch.ns, nth_out, nph_out, nth_out, nph_out, 1, 1,
-                                  out_dev + (size_t)ch.s0 * nd_out, st));
+                                  c->out_dirs.as<float4>(), out_dev + (size_t)ch.s0 * nd_out, st));
       if (adj) {
         float2 *Gf = c->levelB.as<float2>();
         PO_TRY(launch_intensity_adjoint_f32(c->levelA.as<float2>(), adj->dl_di + (size_t)ch.s0 * nd_out, ch.ns,
-                                            nth_out, nph_out, nth_out, nph_out, 1, 1, Gf, st));
+                                            nth_out, nph_out, nth_out, nph_out, 1, 1, c->out_dirs.as<float4>(), Gf,
+                                            st));
         PO_TRY(launch_point_adjoint_mma(P.gsc, c->chunk_begin.as<int32_t>(), (n + 127) / 128, c->center0.as<double>(),
                                         0, Gf, 0, 6 * nd_out, c->dirs.as<float4>(), (int)nd_out, P.sp64_dev + ch.s0,
                                         ch.nl, ch.gc, n, c->grad_acc.as<double>(), st));
@@ -796,11 +802,11 @@ static po_status enqueue_solve(po_ctx *c, const SolvePlan &P, float *out_dev, co
       }
       PO_TRY(rec(c->ev[3]));
       PO_TRY(launch_intensity_f32(cur_lvl, ch.ns, c->R[0], c->Phi[0], nth_out, nph_out, c->mt, c->mp,
-                                  out_dev + (size_t)ch.s0 * nd_out, st));
+                                  c->out_dirs.as<float4>(), out_dev + (size_t)ch.s0 * nd_out, st));
       if (adj) {
         // root adjoint, then the transposed aggregation down to the leaves
         PO_TRY(launch_intensity_adjoint_f32(cur_lvl, adj->dl_di + (size_t)ch.s0 * nd_out, ch.ns, c->R[0], c->Phi[0],
-                                            nth_out, nph_out, c->mt, c->mp, nxt, st));
+                                            nth_out, nph_out, c->mt, c->mp, c->out_dirs.as<float4>(), nxt, st));
         std::swap(cur_lvl, nxt);
         for (int l = 0; l < d; ++l) {
           const int64_t np = P.tree.level[l].count, nc = P.tree.level[l + 1].count;
@@ -1085,7 +1091,7 @@ po_status po_interp_fft(const float *in, int th_c, int ph_c, float *out, int th_
 
 po_status po_compute_intensity(const float *fields, int n_theta, int n_phi, float *intensity, void *stream) {
   if (!fields || !intensity || n_theta <= 0 || n_phi <= 0) return fail(PO_ERR_INVALID_ARGUMENT, "invalid argument");
-  return launch_intensity_f32((const float2 *)fields, 1, n_theta, n_phi, n_theta, n_phi, 1, 1, intensity,
+  return launch_intensity_f32((const float2 *)fields, 1, n_theta, n_phi, n_theta, n_phi, 1, 1, nullptr, intensity,
                               (cudaStream_t)stream);
 }
 
