@@ -178,7 +178,11 @@ __global__ void __launch_bounds__(256, (NPT == 1 && MTW <= 2) ? 3 : 2) k_theta_w
                                                        int64_t n_task) {
   constexpr int TW = 4 * NPT;    // column pairs per warp
   extern __shared__ uint4 sA[];  // [MTW][KS][4][32]
-  const int mt0 = blockIdx.y * MTW;
+  // blockIdx.x = task CTA * groups + row-tile group: the groups of the same tasks run side by side
+  // and read each child's mid from L2 instead of streaming it from DRAM once per group
+  const int nmg = (MT + MTW - 1) / MTW;
+  const int mt0 = (int)(blockIdx.x % nmg) * MTW;
+  const int64_t cta = blockIdx.x / nmg;
   const int nmt = MT - mt0 < MTW ? MT - mt0 : MTW;
   {
     // tiles past MT (last group) are zero, so the k-loop below needs no guard
@@ -189,7 +193,7 @@ __global__ void __launch_bounds__(256, (NPT == 1 && MTW <= 2) ? 3 : 2) k_theta_w
   }
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, tq = lane & 3;
-  const int64_t task = (int64_t)blockIdx.x * (blockDim.x >> 5) + warp;
+  const int64_t task = cta * (blockDim.x >> 5) + warp;
   if (task >= n_task) return;
   const int ct = (int)(task % n_ct);
   int64_t rest = task / n_ct;
@@ -367,9 +371,9 @@ po_status launch_interp_cols_mma(const uint4 *mid, float2 *parent, const int32_t
   const int TW = 4 * NPT;
   const int n_ct = (phi / 2 + TW - 1) / TW;
   const int64_t n_task = (int64_t)n_slots * n_parent * 6 * n_ct;
-  const int64_t gx = (n_task + 7) / 8;
-  if (gx > 2147483647LL || nmg > 65535) return fail(PO_ERR_UNSUPPORTED, "too many nodes for one launch");
-  dim3 grid((unsigned)gx, (unsigned)nmg, 1u);
+  const int64_t gx = (n_task + 7) / 8 * nmg;
+  if (gx > 2147483647LL) return fail(PO_ERR_UNSUPPORTED, "too many nodes for one launch");
+  dim3 grid((unsigned)gx, 1u, 1u);
   const uint4 *A = (const uint4 *)Afrag;
 #define PO_TW(N, M)                                                                                                 \
   if (NPT == N && MTW == M) {                                                                                      \
