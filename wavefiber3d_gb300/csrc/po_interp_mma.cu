@@ -408,7 +408,11 @@ __global__ void __launch_bounds__(256, 2) k_theta_adj_warp(
     int64_t n_parent, int64_t n_child, int phi, int Rc, int Rp, int KS, int MT, const uint4 *__restrict__ Afrag,
     const float4 *__restrict__ trans, int G, int n_ct, int64_t n_task) {
   extern __shared__ uint4 sA[];  // [MTW][KS][4][32]
-  const int mt0 = blockIdx.y * MTW;
+  // blockIdx.x = task CTA * groups + row-tile group (groups of a task side by side: the parent's
+  // pattern is read from L2 once per task)
+  const int nmg = (MT + MTW - 1) / MTW;
+  const int mt0 = (int)(blockIdx.x % nmg) * MTW;
+  const int64_t cta = blockIdx.x / nmg;
   const int nmt = MT - mt0 < MTW ? MT - mt0 : MTW;
   {
     const uint4 *src = Afrag + (size_t)mt0 * KS * 128;
@@ -418,7 +422,7 @@ __global__ void __launch_bounds__(256, 2) k_theta_adj_warp(
   }
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, tq = lane & 3;
-  const int64_t task = (int64_t)blockIdx.x * (blockDim.x >> 5) + warp;
+  const int64_t task = cta * (blockDim.x >> 5) + warp;
   if (task >= n_task) return;
   const int ct = (int)(task % n_ct);
   int64_t rest = task / n_ct;
@@ -527,9 +531,9 @@ po_status launch_interp_cols_adj_mma(const float2 *parent_adj, float2 *mid_adj, 
   const size_t smem = (size_t)MTW * tile_bytes;
   const int n_ct = (phi / 2 + 3) / 4;
   const int64_t n_task = (int64_t)n_slots * n_parent * 6 * n_ct;
-  const int64_t gx = (n_task + 7) / 8;
-  if (gx > 2147483647LL || nmg > 65535) return fail(PO_ERR_UNSUPPORTED, "too many nodes for one launch");
-  dim3 grid((unsigned)gx, (unsigned)nmg, 1u);
+  const int64_t gx = (n_task + 7) / 8 * nmg;
+  if (gx > 2147483647LL) return fail(PO_ERR_UNSUPPORTED, "too many nodes for one launch");
+  dim3 grid((unsigned)gx, 1u, 1u);
   const uint4 *A = (const uint4 *)Afrag;
   switch (MTW) {
 #define PO_TA(M)                                                                                          \
