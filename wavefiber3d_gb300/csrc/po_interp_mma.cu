@@ -102,16 +102,24 @@ static double theta_partner(int Tc, int Tp, int r, int s) {
 // so a warp's shared-memory reads of one u are 512 contiguous bytes.
 size_t theta_pair_words(int Rp, int Kp) { return (size_t)((Rp + 15) / 16) * (Kp / 16) * 4 * 32 * 4; }
 
-void build_theta_matrix(int Tc, int Tp, int Rc, int Rp, int Kp, std::vector<uint32_t> &out) {
+// A_plus / A_minus of one level as dense FP64 [Rp][ld] (columns t < Rc)
+void theta_plus_minus(int Tc, int Tp, int Rc, int Rp, int ld, std::vector<double> &Mplus,
+                      std::vector<double> &Mminus) {
   const int nth_c = Tc / 2;
-  std::vector<double> Mplus((size_t)Rp * Kp, 0.0), Mminus((size_t)Rp * Kp, 0.0);
+  Mplus.assign((size_t)Rp * ld, 0.0);
+  Mminus.assign((size_t)Rp * ld, 0.0);
   for (int r = 0; r < Rp; ++r)
     for (int t = 0; t < Rc; ++t) {
       const double own = theta_own(Tc, Tp, r, t);
       const double partner = (t >= 1 && t < nth_c) ? theta_partner(Tc, Tp, r, t) : 0.0;
-      Mplus[(size_t)r * Kp + t] = 0.5 * (own + partner);
-      Mminus[(size_t)r * Kp + t] = 0.5 * (own - partner);
+      Mplus[(size_t)r * ld + t] = 0.5 * (own + partner);
+      Mminus[(size_t)r * ld + t] = 0.5 * (own - partner);
     }
+}
+
+void build_theta_matrix(int Tc, int Tp, int Rc, int Rp, int Kp, std::vector<uint32_t> &out) {
+  std::vector<double> Mplus, Mminus;
+  theta_plus_minus(Tc, Tp, Rc, Rp, Kp, Mplus, Mminus);
   std::vector<uint32_t> fp, fm;
   a_fragments(Mplus, Rp, Kp, fp);
   a_fragments(Mminus, Rp, Kp, fm);
@@ -162,7 +170,7 @@ void build_theta_matrix_adj(int Tc, int Tp, int Rc, int Rp, int Kp, std::vector<
 // Theta pass as warp tasks (double cover).  A warp owns one (slot, parent,
 // component) and TW = 4 NPT column pairs (j, j + Phi/2), j = j0.., for the
 // CTA's 16-row tiles mt0 .. mt0+MTW-1 (blockIdx.y selects them).
-// mid (from k_interp_rows_mma<true>): per (slot, child, component)
+// mid (from k_interp_rows_mma<1>): per (slot, child, component)
 // [Rc2/2][Phi/2][re, im] uint4 {S hi pair, S lo pair, D hi pair, D lo pair} --
 // a lane's B registers for the S and the D n-tile in one 16-byte load.  The
 // CTA stages its slice of the theta matrices in shared memory once; after
@@ -613,15 +621,24 @@ void build_phi_matrix_adj(int Pc, int Pp, int Kp, std::vector<uint32_t> &out) {
 // D hi pair, D lo pair}, each pair holding rows 2 tp (low half) and 2 tp + 1.
 // Lane g and lane g^1 (4 apart) hold the two rows of a pair; the even lane
 // stores the real parts, the odd lane the imaginary parts.
+// PACK == 2 (forward pass feeding the tcgen05 theta pass, po_theta_tc.cu): the
+// same sums and differences as four bf16 matrices per pattern (S hi, S lo,
+// D hi, D lo) in chunks of 16 rows, [Rr/16][matrix][npad/8][2][8][8]: core
+// matrices of 8 columns x 8 rows (16 B per column row); element (column
+// n = 2j + part, row t) of matrix m at byte
+// (t/16) 128 npad + m 32 npad + (n/8) 256 + ((t/8)%2) 128 + (n%8) 16 + (t%8) 2.
+// Patterns have Rr rows (rows Rc .. Rr-1 are zero); the 32 lanes of a warp
+// store one whole core matrix per matrix and n-tile.
 constexpr int kRowNG = 8;
 // blockIdx.y selects a group of kRowNG n-tiles (output columns); its slice of
 // the phi matrix is staged in shared memory when it fits (b_in_smem), and
 // every warp runs over blocks of 8 rows with the next k-step's input loads in
 // flight while the current one multiplies.
-template <bool PACK>
+template <int PACK>
 __global__ void __launch_bounds__(128, 6) k_interp_rows_mma(const float2 *__restrict__ src, void *__restrict__ dst_,
                                                          int64_t nrows, int Rc, int Pc, int Pp, int Kp,
-                                                         const uint4 *__restrict__ Bm, int b_in_smem) {
+                                                         const uint4 *__restrict__ Bm, int b_in_smem, int Rr,
+                                                         int npad) {
   extern __shared__ uint4 bsm[];
   const int KS = Kp / 16, NTt = PACK ? (Pp / 2 + 3) / 4 : (Pp + 7) / 8;
   const int ng = blockIdx.y * kRowNG;
@@ -633,7 +650,7 @@ __global__ void __launch_bounds__(128, 6) k_interp_rows_mma(const float2 *__rest
   }
   const uint4 *B = b_in_smem ? bsm : Bg;
   const int lane = threadIdx.x & 31, g = lane >> 2, tq = lane & 3;
-  const int Rc2 = Rc + (Rc & 1), half = Pp / 2;
+  const int Rc2 = PACK == 2 ? Rr : Rc + (Rc & 1), half = Pp / 2;
   const int64_t nblk = (nrows + 7) / 8;
   for (int64_t blk = (int64_t)blockIdx.x * 4 + (threadIdx.x >> 5); blk < nblk; blk += (int64_t)gridDim.x * 4) {
     const int64_t r = blk * 8 + g;
@@ -692,7 +709,36 @@ __global__ void __launch_bounds__(128, 6) k_interp_rows_mma(const float2 *__rest
         }
       }
     }
-    if (PACK) {
+    if (PACK == 2) {
+      const bool odd = g & 1;
+      const int64_t pattern = r / Rc2;
+      const int t0 = (int)(r - pattern * Rc2) & ~1;  // the pair's first row
+      uint8_t *base = (uint8_t *)dst_ + (size_t)pattern * 4 * npad * Rc2 * 2;
+      const size_t mat = (size_t)npad * 32;  // matrix stride inside a 16-row chunk
+#pragma unroll
+      for (int q = 0; q < kRowNG; ++q) {
+        if (q >= nq) break;
+        const float sr = acc[q][0] + acc[q][1], dr = acc[q][0] - acc[q][1];
+        const float si = acc[q][2] + acc[q][3], di = acc[q][2] - acc[q][3];
+        const float xs = __shfl_xor_sync(0xffffffffu, odd ? sr : si, 4);
+        const float xd = __shfl_xor_sync(0xffffffffu, odd ? dr : di, 4);
+        const float s0 = odd ? xs : sr, s1 = odd ? si : xs;
+        const float d0 = odd ? xd : dr, d1 = odd ? di : xd;
+        const int j = (ng + q) * 4 + tq;
+        uint32_t sh, sl, dh, dl;
+        split_bf16x2(s0, s1, sh, sl);
+        split_bf16x2(d0, d1, dh, dl);
+        if (rok && j < half) {
+          const int n = 2 * j + (odd ? 1 : 0);
+          const size_t off = (size_t)(t0 >> 4) * 128 * npad + (size_t)(n >> 3) * 256 + ((t0 >> 3) & 1) * 128 +
+                             (n & 7) * 16 + (t0 & 7) * 2;
+          *(uint32_t *)(base + off) = sh;
+          *(uint32_t *)(base + mat + off) = sl;
+          *(uint32_t *)(base + 2 * mat + off) = dh;
+          *(uint32_t *)(base + 3 * mat + off) = dl;
+        }
+      }
+    } else if (PACK == 1) {
       uint4 *dst = (uint4 *)dst_;
       const bool odd = g & 1;
       const int64_t pair_row = r >> 1;  // = pattern * Rc2/2 + t/2, Rc2 even
@@ -725,8 +771,8 @@ __global__ void __launch_bounds__(128, 6) k_interp_rows_mma(const float2 *__rest
   }
 }
 
-static po_status launch_rows(bool pack, const float2 *src, void *dst, int64_t nrows, int Rc, int Pc, int Pp, int Kp,
-                             const uint32_t *Bm, int sm_count, cudaStream_t st) {
+static po_status launch_rows(int pack, const float2 *src, void *dst, int64_t nrows, int Rc, int Pc, int Pp, int Kp,
+                             const uint32_t *Bm, int sm_count, cudaStream_t st, int Rr = 0, int npad = 0) {
   if (nrows <= 0) return PO_OK;
   if (Kp % 16 || Kp < Pc) return fail(PO_ERR_INTERNAL, "phi matrix K padding");
   const int NTt = pack ? (Pp / 2 + 3) / 4 : (Pp + 7) / 8;
@@ -739,12 +785,15 @@ static po_status launch_rows(bool pack, const float2 *src, void *dst, int64_t nr
   if (blocks > cap) blocks = cap;
   if (ngroups > 65535) return fail(PO_ERR_UNSUPPORTED, "angular grid too large for the row pass");
   dim3 grid((unsigned)blocks, (unsigned)ngroups);
-  if (pack)
-    k_interp_rows_mma<true><<<grid, 128, smem, st>>>(src, dst, nrows, Rc, Pc, Pp, Kp, (const uint4 *)Bm,
-                                                     b_smem ? 1 : 0);
+  if (pack == 2)
+    k_interp_rows_mma<2><<<grid, 128, smem, st>>>(src, dst, nrows, Rc, Pc, Pp, Kp, (const uint4 *)Bm,
+                                                  b_smem ? 1 : 0, Rr, npad);
+  else if (pack == 1)
+    k_interp_rows_mma<1><<<grid, 128, smem, st>>>(src, dst, nrows, Rc, Pc, Pp, Kp, (const uint4 *)Bm,
+                                                  b_smem ? 1 : 0, 0, 0);
   else
-    k_interp_rows_mma<false><<<grid, 128, smem, st>>>(src, dst, nrows, Rc, Pc, Pp, Kp, (const uint4 *)Bm,
-                                                      b_smem ? 1 : 0);
+    k_interp_rows_mma<0><<<grid, 128, smem, st>>>(src, dst, nrows, Rc, Pc, Pp, Kp, (const uint4 *)Bm,
+                                                  b_smem ? 1 : 0, 0, 0);
   count_launch();
   PO_CUDA(cudaGetLastError());
   return PO_OK;
@@ -752,13 +801,19 @@ static po_status launch_rows(bool pack, const float2 *src, void *dst, int64_t nr
 
 po_status launch_interp_rows_mma(const float2 *src, float2 *dst, int64_t nrows, int Pc, int Pp, int Kp,
                                  const uint32_t *Bm, int sm_count, cudaStream_t st) {
-  return launch_rows(false, src, dst, nrows, 0, Pc, Pp, Kp, Bm, sm_count, st);
+  return launch_rows(0, src, dst, nrows, 0, Pc, Pp, Kp, Bm, sm_count, st);
 }
 
 po_status launch_interp_rows_packed(const float2 *src, uint4 *dst, int64_t n_patterns, int Rc, int Pc, int Pp,
                                     int Kp, const uint32_t *Bm, int sm_count, cudaStream_t st) {
   const int64_t nrows = n_patterns * (int64_t)(Rc + (Rc & 1));
-  return launch_rows(true, src, dst, nrows, Rc, Pc, Pp, Kp, Bm, sm_count, st);
+  return launch_rows(1, src, dst, nrows, Rc, Pc, Pp, Kp, Bm, sm_count, st);
+}
+
+po_status launch_interp_rows_core(const float2 *src, uint8_t *dst, int64_t n_patterns, int Rc, int Rr, int npad,
+                                  int Pc, int Pp, int Kp, const uint32_t *Bm, int sm_count, cudaStream_t st) {
+  if (Rr % 16 || Rr < Rc || npad % 8 || npad < Pp) return fail(PO_ERR_INTERNAL, "core-matrix row pass padding");
+  return launch_rows(2, src, dst, n_patterns * (int64_t)Rr, Rc, Pc, Pp, Kp, Bm, sm_count, st, Rr, npad);
 }
 
 // Opt-in shared-memory limit of every kernel here, set once per device (the
@@ -769,8 +824,9 @@ po_status init_interp_mma_attributes(int max_smem) {
   PO_CUDA(cudaFuncSetAttribute(k_theta_adj_warp<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
   PO_CUDA(cudaFuncSetAttribute(k_theta_adj_warp<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
   PO_CUDA(cudaFuncSetAttribute(k_theta_adj_warp<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
-  PO_CUDA(cudaFuncSetAttribute(k_interp_rows_mma<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
-  PO_CUDA(cudaFuncSetAttribute(k_interp_rows_mma<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
+  PO_CUDA(cudaFuncSetAttribute(k_interp_rows_mma<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
+  PO_CUDA(cudaFuncSetAttribute(k_interp_rows_mma<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
+  PO_CUDA(cudaFuncSetAttribute(k_interp_rows_mma<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
 #define PO_TW_ATTR(N, M) \
   PO_CUDA(cudaFuncSetAttribute(k_theta_warp<N, M>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
   PO_TW_ATTR(1, 1) PO_TW_ATTR(1, 2) PO_TW_ATTR(1, 3) PO_TW_ATTR(1, 4) PO_TW_ATTR(2, 1) PO_TW_ATTR(2, 2)

@@ -84,6 +84,21 @@ po_status launch_interp_rows_mma(const float2 *src, float2 *dst, int64_t nrows, 
                                  const uint32_t *Bm, int sm_count, cudaStream_t st);
 po_status launch_interp_rows_packed(const float2 *src, uint4 *dst, int64_t n_patterns, int Rc, int Pc, int Pp,
                                     int Kp, const uint32_t *Bm, int sm_count, cudaStream_t st);
+// (core) the same sums / differences as four bf16 core-matrix arrays per pattern
+// (npad columns x Rr rows, rows Rc.. zero) for the tcgen05 theta pass
+po_status launch_interp_rows_core(const float2 *src, uint8_t *dst, int64_t n_patterns, int Rc, int Rr, int npad,
+                                  int Pc, int Pp, int Kp, const uint32_t *Bm, int sm_count, cudaStream_t st);
+void theta_plus_minus(int Tc, int Tp, int Rc, int Rp, int ld, std::vector<double> &Mplus,
+                      std::vector<double> &Mminus);
+// tcgen05 theta pass for levels with more than 128 parent rows (po_theta_tc.cu)
+size_t theta_tc_bytes(int Rp, int Kr);
+int theta_tc_npad(int phi);
+void build_theta_tc(const std::vector<double> &Mplus, const std::vector<double> &Mminus, int Rp, int Rc, int ld,
+                    int Kr, std::vector<uint16_t> &out);
+po_status init_theta_tc_attributes();
+po_status launch_theta_tc(const uint8_t *mid, float2 *parent, const int32_t *child_table, int64_t n_parent,
+                          int64_t n_child, int phi, int Kr, int Rp, const uint8_t *Atc, const float4 *trans,
+                          int n_slots, int G, int *err, cudaStream_t st);
 // adjoint (transposed) passes, double cover only (po_interp_mma.cu)
 void build_theta_matrix_adj(int Tc, int Tp, int Rc, int Rp, int Kp, std::vector<uint32_t> &out);
 void build_phi_matrix_adj(int Pc, int Pp, int Kp, std::vector<uint32_t> &out);

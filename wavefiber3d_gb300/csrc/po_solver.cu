@@ -133,6 +133,7 @@ po_status init_device_attributes(int dev) {
   PO_TRY(init_fft_attributes(smem));
   PO_TRY(init_leaf_mma_attributes());
   PO_TRY(init_point_adjoint_mma_attributes());
+  PO_TRY(init_theta_tc_attributes());
   done.insert(dev);
   return PO_OK;
 }
@@ -161,6 +162,11 @@ struct po_ctx {
   DevBuf amat, bmat;
   DevBuf dir_trig;  // per level: (cos, sin) of the grid's theta rows, then of its phi columns
   DevBuf out_dirs;  // output grid directions (float4), for the intensity and its adjoint
+  // tcgen05 theta pass of the levels with more than 128 parent rows (po_theta_tc.cu)
+  bool tc_level[PO_MAX_DEPTH] = {};
+  int tc_kr[PO_MAX_DEPTH] = {};       // child rows padded to 16 (the K of its products)
+  size_t tc_off[PO_MAX_DEPTH] = {};   // byte offset of the level's theta chunks in tc_amat
+  DevBuf tc_amat, tc_err;
   size_t trig_off[PO_MAX_DEPTH] = {};
   // transposed level matrices of the adjoint (built on the first po_grad)
   bool adj_ready = false;
@@ -345,6 +351,27 @@ po_status po_create(po_ctx **out, const po_config *cfg) {
       c->amat_off[l] = all.size();
       all.insert(all.end(), one.begin(), one.end());
     }
+    // levels with more than 128 parent rows: theta chunks for the tcgen05 pass
+    {
+      std::vector<uint16_t> tall, tone;
+      std::vector<double> Mp, Mm;
+      for (int l = 0; l < d; ++l) {
+        if (c->R[l] <= 128) continue;
+        c->tc_level[l] = true;
+        c->tc_kr[l] = (c->R[l + 1] + 15) / 16 * 16;
+        theta_plus_minus(c->T[l + 1], c->T[l], c->R[l + 1], c->R[l], c->tc_kr[l], Mp, Mm);
+        build_theta_tc(Mp, Mm, c->R[l], c->R[l + 1], c->tc_kr[l], c->tc_kr[l], tone);
+        c->tc_off[l] = tall.size() * sizeof(uint16_t);
+        tall.insert(tall.end(), tone.begin(), tone.end());
+      }
+      s = c->tc_amat.ensure(std::max<size_t>(tall.size() * sizeof(uint16_t), 16));
+      if (s == PO_OK) s = c->tc_err.ensure(sizeof(int));
+      if (s == PO_OK && !tall.empty() &&
+          cudaMemcpy(c->tc_amat.p, tall.data(), tall.size() * sizeof(uint16_t), cudaMemcpyHostToDevice) != cudaSuccess)
+        s = fail(PO_ERR_CUDA, "upload of the tcgen05 theta matrices");
+      if (s == PO_OK && cudaMemset(c->tc_err.p, 0, sizeof(int)) != cudaSuccess) s = fail(PO_ERR_CUDA, "cudaMemset");
+      if (s != PO_OK) { po_destroy(c); return s; }
+    }
     s = c->amat.ensure(sizeof(uint32_t) * std::max<size_t>(all.size(), 1));
     if (s == PO_OK && !all.empty() &&
         cudaMemcpy(c->amat.p, all.data(), sizeof(uint32_t) * all.size(), cudaMemcpyHostToDevice) != cudaSuccess)
@@ -374,7 +401,7 @@ po_status po_destroy(po_ctx *c) {
   for (DevBuf *b : {&c->twiddles, &c->geom_in, &c->geom_sorted, &c->octree_ws, &c->leaf_ctr, &c->dirs, &c->dirs_d,
                     &c->trans, &c->levelA, &c->levelB, &c->mid, &c->slots, &c->kvals, &c->out, &c->cur, &c->partial,
                     &c->tile_ctr, &c->amat, &c->bmat, &c->amat_adj, &c->bmat_adj, &c->slots64, &c->grad_acc,
-                    &c->chunk_begin, &c->center0, &c->dir_trig, &c->out_dirs})
+                    &c->chunk_begin, &c->center0, &c->dir_trig, &c->out_dirs, &c->tc_amat, &c->tc_err})
     b->release();
   for (auto &e : c->ev)
     if (e) cudaEventDestroy(e);
@@ -633,8 +660,13 @@ static po_status prepare_solve(po_ctx *c, const po_geometry *g, const po_illum *
   size_t lvl_max = 0, mid_max = 0;
   for (int l = 0; l <= d; ++l)
     lvl_max = std::max(lvl_max, (size_t)P.tree.level[l].count * 6 * (size_t)c->R[l] * c->Phi[l]);
-  for (int l = 0; l < d; ++l)
-    mid_max = std::max(mid_max, (size_t)P.tree.level[l + 1].count * 6 * (size_t)(c->R[l + 1] + 1) * c->Phi[l]);
+  for (int l = 0; l < d; ++l) {
+    // float2 words per slot: R + 1 rows x Phi (packed pairs), or 4 bf16 matrices of
+    // tc_kr x npad (core matrices of the tcgen05 pass) = tc_kr x npad float2
+    const size_t per = c->tc_level[l] ? (size_t)c->tc_kr[l] * theta_tc_npad(c->Phi[l])
+                                      : (size_t)(c->R[l + 1] + 1) * c->Phi[l];
+    mid_max = std::max(mid_max, (size_t)P.tree.level[l + 1].count * 6 * per);
+  }
   P.chunks = plan_chunks(L, G, chunk_slot_count(budget, 8.0 * (2.0 * lvl_max + mid_max), S));
   const int ns_max = P.chunks.front().ns;
   PO_TRY(c->levelA.ensure(sizeof(float2) * lvl_max * ns_max));
@@ -768,7 +800,11 @@ static po_status enqueue_solve(po_ctx *c, const SolvePlan &P, float *out_dev, co
         const float4 *trans = c->trans.as<float4>() + P.tr_off[l] + (size_t)ch.l0 * c->R[l] * c->Phi[l];
         int64_t nrows = (int64_t)ch.ns * nc * 6 * c->R[l + 1];
         PO_TRY(rec(c->kev[2 + 4 * l]));
-        if (c->tensor_theta) {
+        if (c->tc_level[l]) {
+          PO_TRY(launch_interp_rows_core(cur_lvl, c->mid.as<uint8_t>(), (int64_t)ch.ns * nc * 6, c->R[l + 1],
+                                         c->tc_kr[l], theta_tc_npad(c->Phi[l]), c->Phi[l + 1], c->Phi[l],
+                                         c->bmat_kp[l], c->bmat.as<uint32_t>() + c->bmat_off[l], c->sm_count, st));
+        } else if (c->tensor_theta) {
           PO_TRY(launch_interp_rows_packed(cur_lvl, c->mid.as<uint4>(), (int64_t)ch.ns * nc * 6, c->R[l + 1],
                                            c->Phi[l + 1], c->Phi[l], c->bmat_kp[l],
                                            c->bmat.as<uint32_t>() + c->bmat_off[l], c->sm_count, st));
@@ -784,7 +820,11 @@ static po_status enqueue_solve(po_ctx *c, const SolvePlan &P, float *out_dev, co
         if (nrows > 0) ++T.n_row;
         if (np > 0) ++T.n_col;
         PO_TRY(rec(c->kev[4 + 4 * l]));
-        if (c->tensor_theta) {
+        if (c->tc_level[l]) {
+          PO_TRY(launch_theta_tc(c->mid.as<uint8_t>(), nxt, P.tree.level[l].child, np, nc, c->Phi[l], c->tc_kr[l],
+                                 c->R[l], c->tc_amat.as<uint8_t>() + c->tc_off[l], trans, ch.ns, ch.gc,
+                                 c->tc_err.as<int>(), st));
+        } else if (c->tensor_theta) {
           PO_TRY(launch_interp_cols_mma(c->mid.as<uint4>(), nxt, P.tree.level[l].child, np, nc, c->Phi[l],
                                         c->R[l + 1], c->R[l], c->amat_kp[l], c->amat.as<uint32_t>() + c->amat_off[l],
                                         trans, ch.ns, ch.gc, cfg.interp_tile, st));
@@ -833,6 +873,20 @@ static po_status enqueue_solve(po_ctx *c, const SolvePlan &P, float *out_dev, co
   return PO_OK;
 }
 
+// The error word of the tcgen05 theta pass: nonzero when one of its bounded
+// waits gave up (the level's output is then incomplete).  Read after a
+// synchronous solve; an asynchronous solve leaves it for the next check.
+static po_status check_device_waits(po_ctx *c) {
+  bool any = false;
+  for (int l = 0; l < c->depth; ++l) any = any || c->tc_level[l];
+  if (!any) return PO_OK;
+  int h = 0;
+  PO_CUDA(cudaMemcpy(&h, c->tc_err.p, sizeof(int), cudaMemcpyDeviceToHost));
+  if (h == 0) return PO_OK;
+  PO_CUDA(cudaMemset(c->tc_err.p, 0, sizeof(int)));
+  return fail(PO_ERR_TIMEOUT, "tcgen05 theta pass: a device wait timed out");
+}
+
 static po_status solve_impl(po_ctx *c, const po_geometry *g, const po_illum *il, float *intensity, int out_on_device,
                             cudaStream_t st, po_report *rep, const AdjointArgs *adj = nullptr) {
   const int64_t launches0 = g_launch_count;
@@ -851,7 +905,10 @@ static po_status solve_impl(po_ctx *c, const po_geometry *g, const po_illum *il,
   if (intensity && !out_on_device)
     PO_CUDA(cudaMemcpyAsync(intensity, out_dev, sizeof(float) * (size_t)P.S * P.nd_out, cudaMemcpyDeviceToHost, st));
   PO_CUDA(cudaEventRecord(c->ev[5], st));
-  if (rep || !out_on_device) PO_CUDA(cudaEventSynchronize(c->ev[5]));
+  if (rep || !out_on_device) {
+    PO_CUDA(cudaEventSynchronize(c->ev[5]));
+    PO_TRY(check_device_waits(c));
+  }
   PO_CUDA(cudaGetLastError());
   if (rep) {
     float t[2];

@@ -1,0 +1,411 @@
+// po_theta_tc.cu -- theta pass + translation + child sum on the 5th-generation
+// tensor cores (tcgen05, accumulators in tensor memory) for the tree levels
+// with more than 128 parent rows.
+//
+// Same contraction as k_theta_warp (po_interp_mma.cu; util/interpolation.h:47-77,
+// util/fields.h:92-103 and :153-169): for every child of a parent,
+//   U = A_plus S,  V = A_minus D,  Y_j = U + V,  Y_j' = U - V,
+// rotated by the child's translation phasor and summed over the children.
+//
+// One CTA owns one (slot, parent, component), kTcPairs column pairs (N = 128
+// real columns of S and D) and one 128-row tile of the parent, and runs as
+// three roles:
+//  * lane 0 of the last warp streams K chunks of 16 child rows -- the chunk of
+//    the four split theta matrices (A_plus hi, lo, A_minus hi, lo; 16 KB) and
+//    of the child's four split operands (S hi, lo, D hi, lo; 16 KB) -- with
+//    bulk copies (cp.async.bulk) into a ring of kTcStages shared-memory
+//    stages, each completing an mbarrier by transaction bytes;
+//  * the same thread issues the products (hi*hi + hi*lo + lo*hi per matrix
+//    pair: 6 tcgen05.mma of 128 x 128 x 16 per chunk) into one of two U/V
+//    accumulator pairs in tensor memory (one per child parity), commits each
+//    chunk to the stage's "empty" mbarrier and a child's last chunk to the
+//    accumulator's "full" mbarrier;
+//  * 16 epilogue warps (warp w reads tensor-memory lanes 32 (w % 4) .., i.e.
+//    one parent row per thread, and 16 column pairs per warpgroup) read a
+//    finished child's U and V (tcgen05.ld), rotate and accumulate them in
+//    registers and release the accumulator pair, while the next child's
+//    products run into the other pair.
+// The translation phases of the tile ((x, y) per row and pair, z per row) are
+// staged in shared memory once per CTA and serve all children.
+//
+// Operand layouts (bf16, K-major, no swizzle; core matrices of 8 rows x 16 B):
+// a chunk of one matrix is [rows / 8][2][8][8] (row block, k8 block, row,
+// k), i.e. leading-dimension offset 128 B, stride offset 256 B.  The theta
+// matrices are stored as [tile][chunk][matrix][128 / 8][2][8][8]
+// (build_theta_tc); the row pass writes each child pattern as
+// [chunk][matrix][npad / 8][2][8][8] (launch_interp_rows_core), so that one
+// CTA's share of a chunk is one contiguous 4-KB run per matrix.
+//
+// Every wait is bounded in time: on a timeout the kernel records an error
+// word, stops every role, waits (bounded) for its copies and products in
+// flight, frees its tensor memory and returns.
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <vector>
+
+#include "po_common.cuh"
+#include "po_internal.h"
+#include "po_kernels.h"
+
+namespace wavepo {
+
+namespace {
+
+constexpr int kTcKC = 16;                                 // K (child rows) per chunk
+constexpr int kTcPairs = 64;                              // column pairs per CTA
+constexpr int kTcN = 2 * kTcPairs;                        // real columns per product
+constexpr int kTcEpiWarps = kTcPairs / 4;                 // 4 warps per 16 pairs
+constexpr int kTcThreads = 32 * (kTcEpiWarps + 1);        // + the copy / MMA warp
+constexpr int kTcStages = 4;
+constexpr int kAStage = 4 * 128 * kTcKC * 2;              // 16 KB
+constexpr int kBStage = 4 * kTcN * kTcKC * 2;             // 16 KB
+constexpr int kTransBytes = 128 * kTcPairs * 8 + 128 * 4; // (x, y) per row and pair, z per row
+constexpr int kBarOff = kTcStages * (kAStage + kBStage) + kTransBytes;
+constexpr int kTcSmem = kBarOff + 128;                    // + mbarriers, TMEM slot, abort flag
+constexpr uint32_t kTcTmemCols = 4 * kTcN;                // (U, V) x 2 children = 512 columns
+constexpr unsigned long long kTcWaitNs = 1000000000ull;   // time limit of every wait: 1 s
+static_assert(kTcSmem <= 227 * 1024, "shared memory");
+
+__device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// shared-memory matrix descriptor: K-major, no swizzle, LBO 128 B, SBO 256 B
+__device__ __forceinline__ uint64_t tc_desc(uint32_t addr) {
+  return (uint64_t)((addr >> 4) & 0x3FFF) | ((uint64_t)(128 >> 4) << 16) | ((uint64_t)(256 >> 4) << 32) |
+         ((uint64_t)1 << 46);
+}
+
+__device__ __forceinline__ void tc_mma(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+  asm volatile(
+      "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+      "l"(a), "l"(b), "r"(idesc), "r"(acc));
+}
+
+__device__ __forceinline__ void tc_commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar));
+}
+
+__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
+  uint32_t done;
+  asm volatile(
+      "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(done)
+      : "r"(bar), "r"(parity));
+  return done != 0;
+}
+
+// true once the mbarrier has completed the phase of the given parity; false
+// after the time limit, or as soon as another role has given up (abort)
+__device__ bool mbar_wait(uint32_t bar, uint32_t parity, const volatile int *abort) {
+  const unsigned long long t0 = global_ns();
+  for (int it = 0;; ++it) {
+    if (mbar_try(bar, parity)) return true;
+    if ((it & 63) == 63) {
+      if (abort && *abort) return false;
+      if (global_ns() - t0 > kTcWaitNs) return false;
+    }
+  }
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("{\n.reg .b64 st;\nmbarrier.arrive.shared::cta.b64 st, [%0];\n}\n" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("{\n.reg .b64 st;\nmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n}\n" ::"r"(bar),
+               "r"(bytes)
+               : "memory");
+}
+
+// bulk copy global -> shared, completing `bar` by its byte count
+__device__ __forceinline__ void bulk_copy(uint32_t dst, const void *src, uint32_t bytes, uint32_t bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+               "l"(src), "r"(bytes), "r"(bar)
+               : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t (&r)[8]) {
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+               : "r"(taddr));
+}
+
+}  // namespace
+
+// A operand of one level for the tcgen05 pass: the theta matrices A_plus,
+// A_minus over K = child rows padded to Kr (a multiple of 16), split into
+// bf16 hi + lo, Kr KB per 128-row tile.
+size_t theta_tc_bytes(int Rp, int Kr) {
+  const int MT = (Rp + 127) / 128;
+  return (size_t)MT * Kr * 1024;
+}
+
+static uint16_t bf16_bits(float f) {
+  uint32_t u;
+  std::memcpy(&u, &f, 4);
+  if ((u & 0x7f800000u) == 0x7f800000u) return (uint16_t)(u >> 16);
+  return (uint16_t)((u + 0x7fffu + ((u >> 16) & 1u)) >> 16);
+}
+static float bf16_val(uint16_t h) {
+  uint32_t u = (uint32_t)h << 16;
+  float f;
+  std::memcpy(&f, &u, 4);
+  return f;
+}
+
+// Mplus / Mminus: [Rp][ld] (theta_plus_minus), columns >= Rc are zero padding
+void build_theta_tc(const std::vector<double> &Mplus, const std::vector<double> &Mminus, int Rp, int Rc, int ld,
+                    int Kr, std::vector<uint16_t> &out) {
+  out.assign(theta_tc_bytes(Rp, Kr) / 2, 0);
+  const size_t tile = (size_t)Kr * 512, chunk = kAStage / 2, matrix = 128 * kTcKC;  // in bf16 elements
+  for (int r = 0; r < Rp; ++r)
+    for (int k = 0; k < Rc; ++k)
+      for (int pm = 0; pm < 2; ++pm) {
+        const double v = (pm ? Mminus : Mplus)[(size_t)r * ld + k];
+        const uint16_t h = bf16_bits((float)v);
+        const uint16_t l = bf16_bits((float)(v - (double)bf16_val(h)));
+        const int rr = r % 128, kk = k % kTcKC;
+        const size_t base = (size_t)(r / 128) * tile + (size_t)(k / kTcKC) * chunk;
+        const size_t in_mat = ((size_t)(rr / 8) * 2 + kk / 8) * 64 + (rr % 8) * 8 + (kk % 8);
+        out[base + (size_t)(2 * pm) * matrix + in_mat] = h;
+        out[base + (size_t)(2 * pm + 1) * matrix + in_mat] = l;
+      }
+}
+
+// grid.x = task * MT + tile (task = (slot, parent, component, column chunk)), kTcThreads threads
+__global__ void __launch_bounds__(kTcThreads, 1) k_theta_tc(
+    const uint8_t *__restrict__ mid, float2 *__restrict__ parent, const int32_t *__restrict__ child_table,
+    int64_t n_parent, int64_t n_child, int phi, int Kr, int Npad, int Rp, const uint8_t *__restrict__ Atc,
+    const float4 *__restrict__ trans, int G, int n_nc, int64_t n_task, int *__restrict__ err) {
+  extern __shared__ __align__(1024) uint8_t smem_tc[];
+  uint8_t *sA = smem_tc;                                        // [kTcStages][kAStage]
+  uint8_t *sB = smem_tc + kTcStages * kAStage;                  // [kTcStages][kBStage]
+  float2 *sT = (float2 *)(smem_tc + kTcStages * (kAStage + kBStage));  // [kTcPairs][128] (x, y)
+  float *sZ = (float *)(sT + kTcPairs * 128);                   // [128]
+  uint64_t *bars = (uint64_t *)(smem_tc + kBarOff);
+  uint64_t *full = bars, *empty = bars + kTcStages, *accf = bars + 2 * kTcStages, *acce = accf + 2,
+           *drain = acce + 2;
+  uint32_t *tmem_slot = (uint32_t *)(drain + 1);
+  volatile int *abort_flag = (volatile int *)(tmem_slot + 1);
+  __shared__ int32_t s_child[8];
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int MT = (Rp + 127) / 128, KC = Kr / kTcKC;
+  const int mtile = (int)(blockIdx.x % MT);
+  const int64_t task = blockIdx.x / MT;
+  if (task >= n_task) return;
+  const int nc = (int)(task % n_nc);
+  int64_t rest = task / n_nc;
+  const int comp = (int)(rest % 6);
+  rest /= 6;
+  const int64_t p = rest % n_parent;
+  const int slot = (int)(rest / n_parent), lam = slot / G;
+  const int span = phi / 2;
+
+  if (tid < 8) s_child[tid] = child_table[p * 8 + tid];
+  if (tid == 0) {
+    for (int b = 0; b < kTcStages; ++b) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&full[b])));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&empty[b])));
+    }
+    for (int b = 0; b < 2; ++b) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&accf[b])));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(&acce[b])), "r"(kTcEpiWarps * 32));
+    }
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(drain)));
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(tmem_slot)),
+                 "r"(kTcTmemCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  const uint32_t tmem = *tmem_slot;
+  int kids[8], nkids = 0;
+#pragma unroll
+  for (int o = 0; o < 8; ++o)
+    if (s_child[o] >= 0) kids[nkids++] = o;
+  const size_t pat = (size_t)8 * Npad * Kr;  // bytes of one child pattern component (4 matrices)
+  bool ok = true;
+  int last_load[kTcStages];  // last step copied into each stage (copy role)
+#pragma unroll
+  for (int b = 0; b < kTcStages; ++b) last_load[b] = -1;
+
+  if (warp == kTcEpiWarps) {
+    // ---- copy + MMA role: one thread ----
+    if (lane == 0) {
+      const int nsteps = nkids * KC;
+      const uint8_t *mbase = mid + ((size_t)slot * n_child * 6 + comp) * pat;
+      const uint8_t *abase = Atc + (size_t)mtile * Kr * 1024;
+      const uint32_t bmat = kTcN / 8 * 256;  // bytes of one matrix's share of a chunk
+      auto load = [&](int t) -> bool {
+        const int b = t % kTcStages;
+        if (t >= kTcStages && !mbar_wait(smem_addr(&empty[b]), ((t / kTcStages) - 1) & 1, abort_flag)) return false;
+        const int ci = t / KC, kc = t % KC;
+        const uint32_t fb = smem_addr(&full[b]);
+        mbar_expect_tx(fb, kAStage + 4 * bmat);
+        bulk_copy(smem_addr(sA + b * kAStage), abase + (size_t)kc * kAStage, kAStage, fb);
+        const uint8_t *cb = mbase + (size_t)s_child[kids[ci]] * 6 * pat + (size_t)kc * 128 * Npad +
+                            (size_t)nc * bmat;
+#pragma unroll
+        for (int m = 0; m < 4; ++m)
+          bulk_copy(smem_addr(sB + b * kBStage + m * bmat), cb + (size_t)m * 32 * Npad, bmat, fb);
+        last_load[b] = t;
+        return true;
+      };
+      // D f32, A and B bf16, both K-major, N = kTcN, M = 128
+      const uint32_t idesc =
+          (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kTcN >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
+      for (int t = 0; t < kTcStages - 1 && t < nsteps && ok; ++t) ok = load(t);
+      for (int s = 0; s < nsteps && ok; ++s) {
+        const int b = s % kTcStages, ci = s / KC, kc = s % KC;
+        if (kc == 0 && ci >= 2 && !mbar_wait(smem_addr(&acce[ci & 1]), ((ci >> 1) - 1) & 1, abort_flag)) {
+          ok = false;
+          break;
+        }
+        if (!mbar_wait(smem_addr(&full[b]), (s / kTcStages) & 1, abort_flag)) {
+          ok = false;
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        const uint32_t dU = tmem + (uint32_t)((ci & 1) * 2 * kTcN), dV = dU + kTcN;
+        const uint32_t a0 = smem_addr(sA + b * kAStage), b0 = smem_addr(sB + b * kBStage);
+        const uint32_t first = kc == 0 ? 0u : 1u;
+        const uint32_t am = kAStage / 4, bm = kBStage / 4;
+        tc_mma(dU, tc_desc(a0), tc_desc(b0), idesc, first);                       // A+ hi * S hi
+        tc_mma(dV, tc_desc(a0 + 2 * am), tc_desc(b0 + 2 * bm), idesc, first);     // A- hi * D hi
+        tc_mma(dU, tc_desc(a0), tc_desc(b0 + bm), idesc, 1u);                     // A+ hi * S lo
+        tc_mma(dV, tc_desc(a0 + 2 * am), tc_desc(b0 + 3 * bm), idesc, 1u);        // A- hi * D lo
+        tc_mma(dU, tc_desc(a0 + am), tc_desc(b0), idesc, 1u);                     // A+ lo * S hi
+        tc_mma(dV, tc_desc(a0 + 3 * am), tc_desc(b0 + 2 * bm), idesc, 1u);        // A- lo * D hi
+        tc_commit(smem_addr(&empty[b]));
+        if (kc == KC - 1) tc_commit(smem_addr(&accf[ci & 1]));
+        if (s + kTcStages - 1 < nsteps && !load(s + kTcStages - 1)) ok = false;
+      }
+      if (!ok) {
+        *abort_flag = 1;
+        atomicExch(err, 1);
+      }
+    }
+    __syncwarp();
+  } else {
+    // ---- epilogue role: thread = parent row, warpgroup = 16 column pairs ----
+    const int wg = warp >> 2, quarter = warp & 3, rl = quarter * 32 + lane;
+    const int r = mtile * 128 + rl;
+    {
+      const float4 *tr = trans + (int64_t)lam * Rp * phi;
+      for (int e = tid; e < 128 * kTcPairs; e += kTcEpiWarps * 32) {
+        const int row = e & 127, pl = e >> 7;
+        const int rr = mtile * 128 + row < Rp ? mtile * 128 + row : Rp - 1;
+        const int jq = nc * kTcPairs + pl < span ? nc * kTcPairs + pl : span - 1;
+        const float4 v = __ldg(tr + (int64_t)rr * phi + jq);
+        sT[pl * 128 + row] = make_float2(v.x, v.y);
+        if (pl == 0) sZ[row] = v.z;
+      }
+      asm volatile("bar.sync 1, %0;" ::"r"(kTcEpiWarps * 32));
+    }
+    float acc[16][2][2];
+#pragma unroll
+    for (int q = 0; q < 16; ++q) acc[q][0][0] = acc[q][0][1] = acc[q][1][0] = acc[q][1][1] = 0.f;
+    const float z = sZ[rl];
+    for (int ci = 0; ci < nkids && ok; ++ci) {
+      const int b = ci & 1;
+      ok = __all_sync(0xffffffffu, mbar_wait(smem_addr(&accf[b]), (ci >> 1) & 1, abort_flag)) != 0;
+      if (!ok) break;
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      const int o = kids[ci];
+      const float sgx = (o & 1) ? 1.f : -1.f, sgy = (o & 2) ? -1.f : 1.f, pz = (o & 4) ? -z : z;
+      const uint32_t ta = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(b * 2 * kTcN + 32 * wg);
+#pragma unroll
+      for (int h = 0; h < 4; ++h) {  // 4 column pairs at a time
+        uint32_t u[8], v[8];
+        tmem_ld8(ta + 8 * h, u);
+        tmem_ld8(ta + kTcN + 8 * h, v);
+        asm volatile("tcgen05.wait::ld.sync.aligned;");
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int pl = 16 * wg + 4 * h + q;
+          const float2 xy = sT[pl * 128 + rl];
+          const float pxy = fmaf(sgx, xy.x, sgy * xy.y);
+          const float ur = __uint_as_float(u[2 * q]), ui = __uint_as_float(u[2 * q + 1]);
+          const float vr = __uint_as_float(v[2 * q]), vi = __uint_as_float(v[2 * q + 1]);
+#pragma unroll
+          for (int w = 0; w < 2; ++w) {
+            // table phases are reduced to [-pi, pi], so |pz +- pxy| <= 3 pi
+            float sn, cs;
+            __sincosf(w ? pz - pxy : pz + pxy, &sn, &cs);
+            const float yr = w ? ur - vr : ur + vr, yi = w ? ui - vi : ui + vi;
+            acc[4 * h + q][w][0] += yr * cs - yi * sn;
+            acc[4 * h + q][w][1] += yr * sn + yi * cs;
+          }
+        }
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;");
+      mbar_arrive(smem_addr(&acce[b]));
+    }
+    if (!ok) {
+      *abort_flag = 1;
+      if (lane == 0) atomicExch(err, 1);
+    } else if (r < Rp) {
+      float2 *out = parent + (((int64_t)slot * n_parent + p) * 6 + comp) * (int64_t)Rp * phi + (int64_t)r * phi;
+#pragma unroll
+      for (int q = 0; q < 16; ++q) {
+        const int jq = nc * kTcPairs + 16 * wg + q;
+        if (jq < span) {
+          out[jq] = make_float2(acc[q][0][0], acc[q][0][1]);
+          out[jq + span] = make_float2(acc[q][1][0], acc[q][1][1]);
+        }
+      }
+    }
+  }
+  __syncthreads();  // every role done
+  if (warp == kTcEpiWarps && lane == 0 && *abort_flag) {
+    // let the copies and products in flight land before the memory is released
+    for (int b = 0; b < kTcStages; ++b)
+      if (last_load[b] >= 0) (void)mbar_wait(smem_addr(&full[b]), (last_load[b] / kTcStages) & 1, nullptr);
+    tc_commit(smem_addr(drain));
+    (void)mbar_wait(smem_addr(drain), 0, nullptr);
+  }
+  __syncwarp();
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTcTmemCols));
+}
+
+po_status init_theta_tc_attributes() {
+  PO_CUDA(cudaFuncSetAttribute(k_theta_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem));
+  return PO_OK;
+}
+
+// Columns of the core-matrix child operands: 2 x Phi/2 real columns rounded up
+// to whole column chunks of the CTA.
+int theta_tc_npad(int phi) { return (phi + kTcN - 1) / kTcN * kTcN; }
+
+po_status launch_theta_tc(const uint8_t *mid, float2 *parent, const int32_t *child_table, int64_t n_parent,
+                          int64_t n_child, int phi, int Kr, int Rp, const uint8_t *Atc, const float4 *trans,
+                          int n_slots, int G, int *err, cudaStream_t st) {
+  if (n_parent <= 0 || n_slots <= 0) return PO_OK;
+  if (phi % 2 || Kr % kTcKC || Kr <= 0) return fail(PO_ERR_INTERNAL, "tcgen05 theta pass: grid");
+  const int MT = (Rp + 127) / 128, n_nc = (phi / 2 + kTcPairs - 1) / kTcPairs;
+  const int64_t n_task = (int64_t)n_slots * n_parent * 6 * n_nc;
+  const int64_t gx = n_task * MT;
+  if (gx > 2147483647LL) return fail(PO_ERR_UNSUPPORTED, "too many nodes for one launch");
+  k_theta_tc<<<(unsigned)gx, kTcThreads, kTcSmem, st>>>(mid, parent, child_table, n_parent, n_child, phi, Kr,
+                                                         theta_tc_npad(phi), Rp, Atc, trans, G, n_nc, n_task, err);
+  count_launch();
+  PO_CUDA(cudaGetLastError());
+  return PO_OK;
+}
+
+}  // namespace wavepo
