@@ -98,7 +98,7 @@ void build_theta_tc(const std::vector<double> &Mplus, const std::vector<double> 
 po_status init_theta_tc_attributes();
 po_status launch_theta_tc(const uint8_t *mid, float2 *parent, const int32_t *child_table, int64_t n_parent,
                           int64_t n_child, int phi, int Kr, int Rp, const uint8_t *Atc, const float4 *trans,
-                          int n_slots, int G, int *err, cudaStream_t st);
+                          int n_slots, int G, int *err, size_t mid_bytes, size_t atc_bytes, cudaStream_t st);
 // adjoint (transposed) passes, double cover only (po_interp_mma.cu)
 void build_theta_matrix_adj(int Tc, int Tp, int Rc, int Rp, int Kp, std::vector<uint32_t> &out);
 void build_phi_matrix_adj(int Pc, int Pp, int Kp, std::vector<uint32_t> &out);

@@ -237,6 +237,12 @@ po_status po_config_init(po_config *cfg, int max_depth, int n_theta_out, int n_p
   return PO_OK;
 }
 
+// The tcgen05 theta pass works on 128-row tiles of the parent; it serves the
+// levels whose rows fill at least 3/4 of their tiles, the others keep the
+// warp-level kernel, whose 16-row tiles waste fewer rows (on the ellipsoid
+// workload: 109-, 201- and 361-row levels on tcgen05, 63 rows and fewer not).
+static bool theta_on_tcgen05(int rows) { return rows * 4 >= 3 * 128 * ((rows + 127) / 128); }
+
 po_status po_create(po_ctx **out, const po_config *cfg) {
   if (!out || !cfg) return fail(PO_ERR_INVALID_ARGUMENT, "null argument");
   *out = nullptr;
@@ -351,12 +357,12 @@ po_status po_create(po_ctx **out, const po_config *cfg) {
       c->amat_off[l] = all.size();
       all.insert(all.end(), one.begin(), one.end());
     }
-    // levels with more than 128 parent rows: theta chunks for the tcgen05 pass
+    // theta chunks of the levels on the tcgen05 pass
     {
       std::vector<uint16_t> tall, tone;
       std::vector<double> Mp, Mm;
       for (int l = 0; l < d; ++l) {
-        if (c->R[l] <= 128) continue;
+        if (!theta_on_tcgen05(c->R[l])) continue;
         c->tc_level[l] = true;
         c->tc_kr[l] = (c->R[l + 1] + 15) / 16 * 16;
         theta_plus_minus(c->T[l + 1], c->T[l], c->R[l + 1], c->R[l], c->tc_kr[l], Mp, Mm);
@@ -823,7 +829,7 @@ static po_status enqueue_solve(po_ctx *c, const SolvePlan &P, float *out_dev, co
         if (c->tc_level[l]) {
           PO_TRY(launch_theta_tc(c->mid.as<uint8_t>(), nxt, P.tree.level[l].child, np, nc, c->Phi[l], c->tc_kr[l],
                                  c->R[l], c->tc_amat.as<uint8_t>() + c->tc_off[l], trans, ch.ns, ch.gc,
-                                 c->tc_err.as<int>(), st));
+                                 c->tc_err.as<int>(), c->mid.bytes, c->tc_amat.bytes - c->tc_off[l], st));
         } else if (c->tensor_theta) {
           PO_TRY(launch_interp_cols_mma(c->mid.as<uint4>(), nxt, P.tree.level[l].child, np, nc, c->Phi[l],
                                         c->R[l + 1], c->R[l], c->amat_kp[l], c->amat.as<uint32_t>() + c->amat_off[l],
@@ -884,6 +890,7 @@ static po_status check_device_waits(po_ctx *c) {
   PO_CUDA(cudaMemcpy(&h, c->tc_err.p, sizeof(int), cudaMemcpyDeviceToHost));
   if (h == 0) return PO_OK;
   PO_CUDA(cudaMemset(c->tc_err.p, 0, sizeof(int)));
+  if (h == 2) return fail(PO_ERR_INTERNAL, "tcgen05 theta pass: operand run outside its buffer");
   return fail(PO_ERR_TIMEOUT, "tcgen05 theta pass: a device wait timed out");
 }
 

@@ -1,6 +1,6 @@
 // po_theta_tc.cu -- theta pass + translation + child sum on the 5th-generation
 // tensor cores (tcgen05, accumulators in tensor memory) for the tree levels
-// with more than 128 parent rows.
+// whose parent rows fill 128-row tiles.
 //
 // Same contraction as k_theta_warp (po_interp_mma.cu; util/interpolation.h:47-77,
 // util/fields.h:92-103 and :153-169): for every child of a parent,
@@ -10,23 +10,28 @@
 // One CTA owns one (slot, parent, component), kTcPairs column pairs (N = 128
 // real columns of S and D) and one 128-row tile of the parent, and runs as
 // three roles:
-//  * lane 0 of the last warp streams K chunks of 16 child rows -- the chunk of
+//  * copy warp (one thread): streams K chunks of 16 child rows -- the chunk of
 //    the four split theta matrices (A_plus hi, lo, A_minus hi, lo; 16 KB) and
 //    of the child's four split operands (S hi, lo, D hi, lo; 16 KB) -- with
-//    bulk copies (cp.async.bulk) into a ring of kTcStages shared-memory
-//    stages, each completing an mbarrier by transaction bytes;
-//  * the same thread issues the products (hi*hi + hi*lo + lo*hi per matrix
-//    pair: 6 tcgen05.mma of 128 x 128 x 16 per chunk) into one of two U/V
-//    accumulator pairs in tensor memory (one per child parity), commits each
-//    chunk to the stage's "empty" mbarrier and a child's last chunk to the
-//    accumulator's "full" mbarrier;
+//    bulk copies (cp.async.bulk) into a ring of shared-memory stages, each
+//    completing the stage's "full" mbarrier by transaction bytes;
+//  * MMA warp (one thread): issues the products (hi*hi + hi*lo + lo*hi per
+//    matrix pair: 6 tcgen05.mma of 128 x 128 x 16 per chunk) into one of two
+//    U/V accumulator pairs in tensor memory (one per child parity), commits
+//    each chunk to the stage's "empty" mbarrier and a child's last chunk to
+//    the accumulator's "full" mbarrier;
 //  * 16 epilogue warps (warp w reads tensor-memory lanes 32 (w % 4) .., i.e.
-//    one parent row per thread, and 16 column pairs per warpgroup) read a
+//    one parent row per thread, and 16 column pairs per warpgroup): read a
 //    finished child's U and V (tcgen05.ld), rotate and accumulate them in
 //    registers and release the accumulator pair, while the next child's
 //    products run into the other pair.
-// The translation phases of the tile ((x, y) per row and pair, z per row) are
-// staged in shared memory once per CTA and serve all children.
+// The child's phasor at (row, column j) is e^{i (sz z + sx x + sy y)} and at
+// the mirror column e^{i (sz z - sx x - sy y)}, with the octant's signs s and
+// the reduced phases (x, y, z) of the translation table.  Once per CTA the
+// epilogue warps stage per (row, pair) either e^{i (x + y)} and e^{i (x - y)}
+// (kTable: the octant's phasor is one of them or its conjugate, so a child
+// costs no sincos per element) or (x, y) (one sincos per element), and
+// e^{i z} per row.
 //
 // Operand layouts (bf16, K-major, no swizzle; core matrices of 8 rows x 16 B):
 // a chunk of one matrix is [rows / 8][2][8][8] (row block, k8 block, row,
@@ -36,9 +41,11 @@
 // [chunk][matrix][npad / 8][2][8][8] (launch_interp_rows_core), so that one
 // CTA's share of a chunk is one contiguous 4-KB run per matrix.
 //
-// Every wait is bounded in time: on a timeout the kernel records an error
-// word, stops every role, waits (bounded) for its copies and products in
-// flight, frees its tensor memory and returns.
+// Every wait is bounded in time: on a timeout the kernel records error word 1
+// and every role stops.  Operand runs outside their buffers (checked once per
+// CTA) record error word 2 and nothing is copied.  Before the CTA exits, the
+// copy and MMA threads wait for the last phase of every barrier they armed, so
+// that no copy or commit arrive outlives the CTA.
 #include <cuda_runtime.h>
 
 #include <cstring>
@@ -56,16 +63,26 @@ constexpr int kTcKC = 16;                                 // K (child rows) per 
 constexpr int kTcPairs = 64;                              // column pairs per CTA
 constexpr int kTcN = 2 * kTcPairs;                        // real columns per product
 constexpr int kTcEpiWarps = kTcPairs / 4;                 // 4 warps per 16 pairs
-constexpr int kTcThreads = 32 * (kTcEpiWarps + 1);        // + the copy / MMA warp
-constexpr int kTcStages = 4;
+constexpr int kTcCopyWarp = kTcEpiWarps, kTcMmaWarp = kTcEpiWarps + 1;
+constexpr int kTcThreads = 32 * (kTcEpiWarps + 2);
 constexpr int kAStage = 4 * 128 * kTcKC * 2;              // 16 KB
 constexpr int kBStage = 4 * kTcN * kTcKC * 2;             // 16 KB
-constexpr int kTransBytes = 128 * kTcPairs * 8 + 128 * 4; // (x, y) per row and pair, z per row
-constexpr int kBarOff = kTcStages * (kAStage + kBStage) + kTransBytes;
-constexpr int kTcSmem = kBarOff + 128;                    // + mbarriers, TMEM slot, abort flag
 constexpr uint32_t kTcTmemCols = 4 * kTcN;                // (U, V) x 2 children = 512 columns
 constexpr unsigned long long kTcWaitNs = 1000000000ull;   // time limit of every wait: 1 s
-static_assert(kTcSmem <= 227 * 1024, "shared memory");
+constexpr bool kTcUseTable = false;                       // phasor tables (see above)
+
+// shared-memory plan of one variant of the kernel
+template <bool kTable>
+struct TcPlan {
+  static constexpr int stages = kTable ? 3 : 4;
+  static constexpr int table = kTable ? 2 * kTcPairs * 128 * 8 : kTcPairs * 128 * 8;  // float2 per (row, pair)
+  static constexpr int table_off = stages * (kAStage + kBStage);
+  static constexpr int pz_off = table_off + table;        // e^{i z} per row
+  static constexpr int bar_off = pz_off + 128 * 8;
+  static constexpr int smem = bar_off + 128;              // + mbarriers, TMEM slot, abort flag
+};
+static_assert(TcPlan<true>::smem + 128 <= 227 * 1024, "shared memory (dynamic + the static child table)");
+static_assert(TcPlan<false>::smem + 128 <= 227 * 1024, "shared memory (dynamic + the static child table)");
 
 __device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -131,10 +148,17 @@ __device__ __forceinline__ void bulk_copy(uint32_t dst, const void *src, uint32_
                : "memory");
 }
 
-__device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t (&r)[8]) {
-  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
-               : "r"(taddr));
+// 8 columns of U at ta_u and of V at ta_v for this warp's 32 lanes.  The loads
+// and their wait are one asm statement, so that no compiler-placed instruction
+// can touch a destination register while the asynchronous load is writing it.
+__device__ __forceinline__ void tmem_ld8x2(uint32_t ta_u, uint32_t ta_v, uint32_t (&u)[8], uint32_t (&v)[8]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%16];\n"
+      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%8,%9,%10,%11,%12,%13,%14,%15}, [%17];\n"
+      "tcgen05.wait::ld.sync.aligned;\n"
+      : "=r"(u[0]), "=r"(u[1]), "=r"(u[2]), "=r"(u[3]), "=r"(u[4]), "=r"(u[5]), "=r"(u[6]), "=r"(u[7]), "=r"(v[0]),
+        "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7])
+      : "r"(ta_u), "r"(ta_v));
 }
 
 }  // namespace
@@ -180,19 +204,22 @@ void build_theta_tc(const std::vector<double> &Mplus, const std::vector<double> 
 }
 
 // grid.x = task * MT + tile (task = (slot, parent, component, column chunk)), kTcThreads threads
+template <bool kTable>
 __global__ void __launch_bounds__(kTcThreads, 1) k_theta_tc(
     const uint8_t *__restrict__ mid, float2 *__restrict__ parent, const int32_t *__restrict__ child_table,
     int64_t n_parent, int64_t n_child, int phi, int Kr, int Npad, int Rp, const uint8_t *__restrict__ Atc,
-    const float4 *__restrict__ trans, int G, int n_nc, int64_t n_task, int *__restrict__ err) {
-  extern __shared__ __align__(1024) uint8_t smem_tc[];
-  uint8_t *sA = smem_tc;                                        // [kTcStages][kAStage]
-  uint8_t *sB = smem_tc + kTcStages * kAStage;                  // [kTcStages][kBStage]
-  float2 *sT = (float2 *)(smem_tc + kTcStages * (kAStage + kBStage));  // [kTcPairs][128] (x, y)
-  float *sZ = (float *)(sT + kTcPairs * 128);                   // [128]
-  uint64_t *bars = (uint64_t *)(smem_tc + kBarOff);
-  uint64_t *full = bars, *empty = bars + kTcStages, *accf = bars + 2 * kTcStages, *acce = accf + 2,
-           *drain = acce + 2;
-  uint32_t *tmem_slot = (uint32_t *)(drain + 1);
+    const float4 *__restrict__ trans, int G, int n_nc, int64_t n_task, int *__restrict__ err, size_t mid_bytes,
+    size_t atc_bytes) {
+  using Plan = TcPlan<kTable>;
+  constexpr int NST = Plan::stages;
+  extern __shared__ __align__(128) uint8_t smem_tc[];
+  uint8_t *sA = smem_tc;                                     // [NST][kAStage]
+  uint8_t *sB = smem_tc + NST * kAStage;                     // [NST][kBStage]
+  float2 *sT = (float2 *)(smem_tc + Plan::table_off);        // [2][kTcPairs][128] or [kTcPairs][128]
+  float2 *sPz = (float2 *)(smem_tc + Plan::pz_off);          // [128]
+  uint64_t *full = (uint64_t *)(smem_tc + Plan::bar_off), *empty = full + NST, *accf = empty + NST,
+           *acce = accf + 2;
+  uint32_t *tmem_slot = (uint32_t *)(acce + 2);
   volatile int *abort_flag = (volatile int *)(tmem_slot + 1);
   __shared__ int32_t s_child[8];
 
@@ -211,7 +238,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_theta_tc(
 
   if (tid < 8) s_child[tid] = child_table[p * 8 + tid];
   if (tid == 0) {
-    for (int b = 0; b < kTcStages; ++b) {
+    for (int b = 0; b < NST; ++b) {
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&full[b])));
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&empty[b])));
     }
@@ -219,7 +246,6 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_theta_tc(
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&accf[b])));
       asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(&acce[b])), "r"(kTcEpiWarps * 32));
     }
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(drain)));
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;");
   }
@@ -236,67 +262,99 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_theta_tc(
 #pragma unroll
   for (int o = 0; o < 8; ++o)
     if (s_child[o] >= 0) kids[nkids++] = o;
+  const int nsteps = nkids * KC;
   const size_t pat = (size_t)8 * Npad * Kr;  // bytes of one child pattern component (4 matrices)
-  bool ok = true;
-  int last_load[kTcStages];  // last step copied into each stage (copy role)
-#pragma unroll
-  for (int b = 0; b < kTcStages; ++b) last_load[b] = -1;
 
-  if (warp == kTcEpiWarps) {
-    // ---- copy + MMA role: one thread ----
+  if (warp == kTcCopyWarp) {
+    // ---- copy role ----
     if (lane == 0) {
-      const int nsteps = nkids * KC;
-      const uint8_t *mbase = mid + ((size_t)slot * n_child * 6 + comp) * pat;
+      int last_load[NST];
+#pragma unroll
+      for (int b = 0; b < NST; ++b) last_load[b] = -1;
+      bool ok = (size_t)(mtile + 1) * Kr * 1024 <= atc_bytes;
+      for (int i = 0; i < nkids; ++i) {
+        const int64_t ch = s_child[kids[i]];
+        ok = ok && ch < n_child && ((((size_t)slot * n_child + ch) * 6 + comp) + 1) * pat <= mid_bytes;
+      }
+      if (!ok) {
+        atomicExch(err, 2);
+        *abort_flag = 1;
+      }
       const uint8_t *abase = Atc + (size_t)mtile * Kr * 1024;
-      const uint32_t bmat = kTcN / 8 * 256;  // bytes of one matrix's share of a chunk
-      auto load = [&](int t) -> bool {
-        const int b = t % kTcStages;
-        if (t >= kTcStages && !mbar_wait(smem_addr(&empty[b]), ((t / kTcStages) - 1) & 1, abort_flag)) return false;
-        const int ci = t / KC, kc = t % KC;
+      const size_t comp_off = (size_t)nc * (kTcN / 8) * 256;
+      constexpr uint32_t bmat = kTcN / 8 * 256;  // bytes of one matrix's share of a chunk
+      for (int t = 0; t < nsteps && ok; ++t) {
+        const int b = t % NST, ci = t / KC, kc = t % KC;
+        if (t >= NST && !mbar_wait(smem_addr(&empty[b]), ((t / NST) - 1) & 1, abort_flag)) {
+          ok = false;
+          break;
+        }
         const uint32_t fb = smem_addr(&full[b]);
         mbar_expect_tx(fb, kAStage + 4 * bmat);
         bulk_copy(smem_addr(sA + b * kAStage), abase + (size_t)kc * kAStage, kAStage, fb);
-        const uint8_t *cb = mbase + (size_t)s_child[kids[ci]] * 6 * pat + (size_t)kc * 128 * Npad +
-                            (size_t)nc * bmat;
+        const uint8_t *cb = mid + (((size_t)slot * n_child + s_child[kids[ci]]) * 6 + comp) * pat +
+                            (size_t)kc * 128 * Npad + comp_off;
 #pragma unroll
         for (int m = 0; m < 4; ++m)
           bulk_copy(smem_addr(sB + b * kBStage + m * bmat), cb + (size_t)m * 32 * Npad, bmat, fb);
         last_load[b] = t;
-        return true;
-      };
+      }
+      if (!ok && !*abort_flag) {
+        *abort_flag = 1;
+        atomicCAS(err, 0, 1);
+      }
+      // every copy lands before the CTA exits
+      for (int b = 0; b < NST; ++b)
+        if (last_load[b] >= 0) (void)mbar_wait(smem_addr(&full[b]), (last_load[b] / NST) & 1, nullptr);
+    }
+    __syncwarp();
+  } else if (warp == kTcMmaWarp) {
+    // ---- MMA role ----
+    if (lane == 0) {
       // D f32, A and B bf16, both K-major, N = kTcN, M = 128
       const uint32_t idesc =
           (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kTcN >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
-      for (int t = 0; t < kTcStages - 1 && t < nsteps && ok; ++t) ok = load(t);
-      for (int s = 0; s < nsteps && ok; ++s) {
-        const int b = s % kTcStages, ci = s / KC, kc = s % KC;
+      const uint64_t ad0 = tc_desc(smem_addr(sA)), bd0 = tc_desc(smem_addr(sB));
+      constexpr uint64_t mA = (kAStage / 4) >> 4, mB = (kBStage / 4) >> 4;  // one matrix, in descriptor units
+      bool ok = true;
+      int committed = 0;
+      for (int s = 0; s < nsteps; ++s) {
+        const int b = s % NST, ci = s / KC, kc = s % KC;
         if (kc == 0 && ci >= 2 && !mbar_wait(smem_addr(&acce[ci & 1]), ((ci >> 1) - 1) & 1, abort_flag)) {
           ok = false;
           break;
         }
-        if (!mbar_wait(smem_addr(&full[b]), (s / kTcStages) & 1, abort_flag)) {
+        if (!mbar_wait(smem_addr(&full[b]), (s / NST) & 1, abort_flag)) {
           ok = false;
           break;
         }
         asm volatile("tcgen05.fence::after_thread_sync;");
         const uint32_t dU = tmem + (uint32_t)((ci & 1) * 2 * kTcN), dV = dU + kTcN;
-        const uint32_t a0 = smem_addr(sA + b * kAStage), b0 = smem_addr(sB + b * kBStage);
+        const uint64_t ad = ad0 + (uint64_t)b * (kAStage >> 4), bd = bd0 + (uint64_t)b * (kBStage >> 4);
         const uint32_t first = kc == 0 ? 0u : 1u;
-        const uint32_t am = kAStage / 4, bm = kBStage / 4;
-        tc_mma(dU, tc_desc(a0), tc_desc(b0), idesc, first);                       // A+ hi * S hi
-        tc_mma(dV, tc_desc(a0 + 2 * am), tc_desc(b0 + 2 * bm), idesc, first);     // A- hi * D hi
-        tc_mma(dU, tc_desc(a0), tc_desc(b0 + bm), idesc, 1u);                     // A+ hi * S lo
-        tc_mma(dV, tc_desc(a0 + 2 * am), tc_desc(b0 + 3 * bm), idesc, 1u);        // A- hi * D lo
-        tc_mma(dU, tc_desc(a0 + am), tc_desc(b0), idesc, 1u);                     // A+ lo * S hi
-        tc_mma(dV, tc_desc(a0 + 3 * am), tc_desc(b0 + 2 * bm), idesc, 1u);        // A- lo * D hi
+        tc_mma(dU, ad, bd, idesc, first);                        // A+ hi * S hi
+        tc_mma(dV, ad + 2 * mA, bd + 2 * mB, idesc, first);      // A- hi * D hi
+        tc_mma(dU, ad, bd + mB, idesc, 1u);                      // A+ hi * S lo
+        tc_mma(dV, ad + 2 * mA, bd + 3 * mB, idesc, 1u);         // A- hi * D lo
+        tc_mma(dU, ad + mA, bd, idesc, 1u);                      // A+ lo * S hi
+        tc_mma(dV, ad + 3 * mA, bd + 2 * mB, idesc, 1u);         // A- lo * D hi
         tc_commit(smem_addr(&empty[b]));
         if (kc == KC - 1) tc_commit(smem_addr(&accf[ci & 1]));
-        if (s + kTcStages - 1 < nsteps && !load(s + kTcStages - 1)) ok = false;
+        committed = s + 1;
       }
-      if (!ok) {
+      if (!ok && !*abort_flag) {
         *abort_flag = 1;
-        atomicExch(err, 1);
+        atomicCAS(err, 0, 1);
       }
+      // every commit arrive lands before the CTA exits (only the latest phase
+      // of each barrier is waited on)
+      for (int b = 0; b < NST; ++b) {
+        const int ls = committed - 1 - (((committed - 1 - b) % NST) + NST) % NST;
+        if (ls >= 0) (void)mbar_wait(smem_addr(&empty[b]), (ls / NST) & 1, nullptr);
+      }
+      const int done_kids = committed / KC;
+      for (int ci = done_kids - 2 > 0 ? done_kids - 2 : 0; ci < done_kids; ++ci)
+        (void)mbar_wait(smem_addr(&accf[ci & 1]), (ci >> 1) & 1, nullptr);
     }
     __syncwarp();
   } else {
@@ -310,45 +368,68 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_theta_tc(
         const int rr = mtile * 128 + row < Rp ? mtile * 128 + row : Rp - 1;
         const int jq = nc * kTcPairs + pl < span ? nc * kTcPairs + pl : span - 1;
         const float4 v = __ldg(tr + (int64_t)rr * phi + jq);
-        sT[pl * 128 + row] = make_float2(v.x, v.y);
-        if (pl == 0) sZ[row] = v.z;
+        if (kTable) {
+          float s1, c1, s2, c2;
+          sincosf(v.x + v.y, &s1, &c1);
+          sincosf(v.x - v.y, &s2, &c2);
+          sT[pl * 128 + row] = make_float2(c1, s1);
+          sT[(kTcPairs + pl) * 128 + row] = make_float2(c2, s2);
+        } else {
+          sT[pl * 128 + row] = make_float2(v.x, v.y);
+        }
+        if (pl == 0) {
+          float sz, cz;
+          sincosf(v.z, &sz, &cz);
+          sPz[row] = make_float2(cz, sz);
+        }
       }
       asm volatile("bar.sync 1, %0;" ::"r"(kTcEpiWarps * 32));
     }
     float acc[16][2][2];
 #pragma unroll
     for (int q = 0; q < 16; ++q) acc[q][0][0] = acc[q][0][1] = acc[q][1][0] = acc[q][1][1] = 0.f;
-    const float z = sZ[rl];
+    const float2 ez = sPz[rl];
+    bool ok = true;
     for (int ci = 0; ci < nkids && ok; ++ci) {
       const int b = ci & 1;
       ok = __all_sync(0xffffffffu, mbar_wait(smem_addr(&accf[b]), (ci >> 1) & 1, abort_flag)) != 0;
       if (!ok) break;
       asm volatile("tcgen05.fence::after_thread_sync;");
       const int o = kids[ci];
-      const float sgx = (o & 1) ? 1.f : -1.f, sgy = (o & 2) ? -1.f : 1.f, pz = (o & 4) ? -z : z;
+      // octant signs: x + for o & 1, y + for !(o & 2), z + for !(o & 4)
+      const bool px = (o & 1) != 0, py = (o & 2) == 0;
+      const float pzr = ez.x, pzi = (o & 4) ? -ez.y : ez.y;
+      const float2 *tab = sT + (kTable && px != py ? kTcPairs * 128 : 0);
+      const float cj = px ? 1.f : -1.f;  // table phasor or its conjugate
+      const float sgx = px ? 1.f : -1.f, sgy = py ? 1.f : -1.f;
       const uint32_t ta = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(b * 2 * kTcN + 32 * wg);
 #pragma unroll
       for (int h = 0; h < 4; ++h) {  // 4 column pairs at a time
         uint32_t u[8], v[8];
-        tmem_ld8(ta + 8 * h, u);
-        tmem_ld8(ta + kTcN + 8 * h, v);
-        asm volatile("tcgen05.wait::ld.sync.aligned;");
+        tmem_ld8x2(ta + 8 * h, ta + kTcN + 8 * h, u, v);
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
           const int pl = 16 * wg + 4 * h + q;
-          const float2 xy = sT[pl * 128 + rl];
-          const float pxy = fmaf(sgx, xy.x, sgy * xy.y);
+          float er, ei;  // e^{i (sx x + sy y)}
+          if (kTable) {
+            const float2 t = tab[pl * 128 + rl];
+            er = t.x;
+            ei = cj * t.y;
+          } else {
+            const float2 xy = sT[pl * 128 + rl];
+            // reduced phases: |sx x + sy y| <= 2 pi
+            __sincosf(fmaf(sgx, xy.x, sgy * xy.y), &ei, &er);
+          }
+          // column j: e^{i z'} e;  mirror column: e^{i z'} conj(e)
+          const float w1r = pzr * er - pzi * ei, w1i = pzr * ei + pzi * er;
+          const float w2r = pzr * er + pzi * ei, w2i = pzi * er - pzr * ei;
           const float ur = __uint_as_float(u[2 * q]), ui = __uint_as_float(u[2 * q + 1]);
           const float vr = __uint_as_float(v[2 * q]), vi = __uint_as_float(v[2 * q + 1]);
-#pragma unroll
-          for (int w = 0; w < 2; ++w) {
-            // table phases are reduced to [-pi, pi], so |pz +- pxy| <= 3 pi
-            float sn, cs;
-            __sincosf(w ? pz - pxy : pz + pxy, &sn, &cs);
-            const float yr = w ? ur - vr : ur + vr, yi = w ? ui - vi : ui + vi;
-            acc[4 * h + q][w][0] += yr * cs - yi * sn;
-            acc[4 * h + q][w][1] += yr * sn + yi * cs;
-          }
+          const float y1r = ur + vr, y1i = ui + vi, y2r = ur - vr, y2i = ui - vi;
+          acc[4 * h + q][0][0] += y1r * w1r - y1i * w1i;
+          acc[4 * h + q][0][1] += y1r * w1i + y1i * w1r;
+          acc[4 * h + q][1][0] += y2r * w2r - y2i * w2i;
+          acc[4 * h + q][1][1] += y2r * w2i + y2i * w2r;
         }
       }
       asm volatile("tcgen05.fence::before_thread_sync;");
@@ -356,7 +437,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_theta_tc(
     }
     if (!ok) {
       *abort_flag = 1;
-      if (lane == 0) atomicExch(err, 1);
+      if (lane == 0) atomicCAS(err, 0, 1);
     } else if (r < Rp) {
       float2 *out = parent + (((int64_t)slot * n_parent + p) * 6 + comp) * (int64_t)Rp * phi + (int64_t)r * phi;
 #pragma unroll
@@ -369,22 +450,17 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_theta_tc(
       }
     }
   }
-  __syncthreads();  // every role done
-  if (warp == kTcEpiWarps && lane == 0 && *abort_flag) {
-    // let the copies and products in flight land before the memory is released
-    for (int b = 0; b < kTcStages; ++b)
-      if (last_load[b] >= 0) (void)mbar_wait(smem_addr(&full[b]), (last_load[b] / kTcStages) & 1, nullptr);
-    tc_commit(smem_addr(drain));
-    (void)mbar_wait(smem_addr(drain), 0, nullptr);
-  }
-  __syncwarp();
   asm volatile("tcgen05.fence::before_thread_sync;");
-  __syncthreads();
-  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTcTmemCols));
+  __syncthreads();  // every role done
+  if (warp == 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTcTmemCols));
+  }
 }
 
 po_status init_theta_tc_attributes() {
-  PO_CUDA(cudaFuncSetAttribute(k_theta_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem));
+  PO_CUDA(cudaFuncSetAttribute(k_theta_tc<kTcUseTable>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               TcPlan<kTcUseTable>::smem));
   return PO_OK;
 }
 
@@ -394,15 +470,16 @@ int theta_tc_npad(int phi) { return (phi + kTcN - 1) / kTcN * kTcN; }
 
 po_status launch_theta_tc(const uint8_t *mid, float2 *parent, const int32_t *child_table, int64_t n_parent,
                           int64_t n_child, int phi, int Kr, int Rp, const uint8_t *Atc, const float4 *trans,
-                          int n_slots, int G, int *err, cudaStream_t st) {
+                          int n_slots, int G, int *err, size_t mid_bytes, size_t atc_bytes, cudaStream_t st) {
   if (n_parent <= 0 || n_slots <= 0) return PO_OK;
   if (phi % 2 || Kr % kTcKC || Kr <= 0) return fail(PO_ERR_INTERNAL, "tcgen05 theta pass: grid");
   const int MT = (Rp + 127) / 128, n_nc = (phi / 2 + kTcPairs - 1) / kTcPairs;
   const int64_t n_task = (int64_t)n_slots * n_parent * 6 * n_nc;
   const int64_t gx = n_task * MT;
   if (gx > 2147483647LL) return fail(PO_ERR_UNSUPPORTED, "too many nodes for one launch");
-  k_theta_tc<<<(unsigned)gx, kTcThreads, kTcSmem, st>>>(mid, parent, child_table, n_parent, n_child, phi, Kr,
-                                                         theta_tc_npad(phi), Rp, Atc, trans, G, n_nc, n_task, err);
+  k_theta_tc<kTcUseTable><<<(unsigned)gx, kTcThreads, TcPlan<kTcUseTable>::smem, st>>>(mid, parent, child_table, n_parent, n_child, phi, Kr,
+                                                         theta_tc_npad(phi), Rp, Atc, trans, G, n_nc, n_task, err,
+                                                         mid_bytes, atc_bytes);
   count_launch();
   PO_CUDA(cudaGetLastError());
   return PO_OK;
