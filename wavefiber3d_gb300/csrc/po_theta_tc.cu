@@ -71,15 +71,20 @@ constexpr uint32_t kTcTmemCols = 4 * kTcN;                // (U, V) x 2 children
 constexpr unsigned long long kTcWaitNs = 1000000000ull;   // time limit of every wait: 1 s
 constexpr bool kTcUseTable = false;                       // phasor tables (see above)
 
-// shared-memory plan of one variant of the kernel
+constexpr int kTcLd = 129;  // float2 per pair (or output row) in the staged tables: 128 rows + 1 (bank spread)
+
+// shared-memory plan of one variant of the kernel; after the last child the
+// output tile [128 rows][kTcLd] of (j, j') pairs is transposed through the
+// stage and table space (the barriers behind it stay live)
 template <bool kTable>
 struct TcPlan {
   static constexpr int stages = kTable ? 3 : 4;
-  static constexpr int table = kTable ? 2 * kTcPairs * 128 * 8 : kTcPairs * 128 * 8;  // float2 per (row, pair)
+  static constexpr int table = (kTable ? 2 : 1) * kTcPairs * kTcLd * 8;  // float2 per (pair, row)
   static constexpr int table_off = stages * (kAStage + kBStage);
   static constexpr int pz_off = table_off + table;        // e^{i z} per row
   static constexpr int bar_off = pz_off + 128 * 8;
   static constexpr int smem = bar_off + 128;              // + mbarriers, TMEM slot, abort flag
+  static_assert(128 * kTcLd * 8 <= pz_off, "output transpose overlaps the live tables");
 };
 static_assert(TcPlan<true>::smem + 128 <= 227 * 1024, "shared memory (dynamic + the static child table)");
 static_assert(TcPlan<false>::smem + 128 <= 227 * 1024, "shared memory (dynamic + the static child table)");
@@ -215,7 +220,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_theta_tc(
   extern __shared__ __align__(128) uint8_t smem_tc[];
   uint8_t *sA = smem_tc;                                     // [NST][kAStage]
   uint8_t *sB = smem_tc + NST * kAStage;                     // [NST][kBStage]
-  float2 *sT = (float2 *)(smem_tc + Plan::table_off);        // [2][kTcPairs][128] or [kTcPairs][128]
+  float2 *sT = (float2 *)(smem_tc + Plan::table_off);        // [2][kTcPairs][kTcLd] or [kTcPairs][kTcLd]
   float2 *sPz = (float2 *)(smem_tc + Plan::pz_off);          // [128]
   uint64_t *full = (uint64_t *)(smem_tc + Plan::bar_off), *empty = full + NST, *accf = empty + NST,
            *acce = accf + 2;
@@ -360,27 +365,38 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_theta_tc(
   } else {
     // ---- epilogue role: thread = parent row, warpgroup = 16 column pairs ----
     const int wg = warp >> 2, quarter = warp & 3, rl = quarter * 32 + lane;
-    const int r = mtile * 128 + rl;
     {
+      // thread = one pair (lanes: consecutive pairs, contiguous in the table)
+      // and 16 rows, loaded 8 at a time
       const float4 *tr = trans + (int64_t)lam * Rp * phi;
-      for (int e = tid; e < 128 * kTcPairs; e += kTcEpiWarps * 32) {
-        const int row = e & 127, pl = e >> 7;
-        const int rr = mtile * 128 + row < Rp ? mtile * 128 + row : Rp - 1;
-        const int jq = nc * kTcPairs + pl < span ? nc * kTcPairs + pl : span - 1;
-        const float4 v = __ldg(tr + (int64_t)rr * phi + jq);
-        if (kTable) {
-          float s1, c1, s2, c2;
-          sincosf(v.x + v.y, &s1, &c1);
-          sincosf(v.x - v.y, &s2, &c2);
-          sT[pl * 128 + row] = make_float2(c1, s1);
-          sT[(kTcPairs + pl) * 128 + row] = make_float2(c2, s2);
-        } else {
-          sT[pl * 128 + row] = make_float2(v.x, v.y);
+      const int pl = tid & (kTcPairs - 1);
+      const int jq = nc * kTcPairs + pl < span ? nc * kTcPairs + pl : span - 1;
+#pragma unroll
+      for (int half = 0; half < 2; ++half) {
+        float4 v[8];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+          const int row = (tid / kTcPairs) + 8 * (8 * half + i);
+          const int rr = mtile * 128 + row < Rp ? mtile * 128 + row : Rp - 1;
+          v[i] = __ldg(tr + (int64_t)rr * phi + jq);
         }
-        if (pl == 0) {
-          float sz, cz;
-          sincosf(v.z, &sz, &cz);
-          sPz[row] = make_float2(cz, sz);
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+          const int row = (tid / kTcPairs) + 8 * (8 * half + i);
+          if (kTable) {
+            float s1, c1, s2, c2;
+            sincosf(v[i].x + v[i].y, &s1, &c1);
+            sincosf(v[i].x - v[i].y, &s2, &c2);
+            sT[pl * kTcLd + row] = make_float2(c1, s1);
+            sT[(kTcPairs + pl) * kTcLd + row] = make_float2(c2, s2);
+          } else {
+            sT[pl * kTcLd + row] = make_float2(v[i].x, v[i].y);
+          }
+          if (pl == 0) {
+            float sz, cz;
+            sincosf(v[i].z, &sz, &cz);
+            sPz[row] = make_float2(cz, sz);
+          }
         }
       }
       asm volatile("bar.sync 1, %0;" ::"r"(kTcEpiWarps * 32));
@@ -399,7 +415,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_theta_tc(
       // octant signs: x + for o & 1, y + for !(o & 2), z + for !(o & 4)
       const bool px = (o & 1) != 0, py = (o & 2) == 0;
       const float pzr = ez.x, pzi = (o & 4) ? -ez.y : ez.y;
-      const float2 *tab = sT + (kTable && px != py ? kTcPairs * 128 : 0);
+      const float2 *tab = sT + (kTable && px != py ? kTcPairs * kTcLd : 0);
       const float cj = px ? 1.f : -1.f;  // table phasor or its conjugate
       const float sgx = px ? 1.f : -1.f, sgy = py ? 1.f : -1.f;
       const uint32_t ta = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(b * 2 * kTcN + 32 * wg);
@@ -412,11 +428,11 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_theta_tc(
           const int pl = 16 * wg + 4 * h + q;
           float er, ei;  // e^{i (sx x + sy y)}
           if (kTable) {
-            const float2 t = tab[pl * 128 + rl];
+            const float2 t = tab[pl * kTcLd + rl];
             er = t.x;
             ei = cj * t.y;
           } else {
-            const float2 xy = sT[pl * 128 + rl];
+            const float2 xy = sT[pl * kTcLd + rl];
             // reduced phases: |sx x + sy y| <= 2 pi
             __sincosf(fmaf(sgx, xy.x, sgy * xy.y), &ei, &er);
           }
@@ -438,14 +454,31 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_theta_tc(
     if (!ok) {
       *abort_flag = 1;
       if (lane == 0) atomicCAS(err, 0, 1);
-    } else if (r < Rp) {
-      float2 *out = parent + (((int64_t)slot * n_parent + p) * 6 + comp) * (int64_t)Rp * phi + (int64_t)r * phi;
+    }
+    // all epilogue warps agree (ok everywhere) before the stage space is reused
+    uint32_t all_ok;
+    asm volatile("{\n.reg .pred p, q;\nsetp.ne.u32 q, %1, 0;\nbar.red.and.pred p, 1, %2, q;\nselp.u32 %0, 1, 0, p;\n}\n"
+                 : "=r"(all_ok)
+                 : "r"(ok ? 1u : 0u), "r"(kTcEpiWarps * 32)
+                 : "memory");
+    if (all_ok) {
+      // transpose through shared memory: row rl, pairs (16 wg + q) and 64 + (16 wg + q)
+      float2 *sO = (float2 *)smem_tc;  // [128][kTcLd]
 #pragma unroll
       for (int q = 0; q < 16; ++q) {
-        const int jq = nc * kTcPairs + 16 * wg + q;
-        if (jq < span) {
-          out[jq] = make_float2(acc[q][0][0], acc[q][0][1]);
-          out[jq + span] = make_float2(acc[q][1][0], acc[q][1][1]);
+        sO[rl * kTcLd + 16 * wg + q] = make_float2(acc[q][0][0], acc[q][0][1]);
+        sO[rl * kTcLd + kTcPairs + 16 * wg + q] = make_float2(acc[q][1][0], acc[q][1][1]);
+      }
+      asm volatile("bar.sync 1, %0;" ::"r"(kTcEpiWarps * 32));
+      // warp w stores rows w, w + 16, ...: 64 consecutive pairs of j, then of j'
+      float2 *out = parent + (((int64_t)slot * n_parent + p) * 6 + comp) * (int64_t)Rp * phi;
+      for (int row = warp; row < 128; row += kTcEpiWarps) {
+        const int rg = mtile * 128 + row;
+        if (rg >= Rp) break;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          const int pair = 32 * (k & 1) + lane, jq = nc * kTcPairs + pair;
+          if (jq < span) out[(int64_t)rg * phi + jq + (k >> 1) * span] = sO[row * kTcLd + (k >> 1) * kTcPairs + pair];
         }
       }
     }
