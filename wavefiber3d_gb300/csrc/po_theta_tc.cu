@@ -28,10 +28,10 @@
 // The child's phasor at (row, column j) is e^{i (sz z + sx x + sy y)} and at
 // the mirror column e^{i (sz z - sx x - sy y)}, with the octant's signs s and
 // the reduced phases (x, y, z) of the translation table.  Once per CTA the
-// epilogue warps stage per (row, pair) either e^{i (x + y)} and e^{i (x - y)}
-// (kTable: the octant's phasor is one of them or its conjugate, so a child
-// costs no sincos per element) or (x, y) (one sincos per element), and
-// e^{i z} per row.
+// epilogue warps stage (x, y) per (row, pair) and e^{i z} per row; a child
+// then costs one sincos per (row, pair).  (Staging e^{i (x + y)} and
+// e^{i (x - y)} instead, which removes that sincos, needs twice the table
+// space, leaves room for one stage less and measured slower.)
 //
 // Operand layouts (bf16, K-major, no swizzle; core matrices of 8 rows x 16 B):
 // a chunk of one matrix is [rows / 8][2][8][8] (row block, k8 block, row,
@@ -69,25 +69,22 @@ constexpr int kAStage = 4 * 128 * kTcKC * 2;              // 16 KB
 constexpr int kBStage = 4 * kTcN * kTcKC * 2;             // 16 KB
 constexpr uint32_t kTcTmemCols = 4 * kTcN;                // (U, V) x 2 children = 512 columns
 constexpr unsigned long long kTcWaitNs = 1000000000ull;   // time limit of every wait: 1 s
-constexpr bool kTcUseTable = false;                       // phasor tables (see above)
 
 constexpr int kTcLd = 129;  // float2 per pair (or output row) in the staged tables: 128 rows + 1 (bank spread)
 
-// shared-memory plan of one variant of the kernel; after the last child the
-// output tile [128 rows][kTcLd] of (j, j') pairs is transposed through the
-// stage and table space (the barriers behind it stay live)
-template <bool kTable>
+// shared-memory plan; after the last child the output tile [128 rows][kTcLd]
+// of (j, j') pairs is transposed through the stage and table space (the
+// barriers behind it stay live)
 struct TcPlan {
-  static constexpr int stages = kTable ? 3 : 4;
-  static constexpr int table = (kTable ? 2 : 1) * kTcPairs * kTcLd * 8;  // float2 per (pair, row)
+  static constexpr int stages = 4;
+  static constexpr int table = kTcPairs * kTcLd * 8;     // (x, y) per (pair, row)
   static constexpr int table_off = stages * (kAStage + kBStage);
   static constexpr int pz_off = table_off + table;        // e^{i z} per row
   static constexpr int bar_off = pz_off + 128 * 8;
   static constexpr int smem = bar_off + 128;              // + mbarriers, TMEM slot, abort flag
   static_assert(128 * kTcLd * 8 <= pz_off, "output transpose overlaps the live tables");
 };
-static_assert(TcPlan<true>::smem + 128 <= 227 * 1024, "shared memory (dynamic + the static child table)");
-static_assert(TcPlan<false>::smem + 128 <= 227 * 1024, "shared memory (dynamic + the static child table)");
+static_assert(TcPlan::smem + 128 <= 227 * 1024, "shared memory (dynamic + the static child table)");
 
 __device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -209,18 +206,17 @@ void build_theta_tc(const std::vector<double> &Mplus, const std::vector<double> 
 }
 
 // grid.x = task * MT + tile (task = (slot, parent, component, column chunk)), kTcThreads threads
-template <bool kTable>
 __global__ void __launch_bounds__(kTcThreads, 1) k_theta_tc(
     const uint8_t *__restrict__ mid, float2 *__restrict__ parent, const int32_t *__restrict__ child_table,
     int64_t n_parent, int64_t n_child, int phi, int Kr, int Npad, int Rp, const uint8_t *__restrict__ Atc,
     const float4 *__restrict__ trans, int G, int n_nc, int64_t n_task, int *__restrict__ err, size_t mid_bytes,
     size_t atc_bytes) {
-  using Plan = TcPlan<kTable>;
+  using Plan = TcPlan;
   constexpr int NST = Plan::stages;
   extern __shared__ __align__(128) uint8_t smem_tc[];
   uint8_t *sA = smem_tc;                                     // [NST][kAStage]
   uint8_t *sB = smem_tc + NST * kAStage;                     // [NST][kBStage]
-  float2 *sT = (float2 *)(smem_tc + Plan::table_off);        // [2][kTcPairs][kTcLd] or [kTcPairs][kTcLd]
+  float2 *sT = (float2 *)(smem_tc + Plan::table_off);        // [kTcPairs][kTcLd]
   float2 *sPz = (float2 *)(smem_tc + Plan::pz_off);          // [128]
   uint64_t *full = (uint64_t *)(smem_tc + Plan::bar_off), *empty = full + NST, *accf = empty + NST,
            *acce = accf + 2;
@@ -383,15 +379,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_theta_tc(
 #pragma unroll
         for (int i = 0; i < 8; ++i) {
           const int row = (tid / kTcPairs) + 8 * (8 * half + i);
-          if (kTable) {
-            float s1, c1, s2, c2;
-            sincosf(v[i].x + v[i].y, &s1, &c1);
-            sincosf(v[i].x - v[i].y, &s2, &c2);
-            sT[pl * kTcLd + row] = make_float2(c1, s1);
-            sT[(kTcPairs + pl) * kTcLd + row] = make_float2(c2, s2);
-          } else {
-            sT[pl * kTcLd + row] = make_float2(v[i].x, v[i].y);
-          }
+          sT[pl * kTcLd + row] = make_float2(v[i].x, v[i].y);
           if (pl == 0) {
             float sz, cz;
             sincosf(v[i].z, &sz, &cz);
@@ -415,8 +403,6 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_theta_tc(
       // octant signs: x + for o & 1, y + for !(o & 2), z + for !(o & 4)
       const bool px = (o & 1) != 0, py = (o & 2) == 0;
       const float pzr = ez.x, pzi = (o & 4) ? -ez.y : ez.y;
-      const float2 *tab = sT + (kTable && px != py ? kTcPairs * kTcLd : 0);
-      const float cj = px ? 1.f : -1.f;  // table phasor or its conjugate
       const float sgx = px ? 1.f : -1.f, sgy = py ? 1.f : -1.f;
       const uint32_t ta = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(b * 2 * kTcN + 32 * wg);
 #pragma unroll
@@ -426,16 +412,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_theta_tc(
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
           const int pl = 16 * wg + 4 * h + q;
-          float er, ei;  // e^{i (sx x + sy y)}
-          if (kTable) {
-            const float2 t = tab[pl * kTcLd + rl];
-            er = t.x;
-            ei = cj * t.y;
-          } else {
-            const float2 xy = sT[pl * kTcLd + rl];
-            // reduced phases: |sx x + sy y| <= 2 pi
-            __sincosf(fmaf(sgx, xy.x, sgy * xy.y), &ei, &er);
-          }
+          // e^{i (sx x + sy y)}; reduced phases: |sx x + sy y| <= 2 pi
+          float er, ei;
+          const float2 xy = sT[pl * kTcLd + rl];
+          __sincosf(fmaf(sgx, xy.x, sgy * xy.y), &ei, &er);
           // column j: e^{i z'} e;  mirror column: e^{i z'} conj(e)
           const float w1r = pzr * er - pzi * ei, w1i = pzr * ei + pzi * er;
           const float w2r = pzr * er + pzi * ei, w2i = pzi * er - pzr * ei;
@@ -492,8 +472,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_theta_tc(
 }
 
 po_status init_theta_tc_attributes() {
-  PO_CUDA(cudaFuncSetAttribute(k_theta_tc<kTcUseTable>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               TcPlan<kTcUseTable>::smem));
+  PO_CUDA(cudaFuncSetAttribute(k_theta_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TcPlan::smem));
   return PO_OK;
 }
 
@@ -510,7 +489,7 @@ po_status launch_theta_tc(const uint8_t *mid, float2 *parent, const int32_t *chi
   const int64_t n_task = (int64_t)n_slots * n_parent * 6 * n_nc;
   const int64_t gx = n_task * MT;
   if (gx > 2147483647LL) return fail(PO_ERR_UNSUPPORTED, "too many nodes for one launch");
-  k_theta_tc<kTcUseTable><<<(unsigned)gx, kTcThreads, TcPlan<kTcUseTable>::smem, st>>>(mid, parent, child_table, n_parent, n_child, phi, Kr,
+  k_theta_tc<<<(unsigned)gx, kTcThreads, TcPlan::smem, st>>>(mid, parent, child_table, n_parent, n_child, phi, Kr,
                                                          theta_tc_npad(phi), Rp, Atc, trans, G, n_nc, n_task, err,
                                                          mid_bytes, atc_bytes);
   count_launch();
