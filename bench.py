@@ -232,8 +232,8 @@ def run_engine(args, world, rank, local):
     r = reps[-1]
     classes = {
         "leaf far-field sums": (statistics.mean(x["ms_leaf_kernel"] for x in reps), r["n_leaf_launches"]),
-        "row (phi) FFT interpolation": (statistics.mean(x["ms_rows"] for x in reps), r["n_row_launches"]),
-        "column (theta) FFT interpolation + translation + child sum":
+        "row (phi) interpolation": (statistics.mean(x["ms_rows"] for x in reps), r["n_row_launches"]),
+        "column (theta) interpolation + translation + child sum":
             (statistics.mean(x["ms_cols"] for x in reps), r["n_col_launches"]),
     }
     dom = max(classes, key=lambda k: classes[k][0])
