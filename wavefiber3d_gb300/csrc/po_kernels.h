@@ -39,9 +39,14 @@ po_status launch_leaf(const float *const g[7], const int32_t *leaf_begin, const 
 
 // split hi+lo BF16 tensor-core leaf sums (po_leaf_mma.cu); same layout as launch_leaf
 po_status init_leaf_mma_attributes();
+// fuse_mid != nullptr: also run the phi pass of the level above (Rc x Pc leaf
+// grid to Pp columns, fragments fuse_B with Kp rows) and write its packed
+// output there (leaf_row_fusion_fits must hold)
 po_status launch_leaf_mma(const float *const g[7], const int32_t *leaf_begin, const double *leaf_center,
                           int64_t n_leaves, const SlotParams<float> *slots_dev, int n_lambda, int G,
-                          const float4 *dirs, int ndir, float2 *out, cudaStream_t st);
+                          const float4 *dirs, int ndir, float2 *out, cudaStream_t st, const uint32_t *fuse_B = nullptr,
+                          uint4 *fuse_mid = nullptr, int Rc = 0, int Pc = 0, int Pp = 0, int Kp = 0);
+bool leaf_row_fusion_fits(int Pc, int Pp, int Kp);
 
 int direct_splits(int64_t n, int ndir, int n_lambda, int sm_count);
 // FP32 depth-0 sum about c0: out[slot][comp][dir]; cur[slot][n][6]

@@ -23,6 +23,7 @@
 #include "po_common.cuh"
 #include "po_internal.h"
 #include "po_kernels.h"
+#include "po_rows_block.cuh"
 
 namespace wavepo {
 
@@ -53,13 +54,36 @@ constexpr int kPC = 128;  // points per chunk (16 k-steps of 16 = 8 points x cos
 // of 8 real columns = 2 x 6 GC), 4 warps over the 16-direction row tiles.
 // Dynamic shared memory: s_u[kPC] float4, s_cur[kPC][6 GC] float2,
 // s_b[kPC/8][NT][32] uint4 (B fragments {hi0, hi1, lo0, lo1}).
+// Fused phi pass of the level above (fz.mid set): once the leaf's patterns
+// are complete, the CTA re-reads them (L2) and writes the packed mirror-pair
+// sums and differences of its 6 GC patterns (rows_block<1>, the φ-matrix
+// fragments staged in s_b), which removes the separate row pass of that level.
+struct LeafRowFusion {
+  const uint4 *B;  // phi matrix fragments of the level above (one n-tile group)
+  uint4 *mid;      // packed output (nullptr: no fusion)
+  int KS, nq, Rc, Pc, Pp;
+};
+// The fused phi pass of one CTA (its own register allocation: kept out of the
+// contraction loop's).
+__device__ __noinline__ void leaf_rows_epilogue(const float2 *out, uint4 *s_b, const LeafRowFusion fz, int64_t lam,
+                                                int64_t leaf, int64_t n_leaves, int Gtot, int g0, int GC) {
+  for (int e = threadIdx.x; e < fz.nq * fz.KS * 32; e += blockDim.x) s_b[e] = fz.B[e];
+  __syncthreads();
+  const int Rc2 = fz.Rc + (fz.Rc & 1), warp = threadIdx.x >> 5;
+  for (int s2 = 0; s2 < GC; ++s2) {
+    const int64_t lo = ((lam * Gtot + g0 + s2) * n_leaves + leaf) * 6 * Rc2, hi = lo + 6 * Rc2;
+    for (int64_t blk = lo / 8 + warp; blk * 8 < hi; blk += 4)
+      rows_block<1, true>(blk, lo, hi, out, fz.mid, fz.Rc, Rc2, fz.Pc, fz.Pp, fz.KS, s_b, 0, fz.nq, 0);
+  }
+}
+
 template <int GC>
-__global__ void __launch_bounds__(128) k_leaf_mma(
+__global__ void __launch_bounds__(128, 5) k_leaf_mma(
     const float *__restrict__ x, const float *__restrict__ y, const float *__restrict__ z,
     const float *__restrict__ nx, const float *__restrict__ ny, const float *__restrict__ nz,
     const float *__restrict__ area, const int32_t *__restrict__ leaf_begin, const double *__restrict__ leaf_center,
     const SlotParams<float> *__restrict__ slots, const float4 *__restrict__ dirs, int ndir, int64_t n_leaves,
-    int Gtot, int g0, float2 *__restrict__ out) {
+    int Gtot, int g0, float2 *__restrict__ out, LeafRowFusion fz) {
   constexpr int NC = 6 * GC;            // complex columns
   constexpr int NT = (2 * NC + 7) / 8;  // n-tiles of 8 real columns
   extern __shared__ uint4 smem_leaf[];
@@ -185,6 +209,10 @@ __global__ void __launch_bounds__(128) k_leaf_mma(
     }
     if (cnt == 0) break;  // an empty leaf (root of an empty cloud) was written as zeros
   }
+  if (fz.mid) {
+    __syncthreads();  // the leaf's patterns are written (read back through L2); s_b is free
+    leaf_rows_epilogue(out, s_b, fz, lam, leaf, n_leaves, Gtot, g0, GC);
+  }
 }
 
 template <int GC>
@@ -201,10 +229,24 @@ po_status init_leaf_mma_attributes() {
   return PO_OK;
 }
 
+// Whether the phi pass from a leaf grid of Rc x Pc to Pp parent columns can run
+// fused in the leaf kernel: one n-tile group, fragments within s_b (GC = 1).
+bool leaf_row_fusion_fits(int Pc, int Pp, int Kp) {
+  const int NTt = (Pp / 2 + 3) / 4, KS = Kp / 16;
+  return NTt <= kRowNG && Kp >= Pc && Kp % 16 == 0 && NTt * KS * 32 <= (kPC / 8) * ((12 + 7) / 8) * 32;
+}
+
 po_status launch_leaf_mma(const float *const g[7], const int32_t *leaf_begin, const double *leaf_center,
                           int64_t n_leaves, const SlotParams<float> *slots_dev, int n_lambda, int G,
-                          const float4 *dirs, int ndir, float2 *out, cudaStream_t st) {
+                          const float4 *dirs, int ndir, float2 *out, cudaStream_t st, const uint32_t *fuse_B,
+                          uint4 *fuse_mid, int Rc, int Pc, int Pp, int Kp) {
   if (n_leaves <= 0 || n_lambda <= 0) return PO_OK;
+  LeafRowFusion fz{nullptr, nullptr, 0, 0, 0, 0, 0};
+  if (fuse_mid) {
+    if (!leaf_row_fusion_fits(Pc, Pp, Kp) || (int64_t)Rc * Pc != ndir)
+      return fail(PO_ERR_INTERNAL, "leaf/phi-pass fusion does not fit");
+    fz = LeafRowFusion{(const uint4 *)fuse_B, fuse_mid, Kp / 16, (Pp / 2 + 3) / 4, Rc, Pc, Pp};
+  }
   if (n_lambda > 65535) return fail(PO_ERR_UNSUPPORTED, "too many wavelengths for one launch");
   dim3 grid((unsigned)n_leaves, (unsigned)n_lambda);
   // slots of a wavelength share its phases; groups of up to 4 per launch
@@ -212,7 +254,7 @@ po_status launch_leaf_mma(const float *const g[7], const int32_t *leaf_begin, co
     const int gc = std::min(4, G - g0);
 #define PO_LEAF_MMA(GG)                                                                                          \
   k_leaf_mma<GG><<<grid, 128, leaf_mma_smem<GG>(), st>>>(g[0], g[1], g[2], g[3], g[4], g[5], g[6], leaf_begin, \
-                                                        leaf_center, slots_dev, dirs, ndir, n_leaves, G, g0, out)
+                                                        leaf_center, slots_dev, dirs, ndir, n_leaves, G, g0, out, fz)
     switch (gc) {
       case 1: PO_LEAF_MMA(1); break;
       case 2: PO_LEAF_MMA(2); break;

@@ -792,9 +792,16 @@ static po_status enqueue_solve(po_ctx *c, const SolvePlan &P, float *out_dev, co
     for (const SlotChunk &ch : P.chunks) {
       const SlotParams<float> *sp = c->slots.as<SlotParams<float>>() + ch.s0;
       PO_TRY(rec(c->kev[0]));
+      // the phi pass of the deepest parent level runs in the leaf kernel's epilogue
+      // when its packed output fits one n-tile group
+      const bool fuse_rows = cfg.precision == PO_PREC_SPLIT_BF16 && d >= 1 && c->tensor_theta &&
+                             !c->tc_level[d - 1] && leaf_row_fusion_fits(c->Phi[d], c->Phi[d - 1], c->bmat_kp[d - 1]);
       if (cfg.precision == PO_PREC_SPLIT_BF16)
         PO_TRY(launch_leaf_mma(P.gsc, P.tree.level[d].begin, c->leaf_ctr.as<double>(), P.nleaf, sp, ch.nl, ch.gc,
-                               c->dirs.as<float4>(), c->R[d] * c->Phi[d], c->levelA.as<float2>(), st));
+                               c->dirs.as<float4>(), c->R[d] * c->Phi[d], c->levelA.as<float2>(), st,
+                               fuse_rows ? c->bmat.as<uint32_t>() + c->bmat_off[d - 1] : nullptr,
+                               fuse_rows ? c->mid.as<uint4>() : nullptr, c->R[d], c->Phi[d], c->Phi[d - 1],
+                               d >= 1 ? c->bmat_kp[d - 1] : 0));
       else
         PO_TRY(launch_leaf(P.gsc, P.tree.level[d].begin, c->leaf_ctr.as<double>(), P.nleaf, sp, ch.nl, ch.gc,
                            c->dirs.as<float4>(), c->R[d] * c->Phi[d], c->levelA.as<float2>(), st));
@@ -806,7 +813,9 @@ static po_status enqueue_solve(po_ctx *c, const SolvePlan &P, float *out_dev, co
         const float4 *trans = c->trans.as<float4>() + P.tr_off[l] + (size_t)ch.l0 * c->R[l] * c->Phi[l];
         int64_t nrows = (int64_t)ch.ns * nc * 6 * c->R[l + 1];
         PO_TRY(rec(c->kev[2 + 4 * l]));
-        if (c->tc_level[l]) {
+        if (fuse_rows && l == d - 1) {
+          // written by the leaf kernel
+        } else if (c->tc_level[l]) {
           PO_TRY(launch_interp_rows_core(cur_lvl, c->mid.as<uint8_t>(), (int64_t)ch.ns * nc * 6, c->R[l + 1],
                                          c->tc_kr[l], theta_tc_npad(c->Phi[l]), c->Phi[l + 1], c->Phi[l],
                                          c->bmat_kp[l], c->bmat.as<uint32_t>() + c->bmat_off[l], c->sm_count, st));
@@ -823,7 +832,7 @@ static po_status enqueue_solve(po_ctx *c, const SolvePlan &P, float *out_dev, co
         PO_TRY(rec(c->kev[3 + 4 * l]));
         T.rows_b += 8.0 * nrows * (c->Phi[l + 1] + c->Phi[l]);
         T.cols_b += 8.0 * ch.ns * 6 * ((double)nc * c->R[l + 1] * c->Phi[l] + (double)np * c->R[l] * c->Phi[l]);
-        if (nrows > 0) ++T.n_row;
+        if (nrows > 0 && !(fuse_rows && l == d - 1)) ++T.n_row;
         if (np > 0) ++T.n_col;
         PO_TRY(rec(c->kev[4 + 4 * l]));
         if (c->tc_level[l]) {
