@@ -333,6 +333,23 @@ def test_large_level_grids_vs_fp64_direct(prec):
 
 
 @pytest.mark.parametrize("prec", [api.PO_PREC_FP32, api.PO_PREC_SPLIT_BF16])
+def test_partial_theta_tiles_vs_fp64_direct(prec):
+    """Parent levels of 109, 201 and 241 theta rows (one partly filled 128-row
+    tile, two tiles at 78% and at 94%) on the tcgen05 theta pass, with 54,
+    100 and 120 column pairs (partly filled 64-pair column chunks), a 61-row
+    level on the warp-task kernel, and a 40 x 40 leaf grid whose phi pass to
+    60 columns runs in the leaf kernel's epilogue (split-bf16) or as its own
+    pass (FP32)."""
+    cloud = geometry.ellipsoid((1.5e-6, 1.0e-6, 0.8e-6), 3000)
+    box = [-1.65e-6, -1.1e-6, -0.88e-6, 1.65e-6, 1.1e-6, 0.88e-6]
+    cfg = api.Config(4, [60, 200, 108, 60, 40], [120, 200, 108, 60, 40], box[:3], box[3:], precision=prec)
+    il = api.Illumination([500e-9], [0.3], [0.7], api.PO_POL_TM, 1.55 + 0.1j, 2e-6)
+    out, rep = _solve(cloud, cfg, il)
+    o = oracle.solve_direct(cloud, oracle.make_illum(500e-9, 0.3, 0.7, "M", 1.55 + 0.1j, 2e-6), 60, 120)
+    assert rel(out.reshape(o.shape), o) < TOL_TREE, rep
+
+
+@pytest.mark.parametrize("prec", [api.PO_PREC_FP32, api.PO_PREC_SPLIT_BF16])
 def test_large_leaf_phases_vs_fp64_direct(prec):
     """Leaves of 8.8 um at 500 nm: leaf-local phases reach ~100 rad, so the
     leaf kernels take their range-reduced phasor path (the fast path covers
