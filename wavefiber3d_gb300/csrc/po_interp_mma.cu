@@ -607,6 +607,31 @@ void build_phi_matrix(int Pc, int Pp, int Kp, std::vector<uint32_t> &out) {
               out);
 }
 
+// phi map as the B operand of the tcgen05 row pass (po_rows_tc.cu): per N tile
+// of ntn columns (column n = 2 jl + w: pair j = nt ntn/2 + jl, w = 0 for
+// parent column j and 1 for j + Pp/2) and per 16-row K chunk, the bf16 hi and
+// lo matrices [ntn/8][2][8][8] (K-major core matrices), zero beyond Pc rows and
+// Pp/2 pairs; one tile is Kc/16 chunks of 64 ntn bytes.
+void build_phi_tc(int Pc, int Pp, int Kc, int ntn, int n_nt, std::vector<uint16_t> &out) {
+  const int half = Pp / 2, KC = Kc / 16;
+  const size_t chunk = (size_t)2 * ntn * 16, tile = (size_t)KC * chunk;
+  out.assign(tile * n_nt, 0);
+  for (int nt = 0; nt < n_nt; ++nt)
+    for (int n = 0; n < ntn; ++n) {
+      const int j = nt * (ntn / 2) + (n >> 1);
+      if (j >= half) continue;
+      const int col = j + (n & 1) * half;
+      for (int k = 0; k < Pc; ++k) {
+        const double v = trig_kernel(Pc, (double)col / Pp - (double)k / Pc);
+        const uint16_t h = bf16_rne((float)v), l = bf16_rne((float)(v - (double)bf16_to_f(h)));
+        const size_t base = nt * tile + (size_t)(k / 16) * chunk;
+        const size_t in_mat = ((size_t)(n / 8) * 2 + (k % 16) / 8) * 64 + (n % 8) * 8 + (k % 8);
+        out[base + in_mat] = h;
+        out[base + (size_t)ntn * 16 + in_mat] = l;
+      }
+    }
+}
+
 // transpose of the phi map: child column j (< Pc) from parent columns j' (< Pp)
 void build_phi_matrix_adj(int Pc, int Pp, int Kp, std::vector<uint32_t> &out) {
   b_fragments(Pc, Pp, Kp, [&](int j, int jp) { return trig_kernel(Pc, (double)jp / Pp - (double)j / Pc); }, out);

@@ -101,6 +101,12 @@ int theta_tc_npad(int phi);
 void build_theta_tc(const std::vector<double> &Mplus, const std::vector<double> &Mminus, int Rp, int Rc, int ld,
                     int Kr, std::vector<uint16_t> &out);
 po_status init_theta_tc_attributes();
+void build_phi_tc(int Pc, int Pp, int Kc, int ntn, int n_nt, std::vector<uint16_t> &out);
+bool rows_tc_plan(int Pc, int Pp, int &ntn, int &n_nt);
+po_status init_rows_tc_attributes();
+po_status launch_rows_tc(const float2 *src, uint8_t *dst, size_t dst_bytes, int64_t n_patterns, int Rc, int Rr,
+                         int npad, int Pc, int Pp, const uint8_t *Bt, size_t bt_bytes, int ntn, int n_nt,
+                         int sm_count, int *err, cudaStream_t st);
 po_status launch_theta_tc(const uint8_t *mid, float2 *parent, const int32_t *child_table, int64_t n_parent,
                           int64_t n_child, int phi, int Kr, int Rp, const uint8_t *Atc, const float4 *trans,
                           int n_slots, int G, int *err, size_t mid_bytes, size_t atc_bytes, cudaStream_t st);

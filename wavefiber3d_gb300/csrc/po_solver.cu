@@ -134,6 +134,7 @@ po_status init_device_attributes(int dev) {
   PO_TRY(init_leaf_mma_attributes());
   PO_TRY(init_point_adjoint_mma_attributes());
   PO_TRY(init_theta_tc_attributes());
+  PO_TRY(init_rows_tc_attributes());
   done.insert(dev);
   return PO_OK;
 }
@@ -167,6 +168,11 @@ struct po_ctx {
   int tc_kr[PO_MAX_DEPTH] = {};       // child rows padded to 16 (the K of its products)
   size_t tc_off[PO_MAX_DEPTH] = {};   // byte offset of the level's theta chunks in tc_amat
   DevBuf tc_amat, tc_err;
+  // tcgen05 phi pass feeding those levels (po_rows_tc.cu): phi tiles per level
+  bool rt_level[PO_MAX_DEPTH] = {};
+  int rt_ntn[PO_MAX_DEPTH] = {}, rt_nnt[PO_MAX_DEPTH] = {};
+  size_t rt_off[PO_MAX_DEPTH] = {}, rt_bytes[PO_MAX_DEPTH] = {};
+  DevBuf rt_bmat;
   size_t trig_off[PO_MAX_DEPTH] = {};
   // transposed level matrices of the adjoint (built on the first po_grad)
   bool adj_ready = false;
@@ -370,6 +376,21 @@ po_status po_create(po_ctx **out, const po_config *cfg) {
         c->tc_off[l] = tall.size() * sizeof(uint16_t);
         tall.insert(tall.end(), tone.begin(), tone.end());
       }
+      // the phi pass of those levels on tcgen05 where its phi tile fits shared memory
+      std::vector<uint16_t> rall, rone;
+      for (int l = 0; l < d; ++l) {
+        if (!c->tc_level[l] || !rows_tc_plan(c->Phi[l + 1], c->Phi[l], c->rt_ntn[l], c->rt_nnt[l])) continue;
+        c->rt_level[l] = true;
+        build_phi_tc(c->Phi[l + 1], c->Phi[l], (c->Phi[l + 1] + 15) / 16 * 16, c->rt_ntn[l], c->rt_nnt[l], rone);
+        c->rt_off[l] = rall.size() * sizeof(uint16_t);
+        c->rt_bytes[l] = rone.size() * sizeof(uint16_t);
+        rall.insert(rall.end(), rone.begin(), rone.end());
+      }
+      s = c->rt_bmat.ensure(std::max<size_t>(rall.size() * sizeof(uint16_t), 16));
+      if (s == PO_OK && !rall.empty() &&
+          cudaMemcpy(c->rt_bmat.p, rall.data(), rall.size() * sizeof(uint16_t), cudaMemcpyHostToDevice) != cudaSuccess)
+        s = fail(PO_ERR_CUDA, "upload of the tcgen05 phi tiles");
+      if (s != PO_OK) { po_destroy(c); return s; }
       s = c->tc_amat.ensure(std::max<size_t>(tall.size() * sizeof(uint16_t), 16));
       if (s == PO_OK) s = c->tc_err.ensure(sizeof(int));
       if (s == PO_OK && !tall.empty() &&
@@ -407,7 +428,7 @@ po_status po_destroy(po_ctx *c) {
   for (DevBuf *b : {&c->twiddles, &c->geom_in, &c->geom_sorted, &c->octree_ws, &c->leaf_ctr, &c->dirs, &c->dirs_d,
                     &c->trans, &c->levelA, &c->levelB, &c->mid, &c->slots, &c->kvals, &c->out, &c->cur, &c->partial,
                     &c->tile_ctr, &c->amat, &c->bmat, &c->amat_adj, &c->bmat_adj, &c->slots64, &c->grad_acc,
-                    &c->chunk_begin, &c->center0, &c->dir_trig, &c->out_dirs, &c->tc_amat, &c->tc_err})
+                    &c->chunk_begin, &c->center0, &c->dir_trig, &c->out_dirs, &c->tc_amat, &c->tc_err, &c->rt_bmat})
     b->release();
   for (auto &e : c->ev)
     if (e) cudaEventDestroy(e);
@@ -815,6 +836,11 @@ static po_status enqueue_solve(po_ctx *c, const SolvePlan &P, float *out_dev, co
         PO_TRY(rec(c->kev[2 + 4 * l]));
         if (fuse_rows && l == d - 1) {
           // written by the leaf kernel
+        } else if (c->rt_level[l]) {
+          PO_TRY(launch_rows_tc(cur_lvl, c->mid.as<uint8_t>(), c->mid.bytes, (int64_t)ch.ns * nc * 6, c->R[l + 1],
+                                c->tc_kr[l], theta_tc_npad(c->Phi[l]), c->Phi[l + 1], c->Phi[l],
+                                c->rt_bmat.as<uint8_t>() + c->rt_off[l], c->rt_bytes[l], c->rt_ntn[l], c->rt_nnt[l],
+                                c->sm_count, c->tc_err.as<int>(), st));
         } else if (c->tc_level[l]) {
           PO_TRY(launch_interp_rows_core(cur_lvl, c->mid.as<uint8_t>(), (int64_t)ch.ns * nc * 6, c->R[l + 1],
                                          c->tc_kr[l], theta_tc_npad(c->Phi[l]), c->Phi[l + 1], c->Phi[l],

@@ -54,10 +54,13 @@
 #include "po_common.cuh"
 #include "po_internal.h"
 #include "po_kernels.h"
+#include "po_tc_common.cuh"
 
 namespace wavepo {
 
 namespace {
+
+using namespace tc;
 
 constexpr int kTcKC = 16;                                 // K (child rows) per chunk
 constexpr int kTcPairs = 64;                              // column pairs per CTA
@@ -68,7 +71,6 @@ constexpr int kTcThreads = 32 * (kTcEpiWarps + 2);
 constexpr int kAStage = 4 * 128 * kTcKC * 2;              // 16 KB
 constexpr int kBStage = 4 * kTcN * kTcKC * 2;             // 16 KB
 constexpr uint32_t kTcTmemCols = 4 * kTcN;                // (U, V) x 2 children = 512 columns
-constexpr unsigned long long kTcWaitNs = 1000000000ull;   // time limit of every wait: 1 s
 
 constexpr int kTcLd = 129;  // float2 per pair (or output row) in the staged tables: 128 rows + 1 (bank spread)
 
@@ -85,83 +87,6 @@ struct TcPlan {
   static_assert(128 * kTcLd * 8 <= pz_off, "output transpose overlaps the live tables");
 };
 static_assert(TcPlan::smem + 128 <= 227 * 1024, "shared memory (dynamic + the static child table)");
-
-__device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ unsigned long long global_ns() {
-  unsigned long long t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
-}
-
-// shared-memory matrix descriptor: K-major, no swizzle, LBO 128 B, SBO 256 B
-__device__ __forceinline__ uint64_t tc_desc(uint32_t addr) {
-  return (uint64_t)((addr >> 4) & 0x3FFF) | ((uint64_t)(128 >> 4) << 16) | ((uint64_t)(256 >> 4) << 32) |
-         ((uint64_t)1 << 46);
-}
-
-__device__ __forceinline__ void tc_mma(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
-  asm volatile(
-      "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
-      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
-      "l"(a), "l"(b), "r"(idesc), "r"(acc));
-}
-
-__device__ __forceinline__ void tc_commit(uint32_t bar) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar));
-}
-
-__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
-  uint32_t done;
-  asm volatile(
-      "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
-      : "=r"(done)
-      : "r"(bar), "r"(parity));
-  return done != 0;
-}
-
-// true once the mbarrier has completed the phase of the given parity; false
-// after the time limit, or as soon as another role has given up (abort)
-__device__ bool mbar_wait(uint32_t bar, uint32_t parity, const volatile int *abort) {
-  const unsigned long long t0 = global_ns();
-  for (int it = 0;; ++it) {
-    if (mbar_try(bar, parity)) return true;
-    if ((it & 63) == 63) {
-      if (abort && *abort) return false;
-      if (global_ns() - t0 > kTcWaitNs) return false;
-    }
-  }
-}
-
-__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
-  asm volatile("{\n.reg .b64 st;\nmbarrier.arrive.shared::cta.b64 st, [%0];\n}\n" ::"r"(bar) : "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
-  asm volatile("{\n.reg .b64 st;\nmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n}\n" ::"r"(bar),
-               "r"(bytes)
-               : "memory");
-}
-
-// bulk copy global -> shared, completing `bar` by its byte count
-__device__ __forceinline__ void bulk_copy(uint32_t dst, const void *src, uint32_t bytes, uint32_t bar) {
-  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
-               "l"(src), "r"(bytes), "r"(bar)
-               : "memory");
-}
-
-// 8 columns of U at ta_u and of V at ta_v for this warp's 32 lanes.  The loads
-// and their wait are one asm statement, so that no compiler-placed instruction
-// can touch a destination register while the asynchronous load is writing it.
-__device__ __forceinline__ void tmem_ld8x2(uint32_t ta_u, uint32_t ta_v, uint32_t (&u)[8], uint32_t (&v)[8]) {
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%16];\n"
-      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%8,%9,%10,%11,%12,%13,%14,%15}, [%17];\n"
-      "tcgen05.wait::ld.sync.aligned;\n"
-      : "=r"(u[0]), "=r"(u[1]), "=r"(u[2]), "=r"(u[3]), "=r"(u[4]), "=r"(u[5]), "=r"(u[6]), "=r"(u[7]), "=r"(v[0]),
-        "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7])
-      : "r"(ta_u), "r"(ta_v));
-}
 
 }  // namespace
 
