@@ -23,10 +23,10 @@
 //    Pc are zero);
 //  * 4 or 8 epilogue warps (tensor-memory lane = M row = one part of one
 //    complex row; for tiles wider than 128 columns the two warps of a lane
-//    quarter take alternate 16-column blocks, narrower tiles keep 4 warps so
-//    that two CTAs fit an SM): read the accumulator two blocks per wait and
-//    store the four bf16 values of every pair at their place in the theta
-//    pass's operand layout.
+//    quarter take alternate 16-column blocks and read two blocks per wait;
+//    narrower tiles keep 4 warps, so that two CTAs fit an SM, and one block
+//    per wait): store the four bf16 values of every pair at their place in
+//    the theta pass's operand layout.
 // Every wait is bounded in time (error word 1); the phi tile and the output
 // must lie inside their buffers (checked on the host); the MMA thread waits
 // for its last commit arrives before the CTA exits.
@@ -280,11 +280,19 @@ __global__ void __launch_bounds__(RtWarps<EW>::threads, 1) k_rows_tc(
           *(__nv_bfloat16 *)(e + 3 * mstride) = dl;
         }
       };
-      // this warp's 16-column blocks: wh, wh + NH, ...; two per wait
+      // this warp's 16-column blocks: wh, wh + NH, ...; two per wait with two
+      // warps per lane quarter (one per wait measured faster with one warp)
       const int nblk = ntn / 16;
       for (int b = wh; b < nblk; b += 2 * NH) {
         uint32_t v[16], w[16];
-        if (b + NH < nblk) {
+        if (NH == 1) {
+          tmem_ld16(ta + 16 * b, v);
+          emit(v, 16 * b);
+          if (b + 1 < nblk) {
+            tmem_ld16(ta + 16 * (b + 1), w);
+            emit(w, 16 * (b + 1));
+          }
+        } else if (b + NH < nblk) {
           tmem_ld16x2(ta + 16 * b, ta + 16 * (b + NH), v, w);
           emit(v, 16 * b);
           emit(w, 16 * (b + NH));
