@@ -318,8 +318,14 @@ __global__ void __launch_bounds__(RtWarps<EW>::threads, 1) k_rows_tc(
 }
 
 po_status init_rows_tc_attributes() {
+  // the whole shared-memory carveout, so that the occupancy query (and the
+  // launch) can place two narrow-tile CTAs on an SM
   PO_CUDA(cudaFuncSetAttribute(k_rows_tc<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, kRtMaxSmem));
   PO_CUDA(cudaFuncSetAttribute(k_rows_tc<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, kRtMaxSmem));
+  PO_CUDA(cudaFuncSetAttribute(k_rows_tc<4>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                               (int)cudaSharedmemCarveoutMaxShared));
+  PO_CUDA(cudaFuncSetAttribute(k_rows_tc<8>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                               (int)cudaSharedmemCarveoutMaxShared));
   return PO_OK;
 }
 
@@ -337,14 +343,16 @@ po_status launch_rows_tc(const float2 *src, uint8_t *dst, size_t dst_bytes, int6
   if (smem > kRtMaxSmem) return fail(PO_ERR_INTERNAL, "tcgen05 row pass: shared memory");
   uint32_t tcols = 32;
   while (tcols < (uint32_t)(2 * ntn)) tcols <<= 1;
-  // resident CTAs per SM (registers, shared memory, tensor memory), persistent over row blocks
+  // resident CTAs per SM, persistent over row blocks: registers (allocated in
+  // units of 8 per thread), shared memory (+1 KB reserved per CTA) and tensor
+  // memory
   const bool wide = ntn > 128;
-  int occ = 0;
-  if (wide)
-    PO_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_rows_tc<8>, RtWarps<8>::threads, smem));
-  else
-    PO_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_rows_tc<4>, RtWarps<4>::threads, smem));
-  const int per_sm = std::max(1, std::min(occ, (int)(512 / tcols)));
+  cudaFuncAttributes fa;
+  PO_CUDA(wide ? cudaFuncGetAttributes(&fa, k_rows_tc<8>) : cudaFuncGetAttributes(&fa, k_rows_tc<4>));
+  const int threads = wide ? RtWarps<8>::threads : RtWarps<4>::threads;
+  const int reg_limit = 65536 / (std::max(1, (fa.numRegs + 7) / 8 * 8) * threads);
+  const int smem_limit = 228 * 1024 / (smem + 1024);
+  const int per_sm = std::max(1, std::min(std::min(reg_limit, smem_limit), (int)(512 / tcols)));
   const int64_t n_rb = (n_rows_out + 63) / 64;
   const int64_t ctas_per_tile = std::min<int64_t>(n_rb, std::max(1, sm_count * per_sm / n_nt));
   const int64_t grid = ctas_per_tile * n_nt;
