@@ -116,32 +116,39 @@ def cpu_direct_sample(cloud, lam, dirs):
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during a
+    timed region: the sampler is live (first line written) before the region
+    starts and only lines written after that count; a region shorter than the
+    period gets one immediate sample when it ends."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
          "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
          "clocks_event_reasons.sw_power_cap")
 
     def __init__(self, gpu_index: int):
         self.path = Path(tempfile.mkstemp(prefix="clocks_", suffix=".csv")[1])
+        self.gpu_index = gpu_index
         self.proc = None
+        self.skip = 0
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={gpu_index}", f"--query-gpu={self.Q}",
                                           "--format=csv,noheader,nounits", "-lms", "200"],
                                          stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except (FileNotFoundError, OSError):
             self.proc = None
+        if self.proc is not None:
+            t0 = time.perf_counter()
+            while time.perf_counter() - t0 < 5.0 and self.proc.poll() is None:
+                if self.path.stat().st_size > 0:
+                    break
+                time.sleep(0.02)
+            self.skip = len(self.path.read_text().splitlines())
 
-    def stop(self):
-        if self.proc is None:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
-        self.proc.terminate()
-        try:
-            self.proc.wait(timeout=5)
-        except subprocess.TimeoutExpired:
-            self.proc.kill()
+    @staticmethod
+    def parse(lines):
+        """(sm MHz list, max MHz list, active slowdown reasons) of nvidia-smi CSV lines."""
         sm, mx, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for line in self.path.read_text().splitlines():
+        for line in lines:
             f = [x.strip() for x in line.split(",")]
             if len(f) < 9:
                 continue
@@ -153,6 +160,25 @@ class ClockSampler:
             for nm, v in zip(names, f[5:9]):
                 if v.lower().startswith("active"):
                     reasons.add(nm)
+        return sm, mx, reasons
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        lines = self.path.read_text().splitlines()[self.skip:]
+        if not self.parse(lines)[0]:
+            try:
+                r = subprocess.run(["nvidia-smi", f"--id={self.gpu_index}", f"--query-gpu={self.Q}",
+                                    "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=20)
+                lines = r.stdout.splitlines()
+            except (FileNotFoundError, OSError, subprocess.TimeoutExpired):
+                lines = []
+        sm, mx, reasons = self.parse(lines)
         self.path.unlink(missing_ok=True)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
                 "reasons": sorted(reasons), "samples": len(sm)}
