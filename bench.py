@@ -371,7 +371,7 @@ def run_fiber(args, world, rank, local):
                                     interp_method=INTERP[args.interp])  # treePO.cu:353-359
     solver = api.Solver(cfg)
     out = torch.empty(solver.out_shape(illum), dtype=torch.float32, device=dev)
-    for _ in range(max(1, min(args.warmup, 1))):
+    for _ in range(args.warmup):
         solver.solve(geom_dev, illum, out=out)
     torch.cuda.synchronize()
     evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
@@ -424,7 +424,7 @@ def run_fiber(args, world, rank, local):
         "metric": "Gpoint-dirs/s (equivalent depth-0 terms) of the split-precision tree solve vs the plain FP64 "
                   "direct sum on the same GPU",
         "value": pd / (ms_hier * 1e-3) / 1e9, "unit": "Gpoint-dirs/s", "n_gpus": 1, "steps": args.steps,
-        "warmup": 1, "ms_per_step": ms_hier, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "warmup": args.warmup, "ms_per_step": ms_hier, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "split bf16 hi+lo products, f32 accumulation (f64 phase arguments)" if args.precision == "split_bf16"
                  else "f32 (f64 phase arguments)",
         "data": "synthetic (seeded fiber height field, sampled on the GPU)",
@@ -502,7 +502,7 @@ def run_cylinder_grad(args, world, rank, local):
         loss.backward()
         return loss, hh.grad
 
-    for _ in range(max(1, min(args.warmup, 2))):
+    for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
     evs = []
@@ -582,7 +582,7 @@ def run_cylinder_grad(args, world, rank, local):
     return {
         "metric": "gradient evaluations/s of ||I(h) - I_target||^2 w.r.t. the displacement field h (forward + adjoint)",
         "value": 1000.0 / ms_step, "unit": "gradients/s", "n_gpus": 1, "steps": args.steps,
-        "warmup": max(1, min(args.warmup, 2)), "ms_per_step": ms_step, "higher_is_better": True,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
         "dtype": "split bf16 hi+lo products, f32 accumulation (f64 phase arguments); f64 currents Jacobian"
                  if args.precision == "split_bf16" else "f32 (f64 phase arguments); f64 currents Jacobian",
