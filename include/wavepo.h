@@ -67,21 +67,24 @@ typedef struct po_config {
   int nyquist_quirk;                /* PO_THETA_REFERENCE only: split the theta Nyquist bin
                                        only where interpolation.h:66's launch reaches */
   double distance;                  /* observer distance Dis of the prefactors (sphere.cu:46) */
-  int interp_method;                /* po_interp_method of the theta pass between levels */
+  int interp_method;                /* po_interp_method of the phi and theta passes between levels */
   int64_t max_workspace_bytes;      /* device workspace cap of one solve; the patterns are
                                        processed in chunks of slots that fit (0 = half of
                                        the device's memory) */
-  int interp_tile;                  /* complex columns per CTA of the tensor-core theta pass
-                                       (autotuner knob): 0 = automatic, 8 or 16 */
+  int interp_tile;                  /* complex columns per CTA of the warp-level tensor-core
+                                       theta pass (levels with few rows; autotuner knob):
+                                       0 = automatic, 8 or 16 */
 } po_config;
 
 /* How the theta interpolation + translation + child sum between tree levels
  * is computed (the phi interpolation always uses the shared-memory FFTs). */
 typedef enum po_interp_method {
   PO_INTERP_FFT = 0,    /* shared-memory batched FFTs (any theta mode) */
-  PO_INTERP_TENSOR = 1  /* the level's trigonometric interpolation matrix as a split hi+lo
-                           BF16 tensor-core product (double-cover theta only; reference
-                           theta mode falls back to the FFTs) */
+  PO_INTERP_TENSOR = 1  /* the level's trigonometric interpolation matrices as split hi+lo
+                           BF16 tensor-core products: tcgen05 with tensor-memory
+                           accumulators on levels whose rows fill 128-row tiles,
+                           warp-level mma.sync on the others (double-cover theta
+                           only; reference theta mode falls back to the FFTs) */
 } po_interp_method;
 
 typedef struct po_geometry {
