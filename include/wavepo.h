@@ -76,15 +76,15 @@ typedef struct po_config {
                                        0 = automatic, 8 or 16 */
 } po_config;
 
-/* How the theta interpolation + translation + child sum between tree levels
- * is computed (the phi interpolation always uses the shared-memory FFTs). */
+/* How the angular interpolation between tree levels (phi pass, then theta
+ * pass with translation and child sum) is computed. */
 typedef enum po_interp_method {
   PO_INTERP_FFT = 0,    /* shared-memory batched FFTs (any theta mode) */
   PO_INTERP_TENSOR = 1  /* the level's trigonometric interpolation matrices as split hi+lo
-                           BF16 tensor-core products: tcgen05 with tensor-memory
-                           accumulators on levels whose rows fill 128-row tiles,
-                           warp-level mma.sync on the others (double-cover theta
-                           only; reference theta mode falls back to the FFTs) */
+                           BF16 tensor-core products, for both passes: tcgen05 with
+                           tensor-memory accumulators on levels whose rows fill 128-row
+                           tiles, warp-level mma.sync on the others (double-cover theta
+                           only; the reference theta mode falls back to the FFTs) */
 } po_interp_method;
 
 typedef struct po_geometry {
@@ -125,6 +125,8 @@ typedef struct po_report {
   int chunk_slots;                  /* patterns per chunk (the last may be smaller) */
   double leaf_point_dirs;           /* sum over leaves of points x leaf directions x patterns */
   double rows_bytes, cols_bytes;    /* algorithmic bytes (pattern reads + writes) of the passes */
+  double ms_rows_level[PO_MAX_DEPTH];  /* ms_rows and ms_cols split by parent level l = 0..depth-1 */
+  double ms_cols_level[PO_MAX_DEPTH];
 } po_report;
 
 typedef struct po_ctx po_ctx;
@@ -243,8 +245,10 @@ po_status po_interp_fft(const float *in, int th_c, int ph_c, float *out, int th_
  * and larger requests are rejected with PO_ERR_INVALID_ARGUMENT.  The first
  * call on a device looks up the array's device address (make it before any
  * stream capture).  All calls share the array: calls that overlap on the GPU
- * race.  The output is complete in stream order; the call does not
- * synchronise. */
+ * race.  The looked-up address is cached per device for the life of the
+ * process; after a cudaDeviceReset it would be stale, so a process that resets
+ * a device must not call this function on it again.  The output is complete
+ * in stream order; the call does not synchronise. */
 #define PO_NOALLOC_SCRATCH_BYTES (16u << 20)
 po_status po_interp_fft_noalloc(const float *in, int th_c, int ph_c, float *out, int th_p, int ph_p, int batch,
                                 int theta_mode, int nyquist_quirk, void *stream);

@@ -71,6 +71,9 @@ def lib():
                                                                                ctypes.c_int, ctypes.c_int64, i64p, f64p]
         L.po_oracle_solve_direct_d.argtypes = [ctypes.c_int64] + [f64p] * 7 + [ctypes.POINTER(Illum), f64p,
                                                                               ctypes.c_int, ctypes.c_int, f64p]
+        L.po_oracle_fields_sampled_d.argtypes = [ctypes.c_int64] + [f64p] * 7 + [
+            ctypes.POINTER(Illum), ctypes.c_int, ctypes.c_int, ctypes.c_int64, i64p, ctypes.c_int, f64p]
+        L.po_oracle_project_sampled.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int64, i64p, f64p, f64p]
         L.po_oracle_average.argtypes = [f32p, ctypes.c_int, ctypes.c_int, f32p, ctypes.c_int, ctypes.c_int]
         L.po_oracle_z0.restype = ctypes.c_double
         L.po_oracle_num_threads.restype = ctypes.c_int
@@ -227,3 +230,58 @@ def solve_sampled_f64(samples, il: Illum, n_theta: int, n_phi: int, dirs) -> np.
     lib().po_oracle_solve_sampled_d(a.shape[1], *[np.ascontiguousarray(a[k]) for k in range(7)], ctypes.byref(il),
                                     n_theta, n_phi, d.size, d, out)
     return out
+
+
+def fields_sampled_f64(samples, il: Illum, n_theta: int, n_phi: int, dirs, per_point: bool = False) -> np.ndarray:
+    """FP64 far field of (7, n) float64 samples at the flat direction indices
+    dirs: (m, 6) complex128, or (n, m, 6) with every point's own field."""
+    a = np.ascontiguousarray(samples, dtype=np.float64)
+    d = np.ascontiguousarray(dirs, dtype=np.int64)
+    n = a.shape[1]
+    out = np.zeros(((n if per_point else 1) * d.size, 12), dtype=np.float64)
+    lib().po_oracle_fields_sampled_d(n, *[np.ascontiguousarray(a[k]) for k in range(7)], ctypes.byref(il), n_theta,
+                                     n_phi, d.size, d, 1 if per_point else 0, out)
+    f = out.view(np.complex128)
+    return f.reshape(n, d.size, 6) if per_point else f
+
+
+def project_sampled(fields, n_theta: int, n_phi: int, dirs) -> np.ndarray:
+    """Transverse field E' (util/fields.h:172-204; intensity = |E'|^2) of
+    fields (m, 6) at the flat direction indices dirs: (m, 3) complex128."""
+    d = np.ascontiguousarray(dirs, dtype=np.int64)
+    f = np.ascontiguousarray(fields, dtype=np.complex128).view(np.float64).reshape(-1)
+    out = np.zeros((d.size, 6), dtype=np.float64)
+    lib().po_oracle_project_sampled(n_theta, n_phi, d.size, d, f, out)
+    return out.view(np.complex128)
+
+
+def point_gradient_fd(samples, il: Illum, n_theta: int, n_phi: int, dirs, weights, points, steps) -> np.ndarray:
+    """Central differences, per point and per component, of the FP64 loss
+    L = sum_j weights[j] * I(dirs[j]) of (7, n) float64 samples.
+
+    Perturbing one sample q of one point p changes the field only by that
+    point's own contribution f_p, so the difference is taken on f_p alone:
+      dL/dq = sum_j w_j 2 Re(conj(E'_j(F)) . E'_j(f_p(q + h) - f_p(q - h))) / (2 h)
+    (E' the linear transverse projection, F the total field).  This is the
+    same central difference as (L(q + h) - L(q - h)) / 2h up to O(h^2), without
+    the cancellation of two nearly equal sums over all points.
+    steps: (7,) step per component (the area step is taken relative).
+    Returns (7, len(points))."""
+    a = np.ascontiguousarray(samples, dtype=np.float64)
+    dirs = np.ascontiguousarray(dirs, dtype=np.int64)
+    w = np.asarray(weights, dtype=np.float64)
+    ep = project_sampled(fields_sampled_f64(a, il, n_theta, n_phi, dirs), n_theta, n_phi, dirs)
+    pts = np.asarray(points)
+    pert = np.repeat(a[:, pts], 14, axis=1).reshape(7, pts.size, 7, 2)  # [comp][point][q][+/-]
+    hs = np.zeros((pts.size, 7))
+    for q in range(7):
+        h = steps[q] * (a[6, pts] if q == 6 else 1.0)
+        hs[:, q] = h
+        pert[q, :, q, 0] += h
+        pert[q, :, q, 1] -= h
+    f = fields_sampled_f64(pert.reshape(7, -1), il, n_theta, n_phi, dirs, per_point=True)
+    f = f.reshape(pts.size, 7, 2, dirs.size, 6)
+    df = (f[:, :, 0] - f[:, :, 1]).reshape(-1, 6)
+    dp = project_sampled(df, n_theta, n_phi, np.tile(dirs, pts.size * 7)).reshape(pts.size, 7, dirs.size, 3)
+    g = 2.0 * np.einsum("j,pqjc->pq", w, np.real(np.conj(ep)[None, None] * dp)) / (2.0 * hs)
+    return g.T

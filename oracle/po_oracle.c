@@ -9,7 +9,7 @@
  * values, because the reference takes them in float (tangentplane.h:29-31,
  * :39-40) and the inputs are float32 arrays.
  *
- * Parity pins for this oracle (see tests/test_oracle_pins.py):
+ * Parity pins for this oracle (tests/test_oracle.py):
  *   - outputs of the reference's own CUDA build run on a GB300 on the same
  *     inputs (tests/golden/ref_*.bin, generated by tests/golden/gen_ref_fixtures.py),
  *   - a Mie-series check on spheres (oracle/mie.py),
@@ -318,9 +318,13 @@ void po_oracle_solve_direct_d(int64_t n, const double *x, const double *y, const
 
 /* po_oracle_solve_direct_d on the listed flat direction indices only
  * (intensity out: [m]). */
-void po_oracle_solve_sampled_d(int64_t n, const double *x, const double *y, const double *z, const double *nx,
-                               const double *ny, const double *nz, const double *area, const po_oracle_illum *il,
-                               int nth, int nph, int64_t m, const int64_t *dirs, double *intensity) {
+/* FP64 far field of (x..area) float64 samples at the flat direction indices
+ * dirs (the sum of po_oracle_solve_direct_d about the origin, without the
+ * intensity): fields [m][6] complex (12 doubles per direction).  per_point
+ * != 0 keeps every point's own field instead of the sum: fields [n][m][6]. */
+void po_oracle_fields_sampled_d(int64_t n, const double *x, const double *y, const double *z, const double *nx,
+                                const double *ny, const double *nz, const double *area, const po_oracle_illum *il,
+                                int nth, int nph, int64_t m, const int64_t *dirs, int per_point, double *fld) {
   double wavedir[3], edir[3], hdir[3];
   po_oracle_incident(il->theta_i, il->phi_i, il->mode_te, wavedir, edir, hdir);
   double k0 = 2.0 * M_PI / il->lambda_m, z0 = orc_z0();
@@ -328,30 +332,53 @@ void po_oracle_solve_sampled_d(int64_t n, const double *x, const double *y, cons
   prefactors(k0, il->dis, &ef, &hf);
   cdbl eta = il->eta_re + I * il->eta_im;
   cdbl *cur = (cdbl *)malloc(sizeof(cdbl) * 6 * (size_t)(n > 0 ? n : 1));
-  double *fld = (double *)malloc(sizeof(double) * 12 * (size_t)(m > 0 ? m : 1));
 #pragma omp parallel for schedule(static)
   for (int64_t p = 0; p < n; ++p) {
     double src[3] = {x[p], y[p], z[p]}, nrm[3] = {nx[p], ny[p], nz[p]};
     tangent_plane_point(wavedir, edir, hdir, 1.0, eta, z0, il->sigma, k0, il->mode_te, src, nrm, cur + 6 * p);
     for (int c = 0; c < 6; ++c) cur[6 * p + c] *= area[p] * (c < 3 ? ef : hf);
   }
-#pragma omp parallel for schedule(dynamic, 1)
-  for (int64_t j = 0; j < m; ++j) {
-    double s[3];
-    direction((int)(dirs[j] / nph), (int)(dirs[j] % nph), nth, nph, s);
-    cdbl acc[6] = {0, 0, 0, 0, 0, 0};
-    for (int64_t p = 0; p < n; ++p) {
+  if (per_point) {
+#pragma omp parallel for schedule(static)
+    for (int64_t q = 0; q < n * m; ++q) {
+      int64_t p = q / m, j = q % m;
+      double s[3];
+      direction((int)(dirs[j] / nph), (int)(dirs[j] % nph), nth, nph, s);
       double ph = k0 * (x[p] * s[0] + y[p] * s[1] + z[p] * s[2]);
       cdbl g = cos(ph) + I * sin(ph);
-      for (int k = 0; k < 6; ++k) acc[k] += cur[6 * p + k] * g;
+      for (int k = 0; k < 6; ++k) {
+        cdbl v = cur[6 * p + k] * g;
+        fld[q * 12 + 2 * k] = creal(v);
+        fld[q * 12 + 2 * k + 1] = cimag(v);
+      }
     }
-    for (int k = 0; k < 6; ++k) {
-      fld[j * 12 + 2 * k] = creal(acc[k]);
-      fld[j * 12 + 2 * k + 1] = cimag(acc[k]);
+  } else {
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int64_t j = 0; j < m; ++j) {
+      double s[3];
+      direction((int)(dirs[j] / nph), (int)(dirs[j] % nph), nth, nph, s);
+      cdbl acc[6] = {0, 0, 0, 0, 0, 0};
+      for (int64_t p = 0; p < n; ++p) {
+        double ph = k0 * (x[p] * s[0] + y[p] * s[1] + z[p] * s[2]);
+        cdbl g = cos(ph) + I * sin(ph);
+        for (int k = 0; k < 6; ++k) acc[k] += cur[6 * p + k] * g;
+      }
+      for (int k = 0; k < 6; ++k) {
+        fld[j * 12 + 2 * k] = creal(acc[k]);
+        fld[j * 12 + 2 * k + 1] = cimag(acc[k]);
+      }
     }
   }
-  po_oracle_intensity_sampled(nth, nph, m, dirs, fld, intensity);
   free(cur);
+}
+
+/* Intensity of the FP64 samples at the flat direction indices dirs. */
+void po_oracle_solve_sampled_d(int64_t n, const double *x, const double *y, const double *z, const double *nx,
+                               const double *ny, const double *nz, const double *area, const po_oracle_illum *il,
+                               int nth, int nph, int64_t m, const int64_t *dirs, double *intensity) {
+  double *fld = (double *)malloc(sizeof(double) * 12 * (size_t)(m > 0 ? m : 1));
+  po_oracle_fields_sampled_d(n, x, y, z, nx, ny, nz, area, il, nth, nph, m, dirs, 0, fld);
+  po_oracle_intensity_sampled(nth, nph, m, dirs, fld, intensity);
   free(fld);
 }
 
@@ -399,6 +426,31 @@ void po_oracle_intensity_sampled(int nth, int nph, int64_t m, const int64_t *dir
     cdbl ey = E[1] + (H[2] * s[0] - H[0] * s[2]) * z0;
     cdbl ez = E[2] - (H[1] * s[0] - H[0] * s[1]) * z0;
     intensity[j] = creal(ex * conj(ex)) + creal(ey * conj(ey)) + creal(ez * conj(ez));
+  }
+}
+
+/* The transverse field E' = E_perp - Z0 s x H_perp of fields.h:172-204 (the
+ * intensity is |E'|^2) at the flat direction indices dirs: out [m][3] complex. */
+void po_oracle_project_sampled(int nth, int nph, int64_t m, const int64_t *dirs, const double *fields,
+                               double *out) {
+  double z0 = orc_z0();
+  for (int64_t j = 0; j < m; ++j) {
+    int64_t d = dirs[j];
+    double s[3];
+    direction((int)(d / nph), (int)(d % nph), nth, nph, s);
+    const double *f = fields + j * 12;
+    cdbl E[3], H[3];
+    for (int c = 0; c < 3; ++c) { E[c] = f[2 * c] + I * f[2 * c + 1]; H[c] = f[6 + 2 * c] + I * f[6 + 2 * c + 1]; }
+    cdbl de = E[0] * s[0] + E[1] * s[1] + E[2] * s[2];
+    for (int c = 0; c < 3; ++c) E[c] -= de * s[c];
+    cdbl dh = H[0] * s[0] + H[1] * s[1] + H[2] * s[2];
+    for (int c = 0; c < 3; ++c) H[c] -= dh * s[c];
+    cdbl e3[3] = {E[0] - (H[2] * s[1] - H[1] * s[2]) * z0, E[1] + (H[2] * s[0] - H[0] * s[2]) * z0,
+                  E[2] - (H[1] * s[0] - H[0] * s[1]) * z0};
+    for (int c = 0; c < 3; ++c) {
+      out[j * 6 + 2 * c] = creal(e3[c]);
+      out[j * 6 + 2 * c + 1] = cimag(e3[c]);
+    }
   }
 }
 

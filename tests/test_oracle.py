@@ -329,3 +329,30 @@ def test_acf_oracle_pipeline_properties():
     f, a = acf.acf_from_ft(noisemat, mean)
     assert a.shape == (16, 20) and np.argmax(a) == np.ravel_multi_index((8, 10), (16, 20))
     assert np.allclose(a[1:, 1:], a[1:, 1:][::-1, ::-1], rtol=1e-9, atol=1e-9 * np.abs(a).max())
+
+
+def test_point_gradient_fd_matches_brute_force_differences():
+    """oracle.point_gradient_fd (central differences taken on one point's own
+    field) equals the plain central differences of the whole FP64 loss."""
+    cloud = geometry.ellipsoid((1.5e-6, 1.0e-6, 0.8e-6), 2000)
+    s64 = cloud.soa().astype(np.float64)
+    th, ph = 0.4, -0.7
+    il = oracle.make_illum(600e-9, th, ph, "E", 1.55 + 0.1j, 3e-6)
+    nth, nph = 24, 48
+    dirs = np.arange(nth * nph)
+    w = np.random.default_rng(5).standard_normal(dirs.size)
+    k = np.array([math.cos(th) * math.cos(ph), math.cos(th) * math.sin(ph), math.sin(th)])
+    lit = np.flatnonzero(s64[3:6].T @ k < -0.05)
+    pts = lit[[3, 50, 400]]
+    steps = [2e-10] * 3 + [1e-6] * 3 + [1e-6]
+    g = oracle.point_gradient_fd(s64, il, nth, nph, dirs, w, pts, steps)
+    fd = np.zeros((7, pts.size))
+    for j, p in enumerate(pts):
+        for q in range(7):
+            h = steps[q] * (s64[6, p] if q == 6 else 1.0)
+            a, b = s64.copy(), s64.copy()
+            a[q, p] += h
+            b[q, p] -= h
+            fd[q, j] = (float(w @ oracle.solve_direct_f64(a, il, nth, nph).ravel()) -
+                        float(w @ oracle.solve_direct_f64(b, il, nth, nph).ravel())) / (2 * h)
+    assert np.all(np.linalg.norm(g - fd, axis=1) / np.linalg.norm(fd, axis=1) < 1e-6)

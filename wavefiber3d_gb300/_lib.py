@@ -66,10 +66,14 @@ class po_report(ctypes.Structure):
                 ("ms_leaf_kernel", ctypes.c_double), ("ms_rows", ctypes.c_double), ("ms_cols", ctypes.c_double),
                 ("n_leaf_launches", ctypes.c_int), ("n_row_launches", ctypes.c_int), ("n_col_launches", ctypes.c_int),
                 ("n_chunks", ctypes.c_int), ("chunk_slots", ctypes.c_int),
-                ("leaf_point_dirs", ctypes.c_double), ("rows_bytes", ctypes.c_double), ("cols_bytes", ctypes.c_double)]
+                ("leaf_point_dirs", ctypes.c_double), ("rows_bytes", ctypes.c_double), ("cols_bytes", ctypes.c_double),
+                ("ms_rows_level", ctypes.c_double * PO_MAX_DEPTH), ("ms_cols_level", ctypes.c_double * PO_MAX_DEPTH)]
 
     def as_dict(self):
-        return {f: getattr(self, f) for f, _ in self._fields_}
+        d = {f: getattr(self, f) for f, _ in self._fields_}
+        for k in ("ms_rows_level", "ms_cols_level"):
+            d[k] = list(d[k])
+        return d
 
 
 EXPORTS = ("po_config_init", "po_status_string", "po_last_error", "po_create", "po_destroy", "po_solve",

@@ -11,9 +11,9 @@ scale) it times the candidate schedules on the GPU and keeps the fastest:
   above).
 
 Every candidate computes the same double-cover patterns (their accuracy
-differences are far below the 1e-3 bar; `tests/test_gpu_batch.py` and the
-batch workload check the chosen ones against FP64), so the choice is by time
-alone.  Results are cached per class, in memory and optionally in a JSON
+differences are far below the 1e-3 bar; `tests/test_gpu_batch.py` checks
+every item of a batch built from the chosen schedules against the FP64
+oracle), so the choice is by time alone.  Results are cached per class, in memory and optionally in a JSON
 file, so a batch of many solves tunes each class once.
 """
 from __future__ import annotations

@@ -91,14 +91,7 @@ __device__ __forceinline__ Dual<T, N> dexp(const Dual<T, N> &a) {
   return dchain(a, e, e);
 }
 template <typename T, int N>
-__device__ __forceinline__ Dual<T, N> dacos(const Dual<T, N> &a) {
-  const T q = (T)1 - a.v * a.v;
-  return dchain(a, acos(a.v), q > (T)0 ? (T)-1 / sqrt(q) : (T)0);
-}
-template <typename T, int N>
 __device__ __forceinline__ Dual<T, N> dabs(const Dual<T, N> &a) { return a.v < (T)0 ? -a : a; }
-template <typename T, int N>
-__device__ __forceinline__ Dual<T, N> dsin(const Dual<T, N> &a) { return dchain(a, sin(a.v), cos(a.v)); }
 
 template <typename T, int N = kNT>
 using CDual = cx<Dual<T, N>>;
@@ -136,24 +129,33 @@ __device__ __forceinline__ CDual<T, N> cdsqrt(const CDual<T, N> &z) {
   const Dual<T, N> b = hb.v > (T)0 ? dsqrt(hb) : dconst<T, N>(0);
   return {a, z.im.v < (T)0 ? -b : b};
 }
-// util/util.h:365-382 with a dual angle and constant indices
+// util/util.h:365-382, differentiated in terms of x = cos(theta) = |k.n|
+// and s2 = sin^2(theta) = 1 - x^2 instead of theta itself.  The reference
+// evaluates sqrt(1 - (sin(theta)/n)^2) with theta = acos(x); the values agree,
+// but the derivative of acos (-1/sqrt(1 - x^2)) and of sin are singular at
+// normal incidence and cancel only analytically: in FP32 their product loses
+// about eps/theta^2 of relative accuracy, which near the specular points of a
+// surface swamps the normal gradient.  d(s2)/dx = -2x carries no such factor.
+// For the incident medium n = 1 the angle cosine is x itself.
 template <typename T, int N>
-__device__ __forceinline__ CDual<T, N> d_cos_internal(const CDual<T, N> &n, const Dual<T, N> &theta) {
-  Dual<T, N> s = dsin(theta);
-  CDual<T, N> q = cddiv(CDual<T, N>{s, dconst<T, N>(0)}, n);
-  q = cddiv(q * s, n);
+__device__ __forceinline__ CDual<T, N> d_cos_internal(const CDual<T, N> &n, const Dual<T, N> &x, const Dual<T, N> &s2) {
+  if (n.re.v == (T)1 && n.im.v == (T)0) return {x, dconst<T, N>(0)};
+  CDual<T, N> q = cddiv(CDual<T, N>{s2, dconst<T, N>(0)}, n);
+  q = cddiv(q, n);
   return cdsqrt(CDual<T, N>{dconst<T, N>(1) - q.re, -q.im});
 }
 template <typename T, int N>
-__device__ __forceinline__ CDual<T, N> d_rs(const Dual<T, N> &theta, const CDual<T, N> &n0, const CDual<T, N> &nt) {
-  CDual<T, N> p0 = n0 * d_cos_internal(n0, theta);
-  CDual<T, N> pt = nt * d_cos_internal(cddiv(nt, n0), theta);
+__device__ __forceinline__ CDual<T, N> d_rs(const Dual<T, N> &x, const Dual<T, N> &s2, const CDual<T, N> &n0,
+                                            const CDual<T, N> &nt) {
+  CDual<T, N> p0 = n0 * d_cos_internal(n0, x, s2);
+  CDual<T, N> pt = nt * d_cos_internal(cddiv(nt, n0), x, s2);
   return cddiv(p0 - pt, p0 + pt);
 }
 template <typename T, int N>
-__device__ __forceinline__ CDual<T, N> d_rp(const Dual<T, N> &theta, const CDual<T, N> &n0, const CDual<T, N> &nt) {
-  CDual<T, N> q0 = cddiv(d_cos_internal(n0, theta), n0);
-  CDual<T, N> qt = cddiv(d_cos_internal(nt, theta), nt);
+__device__ __forceinline__ CDual<T, N> d_rp(const Dual<T, N> &x, const Dual<T, N> &s2, const CDual<T, N> &n0,
+                                            const CDual<T, N> &nt) {
+  CDual<T, N> q0 = cddiv(d_cos_internal(n0, x, s2), n0);
+  CDual<T, N> qt = cddiv(d_cos_internal(nt, x, s2), nt);
   return cddiv(q0 - qt, q0 + qt);
 }
 
@@ -221,9 +223,10 @@ __device__ __forceinline__ void tangent_plane_jvp(const SlotParams<double> &P, f
       Hpar[1] = (Epar[0] * kd[2] - Epar[2] * kd[0]) * iz;
       Hpar[2] = (Epar[1] * kd[0] - Epar[0] * kd[1]) * iz;
       for (int c = 0; c < 3; ++c) Hperp[c] = Hi[c] - Hpar[c];
-      const Dual<T, N> lphi = dacos(dabs(dotvalue));
-      const CDual<T, N> Rs = d_rs(lphi, eta_in, eta_out);
-      const CDual<T, N> Rp = d_rp(lphi, eta_in, eta_out);
+      const Dual<T, N> xc = dabs(dotvalue);  // cos of the local angle acos|k.n|
+      const Dual<T, N> s2 = dconst<T, N>(1) - xc * xc;
+      const CDual<T, N> Rs = d_rs(xc, s2, eta_in, eta_out);
+      const CDual<T, N> Rp = d_rp(xc, s2, eta_in, eta_out);
       for (int c = 0; c < 3; ++c) {
         Es[c] = Eperp[c] * Rs - Epar[c] * Rp;
         Hs[c] = Hpar[c] * Rp - Hperp[c] * Rs;

@@ -526,6 +526,7 @@ struct SolvePlan {
 // Per-kernel-class device times of a solve (CUDA events; requested by a report).
 struct SolveTimes {
   double leaf = 0, agg = 0, inten = 0, leafk = 0, rows = 0, cols = 0;
+  double rows_l[PO_MAX_DEPTH] = {}, cols_l[PO_MAX_DEPTH] = {};
   int n_leaf = 0, n_row = 0, n_col = 0;
   double leaf_pd = 0, rows_b = 0, cols_b = 0;
 };
@@ -744,8 +745,14 @@ static po_status enqueue_solve(po_ctx *c, const SolvePlan &P, float *out_dev, co
     if (cudaEventElapsedTime(&t, c->ev[3], c->ev[4]) == cudaSuccess) times->inten += t;
     if (tree_levels)
       for (int l = 0; l < d; ++l) {
-        if (cudaEventElapsedTime(&t, c->kev[2 + 4 * l], c->kev[3 + 4 * l]) == cudaSuccess) times->rows += t;
-        if (cudaEventElapsedTime(&t, c->kev[4 + 4 * l], c->kev[5 + 4 * l]) == cudaSuccess) times->cols += t;
+        if (cudaEventElapsedTime(&t, c->kev[2 + 4 * l], c->kev[3 + 4 * l]) == cudaSuccess) {
+          times->rows += t;
+          times->rows_l[l] += t;
+        }
+        if (cudaEventElapsedTime(&t, c->kev[4 + 4 * l], c->kev[5 + 4 * l]) == cudaSuccess) {
+          times->cols += t;
+          times->cols_l[l] += t;
+        }
       }
     cudaGetLastError();
     return PO_OK;
@@ -925,8 +932,8 @@ static po_status check_device_waits(po_ctx *c) {
   PO_CUDA(cudaMemcpy(&h, c->tc_err.p, sizeof(int), cudaMemcpyDeviceToHost));
   if (h == 0) return PO_OK;
   PO_CUDA(cudaMemset(c->tc_err.p, 0, sizeof(int)));
-  if (h == 2) return fail(PO_ERR_INTERNAL, "tcgen05 theta pass: operand run outside its buffer");
-  return fail(PO_ERR_TIMEOUT, "tcgen05 theta pass: a device wait timed out");
+  if (h == 2) return fail(PO_ERR_INTERNAL, "tcgen05 theta/phi pass: operand run outside its buffer");
+  return fail(PO_ERR_TIMEOUT, "tcgen05 theta/phi pass: a device wait timed out");
 }
 
 static po_status solve_impl(po_ctx *c, const po_geometry *g, const po_illum *il, float *intensity, int out_on_device,
@@ -988,6 +995,10 @@ static po_status solve_impl(po_ctx *c, const po_geometry *g, const po_illum *il,
     rep->ms_leaf_kernel = T.leafk;
     rep->ms_rows = T.rows;
     rep->ms_cols = T.cols;
+    for (int l = 0; l < PO_MAX_DEPTH; ++l) {
+      rep->ms_rows_level[l] = T.rows_l[l];
+      rep->ms_cols_level[l] = T.cols_l[l];
+    }
     cudaGetLastError();
   }
   return PO_OK;
@@ -1171,8 +1182,8 @@ po_status po_interp_fft(const float *in, int th_c, int ph_c, float *out, int th_
   if (e != cudaSuccess) { cudaFreeAsync(tw, st); return cuda_fail(e, "cudaMallocAsync(scratch)"); }
   for (int n : lens)
     if (s == PO_OK) s = launch_twiddles(n, (float2 *)tw + off[n], st);
-  int sm = 152;
-  cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, 0);
+  int sm = 152, dev = 0;
+  if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, dev);
   if (s == PO_OK)
     s = launch_interp_rows((const float2 *)in, (float2 *)mid, (int64_t)batch * th_c, make_plan(ph_c, off[ph_c]),
                            make_plan(ph_p, off[ph_p]), (const float2 *)tw, 1.0f / (float)ph_c, sm,
