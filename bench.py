@@ -1,24 +1,36 @@
 #!/usr/bin/env python
-"""Benchmark of the GB300 PO engine on the hierarchical ellipsoid workload.
+"""Benchmark of the GB300 PO engine.
 
-Workload (one step = one full solve): ellipsoid with radii 8 x 5 x 5 um,
-400,000 area-weighted Fibonacci-lattice points with analytic normals,
-index of refraction 1.55+0.1i, 25 wavelengths 400 + 12 i nm (i = 0..24, the
-reference's even spacing, compareMie/sphere.cu:489), one incidence along +x
-(theta_i = phi_i = 0), TM, octree depth 5 with the reference's level grids
-(extent 16 um, ratio 1.3: 197/108/62/37/24), output 180 x 360, FP32 patterns
-with FP64 phase arguments, double-cover theta interpolation.  Synthetic,
-seeded geometry stands in for the reference's meshes.
+Headline workload (default; one step = one full solve): the synthetic fiber
+segment -- elliptical cross-section 25 x 20 um, 60 um long, cuticle sawtooth
+(5 um scales, 0.4 um step, 3 degree tilt) and seeded Gaussian height noise
+(sigma 0.05 um, correlation 1 um), sampled at 0.05 um (3.40M points) by the
+GPU height-field sampler; index 1.55+0.1i, 25 wavelengths 400 + 12 i nm
+(i = 0..24, the reference's even spacing, compareMie/sphere.cu:489), 64
+incidences (theta sweep at phi = 0, fibersim/treePO.cu:559-564), TM, octree
+depth 7 with the reference's level grids (fibersim/treePO.cu:353-373),
+output 180 x 360; split hi+lo BF16 tensor-core leaf products with FP32
+accumulation and FP64 phase arguments, double-cover theta interpolation.
+The same line carries the plain FP64 direct sum on the same GPU (timed on
+the full point set for one pattern, scaled by the pattern count), the
+end-to-end time through po_solve with host buffers, the roofline of the
+dominant kernel class and the FP64 oracle on the host cores.
+
+Other workloads (--workload): ellipsoid (8 x 5 x 5 um, 400k points, 25
+wavelengths, depth 5), cylinder-grad (the gradient of ||I(h) - I_t||^2 with
+respect to a displacement field), batch (256 independent solves in one CUDA
+graph).
 
 Metric: Gpoint-dirs/s = N * 180*360 * L * I * P / time / 1e9 (the equivalent
 depth-0 count), plus patterns/s; accuracy is the rel-L2 of intensity against
-the FP64 direct sum on a seeded sample of output directions.
+the FP64 direct sum.
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--workload W]
 
 `--impl reference` times the reference path's CPU implementation: the
 reference ships CUDA only, so this is the FP64 direct-sum restatement of its
-algorithm (oracle/) on all host cores, on a bounded direction sample.
+algorithm (oracle/) on all host cores, on a bounded direction sample of the
+same workload.
 """
 from __future__ import annotations
 
@@ -333,8 +345,15 @@ FIBER_LENGTH = 60e-6
 FIBER_DEPTH = 7
 FIBER_SIGMA = 10e-6          # Gaussian beam width of the reference's fiber presets 0/1 (treePO.cu:47)
 FIBER_INC = 64               # theta sweep at phi_i = 0: theta_i = -pi/2 + 1e-10 + pi/180 * idx, idx = 58..121
+FIBER_SEED = 11
 FIBER_WORKLOAD = ("fiber segment 25x20um x 60um, cuticle 5um/0.4um/3deg + Gaussian noise 0.05um/1um, "
-                  "0.05um spacing (3.40M points), depth 7, 64 incidences x TM per wavelength, 180x360 grid")
+                  "0.05um spacing (3.40M points), depth 7, 25 wavelengths x 64 incidences x TM, 180x360 grid")
+FIBER_BOX_MIN = [-1.1 * FIBER_RADII[0], -1.1 * FIBER_RADII[1], -0.55 * FIBER_LENGTH]  # treePO.cu:96-98
+FIBER_BOX_MAX = [-v for v in FIBER_BOX_MIN]
+# DRAM bytes per algorithmic byte of the aggregation passes, from the ncu capture summarised in
+# profiles/aggregation_fiber.md (dram__bytes_read.sum + dram__bytes_write.sum of the phi and theta
+# launches of one wavelength, over the per-level algorithmic bytes of the same launches)
+FIBER_AGG_TRAFFIC_RATIO = None
 
 
 def fiber_incidences():
@@ -342,10 +361,19 @@ def fiber_incidences():
     return list(-math.pi / 2 + 1e-10 + math.pi / 180 * idx), [0.0] * FIBER_INC
 
 
+def fiber_config(precision: str, interp: str = "tensor"):
+    from wavefiber3d_gb300 import api
+    return api.Config.reference_rule(FIBER_DEPTH, N_THETA, N_PHI, FIBER_BOX_MIN, FIBER_BOX_MAX, FIBER_LENGTH,
+                                     2 * max(FIBER_RADII), 1.2, precision=PRECISIONS[precision],
+                                     interp_method=INTERP[interp])  # treePO.cu:353-359
+
+
 def run_fiber(args, world, rank, local):
-    """Split-precision hierarchical solve of the fiber segment against the plain
-    FP64 direct sum on the same GPU (timed on every 64th point and scaled by
-    the point count, which the direct sum is linear in)."""
+    """Config 3, the headline: the split-precision hierarchical solve of the
+    3.4M-point fiber segment over 25 wavelengths x 64 incidences per step,
+    against the plain FP64 direct sum on the same GPU (B1, timed on the full
+    point set for one (wavelength, incidence) pair and scaled by the pattern
+    count) and the FP64 oracle on the host cores."""
     import torch
 
     from wavefiber3d_gb300 import api, geometry
@@ -354,99 +382,177 @@ def run_fiber(args, world, rank, local):
     dev = torch.device("cuda", local)
     torch.cuda.set_device(dev)
     st = torch.cuda.current_stream()
-    hf = geometry.fiber_height_field(FIBER_RADII, FIBER_LENGTH, seed=11)
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    bf16_peak = peaks.get("bf16_tflops_sustained", 1700.0)
+    peak_src = "measured" if peaks else "fallback"
+    hf = geometry.fiber_height_field(FIBER_RADII, FIBER_LENGTH, seed=FIBER_SEED)
     t0 = time.perf_counter()
     g_dev = api.height_field_points(hf)  # the GPU height-field sampler (util/geometry.h:76-179)
     torch.cuda.synchronize()
     t_geom = time.perf_counter() - t0
     n = g_dev.shape[1]
     geom_dev = tuple(g_dev[k] for k in range(7))
-    bmin = [-1.1 * FIBER_RADII[0], -1.1 * FIBER_RADII[1], -0.55 * FIBER_LENGTH]  # treePO.cu:96-98
-    bmax = [-v for v in bmin]
+    g_host = g_dev.cpu().pin_memory()
+    geom_host = tuple(g_host[k] for k in range(7))
     lams = LAMBDAS[: args.fiber_lambdas]
     th, ph = fiber_incidences()
     illum = api.Illumination(lams, th, ph, api.PO_POL_TM, ETA, FIBER_SIGMA)
-    cfg = api.Config.reference_rule(FIBER_DEPTH, N_THETA, N_PHI, bmin, bmax, FIBER_LENGTH,
-                                    2 * max(FIBER_RADII), 1.2, precision=PRECISIONS[args.precision],
-                                    interp_method=INTERP[args.interp])  # treePO.cu:353-359
+    cfg = fiber_config(args.precision, args.interp)
     solver = api.Solver(cfg)
     out = torch.empty(solver.out_shape(illum), dtype=torch.float32, device=dev)
+    out_host = torch.empty(solver.out_shape(illum), dtype=torch.float32).pin_memory()
+    pd_step = float(n) * N_THETA * N_PHI * illum.n_patterns
+
     for _ in range(args.warmup):
-        solver.solve(geom_dev, illum, out=out)
+        solver.solve(geom_dev, illum, out=out, report=False)
     torch.cuda.synchronize()
+
+    # ---- device-resident timed region (inputs, tree and level buffers are far larger than L2)
     evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    reps = []
     clocks = ClockSampler(local)
+    barrier(world)
+    torch.cuda.synchronize()
+    t_wall0 = time.perf_counter()
     for i in range(args.steps):
         evs[i][0].record(st)
-        solver.solve(geom_dev, illum, out=out)
+        solver.solve(geom_dev, illum, out=out, report=False)
         evs[i][1].record(st)
-        reps.append(dict(solver.last_report))
     torch.cuda.synchronize()
+    barrier(world)
+    t_wall = time.perf_counter() - t_wall0
     clk = clocks.stop()
-    ms_hier = statistics.mean(a.elapsed_time(b) for a, b in evs)
-    solver.close()
+    ms_step = statistics.mean(a.elapsed_time(b) for a, b in evs)
+    ms_step_max = max_over_ranks(ms_step, world)
 
-    # plain FP64 direct sum, same GPU, same wavelengths and incidences, every 64th point
-    stride = 64
-    sub = g_dev[:, ::stride].contiguous()
-    n_sub = sub.shape[1]
-    cfg64 = api.Config(0, [N_THETA], [N_PHI], bmin, bmax, precision=api.PO_PREC_FP64)
-    il64 = api.Illumination(lams[:1], th, ph, api.PO_POL_TM, ETA, FIBER_SIGMA)
+    # ---- per-kernel-class breakdown: one more solve with its report (events inside the solve), untimed
+    solver.solve(geom_dev, illum, out=out)
+    r = dict(solver.last_report)
+
+    # ---- end to end through the C ABI with host buffers (geometry H2D and intensity D2H inside)
+    n_e2e = max(1, min(args.steps, args.e2e_steps))
+    e2e_ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(n_e2e)]
+    barrier(world)
+    torch.cuda.synchronize()
+    for i in range(n_e2e):
+        e2e_ev[i][0].record(st)
+        solver.solve(geom_host, illum, out=out_host, report=False)
+        e2e_ev[i][1].record(st)
+    torch.cuda.synchronize()
+    barrier(world)
+    e2e_ms = max_over_ranks(statistics.mean(a.elapsed_time(b) for a, b in e2e_ev), world)
+    e2e_same = bool(torch.equal(out_host, out.cpu()))
+    solver.close()
+    result = None
+    if rank != 0:
+        return None
+
+    # ---- plain FP64 direct sum on the same GPU (B1): full point set, one (wavelength, incidence) pair
+    cfg64 = api.Config(0, [N_THETA], [N_PHI], FIBER_BOX_MIN, FIBER_BOX_MAX, precision=api.PO_PREC_FP64)
+    il64 = api.Illumination(lams[:1], th[:1], ph[:1], api.PO_POL_TM, ETA, FIBER_SIGMA)
     with api.Solver(cfg64) as s64:
         o64 = torch.empty(s64.out_shape(il64), dtype=torch.float32, device=dev)
-        s64.solve(tuple(sub[k] for k in range(7)), il64, out=o64)
-        torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(st)
-        s64.solve(tuple(sub[k] for k in range(7)), il64, out=o64)
+        s64.solve(geom_dev, il64, out=o64, report=False)
         e1.record(st)
         torch.cuda.synchronize()
-        ms64_sub = e0.elapsed_time(e1)
-    ms64_full = ms64_sub * (n / n_sub) * len(lams)  # linear in points and wavelengths
+        ms64_pair = e0.elapsed_time(e1)
+    ms64_full = ms64_pair * illum.n_patterns  # linear in the pattern count (one sum per pattern)
+    ref64 = o64[0, 0, 0].double()
+    rel_full_grid = float((out[0, 0, 0].double() - ref64).norm() / ref64.norm())
 
-    # accuracy: FP64 oracle on the host for two incidences, sampled directions
+    # ---- accuracy against the FP64 oracle on the host (two incidences, sampled directions)
     import oracle
-    cloud = geometry.PointCloud.from_soa(g_dev.cpu().numpy())
+    cloud = geometry.PointCloud.from_soa(g_host.numpy())
     dirs = sample_directions(args.fiber_dirs)
     errs = []
+    ctr = [0.5 * (a + b) for a, b in zip(np.float32(FIBER_BOX_MIN), np.float32(FIBER_BOX_MAX))]
     for ii in (0, FIBER_INC - 1):
         il = oracle.make_illum(lams[0], th[ii], ph[ii], "M", ETA, FIBER_SIGMA)
         cur = oracle.currents(cloud, il)
-        ctr = [0.5 * (a + b) for a, b in zip(np.float32(bmin), np.float32(bmax))]
         f = oracle.far_field_sampled(cloud, cur, 2 * math.pi / lams[0], ctr, N_THETA, N_PHI, dirs)
         ref = oracle.intensity_sampled(f, N_THETA, N_PHI, dirs)
         got = out[0, ii, 0].reshape(-1).cpu().numpy()[dirs].astype(np.float64)
         errs.append(float(np.linalg.norm(got - ref) / np.linalg.norm(ref)))
-    pd = float(n) * N_THETA * N_PHI * illum.n_patterns
-    r = reps[-1]
-    return {
-        "metric": "Gpoint-dirs/s (equivalent depth-0 terms) of the split-precision tree solve vs the plain FP64 "
-                  "direct sum on the same GPU",
-        "value": pd / (ms_hier * 1e-3) / 1e9, "unit": "Gpoint-dirs/s", "n_gpus": 1, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms_hier, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "split bf16 hi+lo products, f32 accumulation (f64 phase arguments)" if args.precision == "split_bf16"
-                 else "f32 (f64 phase arguments)",
+
+    # ---- CPU baseline: the FP64 oracle direct sum on all host cores, bounded direction sample
+    cdirs = sample_directions(args.cpu_dirs, seed=5)
+    il = oracle.make_illum(lams[0], th[0], ph[0], "M", ETA, FIBER_SIGMA)
+    t0 = time.perf_counter()
+    cur = oracle.currents(cloud, il)
+    f = oracle.far_field_sampled(cloud, cur, 2 * math.pi / lams[0], ctr, N_THETA, N_PHI, cdirs)
+    oracle.intensity_sampled(f, N_THETA, N_PHI, cdirs)
+    cpu_s = time.perf_counter() - t0
+    cpu_value = float(n) * cdirs.size / cpu_s / 1e9
+
+    # ---- roofline of the dominant kernel class (CUDA events inside the solve)
+    agg_ms = r["ms_rows"] + r["ms_cols"]
+    classes = {"leaf far-field contraction": r["ms_leaf_kernel"],
+               "aggregation (phi + theta passes, translation, child sums)": agg_ms}
+    dom = max(classes, key=classes.get)
+    if dom.startswith("leaf"):
+        flops = r["leaf_point_dirs"] * (8 * 6 + 5)
+        achieved = flops / (r["ms_leaf_kernel"] * 1e-3) / 1e12
+        roof = {"bound": "tensor", "kernel": dom, "achieved": achieved, "peak": bf16_peak, "unit": "TFLOP/s",
+                "frac": achieved / bf16_peak, "traffic": None,
+                "note": f"algorithmic flops = leaf point-directions x (8 x 6 + 5); peak = {peak_src} sustained bf16 "
+                        "dense (the hi/lo split products are not counted as work)"}
+    else:
+        achieved = r["agg_bytes"] / (agg_ms * 1e-3) / 1e9
+        traffic = None if FIBER_AGG_TRAFFIC_RATIO is None else FIBER_AGG_TRAFFIC_RATIO * r["agg_bytes"]
+        roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                "frac": achieved / hbm_peak, "traffic": traffic,
+                "note": "algorithmic bytes = per level, the child patterns read at the child grid + the parent "
+                        f"patterns written (8 B per complex sample); peak = {peak_src} copy bandwidth; traffic = "
+                        "ncu DRAM bytes per step scaled from a one-wavelength capture"}
+    result = {
+        "metric": "Gpoint-dirs/s (equivalent depth-0 point x direction terms) at rel-L2<=1e-3 vs FP64 direct sum",
+        "value": pd_step * world / (ms_step_max * 1e-3) / 1e9,
+        "unit": "Gpoint-dirs/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms_step_max, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "split bf16 hi+lo tensor-core products, f32 accumulation (f64 phase arguments)"
+                 if args.precision == "split_bf16" else "f32 (f64 phase arguments)",
         "data": "synthetic (seeded fiber height field, sampled on the GPU)",
         "config": {"workload": FIBER_WORKLOAD, "points": n, "numel": hf.numel, "numelvert": hf.numelvert,
-                   "wavelengths": len(lams), "incidences": FIBER_INC, "depth": FIBER_DEPTH,
-                   "level_grids": [list(cfg.n_theta), list(cfg.n_phi)], "precision": args.precision,
-                   "theta_interpolation": args.interp, "beam_sigma_m": FIBER_SIGMA,
-                   "l2": "inputs and patterns far larger than L2"},
-        "patterns_per_s": illum.n_patterns / (ms_hier * 1e-3),
-        "plain_fp64_direct": {"ms_per_step_scaled": ms64_full, "ms_measured": ms64_sub, "points_measured": n_sub,
-                              "note": f"FP64 depth-0 sum on every {stride}th point, scaled by {n / n_sub:.2f} "
-                                      f"(points) x {len(lams)} (wavelengths)",
-                              "value": pd / (ms64_full * 1e-3) / 1e9},
-        "speedup_vs_plain_fp64": ms64_full / ms_hier,
-        "rel_l2_vs_fp64": max(errs), "rel_l2_per_incidence": errs,
-        "accuracy_sample": f"{dirs.size} seeded directions, lambda={lams[0] * 1e9:.0f} nm, incidences 0 and "
-                           f"{FIBER_INC - 1}, FP64 oracle on the host",
+                   "wavelengths": len(lams), "incidences": FIBER_INC, "polarisations": 1, "depth": FIBER_DEPTH,
+                   "directions": N_THETA * N_PHI, "level_grids": [list(cfg.n_theta), list(cfg.n_phi)],
+                   "precision": args.precision, "theta_mode": "double cover", "theta_interpolation": args.interp,
+                   "beam_sigma_m": FIBER_SIGMA,
+                   "l2": "no flush: inputs (95 MB), tree and level buffers (>100 GB) are far larger than L2",
+                   "parallelism": f"replicas x{world}"},
+        "patterns_per_s": illum.n_patterns * world / (ms_step_max * 1e-3),
+        "e2e": {"value": pd_step * world / (e2e_ms * 1e-3) / 1e9, "unit": "Gpoint-dirs/s", "ms_per_step": e2e_ms,
+                "steps": n_e2e, "h2d_bytes_per_step": int(g_host.numel() * 4),
+                "d2h_bytes_per_step": int(out_host.numel() * 4), "equals_device_output": e2e_same,
+                "path": "po_solve with host geometry and host intensity (copies inside the call)"},
+        "plain_fp64_gpu": {"ms_per_pattern_measured": ms64_pair, "ms_per_step_scaled": ms64_full,
+                           "value": pd_step / (ms64_full * 1e-3) / 1e9,
+                           "note": f"FP64 depth-0 sum (k_direct_f64) over all {n} points and 64800 directions for "
+                                   f"lambda={lams[0] * 1e9:.0f} nm, incidence 0; scaled by the "
+                                   f"{illum.n_patterns} patterns of a step"},
+        "speedup_vs_plain_fp64_gpu": ms64_full / ms_step_max,
+        "rel_l2_vs_fp64": max(errs + [rel_full_grid]),
+        "rel_l2_vs_fp64_gpu_full_grid": rel_full_grid,
+        "rel_l2_vs_fp64_oracle_per_incidence": errs,
+        "accuracy_sample": f"all 64800 directions of lambda={lams[0] * 1e9:.0f} nm, incidence 0 against the FP64 GPU "
+                           f"sum; {dirs.size} seeded directions of incidences 0 and {FIBER_INC - 1} against the "
+                           "FP64 oracle on the host",
+        "roofline": roof,
+        "kernel_ms_per_step": {"leaf": r["ms_leaf_kernel"], "phi passes": r["ms_rows"], "theta passes": r["ms_cols"],
+                               "phi by level": r["ms_rows_level"][:FIBER_DEPTH],
+                               "theta by level": r["ms_cols_level"][:FIBER_DEPTH]},
+        "cpu_baseline": {"value": cpu_value, "unit": "Gpoint-dirs/s", "cores": oracle.num_threads(), "kind": "port",
+                         "sample": f"FP64 direct sum (oracle/po_oracle.c) of all {n} points x {cdirs.size} seeded "
+                                   f"directions, lambda={lams[0] * 1e9:.0f} nm, incidence 0",
+                         "seconds": cpu_s},
         "geometry_build_ms": t_geom * 1e3,
-        "gpu_launches": int(sum(x["kernel_launches"] for x in reps)),
+        "gpu_launches": int(args.steps * r["kernel_launches"]),  # launches per solve are fixed
         "clocks": clk,
+        "wall_s_timed_region": t_wall,
         "report": r,
     }
+    return result
 
 
 # ---------------------------------------------------- differentiation workload
@@ -740,31 +846,54 @@ def run_batch(args, world, rank, local):
 
 
 def run_reference(args, world, rank):
-    """CPU implementation of the path (FP64 direct sum restatement), all host cores."""
+    """CPU implementation of the path on all host cores: the reference ships
+    CUDA only, so this is the FP64 direct-sum restatement of its algorithm
+    (oracle/), on a bounded direction sample of the workload's geometry."""
     if rank != 0:
         return None
+    import oracle
     from wavefiber3d_gb300 import geometry
-    cloud = geometry.ellipsoid(RADII, N_POINTS)
-    dirs = sample_directions(args.cpu_dirs)
+    if args.workload == "ellipsoid":
+        cloud = geometry.ellipsoid(RADII, N_POINTS)
+        wl, lam_list, incs, sigma, ctr = WORKLOAD, LAMBDAS, [(0.0, 0.0)], SIGMA, [0.0, 0.0, 0.0]
+        data = "synthetic (seeded ellipsoid, analytic normals)"
+    else:
+        hf = geometry.fiber_height_field(FIBER_RADII, FIBER_LENGTH, seed=FIBER_SEED)
+        soa, bad = oracle.height_field(hf)  # util/geometry.h:76-179 on the host (bit-exact with the GPU sampler)
+        assert not bad
+        cloud = geometry.PointCloud.from_soa(soa)
+        th, ph = fiber_incidences()
+        wl, lam_list, incs, sigma = FIBER_WORKLOAD, LAMBDAS, list(zip(th, ph)), FIBER_SIGMA
+        ctr = [0.5 * (a + b) for a, b in zip(np.float32(FIBER_BOX_MIN), np.float32(FIBER_BOX_MAX))]
+        data = "synthetic (seeded fiber height field, sampled on the host)"
+    dirs = sample_directions(args.ref_dirs)
+
+    def one(i, d):
+        lam = lam_list[i % len(lam_list)]
+        t, p = incs[(i // len(lam_list)) % len(incs)]
+        il = oracle.make_illum(lam, t, p, "M", ETA, sigma)
+        t0 = time.perf_counter()
+        cur = oracle.currents(cloud, il)
+        f = oracle.far_field_sampled(cloud, cur, 2 * math.pi / lam, ctr, N_THETA, N_PHI, d)
+        oracle.intensity_sampled(f, N_THETA, N_PHI, d)
+        return time.perf_counter() - t0
+
     for _ in range(max(0, min(args.warmup, 1))):
-        cpu_direct_sample(cloud, LAMBDAS[0], dirs[:64])
-    secs = []
-    threads = 1
-    for i in range(args.steps):
-        _, s, threads = cpu_direct_sample(cloud, LAMBDAS[i % len(LAMBDAS)], dirs)
-        secs.append(s)
+        one(0, dirs[:64])
+    secs = [one(i, dirs) for i in range(args.steps)]
     per = sum(secs) / len(secs)
-    value = N_POINTS * dirs.size / per / 1e9
+    value = cloud.n * dirs.size / per / 1e9
     return {
         "impl": "reference",
         "metric": "Gpoint-dirs/s (equivalent depth-0 point x direction terms) at rel-L2<=1e-3 vs FP64 direct sum",
         "value": value, "unit": "Gpoint-dirs/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": per * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64", "data": "synthetic (seeded ellipsoid, analytic normals)",
-        "config": {"workload": WORKLOAD, "points": N_POINTS, "directions": N_THETA * N_PHI,
-                   "step": f"bounded sample: {dirs.size} directions x 1 wavelength per step"},
-        "cpu_baseline": {"value": value, "unit": "Gpoint-dirs/s", "cores": threads, "kind": "port",
-                         "sample": f"FP64 direct sum (oracle/po_oracle.c), {N_POINTS} points x {dirs.size} "
+        "dtype": "f64", "data": data,
+        "config": {"workload": wl, "points": cloud.n, "directions": N_THETA * N_PHI,
+                   "step": f"bounded sample: {dirs.size} directions x 1 (wavelength, incidence) per step, cycling "
+                           "through the workload's wavelengths and incidences"},
+        "cpu_baseline": {"value": value, "unit": "Gpoint-dirs/s", "cores": oracle.num_threads(), "kind": "port",
+                         "sample": f"FP64 direct sum (oracle/po_oracle.c), {cloud.n} points x {dirs.size} "
                                    "directions per step; the reference ships no CPU path and its CUDA build "
                                    "needs a GPU"},
         "e2e": {"value": value, "unit": "Gpoint-dirs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -774,10 +903,10 @@ def run_reference(args, world, rank):
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["engine", "reference"], default="engine")
-    ap.add_argument("--cpu-dirs", type=int, default=2048, help="directions of the FP64 CPU sample")
+    ap.add_argument("--cpu-dirs", type=int, default=1024, help="directions of the FP64 CPU baseline sample")
     ap.add_argument("--precision", choices=sorted(PRECISIONS), default=None,
                     help="leaf precision (default: split_bf16 for the ellipsoid and the fiber -- the faster one at "
                          "the same accuracy on GB300 -- and fp32 for the cylinder gradient)")
@@ -786,10 +915,13 @@ def main():
                     help="complex columns per CTA of the tensor-core theta pass (0: automatic)")
     ap.add_argument("--lambdas", type=int, default=25,
                     help="wavelengths of the ellipsoid workload (25 = the headline; fewer for profiling runs)")
-    ap.add_argument("--workload", choices=["ellipsoid", "fiber", "cylinder-grad", "batch"], default="ellipsoid",
-                    help="ellipsoid: the headline 400k-point depth-5 workload; fiber: the 3.4M-point fiber "
-                         "segment (split precision vs plain FP64 on the same GPU)")
-    ap.add_argument("--fiber-lambdas", type=int, default=1, help="wavelengths per fiber step (400 nm first)")
+    ap.add_argument("--workload", choices=["fiber", "ellipsoid", "cylinder-grad", "batch"], default="fiber",
+                    help="fiber: the headline, the 3.4M-point fiber segment, 25 wavelengths x 64 incidences, depth 7 "
+                         "(split precision vs plain FP64 on the same GPU); ellipsoid: 400k points, 25 wavelengths, "
+                         "depth 5; cylinder-grad: the gradient workload; batch: 256 independent solves")
+    ap.add_argument("--fiber-lambdas", type=int, default=25, help="wavelengths per fiber step (25 = the workload)")
+    ap.add_argument("--e2e-steps", type=int, default=2, help="steps of the end-to-end (host buffers) timing")
+    ap.add_argument("--ref-dirs", type=int, default=256, help="directions per step of the --impl reference arm")
     ap.add_argument("--fiber-dirs", type=int, default=512, help="directions of the fiber accuracy sample")
     ap.add_argument("--cyl-lambdas", type=int, default=25, help="wavelengths of the cylinder gradient step")
     ap.add_argument("--cyl-fd-dirs", type=int, default=256, help="directions of the cylinder FD check")
@@ -806,7 +938,7 @@ def main():
     if args.impl == "reference":
         res = run_reference(args, world, rank)
     elif args.workload == "fiber":
-        res = run_fiber(args, world, rank, local) if rank == 0 else None
+        res = run_fiber(args, world, rank, local)
     elif args.workload == "cylinder-grad":
         res = run_cylinder_grad(args, world, rank, local) if rank == 0 else None
     elif args.workload == "batch":

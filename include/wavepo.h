@@ -127,6 +127,9 @@ typedef struct po_report {
   double rows_bytes, cols_bytes;    /* algorithmic bytes (pattern reads + writes) of the passes */
   double ms_rows_level[PO_MAX_DEPTH];  /* ms_rows and ms_cols split by parent level l = 0..depth-1 */
   double ms_cols_level[PO_MAX_DEPTH];
+  double agg_bytes;                 /* algorithmic bytes of the aggregation: per level, the child
+                                       patterns read at the child grid + the parent patterns written */
+  int64_t n_nodes_level[PO_MAX_DEPTH + 1];  /* active nodes per level (0 = root) */
 } po_report;
 
 typedef struct po_ctx po_ctx;

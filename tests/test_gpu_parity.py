@@ -361,3 +361,71 @@ def test_large_leaf_phases_vs_fp64_direct(prec):
     out, rep = _solve(cloud, cfg, il)
     o = oracle.solve_direct(cloud, oracle.make_illum(500e-9, 0.3, 0.7, "M", 1.55 + 0.1j, 2e-5), 24, 48)
     assert rel(out.reshape(o.shape), o) < TOL_TREE, rep
+
+
+# ------------------------------------------------------- tcgen05 leaf sums
+def _many_incidences(n_inc, seed=3):
+    rng = np.random.default_rng(seed)
+    return list(rng.uniform(-1.3, 1.3, n_inc)), list(rng.uniform(0.0, 2 * math.pi, n_inc))
+
+
+def test_leaf_tcgen05_vs_fp64_direct_and_fp32():
+    """35 incidences x both polarisations per wavelength (70 patterns: two
+    slot groups of the tcgen05 leaf kernel, 64 + 6, and a partly filled
+    column tile): every pattern against the FP32 CUDA-core path, and four of
+    them against the FP64 oracle direct sum."""
+    cloud = geometry.ellipsoid((1.5e-6, 1.0e-6, 0.8e-6), 3000)
+    box = [-1.65e-6, -1.1e-6, -0.88e-6, 1.65e-6, 1.1e-6, 0.88e-6]
+    th, ph = _many_incidences(35)
+    il = api.Illumination([480e-9], th, ph, api.PO_POL_TM | api.PO_POL_TE, 1.55 + 0.1j, 2e-6)
+    outs, reps = [], []
+    for prec in (api.PO_PREC_FP32, api.PO_PREC_SPLIT_BF16):
+        cfg = api.Config.reference_rule(2, 32, 64, box[:3], box[3:], 1.6e-6, 3.0e-6, 1.2, precision=prec)
+        o, r = _solve(cloud, cfg, il)
+        outs.append(o.reshape(35, 2, 32, 64))
+        reps.append(r)
+    assert reps[1]["n_leaf_launches"] == 4, reps[1]  # operands + sums, two slot groups
+    assert rel(outs[1], outs[0]) < 1e-4
+    ctr = [(box[i] + box[i + 3]) / 2 for i in range(3)]
+    for ii, pol in ((0, 0), (17, 1), (34, 0), (34, 1)):
+        o = oracle.solve_direct(cloud, oracle.make_illum(480e-9, th[ii], ph[ii], "E" if pol else "M", 1.55 + 0.1j,
+                                                         2e-6), 32, 64, center=ctr)
+        assert rel(outs[1][ii, pol], o) < TOL_TREE, (ii, pol)
+
+
+def test_leaf_tcgen05_large_phases_vs_fp64_direct():
+    """Leaves of 8.8 um at 500 nm (leaf-local phases up to ~100 rad: the
+    range-reduced phasor path) with 8 incidences, the smallest pattern count
+    that takes the tcgen05 leaf kernel."""
+    cloud = geometry.fibonacci_sphere(8.0e-6, 4000)
+    box = [-8.8e-6] * 3 + [8.8e-6] * 3
+    th, ph = _many_incidences(8, seed=9)
+    cfg = api.Config.reference_rule(1, 24, 48, box[:3], box[3:], 17.6e-6, 17.6e-6, 1.2,
+                                    precision=api.PO_PREC_SPLIT_BF16)
+    il = api.Illumination([500e-9], th, ph, api.PO_POL_TM, 1.55 + 0.1j, 2e-5)
+    out, rep = _solve(cloud, cfg, il)
+    out = out.reshape(8, 24, 48)
+    for ii in (0, 7):
+        o = oracle.solve_direct(cloud, oracle.make_illum(500e-9, th[ii], ph[ii], "M", 1.55 + 0.1j, 2e-5), 24, 48)
+        assert rel(out[ii], o) < TOL_TREE, (ii, rep)
+
+
+def test_leaf_tcgen05_chunked_matches_single_pass():
+    """Workspace caps that split 2 wavelengths x 9 incidences into single
+    slots, runs inside a wavelength and whole wavelengths give the single-pass
+    result bit for bit (every output column of the tcgen05 products depends
+    on its own column of the currents only)."""
+    cloud = geometry.ellipsoid((1.5e-6, 1.0e-6, 0.8e-6), 3000)
+    box = [-1.65e-6, -1.1e-6, -0.88e-6, 1.65e-6, 1.1e-6, 0.88e-6]
+    th, ph = _many_incidences(9, seed=4)
+    il = api.Illumination([450e-9, 620e-9], th, ph, api.PO_POL_TM, 1.55 + 0.1j, 2e-6)
+    cfg = api.Config.reference_rule(2, 24, 48, box[:3], box[3:], 1.6e-6, 3.0e-6, 1.2,
+                                    precision=api.PO_PREC_SPLIT_BF16)
+    full, rep = _solve(cloud, cfg, il)
+    assert rep["n_chunks"] == 1
+    per_slot = rep["workspace_bytes"] / 18.0
+    for cap in (1, int(per_slot * 4), int(per_slot * 11)):
+        cfg.max_workspace_bytes = cap
+        out, r = _solve(cloud, cfg, il)
+        assert r["n_chunks"] > 1
+        assert np.array_equal(out, full), (cap, r["n_chunks"], r["chunk_slots"])

@@ -67,11 +67,12 @@ class po_report(ctypes.Structure):
                 ("n_leaf_launches", ctypes.c_int), ("n_row_launches", ctypes.c_int), ("n_col_launches", ctypes.c_int),
                 ("n_chunks", ctypes.c_int), ("chunk_slots", ctypes.c_int),
                 ("leaf_point_dirs", ctypes.c_double), ("rows_bytes", ctypes.c_double), ("cols_bytes", ctypes.c_double),
-                ("ms_rows_level", ctypes.c_double * PO_MAX_DEPTH), ("ms_cols_level", ctypes.c_double * PO_MAX_DEPTH)]
+                ("ms_rows_level", ctypes.c_double * PO_MAX_DEPTH), ("ms_cols_level", ctypes.c_double * PO_MAX_DEPTH),
+                ("agg_bytes", ctypes.c_double), ("n_nodes_level", ctypes.c_int64 * (PO_MAX_DEPTH + 1))]
 
     def as_dict(self):
         d = {f: getattr(self, f) for f, _ in self._fields_}
-        for k in ("ms_rows_level", "ms_cols_level"):
+        for k in ("ms_rows_level", "ms_cols_level", "n_nodes_level"):
             d[k] = list(d[k])
         return d
 

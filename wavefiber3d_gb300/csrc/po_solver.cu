@@ -135,6 +135,7 @@ po_status init_device_attributes(int dev) {
   PO_TRY(init_point_adjoint_mma_attributes());
   PO_TRY(init_theta_tc_attributes());
   PO_TRY(init_rows_tc_attributes());
+  PO_TRY(init_leaf_tc_attributes());
   done.insert(dev);
   return PO_OK;
 }
@@ -183,6 +184,8 @@ struct po_ctx {
   DevBuf twiddles;
   DevBuf geom_in, geom_sorted, octree_ws, leaf_ctr, dirs, dirs_d, trans, levelA, levelB, mid, slots, kvals, out,
       cur, partial, tile_ctr;
+  // tcgen05 leaf sums (po_leaf_tc.cu): per-leaf chunk bases, chunk -> leaf, operand scratch
+  DevBuf leaf_kc0, leaf_chunk, leaf_bop, leaf_uop;
   cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   // per kernel class: [0..1] leaf/direct kernel, then rows and cols per level
   cudaEvent_t kev[2 + 4 * PO_MAX_DEPTH] = {};
@@ -418,6 +421,12 @@ po_status po_create(po_ctx **out, const po_config *cfg) {
       s = fail(PO_ERR_CUDA, "upload of the interpolation matrices");
     if (s != PO_OK) { po_destroy(c); return s; }
   }
+  // error word of the bounded device waits (tcgen05 passes and leaf sums)
+  if (!c->tc_err.p) {
+    s = c->tc_err.ensure(sizeof(int));
+    if (s == PO_OK && cudaMemset(c->tc_err.p, 0, sizeof(int)) != cudaSuccess) s = fail(PO_ERR_CUDA, "cudaMemset");
+    if (s != PO_OK) { po_destroy(c); return s; }
+  }
   if (cudaDeviceSynchronize() != cudaSuccess) { po_destroy(c); return fail(PO_ERR_CUDA, "set-up kernels failed"); }
   *out = c;
   return PO_OK;
@@ -428,7 +437,8 @@ po_status po_destroy(po_ctx *c) {
   for (DevBuf *b : {&c->twiddles, &c->geom_in, &c->geom_sorted, &c->octree_ws, &c->leaf_ctr, &c->dirs, &c->dirs_d,
                     &c->trans, &c->levelA, &c->levelB, &c->mid, &c->slots, &c->kvals, &c->out, &c->cur, &c->partial,
                     &c->tile_ctr, &c->amat, &c->bmat, &c->amat_adj, &c->bmat_adj, &c->slots64, &c->grad_acc,
-                    &c->chunk_begin, &c->center0, &c->dir_trig, &c->out_dirs, &c->tc_amat, &c->tc_err, &c->rt_bmat})
+                    &c->chunk_begin, &c->center0, &c->dir_trig, &c->out_dirs, &c->tc_amat, &c->tc_err, &c->rt_bmat,
+                    &c->leaf_kc0, &c->leaf_chunk, &c->leaf_bop, &c->leaf_uop})
     b->release();
   for (auto &e : c->ev)
     if (e) cudaEventDestroy(e);
@@ -521,12 +531,15 @@ struct SolvePlan {
   const double *k_lambda = nullptr, *k_slot = nullptr;
   const SlotParams<double> *sp64_dev = nullptr;
   const int32_t *perm_out = nullptr;  // sorted position -> input index of the gradient
+  bool leaf_tc = false;               // leaf sums on tcgen05 (po_leaf_tc.cu)
+  int64_t leaf_chunks = 0;            // 16-point chunks over all leaves
 };
 
 // Per-kernel-class device times of a solve (CUDA events; requested by a report).
 struct SolveTimes {
   double leaf = 0, agg = 0, inten = 0, leafk = 0, rows = 0, cols = 0;
   double rows_l[PO_MAX_DEPTH] = {}, cols_l[PO_MAX_DEPTH] = {};
+  double agg_b = 0;
   int n_leaf = 0, n_row = 0, n_col = 0;
   double leaf_pd = 0, rows_b = 0, cols_b = 0;
 };
@@ -683,6 +696,33 @@ static po_status prepare_solve(po_ctx *c, const po_geometry *g, const po_illum *
                                                                        c->leaf_ctr.as<double>());
     count_launch();
   }
+  // tcgen05 leaf sums when a wavelength has many patterns: the leaves' points
+  // in chunks of 16 (bases computed on the host from the leaf ranges)
+  P.leaf_tc = cfg.precision == PO_PREC_SPLIT_BF16 && G >= kLeafTcMinSlots && P.nleaf > 0;
+  double leaf_tc_per_slot = 0;
+  if (P.leaf_tc) {
+    std::vector<int32_t> lb((size_t)P.nleaf + 1);
+    PO_CUDA(cudaMemcpyAsync(lb.data(), P.tree.level[d].begin, sizeof(int32_t) * lb.size(), cudaMemcpyDeviceToHost,
+                            st));
+    PO_CUDA(cudaStreamSynchronize(st));
+    std::vector<int32_t> kc0((size_t)P.nleaf + 1);
+    int64_t tot = 0;
+    for (int64_t l = 0; l < P.nleaf; ++l) {
+      kc0[l] = (int32_t)tot;
+      tot += (lb[l + 1] - lb[l] + 15) / 16;
+    }
+    if (tot > 2147483647LL) return fail(PO_ERR_UNSUPPORTED, "too many points for the tcgen05 leaf sums");
+    kc0[P.nleaf] = (int32_t)tot;
+    std::vector<int32_t> cl((size_t)std::max<int64_t>(tot, 1), 0);
+    for (int64_t l = 0; l < P.nleaf; ++l)
+      for (int32_t k = kc0[l]; k < kc0[l + 1]; ++k) cl[k] = (int32_t)l;
+    PO_TRY(c->leaf_kc0.ensure(sizeof(int32_t) * kc0.size()));
+    PO_TRY(c->leaf_chunk.ensure(sizeof(int32_t) * cl.size()));
+    PO_CUDA(cudaMemcpy(c->leaf_kc0.p, kc0.data(), sizeof(int32_t) * kc0.size(), cudaMemcpyHostToDevice));
+    PO_CUDA(cudaMemcpy(c->leaf_chunk.p, cl.data(), sizeof(int32_t) * cl.size(), cudaMemcpyHostToDevice));
+    P.leaf_chunks = tot;
+    leaf_tc_per_slot = (double)tot * (double)leaf_tc_block_bytes() * 12.0 / 128.0;
+  }
   // pattern buffers per slot: two level buffers + the row-pass output (R + 1
   // rows: the packed tensor-core row pass pads odd row counts to even)
   size_t lvl_max = 0, mid_max = 0;
@@ -695,8 +735,18 @@ static po_status prepare_solve(po_ctx *c, const po_geometry *g, const po_illum *
                                       : (size_t)(c->R[l + 1] + 1) * c->Phi[l];
     mid_max = std::max(mid_max, (size_t)P.tree.level[l + 1].count * 6 * per);
   }
-  P.chunks = plan_chunks(L, G, chunk_slot_count(budget, 8.0 * (2.0 * lvl_max + mid_max), S));
+  P.chunks = plan_chunks(L, G, chunk_slot_count(budget, 8.0 * (2.0 * lvl_max + mid_max) + leaf_tc_per_slot, S));
   const int ns_max = P.chunks.front().ns;
+  if (P.leaf_tc) {
+    size_t bop = 0;
+    int nl_max = 1;
+    for (const SlotChunk &ch : P.chunks) {
+      bop = std::max(bop, (size_t)ch.nl * P.leaf_chunks * leaf_tc_col_tiles(ch.gc) * leaf_tc_block_bytes());
+      nl_max = std::max(nl_max, ch.nl);
+    }
+    PO_TRY(c->leaf_bop.ensure(bop));
+    PO_TRY(c->leaf_uop.ensure(sizeof(float4) * 16 * (size_t)nl_max * P.leaf_chunks));
+  }
   PO_TRY(c->levelA.ensure(sizeof(float2) * lvl_max * ns_max));
   PO_TRY(c->levelB.ensure(sizeof(float2) * lvl_max * ns_max));
   PO_TRY(c->mid.ensure(sizeof(float2) * std::max<size_t>(mid_max * ns_max, 1)));
@@ -822,9 +872,15 @@ static po_status enqueue_solve(po_ctx *c, const SolvePlan &P, float *out_dev, co
       PO_TRY(rec(c->kev[0]));
       // the phi pass of the deepest parent level runs in the leaf kernel's epilogue
       // when its packed output fits one n-tile group
-      const bool fuse_rows = cfg.precision == PO_PREC_SPLIT_BF16 && d >= 1 && c->tensor_theta &&
+      const bool fuse_rows = cfg.precision == PO_PREC_SPLIT_BF16 && !P.leaf_tc && d >= 1 && c->tensor_theta &&
                              !c->tc_level[d - 1] && leaf_row_fusion_fits(c->Phi[d], c->Phi[d - 1], c->bmat_kp[d - 1]);
-      if (cfg.precision == PO_PREC_SPLIT_BF16)
+      if (P.leaf_tc)
+        PO_TRY(launch_leaf_tc(P.gsc, P.tree.level[d].begin, c->leaf_kc0.as<int32_t>(), c->leaf_chunk.as<int32_t>(),
+                              P.leaf_chunks, c->leaf_ctr.as<double>(), P.nleaf, sp, ch.nl, ch.gc, 0, ch.gc,
+                              c->dirs.as<float4>(), c->R[d] * c->Phi[d], c->leaf_bop.as<uint8_t>(), c->leaf_bop.bytes,
+                              c->leaf_uop.as<float4>(), c->leaf_uop.bytes, c->levelA.as<float2>(), c->tc_err.as<int>(),
+                              st));
+      else if (cfg.precision == PO_PREC_SPLIT_BF16)
         PO_TRY(launch_leaf_mma(P.gsc, P.tree.level[d].begin, c->leaf_ctr.as<double>(), P.nleaf, sp, ch.nl, ch.gc,
                                c->dirs.as<float4>(), c->R[d] * c->Phi[d], c->levelA.as<float2>(), st,
                                fuse_rows ? c->bmat.as<uint32_t>() + c->bmat_off[d - 1] : nullptr,
@@ -834,7 +890,7 @@ static po_status enqueue_solve(po_ctx *c, const SolvePlan &P, float *out_dev, co
         PO_TRY(launch_leaf(P.gsc, P.tree.level[d].begin, c->leaf_ctr.as<double>(), P.nleaf, sp, ch.nl, ch.gc,
                            c->dirs.as<float4>(), c->R[d] * c->Phi[d], c->levelA.as<float2>(), st));
       PO_TRY(rec(c->kev[1]));
-      T.n_leaf += P.nleaf > 0 ? (ch.gc + 3) / 4 : 0;
+      T.n_leaf += P.nleaf <= 0 ? 0 : P.leaf_tc ? 2 * ((ch.gc + kLeafTcMaxSlots - 1) / kLeafTcMaxSlots) : (ch.gc + 3) / 4;
       float2 *cur_lvl = c->levelA.as<float2>(), *nxt = c->levelB.as<float2>();
       for (int l = d - 1; l >= 0; --l) {
         const int64_t nc = P.tree.level[l + 1].count, np = P.tree.level[l].count;
@@ -865,6 +921,7 @@ static po_status enqueue_solve(po_ctx *c, const SolvePlan &P, float *out_dev, co
         PO_TRY(rec(c->kev[3 + 4 * l]));
         T.rows_b += 8.0 * nrows * (c->Phi[l + 1] + c->Phi[l]);
         T.cols_b += 8.0 * ch.ns * 6 * ((double)nc * c->R[l + 1] * c->Phi[l] + (double)np * c->R[l] * c->Phi[l]);
+        T.agg_b += 8.0 * ch.ns * 6 * ((double)nc * c->R[l + 1] * c->Phi[l + 1] + (double)np * c->R[l] * c->Phi[l]);
         if (nrows > 0 && !(fuse_rows && l == d - 1)) ++T.n_row;
         if (np > 0) ++T.n_col;
         PO_TRY(rec(c->kev[4 + 4 * l]));
@@ -925,15 +982,13 @@ static po_status enqueue_solve(po_ctx *c, const SolvePlan &P, float *out_dev, co
 // waits gave up (the level's output is then incomplete).  Read after a
 // synchronous solve; an asynchronous solve leaves it for the next check.
 static po_status check_device_waits(po_ctx *c) {
-  bool any = false;
-  for (int l = 0; l < c->depth; ++l) any = any || c->tc_level[l];
-  if (!any) return PO_OK;
+  if (!c->tc_err.p) return PO_OK;
   int h = 0;
   PO_CUDA(cudaMemcpy(&h, c->tc_err.p, sizeof(int), cudaMemcpyDeviceToHost));
   if (h == 0) return PO_OK;
   PO_CUDA(cudaMemset(c->tc_err.p, 0, sizeof(int)));
-  if (h == 2) return fail(PO_ERR_INTERNAL, "tcgen05 theta/phi pass: operand run outside its buffer");
-  return fail(PO_ERR_TIMEOUT, "tcgen05 theta/phi pass: a device wait timed out");
+  if (h == 2) return fail(PO_ERR_INTERNAL, "tcgen05 pass: operand run outside its buffer");
+  return fail(PO_ERR_TIMEOUT, "tcgen05 pass (leaf sums or theta/phi interpolation): a device wait timed out");
 }
 
 static po_status solve_impl(po_ctx *c, const po_geometry *g, const po_illum *il, float *intensity, int out_on_device,
@@ -974,13 +1029,17 @@ static po_status solve_impl(po_ctx *c, const po_geometry *g, const po_illum *il,
       const int tdepth = c->depth > 0 ? c->depth : 6;
       rep->n_leaves = P.tree.level[tdepth].count;
       int64_t tot = 0;
-      for (int l = 0; l <= tdepth; ++l) tot += P.tree.level[l].count;
+      for (int l = 0; l <= tdepth; ++l) {
+        tot += P.tree.level[l].count;
+        if (l <= PO_MAX_DEPTH) rep->n_nodes_level[l] = P.tree.level[l].count;
+      }
       rep->n_nodes_total = tot;
     }
     int64_t ws = 0;
     for (DevBuf *b : {&c->twiddles, &c->geom_in, &c->geom_sorted, &c->octree_ws, &c->leaf_ctr, &c->dirs, &c->dirs_d,
                       &c->trans, &c->levelA, &c->levelB, &c->mid, &c->slots, &c->kvals, &c->out, &c->cur, &c->partial,
-                      &c->tile_ctr, &c->slots64, &c->grad_acc, &c->chunk_begin, &c->amat_adj, &c->bmat_adj})
+                      &c->tile_ctr, &c->slots64, &c->grad_acc, &c->chunk_begin, &c->amat_adj, &c->bmat_adj,
+                      &c->leaf_kc0, &c->leaf_chunk, &c->leaf_bop, &c->leaf_uop})
       ws += (int64_t)b->bytes;
     rep->workspace_bytes = ws;
     rep->kernel_launches = g_launch_count - launches0;
@@ -992,6 +1051,7 @@ static po_status solve_impl(po_ctx *c, const po_geometry *g, const po_illum *il,
     rep->leaf_point_dirs = T.leaf_pd;
     rep->rows_bytes = T.rows_b;
     rep->cols_bytes = T.cols_b;
+    rep->agg_bytes = T.agg_b;
     rep->ms_leaf_kernel = T.leafk;
     rep->ms_rows = T.rows;
     rep->ms_cols = T.cols;
