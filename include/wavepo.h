@@ -158,6 +158,15 @@ po_status po_destroy(po_ctx *ctx);
 po_status po_solve(po_ctx *ctx, const po_geometry *geom, const po_illum *illum, float *intensity,
                    int out_on_device, void *stream, po_report *report);
 
+/* No counterpart in the reference (it reports failures only by exit()).
+ * Waits for the stream and reports whether a bounded device wait of the
+ * context's kernels gave up since the last check (the output of that solve
+ * is then incomplete): PO_ERR_TIMEOUT, or PO_ERR_INTERNAL for an operand run
+ * outside its buffer; clears the record.  A synchronous solve (report
+ * requested or host output) performs this check itself; callers of
+ * asynchronous solves call po_check before they trust the output. */
+po_status po_check(po_ctx *ctx, void *stream);
+
 /* No counterpart in the reference (it has no gradients).  Gradient of a
  * scalar loss L with respect to every surface sample, given dL/dI on the
  * output grid: dl_di [n_lambda][n_inc][n_pol][n_theta[0]][n_phi[0]] float32
@@ -193,6 +202,9 @@ typedef struct po_batch_item {
 po_status po_batch_create(po_batch **batch, int n_items, const po_config *configs, int n_streams);
 po_status po_batch_prepare(po_batch *batch, const po_batch_item *items, void *stream);
 po_status po_batch_launch(po_batch *batch, void *stream);
+/* po_check for every item of a replayed batch (waits for the stream): the
+ * first item whose kernels gave up a bounded wait, or PO_OK. */
+po_status po_batch_check(po_batch *batch, void *stream);
 /* graph nodes, device workspace of all items, host+device time of the last
  * prepare (ms); any pointer may be NULL */
 po_status po_batch_info(const po_batch *batch, int64_t *graph_nodes, int64_t *workspace_bytes, double *ms_prepare);
@@ -315,6 +327,16 @@ po_status po_shifted_fft2(const float *in, float *out, int batch, int n_theta, i
  * acf = Re ForwardFFT_shifted(spectrum^2). */
 po_status po_acf_from_patterns(const float *patterns, int n_inst, int n_theta, int n_phi, float *mean,
                                float *spectrum, float *acf, void *stream);
+
+/* No counterpart in the reference.  Self-test of the failure handling of the
+ * bounded device waits: launches one tcgen05 kernel of the engine on small
+ * internal buffers, arranged so that it must fail, and returns the status its
+ * error word maps to.  which = 1: the theta pass sees its operand buffer as
+ * too small (expected PO_ERR_INTERNAL, no copy issued); 2: the theta pass
+ * with its first copy stage withheld (expected PO_ERR_TIMEOUT after the 1-s
+ * wait limit); 3: the tcgen05 leaf sums likewise (PO_ERR_TIMEOUT).  PO_OK
+ * would mean the failure went undetected.  The CUDA context stays usable. */
+po_status po_selftest_device_waits(int which, void *stream);
 
 /* Library build identification (sm arch, version). */
 const char *po_version(void);

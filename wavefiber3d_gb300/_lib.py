@@ -81,7 +81,8 @@ EXPORTS = ("po_config_init", "po_status_string", "po_last_error", "po_create", "
            "po_tangent_plane_currents", "po_build_octree", "po_far_field_direct", "po_interp_fft",
            "po_compute_intensity", "po_version", "po_interp_fft_noalloc", "po_height_field_points",
            "po_average_pattern", "po_grad", "po_height_field_adjoint", "po_batch_create", "po_batch_prepare",
-           "po_batch_launch", "po_batch_info", "po_batch_destroy", "po_shifted_fft2", "po_acf_from_patterns")
+           "po_batch_launch", "po_batch_info", "po_batch_destroy", "po_shifted_fft2", "po_acf_from_patterns",
+           "po_check", "po_batch_check", "po_selftest_device_waits")
 
 _lib = None
 
@@ -120,6 +121,9 @@ def load():
     L.po_batch_info.argtypes = [vp, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64),
                                 ctypes.POINTER(ctypes.c_double)]
     L.po_batch_destroy.argtypes = [vp]
+    L.po_check.argtypes = [vp, vp]
+    L.po_batch_check.argtypes = [vp, vp]
+    L.po_selftest_device_waits.argtypes = [i32, vp]
     L.po_shifted_fft2.argtypes = [vp, vp, i32, i32, i32, i32, vp]
     L.po_acf_from_patterns.argtypes = [vp, i32, i32, i32, vp, vp, vp, vp]
     L.po_average_pattern.argtypes = [vp, i32, i32, vp, i32, i32, i32, vp]

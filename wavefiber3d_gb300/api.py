@@ -175,6 +175,11 @@ class Solver:
         return (len(illum.wavelengths_m), len(illum.theta_i), npol, int(self.config.n_theta[0]),
                 int(self.config.n_phi[0]))
 
+    def check(self, stream=None):
+        """po_check: waits for the stream; raises if a bounded device wait of
+        this context's kernels gave up since the last check."""
+        check(_lib.load().po_check(self._h, _stream_ptr(stream)))
+
     def solve(self, cloud, illum: Illumination, out=None, stream=None, report: bool = True):
         """cloud: PointCloud (host numpy) or a (7, n) float32 CUDA tensor / tuple of 7 CUDA tensors.
         Returns intensity [L][I][P][n_theta][n_phi] float32 (numpy for host geometry without `out`,
@@ -413,6 +418,11 @@ class Batch:
         check(_lib.load().po_batch_launch(self._h, _stream_ptr(stream)))
         return self.outputs
 
+    def check(self, stream=None):
+        """po_batch_check: waits for the stream; raises if an item's kernels
+        gave up a bounded device wait."""
+        check(_lib.load().po_batch_check(self._h, _stream_ptr(stream)))
+
     def info(self) -> dict:
         nodes, ws, ms = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_double()
         check(_lib.load().po_batch_info(self._h, ctypes.byref(nodes), ctypes.byref(ws), ctypes.byref(ms)))
@@ -434,3 +444,9 @@ class Batch:
 
     def __exit__(self, *a):
         self.close()
+
+
+def selftest_device_waits(which: int, stream=None) -> int:
+    """po_selftest_device_waits: the status (an int, not raised) that the
+    deliberately failing kernel launch of case `which` (1..3) reported."""
+    return int(_lib.load().po_selftest_device_waits(int(which), _stream_ptr(stream)))

@@ -63,7 +63,7 @@ po_status launch_leaf_tc(const float *const g[7], const int32_t *leaf_begin, con
                          const int32_t *chunk_leaf, int64_t n_chunks, const double *leaf_center, int64_t n_leaves,
                          const SlotParams<float> *slots_dev, int n_lambda, int Gtot, int g0, int G,
                          const float4 *dirs, int ndir, uint8_t *bop, size_t bop_bytes, float4 *uop,
-                         size_t uop_bytes, float2 *out, int *err, cudaStream_t st);
+                         size_t uop_bytes, float2 *out, int *err, cudaStream_t st, int withhold = 0);
 
 int direct_splits(int64_t n, int ndir, int n_lambda, int sm_count);
 // FP32 depth-0 sum about c0: out[slot][comp][dir]; cur[slot][n][6]
@@ -126,7 +126,8 @@ po_status launch_rows_tc(const float2 *src, uint8_t *dst, size_t dst_bytes, int6
                          int sm_count, int *err, cudaStream_t st);
 po_status launch_theta_tc(const uint8_t *mid, float2 *parent, const int32_t *child_table, int64_t n_parent,
                           int64_t n_child, int phi, int Kr, int Rp, const uint8_t *Atc, const float4 *trans,
-                          int n_slots, int G, int *err, size_t mid_bytes, size_t atc_bytes, cudaStream_t st);
+                          int n_slots, int G, int *err, size_t mid_bytes, size_t atc_bytes, cudaStream_t st,
+                          int withhold = 0);
 // adjoint (transposed) passes, double cover only (po_interp_mma.cu)
 void build_theta_matrix_adj(int Tc, int Tp, int Rc, int Rp, int Kp, std::vector<uint32_t> &out);
 void build_phi_matrix_adj(int Pc, int Pp, int Kp, std::vector<uint32_t> &out);

@@ -39,7 +39,8 @@
 //    so that one CTA's epilogue overlaps the other's products.
 // Every wait is bounded in time (error word 1) and aborts the other roles;
 // the copy and MMA threads wait for their last copy / commit before the CTA
-// exits.
+// exits.  `withhold` (a self-test switch) leaves the first stage's copy
+// unissued so that the timeout path runs.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -143,7 +144,7 @@ __global__ void __launch_bounds__(256) k_leaf_tc_operands(
 __global__ void __launch_bounds__(kLtThreads, 2) k_leaf_tc(
     const uint8_t *__restrict__ bop, const float4 *__restrict__ uop, const int32_t *__restrict__ kc0,
     int64_t n_chunks, const float4 *__restrict__ dirs, int ndir, int64_t n_leaves, int Gtot, int g0, int G, int NT,
-    float2 *__restrict__ out, int *__restrict__ err) {
+    float2 *__restrict__ out, int *__restrict__ err, int withhold) {
   extern __shared__ __align__(1024) uint8_t smem_lt[];
   uint8_t *sA = smem_lt;                                   // [stages][kLtAStage]
   uint8_t *sB = smem_lt + kLtStages * kLtAStage;           // [stages][kLtBBlock]
@@ -197,6 +198,7 @@ __global__ void __launch_bounds__(kLtThreads, 2) k_leaf_tc(
             ok = false;
             break;
           }
+          if (withhold && step == 0) continue;  // self-test: stage 0 never filled, its consumers give up
           mbar_expect_tx(smem_addr(&bfull[s]), kLtBBlock);
           bulk_copy(smem_addr(sB + s * kLtBBlock), bl + ((size_t)kc * NT + n) * kLtBBlock, kLtBBlock,
                     smem_addr(&bfull[s]));
@@ -373,7 +375,7 @@ po_status launch_leaf_tc(const float *const g[7], const int32_t *leaf_begin, con
                          const int32_t *chunk_leaf, int64_t n_chunks, const double *leaf_center, int64_t n_leaves,
                          const SlotParams<float> *slots_dev, int n_lambda, int Gtot, int g0, int G,
                          const float4 *dirs, int ndir, uint8_t *bop, size_t bop_bytes, float4 *uop,
-                         size_t uop_bytes, float2 *out, int *err, cudaStream_t st) {
+                         size_t uop_bytes, float2 *out, int *err, cudaStream_t st, int withhold) {
   if (n_leaves <= 0 || n_lambda <= 0 || G <= 0) return PO_OK;
   if (n_chunks <= 0 || n_lambda > 65535 || n_leaves > 2147483647LL || n_chunks > 2147483647LL)
     return fail(PO_ERR_INTERNAL, "tcgen05 leaf: launch shape");
@@ -389,7 +391,7 @@ po_status launch_leaf_tc(const float *const g[7], const int32_t *leaf_begin, con
         g0 + gs, gc, NT, n_chunks, bop, uop);
     count_launch();
     k_leaf_tc<<<dim3((unsigned)n_leaves, (unsigned)n_lambda), kLtThreads, kLtSmem, st>>>(
-        bop, uop, kc0, n_chunks, dirs, ndir, n_leaves, Gtot, g0 + gs, gc, NT, out, err);
+        bop, uop, kc0, n_chunks, dirs, ndir, n_leaves, Gtot, g0 + gs, gc, NT, out, err, withhold);
     count_launch();
   }
   PO_CUDA(cudaGetLastError());

@@ -1087,6 +1087,12 @@ po_status po_solve(po_ctx *c, const po_geometry *g, const po_illum *il, float *i
   return solve_impl(c, g, il, intensity, out_on_device, (cudaStream_t)stream, rep);
 }
 
+po_status po_check(po_ctx *c, void *stream) {
+  if (!c) return fail(PO_ERR_INVALID_ARGUMENT, "null argument");
+  PO_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+  return check_device_waits(c);
+}
+
 // ---------------------------------------------------------------- single steps
 po_status po_grad(po_ctx *c, const po_geometry *g, const po_illum *il, const float *dl_di, float *grad,
                   float *intensity, void *stream, po_report *rep) {
@@ -1446,6 +1452,21 @@ po_status po_batch_launch(po_batch *b, void *stream) {
   if (!b->exec) return fail(PO_ERR_INVALID_ARGUMENT, "po_batch_prepare has not captured a graph");
   PO_CUDA(cudaGraphLaunch(b->exec, (cudaStream_t)stream));
   return PO_OK;
+}
+
+po_status po_batch_check(po_batch *b, void *stream) {
+  if (!b) return fail(PO_ERR_INVALID_ARGUMENT, "null batch");
+  PO_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+  po_status first = PO_OK;
+  std::string msg;
+  for (size_t i = 0; i < b->ctx.size(); ++i) {
+    const po_status s = check_device_waits(b->ctx[i]);
+    if (s != PO_OK && first == PO_OK) {
+      first = s;
+      msg = "batch item " + std::to_string(i) + ": " + po_last_error();
+    }
+  }
+  return first == PO_OK ? PO_OK : fail(first, msg);
 }
 
 po_status po_batch_info(const po_batch *b, int64_t *graph_nodes, int64_t *workspace_bytes, double *ms_prepare) {

@@ -42,7 +42,8 @@
 // CTA's share of a chunk is one contiguous 4-KB run per matrix.
 //
 // Every wait is bounded in time: on a timeout the kernel records error word 1
-// and every role stops.  Operand runs outside their buffers (checked once per
+// and every role stops (`withhold`, a self-test switch, leaves the first
+// stage unfilled so that this path runs).  Operand runs outside their buffers (checked once per
 // CTA) record error word 2 and nothing is copied.  Before the CTA exits, the
 // copy and MMA threads wait for the last phase of every barrier they armed, so
 // that no copy or commit arrive outlives the CTA.
@@ -135,7 +136,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_theta_tc(
     const uint8_t *__restrict__ mid, float2 *__restrict__ parent, const int32_t *__restrict__ child_table,
     int64_t n_parent, int64_t n_child, int phi, int Kr, int Npad, int Rp, const uint8_t *__restrict__ Atc,
     const float4 *__restrict__ trans, int G, int n_nc, int64_t n_task, int *__restrict__ err, size_t mid_bytes,
-    size_t atc_bytes) {
+    size_t atc_bytes, int withhold) {
   using Plan = TcPlan;
   constexpr int NST = Plan::stages;
   extern __shared__ __align__(128) uint8_t smem_tc[];
@@ -215,6 +216,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_theta_tc(
           ok = false;
           break;
         }
+        if (withhold && t == 0) continue;  // self-test: stage 0 never filled, its consumers give up
         const uint32_t fb = smem_addr(&full[b]);
         mbar_expect_tx(fb, kAStage + 4 * bmat);
         bulk_copy(smem_addr(sA + b * kAStage), abase + (size_t)kc * kAStage, kAStage, fb);
@@ -407,7 +409,8 @@ int theta_tc_npad(int phi) { return (phi + kTcN - 1) / kTcN * kTcN; }
 
 po_status launch_theta_tc(const uint8_t *mid, float2 *parent, const int32_t *child_table, int64_t n_parent,
                           int64_t n_child, int phi, int Kr, int Rp, const uint8_t *Atc, const float4 *trans,
-                          int n_slots, int G, int *err, size_t mid_bytes, size_t atc_bytes, cudaStream_t st) {
+                          int n_slots, int G, int *err, size_t mid_bytes, size_t atc_bytes, cudaStream_t st,
+                          int withhold) {
   if (n_parent <= 0 || n_slots <= 0) return PO_OK;
   if (phi % 2 || Kr % kTcKC || Kr <= 0) return fail(PO_ERR_INTERNAL, "tcgen05 theta pass: grid");
   const int MT = (Rp + 127) / 128, n_nc = (phi / 2 + kTcPairs - 1) / kTcPairs;
@@ -416,7 +419,7 @@ po_status launch_theta_tc(const uint8_t *mid, float2 *parent, const int32_t *chi
   if (gx > 2147483647LL) return fail(PO_ERR_UNSUPPORTED, "too many nodes for one launch");
   k_theta_tc<<<(unsigned)gx, kTcThreads, TcPlan::smem, st>>>(mid, parent, child_table, n_parent, n_child, phi, Kr,
                                                          theta_tc_npad(phi), Rp, Atc, trans, G, n_nc, n_task, err,
-                                                         mid_bytes, atc_bytes);
+                                                         mid_bytes, atc_bytes, withhold);
   count_launch();
   PO_CUDA(cudaGetLastError());
   return PO_OK;
