@@ -845,6 +845,94 @@ def run_batch(args, world, rank, local):
     }
 
 
+def run_reference_cuda(args, world, rank, local):
+    """The reference's own CUDA path timed on this GPU (baseline B2): the
+    unmodified util/*.h driven in the order of compareMie/sphere.cu:212-936 by
+    oracle/ref_harness.cu, on the plain-method sphere (config 1, in full) and
+    on one (wavelength, incidence) pair of the ellipsoid (config 2: the leaf
+    loop on a subset of its directions and each level on a subset of its
+    children, extrapolated linearly by the counts, which the reference's
+    per-direction and per-child launches make exact up to launch jitter).
+    The fiber (config 3) is not run: its depth-7 CDP octree issues 299,593
+    device launches (util/tree.h:710-712) against the pending-launch limit of
+    32,768 that the reference sets."""
+    if rank != 0:
+        return None
+    import torch
+
+    from wavefiber3d_gb300 import api, geometry
+    import __graft_entry__
+    __graft_entry__.build()
+    harness = ROOT / "oracle" / "_ref" / "ref_harness"
+    if not harness.exists():
+        return {"impl": "reference-cuda", "unavailable": "oracle/_ref/ref_harness not built (no staged headers)"}
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    tmp = Path(tempfile.mkdtemp(prefix="refcuda_"))
+
+    def run(cloud, box, depth, nth, nph, lam, th, ph, eta, sigma, caps):
+        gpath, opath = tmp / "geom.bin", tmp / "out.bin"
+        cloud.soa().astype(np.float32).tofile(gpath)
+        cmd = [str(harness), "time", str(gpath), str(cloud.n), *[repr(float(v)) for v in box], str(depth)]
+        for a, b in zip(nth, nph):
+            cmd += [str(a), str(b)]
+        cmd += [repr(lam), repr(th), repr(ph), "M", repr(eta.real), repr(eta.imag), repr(sigma), str(opath),
+                *[str(c) for c in caps]]
+        t0 = time.perf_counter()
+        r = subprocess.run(cmd, capture_output=True, text=True, timeout=1200)
+        wall = time.perf_counter() - t0
+        if r.returncode != 0:
+            raise RuntimeError(f"ref_harness failed ({r.returncode}): {r.stderr[-2000:]}")
+        line = [x for x in r.stdout.splitlines() if x.startswith("{")][-1]
+        t = json.loads(line)
+        leaf = t["leaf_ms"] * t["leaf_dirs"] / max(1, t["leaf_dirs_done"])
+        levels = sum(v["ms"] * v["children"] / max(1, v["children_done"]) for v in t["levels"] if v["children_done"])
+        total = t["tree_ms"] + t["setup_ms"] + leaf + levels + t["intensity_ms"]
+        out = np.fromfile(opath, dtype=np.float32) if opath.exists() else None
+        return t, total, wall, out
+
+    # ---- config 1: 20,000-point sphere, depth 0, 180 x 360, one pattern, complete
+    sph = geometry.fibonacci_sphere(2e-6, 20000)
+    box1 = [-2.2e-6] * 3 + [2.2e-6] * 3
+    t1, ms1, wall1, out1 = run(sph, box1, 0, [N_THETA], [N_PHI], 500e-9, math.pi / 2, math.pi, 1.55 + 0j, 1e-2,
+                               (0, 0, 0))
+    cfg1 = api.Config(0, [N_THETA], [N_PHI], box1[:3], box1[3:], precision=api.PO_PREC_FP32)
+    il1 = api.Illumination([500e-9], [math.pi / 2], [math.pi], api.PO_POL_TM, 1.55 + 0j, 1e-2)
+    with api.Solver(cfg1) as s:
+        eng1 = s.solve(sph, il1).reshape(-1).astype(np.float64)
+    agree1 = float(np.linalg.norm(out1 - eng1) / np.linalg.norm(eng1))
+
+    # ---- config 2: 400k-point ellipsoid, depth 5, one (wavelength, incidence) pair, capped loops
+    ell = geometry.ellipsoid(RADII, N_POINTS)
+    box2 = [-1.1 * r for r in RADII] + [1.1 * r for r in RADII]
+    cfg2 = api.Config.reference_rule(DEPTH, N_THETA, N_PHI, box2[:3], box2[3:], 16e-6, 16e-6, 1.3)
+    caps2 = (args.ref_leaf_dirs, args.ref_children, 1)
+    t2, ms2, wall2, _ = run(ell, box2, DEPTH, cfg2.n_theta, cfg2.n_phi, LAMBDAS[0], 0.0, 0.0, ETA, SIGMA, caps2)
+    return {
+        "impl": "reference-cuda",
+        "metric": "ms per pattern of the reference's own CUDA build (baseline B2)",
+        "unit": "ms", "higher_is_better": False, "n_gpus": 1,
+        "data": "synthetic (seeded sphere and ellipsoid)",
+        "plain_sphere_20k_depth0": {
+            "ms_per_pattern": ms1, "wall_s": wall1, "phases": t1,
+            "gpoint_dirs_per_s": sph.n * N_THETA * N_PHI / (ms1 * 1e-3) / 1e9,
+            "rel_l2_vs_engine_fp32": agree1,
+            "note": "complete run: CDP octree of depth 0, 64,800 x (transform + thrust::reduce + fill), intensity"},
+        "ellipsoid_400k_depth5": {
+            "ms_per_pattern_extrapolated": ms2, "ms_per_step_extrapolated": ms2 * len(LAMBDAS),
+            "wall_s": wall2, "phases": t2,
+            "gpoint_dirs_per_s": N_POINTS * N_THETA * N_PHI / (ms2 * 1e-3) / 1e9,
+            "note": f"lambda={LAMBDAS[0] * 1e9:.0f} nm, incidence +x: leaf loop timed on {t2['leaf_dirs_done']} of "
+                    f"{t2['leaf_dirs']} directions, levels 4..1 on up to {args.ref_children} children each, "
+                    "extrapolated by the counts; the root level (197 -> 180 theta samples, a downsampling the "
+                    "reference's interpolation cannot do) and the intensity are left out, so this is a lower "
+                    f"bound; the step figure scales by the {len(LAMBDAS)} wavelengths"},
+        "fiber_3p4m_depth7": {"unavailable": "the reference's depth-7 CDP octree issues 299,593 device-side "
+                                             "launches (util/tree.h:710-712) against its pending-launch limit of "
+                                             "32,768; not run on this pool"},
+    }
+
+
 def run_reference(args, world, rank):
     """CPU implementation of the path on all host cores: the reference ships
     CUDA only, so this is the FP64 direct-sum restatement of its algorithm
@@ -915,10 +1003,14 @@ def main():
                     help="complex columns per CTA of the tensor-core theta pass (0: automatic)")
     ap.add_argument("--lambdas", type=int, default=25,
                     help="wavelengths of the ellipsoid workload (25 = the headline; fewer for profiling runs)")
-    ap.add_argument("--workload", choices=["fiber", "ellipsoid", "cylinder-grad", "batch"], default="fiber",
+    ap.add_argument("--workload", choices=["fiber", "ellipsoid", "cylinder-grad", "batch", "reference-cuda"],
+                    default="fiber",
                     help="fiber: the headline, the 3.4M-point fiber segment, 25 wavelengths x 64 incidences, depth 7 "
                          "(split precision vs plain FP64 on the same GPU); ellipsoid: 400k points, 25 wavelengths, "
-                         "depth 5; cylinder-grad: the gradient workload; batch: 256 independent solves")
+                         "depth 5; cylinder-grad: the gradient workload; batch: 256 independent solves; "
+                         "reference-cuda: the reference's own CUDA build on configs 1 and 2 (baseline B2)")
+    ap.add_argument("--ref-leaf-dirs", type=int, default=24, help="reference-cuda: leaf directions timed")
+    ap.add_argument("--ref-children", type=int, default=48, help="reference-cuda: children timed per level")
     ap.add_argument("--fiber-lambdas", type=int, default=25, help="wavelengths per fiber step (25 = the workload)")
     ap.add_argument("--e2e-steps", type=int, default=2, help="steps of the end-to-end (host buffers) timing")
     ap.add_argument("--ref-dirs", type=int, default=256, help="directions per step of the --impl reference arm")
@@ -943,6 +1035,8 @@ def main():
         res = run_cylinder_grad(args, world, rank, local) if rank == 0 else None
     elif args.workload == "batch":
         res = run_batch(args, world, rank, local) if rank == 0 else None
+    elif args.workload == "reference-cuda":
+        res = run_reference_cuda(args, world, rank, local)
     else:
         res = run_engine(args, world, rank, local)
     if rank == 0 and res is not None:

@@ -238,7 +238,53 @@ static int cmd_octree(char **a) {
 
 // solve <geom> <n> <6 box floats> <depth> <th0> <ph0> [<th_i> <ph_i> for i=1..depth]
 //       <lambda_m> <theta_i> <phi_i> <M|E> <eta_re> <eta_im> <sigma> <out>
-static int cmd_solve(char **a) {
+// Times of the phases of one solve (ms, CUDA events on the legacy stream,
+// which the reference's calls use) and the counts needed to extrapolate the
+// capped loops: the leaf loop runs `leaf_dirs_done` of `leaf_dirs` directions
+// and each level `children_done[i]` of `children[i]` active children.
+struct SolveTiming {
+  double tree = 0, setup = 0, leaf = 0, level[16] = {}, intensity = 0;
+  int leaf_dirs = 0, leaf_dirs_done = 0, children[16] = {}, children_done[16] = {};
+};
+
+static float ev_ms(cudaEvent_t a, cudaEvent_t b) {
+  float t = 0;
+  cudaEventSynchronize(b);
+  cudaEventElapsedTime(&t, a, b);
+  return t;
+}
+
+static int run_solve(char **a, int max_leaf_dirs, int max_children, SolveTiming *tm, bool skip_root = false);
+static int cmd_solve(char **a) { return run_solve(a, 0, 0, nullptr); }
+
+// time <solve arguments> <max leaf directions (0: all)> <max children per level (0: all)> <skip root>
+// Prints one line: the measured phase times and the counts of the capped loops.
+// skip root = 1 leaves out the root level and the intensity: the reference's
+// interpolation only upsamples (util/interpolation.h:29-30 index the padding
+// from the size difference), so a level-1 grid finer than the output grid is
+// outside what it can run.
+static int cmd_time(char **a, int argc) {
+  int max_depth = atoi(a[8]);
+  const int extra = 9 + 2 * (max_depth + 1) + 8;
+  if (argc < extra + 3) { fprintf(stderr, "time: missing caps\n"); return 2; }
+  SolveTiming tm;
+  const int rc = run_solve(a, atoi(a[extra]), atoi(a[extra + 1]), &tm, atoi(a[extra + 2]) != 0);
+  if (rc) return rc;
+  printf("{\"tree_ms\": %.4f, \"setup_ms\": %.4f, \"leaf_ms\": %.4f, \"leaf_dirs\": %d, \"leaf_dirs_done\": %d, "
+         "\"intensity_ms\": %.4f, \"levels\": [", tm.tree, tm.setup, tm.leaf, tm.leaf_dirs, tm.leaf_dirs_done,
+         tm.intensity);
+  for (int i = 0; i < max_depth; ++i)
+    printf("%s{\"level\": %d, \"ms\": %.4f, \"children\": %d, \"children_done\": %d}", i ? ", " : "", i,
+           tm.level[i], tm.children[i], tm.children_done[i]);
+  printf("]}\n");
+  return 0;
+}
+
+static int run_solve(char **a, int max_leaf_dirs, int max_children, SolveTiming *tm, bool skip_root) {
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaEventRecord(e0, 0);
   int n = atoi(a[1]);
   Geom g = load_geom(a[0], n);
   float box[6];
@@ -263,6 +309,9 @@ static int cmd_solve(char **a) {
   deviceFvec x_d0 = g.x, y_d0 = g.y, z_d0 = g.z, nx_d0 = g.nx, ny_d0 = g.ny, nz_d0 = g.nz, a_d0 = g.a;
   Tree t = build_tree(x_d0, y_d0, z_d0, nx_d0, ny_d0, nz_d0, a_d0, box, max_depth);
   std::vector<Octree_node> &host_nodes = t.nodes;
+  cudaEventRecord(e1, 0);
+  if (tm) tm->tree = ev_ms(e0, e1);
+  cudaEventRecord(e0, 0);
 
   // active lists, leaf to top (sphere.cu:255-307)
   std::vector<std::vector<int>> nonempty;
@@ -372,12 +421,20 @@ static int cmd_solve(char **a) {
   field_times_area(cur, a_d0);
   multiply_current_factor(cur, Efactor, Hfactor);
 
+  cudaEventRecord(e1, 0);
+  if (tm) tm->setup = ev_ms(e0, e1);
   for (int i = max_depth; i >= 0; i--) {
+    if (skip_root && i == 0 && max_depth > 0) break;
     int s = (int)((pow(8, i) - 1) / 7), e = (int)((pow(8, i + 1) - 1) / 7);
+    cudaEventRecord(e0, 0);
     if (i == max_depth) {  // sphere.cu:602-658
+      int dirs_done = 0;
       for (int it = 0; it < thn[i]; it++) {
+        if (max_leaf_dirs > 0 && dirs_done >= max_leaf_dirs) break;
         float th = -M_PI / 2 + thetastartoffset + M_PI / thn[i] * it;
         for (int ip = 0; ip < phn[i]; ip++) {
+          if (max_leaf_dirs > 0 && dirs_done >= max_leaf_dirs) break;
+          ++dirs_done;
           int dirindex = it * phn[i] + ip;
           float ph = 2 * M_PI / (phn[i]) * ip;
           Float3 dir = Float3(cos(th) * cos(ph), cos(th) * sin(ph), sin(th));
@@ -405,6 +462,12 @@ static int cmd_solve(char **a) {
           }
         }
       }
+      cudaEventRecord(e1, 0);
+      if (tm) {
+        tm->leaf = ev_ms(e0, e1);
+        tm->leaf_dirs = an[i];
+        tm->leaf_dirs_done = dirs_done;
+      }
     } else {  // sphere.cu:659-884 (ping-pong by parity)
       bool odd = ((max_depth - i) % 2 == 1);
       devicef2vec *dst = odd ? F1 : F0;
@@ -415,7 +478,9 @@ static int cmd_solve(char **a) {
       for (int l = 0; l < i; ++l) sofar += an[l];
       int leveloffset = 8 * sofar;
       int curact = (i > 0) ? (int)nonempty[max_depth - i].size() : 1;
+      int kids_total = (int)nonempty[max_depth - i - 1].size(), kids_done = 0;
       for (int v = 0; v < curact; ++v) {
+        if (max_children > 0 && kids_done >= max_children) break;
         int nodeindex = (i > 0) ? nonempty[max_depth - i][v] : 0;
         int parentstart = v * ndt;
         const std::vector<int> &childlist = nonempty[max_depth - i - 1];
@@ -426,6 +491,7 @@ static int cmd_solve(char **a) {
             for (int comp = 0; comp < 6; ++comp)
               copyandinterp(srcv[comp], (int)si, ndn, T1[comp], tmp2, ndt, p_phi[i], p_iphi[i], p_th[i], p_ith[i],
                             phn[i + 1], phn[i], thn[i + 1], thn[i], thn[i + 1], phn[i]);
+            ++kids_done;
             translation_compute(T1[0], T1[1], T1[2], T1[3], T1[4], T1[5], factor1_d, 0, ndt, leveloffset + c * ndt);
             int nb = std::ceil(ndt / NT) + 1;
             sumchildren<<<nb, NT>>>(thrust::raw_pointer_cast(T1[0].data()), thrust::raw_pointer_cast(T1[1].data()),
@@ -441,8 +507,15 @@ static int cmd_solve(char **a) {
           }
         }
       }
+      cudaEventRecord(e1, 0);
+      if (tm) {
+        tm->level[i] = ev_ms(e0, e1);
+        tm->children[i] = kids_total;
+        tm->children_done[i] = kids_done;
+      }
     }
     if (i == 0) {  // sphere.cu:888-932
+      cudaEventRecord(e0, 0);
       devicef2vec *fin = ((max_depth - i) % 2 == 1) ? F1 : F0;
       int nb = std::ceil((float)obnum / NT) + 1;
       computeintensity<<<nb, NT>>>(thrust::raw_pointer_cast(scattering.data()), obnum,
@@ -453,6 +526,8 @@ static int cmd_solve(char **a) {
       checkCudaErrors(cudaGetLastError());
       checkCudaErrors(cudaDeviceSynchronize());
       hostFvec h = scattering;
+      cudaEventRecord(e1, 0);
+      if (tm) tm->intensity = ev_ms(e0, e1);
       write_bytes(outpath, &h[0], sizeof(float) * obnum);
     }
   }
@@ -503,6 +578,7 @@ int main(int argc, char **argv) {
   if (c == "interp" && argc >= 8) return cmd_interp(argv + 2);
   if (c == "octree" && argc >= 12) return cmd_octree(argv + 2);
   if (c == "solve" && argc >= 12) return cmd_solve(argv + 2);
+  if (c == "time" && argc >= 12) return cmd_time(argv + 2, argc - 2);
   if (c == "heightfield" && argc >= 10) return cmd_heightfield(argv + 2);
   if (c == "average" && argc >= 8) return cmd_average(argv + 2);
   fprintf(stderr, "bad arguments\n");

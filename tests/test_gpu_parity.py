@@ -199,24 +199,26 @@ def test_solve_tree_vs_fp64_direct(cases, name):
     assert rel(out.reshape(o.shape), o) < TOL_TREE, rep
 
 
+@pytest.mark.parametrize("interp", [api.PO_INTERP_TENSOR, api.PO_INTERP_FFT])
 @pytest.mark.parametrize("name", ["ref_solve_sphere_d3", "ref_solve_ellipsoid_d2", "ref_solve_sphere_quirk_d1"])
-def test_solve_reference_mode_vs_oracle_tree(cases, name):
+def test_solve_reference_mode_vs_oracle_tree(cases, name, interp):
     c = cases[name]
     cloud, il = load_case_geometry(c), case_illum(c)
     cfg = api.Config(c["depth"], c["n_theta"], c["n_phi"], c["box"][:3], c["box"][3:],
-                     theta_mode=api.PO_THETA_REFERENCE, nyquist_quirk=True)
+                     theta_mode=api.PO_THETA_REFERENCE, nyquist_quirk=True, interp_method=interp)
     out, _ = _solve(cloud, cfg, illum_of(c))
     o = oracle.solve_tree(cloud, il, c["box"][:3], c["box"][3:], c["depth"], c["n_theta"], c["n_phi"], True)
     assert rel(out.reshape(o.shape), o) < TOL_TREE
 
 
+@pytest.mark.parametrize("interp", [api.PO_INTERP_TENSOR, api.PO_INTERP_FFT])
 @pytest.mark.parametrize("name", ["ref_solve_sphere_d0", "ref_solve_sphere_d3", "ref_solve_ellipsoid_d2",
                                   "ref_solve_sphere_quirk_d1"])
-def test_solve_vs_reference_build(cases, name):
+def test_solve_vs_reference_build(cases, name, interp):
     c = cases[name]
     cloud = load_case_geometry(c)
     cfg = api.Config(c["depth"], c["n_theta"], c["n_phi"], c["box"][:3], c["box"][3:],
-                     theta_mode=api.PO_THETA_REFERENCE, nyquist_quirk=True)
+                     theta_mode=api.PO_THETA_REFERENCE, nyquist_quirk=True, interp_method=interp)
     out, _ = _solve(cloud, cfg, illum_of(c))
     r = ref_fixture(name).reshape(c["n_theta"][0], c["n_phi"][0])
     assert rel(out.reshape(r.shape), r) < TOL_TREE
@@ -429,3 +431,24 @@ def test_leaf_tcgen05_chunked_matches_single_pass():
         out, r = _solve(cloud, cfg, il)
         assert r["n_chunks"] > 1
         assert np.array_equal(out, full), (cap, r["n_chunks"], r["chunk_slots"])
+
+
+def test_reference_mode_tensor_path_on_large_grids():
+    """The reference theta mode on the tensor cores where its maps are real and
+    column-independent: a 2,000-point sphere with even parent grids (the
+    levels take the tcgen05 and warp-level tensor kernels) against the oracle's
+    restatement of the reference's FFT interpolation, and the same solve with
+    the FFT path."""
+    cloud = geometry.fibonacci_sphere(1.0e-6, 2000)
+    box = [-1.1e-6] * 3 + [1.1e-6] * 3
+    nth, nph = [100, 75, 41], [200, 74, 40]  # root on the tcgen05 theta pass, level 1 on the warp-level one
+    il = api.Illumination([500e-9], [0.3], [0.7], api.PO_POL_TM, 1.55 + 0.1j, 2e-6)
+    outs = []
+    for interp in (api.PO_INTERP_TENSOR, api.PO_INTERP_FFT):
+        cfg = api.Config(2, nth, nph, box[:3], box[3:], theta_mode=api.PO_THETA_REFERENCE, nyquist_quirk=True,
+                         interp_method=interp)
+        outs.append(_solve(cloud, cfg, il)[0].reshape(nth[0], nph[0]))
+    o = oracle.solve_tree(cloud, oracle.make_illum(500e-9, 0.3, 0.7, "M", 1.55 + 0.1j, 2e-6), box[:3], box[3:], 2,
+                          nth, nph, True)
+    assert rel(outs[0], o) < TOL_TREE
+    assert rel(outs[0], outs[1]) < TOL_TREE

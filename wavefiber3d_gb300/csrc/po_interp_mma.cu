@@ -103,10 +103,13 @@ static double theta_partner(int Tc, int Tp, int r, int s) {
 // so a warp's shared-memory reads of one u are 512 contiguous bytes.
 size_t theta_pair_words(int Rp, int Kp) { return (size_t)((Rp + 15) / 16) * (Kp / 16) * 4 * 32 * 4; }
 
-// A_plus / A_minus of one level as dense FP64 [Rp][ld] (columns t < Rc)
+// A_plus / A_minus of one level as dense FP64 [Rp][ld] (columns t < Rc).
+// Without the mirror (the reference's pi-periodic theta, all T rows stored) the
+// partner term vanishes and A_plus = A_minus = A_own / 2, so that
+// Y_j = U + V = A_own h_j and Y_j' = U - V = A_own h_j' with the same kernels.
 void theta_plus_minus(int Tc, int Tp, int Rc, int Rp, int ld, std::vector<double> &Mplus,
-                      std::vector<double> &Mminus) {
-  const int nth_c = Tc / 2;
+                      std::vector<double> &Mminus, bool mirror) {
+  const int nth_c = mirror ? Tc / 2 : 0;
   Mplus.assign((size_t)Rp * ld, 0.0);
   Mminus.assign((size_t)Rp * ld, 0.0);
   for (int r = 0; r < Rp; ++r)
@@ -118,9 +121,9 @@ void theta_plus_minus(int Tc, int Tp, int Rc, int Rp, int ld, std::vector<double
     }
 }
 
-void build_theta_matrix(int Tc, int Tp, int Rc, int Rp, int Kp, std::vector<uint32_t> &out) {
+void build_theta_matrix(int Tc, int Tp, int Rc, int Rp, int Kp, std::vector<uint32_t> &out, bool mirror) {
   std::vector<double> Mplus, Mminus;
-  theta_plus_minus(Tc, Tp, Rc, Rp, Kp, Mplus, Mminus);
+  theta_plus_minus(Tc, Tp, Rc, Rp, Kp, Mplus, Mminus, mirror);
   std::vector<uint32_t> fp, fm;
   a_fragments(Mplus, Rp, Kp, fp);
   a_fragments(Mminus, Rp, Kp, fm);

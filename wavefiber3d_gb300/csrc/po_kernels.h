@@ -93,7 +93,7 @@ po_status launch_interp_cols(const float2 *mid, float2 *parent, const int32_t *c
 // output of launch_interp_rows_packed; Kp = Rc rounded up to even, then to 16.
 size_t theta_matrix_words(int Rp, int Kp);
 size_t theta_pair_words(int Rp, int Kp);
-void build_theta_matrix(int Tc, int Tp, int Rc, int Rp, int Kp, std::vector<uint32_t> &out);
+void build_theta_matrix(int Tc, int Tp, int Rc, int Rp, int Kp, std::vector<uint32_t> &out, bool mirror = true);
 po_status launch_interp_cols_mma(const uint4 *mid, float2 *parent, const int32_t *child_table, int64_t n_parent,
                                  int64_t n_child, int phi, int Rc, int Rp, int Kp, const uint32_t *Afrag,
                                  const float4 *trans, int n_slots, int G, int tile, cudaStream_t st);
@@ -111,7 +111,7 @@ po_status launch_interp_rows_packed(const float2 *src, uint4 *dst, int64_t n_pat
 po_status launch_interp_rows_core(const float2 *src, uint8_t *dst, int64_t n_patterns, int Rc, int Rr, int npad,
                                   int Pc, int Pp, int Kp, const uint32_t *Bm, int sm_count, cudaStream_t st);
 void theta_plus_minus(int Tc, int Tp, int Rc, int Rp, int ld, std::vector<double> &Mplus,
-                      std::vector<double> &Mminus);
+                      std::vector<double> &Mminus, bool mirror = true);
 // tcgen05 theta pass for levels with more than 128 parent rows (po_theta_tc.cu)
 size_t theta_tc_bytes(int Rp, int Kr);
 int theta_tc_npad(int phi);

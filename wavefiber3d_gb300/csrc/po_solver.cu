@@ -156,7 +156,8 @@ struct po_ctx {
   int R[PO_MAX_DEPTH + 1];    // theta rows stored per level (mirror: nth + 1, else T)
   int Phi[PO_MAX_DEPTH + 1];
   int mirror = 0;             // double cover stored as rows 0..nth (see k_interp_cols)
-  bool tensor_theta = false;  // theta pass on the tensor cores (po_interp_mma.cu)
+  bool tensor_theta = false;  // some level interpolates on the tensor cores (po_interp_mma.cu)
+  bool tt_level[PO_MAX_DEPTH] = {};  // level l (parent) interpolates on the tensor cores
   size_t amat_off[PO_MAX_DEPTH] = {};
   int amat_kp[PO_MAX_DEPTH] = {};
   size_t bmat_off[PO_MAX_DEPTH] = {};
@@ -356,13 +357,28 @@ po_status po_create(po_ctx **out, const po_config *cfg) {
     if (cudaEventCreate(&e) != cudaSuccess) { po_destroy(c); return fail(PO_ERR_CUDA, "cudaEventCreate"); }
   }
   // constant theta-interpolation matrices of every level (tensor-core path)
-  c->tensor_theta = cfg->interp_method == PO_INTERP_TENSOR && c->mirror;
+  // Double cover: every level.  Reference theta mode: the levels whose maps are
+  // real and column-independent -- not where the Nyquist quirk of
+  // interpolation.h:66 reaches a parent column (columns past it keep the
+  // unsplit Nyquist bin: a complex, column-dependent map), not between equal
+  // sizes (the reference halves the Nyquist bin there) and only with an even
+  // parent phi grid (mirror column pairs); the other levels keep the FFTs.
+  for (int l = 0; l < d; ++l) {
+    if (cfg->interp_method != PO_INTERP_TENSOR) break;
+    if (c->mirror) {
+      c->tt_level[l] = true;
+    } else {
+      const bool quirk = cfg->nyquist_quirk && c->T[l + 1] % 2 == 0 && c->Phi[l] > 256 * (c->T[l + 1] / 256 + 1);
+      c->tt_level[l] = !quirk && c->T[l + 1] != c->T[l] && c->Phi[l + 1] != c->Phi[l] && c->Phi[l] % 2 == 0;
+    }
+    c->tensor_theta = c->tensor_theta || c->tt_level[l];
+  }
   if (c->tensor_theta) {
     std::vector<uint32_t> all, one;
     for (int l = 0; l < d; ++l) {
       const int Rc2 = c->R[l + 1] + (c->R[l + 1] & 1);
       c->amat_kp[l] = (Rc2 + 15) / 16 * 16;
-      build_theta_matrix(c->T[l + 1], c->T[l], c->R[l + 1], c->R[l], c->amat_kp[l], one);
+      build_theta_matrix(c->T[l + 1], c->T[l], c->R[l + 1], c->R[l], c->amat_kp[l], one, c->mirror != 0);
       c->amat_off[l] = all.size();
       all.insert(all.end(), one.begin(), one.end());
     }
@@ -371,10 +387,10 @@ po_status po_create(po_ctx **out, const po_config *cfg) {
       std::vector<uint16_t> tall, tone;
       std::vector<double> Mp, Mm;
       for (int l = 0; l < d; ++l) {
-        if (!theta_on_tcgen05(c->R[l])) continue;
+        if (!c->tt_level[l] || !theta_on_tcgen05(c->R[l])) continue;
         c->tc_level[l] = true;
         c->tc_kr[l] = (c->R[l + 1] + 15) / 16 * 16;
-        theta_plus_minus(c->T[l + 1], c->T[l], c->R[l + 1], c->R[l], c->tc_kr[l], Mp, Mm);
+        theta_plus_minus(c->T[l + 1], c->T[l], c->R[l + 1], c->R[l], c->tc_kr[l], Mp, Mm, c->mirror != 0);
         build_theta_tc(Mp, Mm, c->R[l], c->R[l + 1], c->tc_kr[l], c->tc_kr[l], tone);
         c->tc_off[l] = tall.size() * sizeof(uint16_t);
         tall.insert(tall.end(), tone.begin(), tone.end());
@@ -872,7 +888,7 @@ static po_status enqueue_solve(po_ctx *c, const SolvePlan &P, float *out_dev, co
       PO_TRY(rec(c->kev[0]));
       // the phi pass of the deepest parent level runs in the leaf kernel's epilogue
       // when its packed output fits one n-tile group
-      const bool fuse_rows = cfg.precision == PO_PREC_SPLIT_BF16 && !P.leaf_tc && d >= 1 && c->tensor_theta &&
+      const bool fuse_rows = cfg.precision == PO_PREC_SPLIT_BF16 && !P.leaf_tc && d >= 1 && c->tt_level[d - 1] &&
                              !c->tc_level[d - 1] && leaf_row_fusion_fits(c->Phi[d], c->Phi[d - 1], c->bmat_kp[d - 1]);
       if (P.leaf_tc)
         PO_TRY(launch_leaf_tc(P.gsc, P.tree.level[d].begin, c->leaf_kc0.as<int32_t>(), c->leaf_chunk.as<int32_t>(),
@@ -908,7 +924,7 @@ static po_status enqueue_solve(po_ctx *c, const SolvePlan &P, float *out_dev, co
           PO_TRY(launch_interp_rows_core(cur_lvl, c->mid.as<uint8_t>(), (int64_t)ch.ns * nc * 6, c->R[l + 1],
                                          c->tc_kr[l], theta_tc_npad(c->Phi[l]), c->Phi[l + 1], c->Phi[l],
                                          c->bmat_kp[l], c->bmat.as<uint32_t>() + c->bmat_off[l], c->sm_count, st));
-        } else if (c->tensor_theta) {
+        } else if (c->tt_level[l]) {
           PO_TRY(launch_interp_rows_packed(cur_lvl, c->mid.as<uint4>(), (int64_t)ch.ns * nc * 6, c->R[l + 1],
                                            c->Phi[l + 1], c->Phi[l], c->bmat_kp[l],
                                            c->bmat.as<uint32_t>() + c->bmat_off[l], c->sm_count, st));
@@ -929,7 +945,7 @@ static po_status enqueue_solve(po_ctx *c, const SolvePlan &P, float *out_dev, co
           PO_TRY(launch_theta_tc(c->mid.as<uint8_t>(), nxt, P.tree.level[l].child, np, nc, c->Phi[l], c->tc_kr[l],
                                  c->R[l], c->tc_amat.as<uint8_t>() + c->tc_off[l], trans, ch.ns, ch.gc,
                                  c->tc_err.as<int>(), c->mid.bytes, c->tc_amat.bytes - c->tc_off[l], st));
-        } else if (c->tensor_theta) {
+        } else if (c->tt_level[l]) {
           PO_TRY(launch_interp_cols_mma(c->mid.as<uint4>(), nxt, P.tree.level[l].child, np, nc, c->Phi[l],
                                         c->R[l + 1], c->R[l], c->amat_kp[l], c->amat.as<uint32_t>() + c->amat_off[l],
                                         trans, ch.ns, ch.gc, cfg.interp_tile, st));
@@ -1110,7 +1126,7 @@ po_status po_grad(po_ctx *c, const po_geometry *g, const po_illum *il, const flo
   if (!(il->sigma > 0)) return fail(PO_ERR_INVALID_ARGUMENT, "beam sigma must be > 0");
   const int npol = ((il->pol_mask & PO_POL_TM) ? 1 : 0) + ((il->pol_mask & PO_POL_TE) ? 1 : 0);
   if ((int64_t)il->n_lambda * il->n_inc * npol > 65535) return fail(PO_ERR_UNSUPPORTED, "too many patterns per call");
-  if (c->depth > 0 && !c->tensor_theta)
+  if (c->depth > 0 && !(c->tensor_theta && c->mirror))
     return fail(PO_ERR_UNSUPPORTED, "the adjoint of a tree solve needs double-cover theta and PO_INTERP_TENSOR");
   int dev = 0;
   PO_CUDA(cudaGetDevice(&dev));
