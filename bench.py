@@ -64,7 +64,8 @@ PRECISIONS = {"fp32": 0, "split_bf16": 2}
 INTERP = {"fft": 0, "tensor": 1}
 
 
-def make_workload(precision: str = "fp32", interp: str = "tensor", tile: int = 0, n_lambda: int = 25):
+def make_workload(precision: str = "fp32", interp: str = "tensor", tile: int = 0, n_lambda: int = 25,
+                  n_inc: int = 1):
     from wavefiber3d_gb300 import api, geometry
     cloud = geometry.ellipsoid(RADII, N_POINTS)
     bmin = [-1.1 * r for r in RADII]
@@ -72,7 +73,10 @@ def make_workload(precision: str = "fp32", interp: str = "tensor", tile: int = 0
     cfg = api.Config.reference_rule(DEPTH, N_THETA, N_PHI, bmin, bmax, 16e-6, 16e-6, 1.3,
                                     precision=PRECISIONS[precision], interp_method=INTERP[interp],
                                     interp_tile=tile)
-    illum = api.Illumination(LAMBDAS[:n_lambda], [0.0], [0.0], api.PO_POL_TM, ETA, SIGMA)
+    # one incidence along +x (the workload); more for profiling runs: a theta sweep at phi = 0.3
+    th = [0.0] if n_inc == 1 else list(np.linspace(-1.0, 1.0, n_inc))
+    ph = [0.0] if n_inc == 1 else [0.3] * n_inc
+    illum = api.Illumination(LAMBDAS[:n_lambda], th, ph, api.PO_POL_TM, ETA, SIGMA)
     return cloud, cfg, illum
 
 
@@ -115,11 +119,11 @@ def sample_directions(k: int, seed: int = 20231203) -> np.ndarray:
     return np.sort(rng.choice(N_THETA * N_PHI, size=k, replace=False)).astype(np.int64)
 
 
-def cpu_direct_sample(cloud, lam, dirs):
+def cpu_direct_sample(cloud, lam, dirs, theta_i=0.0, phi_i=0.0):
     """FP64 oracle direct sum (all host cores) on the sampled directions; returns
     (intensity, seconds, threads)."""
     import oracle
-    il = oracle.make_illum(lam, 0.0, 0.0, "M", ETA, SIGMA)
+    il = oracle.make_illum(lam, theta_i, phi_i, "M", ETA, SIGMA)
     t0 = time.perf_counter()
     cur = oracle.currents(cloud, il)
     f = oracle.far_field_sampled(cloud, cur, 2 * math.pi / lam, [0.0, 0.0, 0.0], N_THETA, N_PHI, dirs)
@@ -209,7 +213,7 @@ def run_engine(args, world, rank, local):
     bf16_peak = peaks.get("bf16_tflops", 1900.0)
     peak_src = "measured" if peaks else "fallback"
 
-    cloud, cfg, illum = make_workload(args.precision, args.interp, args.interp_tile, args.lambdas)
+    cloud, cfg, illum = make_workload(args.precision, args.interp, args.interp_tile, args.lambdas, args.incidences)
     pd_step = point_dirs_per_step(illum)
     st = torch.cuda.current_stream()
     g_dev = torch.from_numpy(cloud.soa()).to(dev)
@@ -293,7 +297,7 @@ def run_engine(args, world, rank, local):
     result = None
     if rank == 0:
         dirs = sample_directions(args.cpu_dirs)
-        cpu_inten, cpu_s, threads = cpu_direct_sample(cloud, LAMBDAS[0], dirs)
+        cpu_inten, cpu_s, threads = cpu_direct_sample(cloud, LAMBDAS[0], dirs, illum.theta_i[0], illum.phi_i[0])
         gpu_inten = out_dev[0, 0, 0].reshape(-1).cpu().numpy()[dirs].astype(np.float64)
         acc = float(np.linalg.norm(gpu_inten - cpu_inten) / np.linalg.norm(cpu_inten))
         cpu_value = N_POINTS * dirs.size / cpu_s / 1e9
@@ -313,7 +317,8 @@ def run_engine(args, world, rank, local):
                      "split bf16 hi+lo leaf products, f32 accumulation (f64 phase arguments)",
             "data": "synthetic (seeded ellipsoid, analytic normals)",
             "config": {"workload": WORKLOAD, "points": N_POINTS, "directions": N_THETA * N_PHI,
-                       "wavelengths": len(illum.wavelengths_m), "incidences": 1, "polarisations": 1, "depth": DEPTH,
+                       "wavelengths": len(illum.wavelengths_m), "incidences": len(illum.theta_i), "polarisations": 1,
+                       "depth": DEPTH,
                        "level_grids": [list(cfg.n_theta), list(cfg.n_phi)], "theta_mode": "double cover",
                        "precision": args.precision, "theta_interpolation": args.interp,
                        "theta_tile": args.interp_tile,
@@ -356,9 +361,9 @@ FIBER_BOX_MAX = [-v for v in FIBER_BOX_MIN]
 FIBER_AGG_TRAFFIC_RATIO = None
 
 
-def fiber_incidences():
-    idx = np.arange(58, 58 + FIBER_INC)
-    return list(-math.pi / 2 + 1e-10 + math.pi / 180 * idx), [0.0] * FIBER_INC
+def fiber_incidences(n: int = FIBER_INC):
+    idx = np.arange(58, 58 + n)
+    return list(-math.pi / 2 + 1e-10 + math.pi / 180 * idx), [0.0] * n
 
 
 def fiber_config(precision: str, interp: str = "tensor"):
@@ -396,7 +401,8 @@ def run_fiber(args, world, rank, local):
     g_host = g_dev.cpu().pin_memory()
     geom_host = tuple(g_host[k] for k in range(7))
     lams = LAMBDAS[: args.fiber_lambdas]
-    th, ph = fiber_incidences()
+    n_inc = max(1, min(FIBER_INC, args.fiber_incidences))
+    th, ph = fiber_incidences(n_inc)
     illum = api.Illumination(lams, th, ph, api.PO_POL_TM, ETA, FIBER_SIGMA)
     cfg = fiber_config(args.precision, args.interp)
     solver = api.Solver(cfg)
@@ -468,7 +474,7 @@ def run_fiber(args, world, rank, local):
     dirs = sample_directions(args.fiber_dirs)
     errs = []
     ctr = [0.5 * (a + b) for a, b in zip(np.float32(FIBER_BOX_MIN), np.float32(FIBER_BOX_MAX))]
-    for ii in (0, FIBER_INC - 1):
+    for ii in sorted({0, n_inc - 1}):
         il = oracle.make_illum(lams[0], th[ii], ph[ii], "M", ETA, FIBER_SIGMA)
         cur = oracle.currents(cloud, il)
         f = oracle.far_field_sampled(cloud, cur, 2 * math.pi / lams[0], ctr, N_THETA, N_PHI, dirs)
@@ -515,7 +521,7 @@ def run_fiber(args, world, rank, local):
                  if args.precision == "split_bf16" else "f32 (f64 phase arguments)",
         "data": "synthetic (seeded fiber height field, sampled on the GPU)",
         "config": {"workload": FIBER_WORKLOAD, "points": n, "numel": hf.numel, "numelvert": hf.numelvert,
-                   "wavelengths": len(lams), "incidences": FIBER_INC, "polarisations": 1, "depth": FIBER_DEPTH,
+                   "wavelengths": len(lams), "incidences": n_inc, "polarisations": 1, "depth": FIBER_DEPTH,
                    "directions": N_THETA * N_PHI, "level_grids": [list(cfg.n_theta), list(cfg.n_phi)],
                    "precision": args.precision, "theta_mode": "double cover", "theta_interpolation": args.interp,
                    "beam_sigma_m": FIBER_SIGMA,
@@ -536,7 +542,7 @@ def run_fiber(args, world, rank, local):
         "rel_l2_vs_fp64_gpu_full_grid": rel_full_grid,
         "rel_l2_vs_fp64_oracle_per_incidence": errs,
         "accuracy_sample": f"all 64800 directions of lambda={lams[0] * 1e9:.0f} nm, incidence 0 against the FP64 GPU "
-                           f"sum; {dirs.size} seeded directions of incidences 0 and {FIBER_INC - 1} against the "
+                           f"sum; {dirs.size} seeded directions of incidences 0 and {n_inc - 1} against the "
                            "FP64 oracle on the host",
         "roofline": roof,
         "kernel_ms_per_step": {"leaf": r["ms_leaf_kernel"], "phi passes": r["ms_rows"], "theta passes": r["ms_cols"],
@@ -902,12 +908,46 @@ def run_reference_cuda(args, world, rank, local):
         eng1 = s.solve(sph, il1).reshape(-1).astype(np.float64)
     agree1 = float(np.linalg.norm(out1 - eng1) / np.linalg.norm(eng1))
 
+    # the engine (B1 FP64, B3 FP32) and the host FP64 oracle (B0) on the same configs
+    st = torch.cuda.current_stream()
+    g1 = torch.from_numpy(sph.soa()).to(dev)
+
+    def engine_ms(cfg, g, il, reps=5):
+        with api.Solver(cfg) as s:
+            out = torch.empty(s.out_shape(il), dtype=torch.float32, device=dev)
+            geom = tuple(g[k] for k in range(7))
+            for _ in range(2):
+                s.solve(geom, il, out=out, report=False)
+            ts = []
+            for _ in range(reps):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(st)
+                s.solve(geom, il, out=out, report=False)
+                e1.record(st)
+                torch.cuda.synchronize()
+                ts.append(e0.elapsed_time(e1))
+            return statistics.median(ts)
+    import oracle
+    eng = {"sphere_20k_depth0": {
+        "b1_fp64_gpu_ms": engine_ms(api.Config(0, [N_THETA], [N_PHI], box1[:3], box1[3:], precision=api.PO_PREC_FP64),
+                                    g1, il1),
+        "b3_fp32_gpu_ms": engine_ms(cfg1, g1, il1)}}
+    t0 = time.perf_counter()
+    oracle.solve_direct(sph, oracle.make_illum(500e-9, math.pi / 2, math.pi, "M", 1.55, 1e-2), N_THETA, N_PHI)
+    eng["sphere_20k_depth0"]["b0_fp64_host_ms"] = (time.perf_counter() - t0) * 1e3
+    eng["sphere_20k_depth0"]["b0_cores"] = oracle.num_threads()
+
     # ---- config 2: 400k-point ellipsoid, depth 5, one (wavelength, incidence) pair, capped loops
     ell = geometry.ellipsoid(RADII, N_POINTS)
     box2 = [-1.1 * r for r in RADII] + [1.1 * r for r in RADII]
     cfg2 = api.Config.reference_rule(DEPTH, N_THETA, N_PHI, box2[:3], box2[3:], 16e-6, 16e-6, 1.3)
     caps2 = (args.ref_leaf_dirs, args.ref_children, 1)
     t2, ms2, wall2, _ = run(ell, box2, DEPTH, cfg2.n_theta, cfg2.n_phi, LAMBDAS[0], 0.0, 0.0, ETA, SIGMA, caps2)
+    g2 = torch.from_numpy(ell.soa()).to(dev)
+    il2 = api.Illumination(LAMBDAS[:1], [0.0], [0.0], api.PO_POL_TM, ETA, SIGMA)
+    eng["ellipsoid_400k_depth5"] = {
+        "b1_fp64_gpu_ms_per_pattern": engine_ms(
+            api.Config(0, [N_THETA], [N_PHI], box2[:3], box2[3:], precision=api.PO_PREC_FP64), g2, il2, reps=2)}
     return {
         "impl": "reference-cuda",
         "metric": "ms per pattern of the reference's own CUDA build (baseline B2)",
@@ -927,6 +967,7 @@ def run_reference_cuda(args, world, rank, local):
                     "extrapolated by the counts; the root level (197 -> 180 theta samples, a downsampling the "
                     "reference's interpolation cannot do) and the intensity are left out, so this is a lower "
                     f"bound; the step figure scales by the {len(LAMBDAS)} wavelengths"},
+        "engine_and_host_same_configs": eng,
         "fiber_3p4m_depth7": {"unavailable": "the reference's depth-7 CDP octree issues 299,593 device-side "
                                              "launches (util/tree.h:710-712) against its pending-launch limit of "
                                              "32,768; not run on this pool"},
@@ -1002,7 +1043,11 @@ def main():
     ap.add_argument("--interp-tile", type=int, choices=[0, 8, 16], default=0,
                     help="complex columns per CTA of the tensor-core theta pass (0: automatic)")
     ap.add_argument("--lambdas", type=int, default=25,
-                    help="wavelengths of the ellipsoid workload (25 = the headline; fewer for profiling runs)")
+                    help="wavelengths of the ellipsoid workload (25 = the workload; fewer for profiling runs)")
+    ap.add_argument("--incidences", type=int, default=1,
+                    help="incidences of the ellipsoid workload (1 = the workload; more for profiling runs)")
+    ap.add_argument("--fiber-incidences", type=int, default=64,
+                    help="incidences per fiber step (64 = the workload; fewer for profiling runs)")
     ap.add_argument("--workload", choices=["fiber", "ellipsoid", "cylinder-grad", "batch", "reference-cuda"],
                     default="fiber",
                     help="fiber: the headline, the 3.4M-point fiber segment, 25 wavelengths x 64 incidences, depth 7 "
