@@ -248,10 +248,16 @@ po_status po_config_init(po_config *cfg, int max_depth, int n_theta_out, int n_p
 }
 
 // The tcgen05 theta pass works on 128-row tiles of the parent; it serves the
-// levels whose rows fill at least 3/4 of their tiles, the others keep the
-// warp-level kernel, whose 16-row tiles waste fewer rows (on the ellipsoid
-// workload: 109-, 201- and 361-row levels on tcgen05, 63 rows and fewer not).
-static bool theta_on_tcgen05(int rows) { return rows * 4 >= 3 * 128 * ((rows + 127) / 128); }
+// levels whose rows fill at least 60% of their tiles, the others keep the
+// warp-level kernel, whose 16-row tiles waste fewer rows (ellipsoid workload:
+// the 109-, 201- and 361-row levels on tcgen05, 64 rows and fewer not; fiber
+// workload: every level from 97 rows up).  Its column chunks of 64 mirror
+// pairs are padded too, but even the fiber's 97 x 84 level (66% of its
+// columns) runs 1.4x faster on tcgen05 than on the warp-level kernel.
+static bool theta_on_tcgen05(int rows, int phi) {
+  (void)phi;
+  return rows * 5 >= 3 * 128 * ((rows + 127) / 128);
+}
 
 po_status po_create(po_ctx **out, const po_config *cfg) {
   if (!out || !cfg) return fail(PO_ERR_INVALID_ARGUMENT, "null argument");
@@ -387,7 +393,7 @@ po_status po_create(po_ctx **out, const po_config *cfg) {
       std::vector<uint16_t> tall, tone;
       std::vector<double> Mp, Mm;
       for (int l = 0; l < d; ++l) {
-        if (!c->tt_level[l] || !theta_on_tcgen05(c->R[l])) continue;
+        if (!c->tt_level[l] || !theta_on_tcgen05(c->R[l], c->Phi[l])) continue;
         c->tc_level[l] = true;
         c->tc_kr[l] = (c->R[l + 1] + 15) / 16 * 16;
         theta_plus_minus(c->T[l + 1], c->T[l], c->R[l + 1], c->R[l], c->tc_kr[l], Mp, Mm, c->mirror != 0);
