@@ -356,9 +356,10 @@ FIBER_WORKLOAD = ("fiber segment 25x20um x 60um, cuticle 5um/0.4um/3deg + Gaussi
 FIBER_BOX_MIN = [-1.1 * FIBER_RADII[0], -1.1 * FIBER_RADII[1], -0.55 * FIBER_LENGTH]  # treePO.cu:96-98
 FIBER_BOX_MAX = [-v for v in FIBER_BOX_MIN]
 # DRAM bytes per algorithmic byte of the aggregation passes, from the ncu capture summarised in
-# profiles/aggregation_fiber.md (dram__bytes_read.sum + dram__bytes_write.sum of the phi and theta
-# launches of one wavelength, over the per-level algorithmic bytes of the same launches)
-FIBER_AGG_TRAFFIC_RATIO = None
+# profiles/aggregation_traffic_fiber_8inc.md (dram__bytes_read.sum + dram__bytes_write.sum of every phi
+# and theta launch of one 8-incidence solve of this workload, 165.45 GB, over the per-level
+# algorithmic bytes of the same solve, 49.42 GB)
+FIBER_AGG_TRAFFIC_RATIO = 165.45 / 49.42
 
 
 def fiber_incidences(n: int = FIBER_INC):
@@ -511,7 +512,8 @@ def run_fiber(args, world, rank, local):
                 "frac": achieved / hbm_peak, "traffic": traffic,
                 "note": "algorithmic bytes = per level, the child patterns read at the child grid + the parent "
                         f"patterns written (8 B per complex sample); peak = {peak_src} copy bandwidth; traffic = "
-                        "ncu DRAM bytes per step scaled from a one-wavelength capture"}
+                        "ncu DRAM bytes per algorithmic byte of an 8-incidence capture of the same kernels "
+                        "(profiles/aggregation_traffic_fiber_8inc.md) times this step's algorithmic bytes"}
     result = {
         "metric": "Gpoint-dirs/s (equivalent depth-0 point x direction terms) at rel-L2<=1e-3 vs FP64 direct sum",
         "value": pd_step * world / (ms_step_max * 1e-3) / 1e9,
