@@ -770,11 +770,11 @@ def run_batch(args, world, rank, local):
         g = torch.from_numpy(cloud.soa()).to(dev)
         il = api.Illumination([lam], [th], [ph], api.PO_POL_TM, ETA, 1.0)
 
-        def make(depth, prec, tile, box=box, r=r):
+        def make(depth, prec, box=box, r=r):
             return api.Config.reference_rule(depth, N_THETA, N_PHI, box[0], box[1], 2 * r, 2 * r, 1.3,
-                                             precision=prec, interp_tile=tile)
+                                             precision=prec)
         ch = tuner.choose(g, il, make, 2 * r)
-        configs.append(make(ch["depth"], ch["precision"], ch["tile"]))
+        configs.append(autotune.apply(make(ch["depth"], ch["precision"]), ch))
         samples.append(g)
         illums.append(il)
         choices.append(ch)
@@ -798,6 +798,7 @@ def run_batch(args, world, rank, local):
         evs.append((e0, e1))
     torch.cuda.synchronize()
     clk = clocks.stop()
+    batch.check(st)  # raises if an item's kernels gave up a bounded device wait
     ms_graph = statistics.mean(a.elapsed_time(b) for a, b in evs)
     info = batch.info()
     # the same solves one by one (po_solve, no graph)
@@ -840,7 +841,9 @@ def run_batch(args, world, rank, local):
         "config": {"workload": BATCH_WORKLOAD, "solves": len(items), "points_total": npts,
                    "streams": args.batch_streams, "depths": depth_hist,
                    "split_bf16_solves": sum(1 for c in choices if c["precision"] == api.PO_PREC_SPLIT_BF16),
-                   "tiles": {t: sum(1 for c in choices if c["tile"] == t) for t in (0, 8, 16)}},
+                   "tiles": {t: sum(1 for c in choices if c["tile"] == t) for t in (0, 8, 16)},
+                   "leaf_kernels": {k: sum(1 for c in choices if c.get("leaf_kernel", 0) == v)
+                                    for k, v in (("auto", 0), ("warp", 1), ("tcgen05", 2))}},
         "solves_per_s": len(items) / (ms_graph * 1e-3),
         "ms_same_solves_one_by_one": ms_serial, "graph_speedup": ms_serial / ms_graph,
         "graph_equals_one_by_one": same,

@@ -53,6 +53,13 @@ typedef enum po_theta_mode {
   PO_THETA_REFERENCE = 1
 } po_theta_mode;
 
+/* Which kernel computes the leaf sums of a split-BF16 tree solve. */
+typedef enum po_leaf_kernel {
+  PO_LEAF_AUTO = 0,    /* tcgen05 from 8 patterns per wavelength, warp-level below */
+  PO_LEAF_WARP = 1,    /* warp-level mma.sync, 4 patterns per CTA */
+  PO_LEAF_TCGEN05 = 2  /* tcgen05 with tensor-memory accumulators, leaf_slots patterns per pass */
+} po_leaf_kernel;
+
 /* Polarisation mask: 'M' (TM) and 'E' (TE) of compareMie/sphere.cu:551-579. */
 #define PO_POL_TM 1
 #define PO_POL_TE 2
@@ -74,6 +81,9 @@ typedef struct po_config {
   int interp_tile;                  /* complex columns per CTA of the warp-level tensor-core
                                        theta pass (levels with few rows; autotuner knob):
                                        0 = automatic, 8 or 16 */
+  int leaf_kernel;                  /* po_leaf_kernel (split BF16 only; autotuner knob) */
+  int leaf_slots;                   /* patterns of one wavelength per pass of the tcgen05 leaf
+                                       kernel: 0 = 64, else a multiple of 8 up to 64 */
 } po_config;
 
 /* How the angular interpolation between tree levels (phi pass, then theta

@@ -71,6 +71,12 @@ def test_invalid_configurations_fail_before_touching_cuda(lib):
     lib.po_config_init(ctypes.byref(c), 2, 16, 32, b0, b1, 1e-6, 1e-6, 1.3, 6.0, 0.4e-6)
     c.precision = 1  # FP64 is the depth-0 plain sum only
     assert lib.po_create(ctypes.byref(h), ctypes.byref(c)) == 4
+    # leaf schedule: a known kernel, for split-BF16 trees only; whole groups of 8 patterns up to 64
+    for prec, kern, slots in ((2, 3, 0), (0, 2, 0), (2, 0, 12), (2, 2, 72), (2, 1, -8)):
+        lib.po_config_init(ctypes.byref(c), 2, 16, 32, b0, b1, 1e-6, 1e-6, 1.3, 6.0, 0.4e-6)
+        c.precision, c.leaf_kernel, c.leaf_slots = prec, kern, slots
+        assert lib.po_create(ctypes.byref(h), ctypes.byref(c)) == 1, (prec, kern, slots)
+        assert b"leaf" in lib.po_last_error()
     for s in range(7):
         assert lib.po_status_string(s)
     assert b"sm_103a" in lib.po_version()

@@ -8,6 +8,7 @@ Tolerances (relative L2 over the whole output):
   tree solve, reference theta mode vs oracle tree  : 1e-4
   anything vs the reference's FP32 CUDA build      : 1e-4
 """
+import dataclasses
 import math
 
 import numpy as np
@@ -431,6 +432,36 @@ def test_leaf_tcgen05_chunked_matches_single_pass():
         out, r = _solve(cloud, cfg, il)
         assert r["n_chunks"] > 1
         assert np.array_equal(out, full), (cap, r["n_chunks"], r["chunk_slots"])
+
+
+@pytest.mark.parametrize("n_inc,kernel,slots", [(1, api.PO_LEAF_TCGEN05, 8), (3, api.PO_LEAF_TCGEN05, 0),
+                                                 (20, api.PO_LEAF_TCGEN05, 16), (9, api.PO_LEAF_WARP, 0)])
+def test_leaf_schedule_choices_vs_fp64_direct(n_inc, kernel, slots):
+    """The autotuner's leaf-batch schedules: the tcgen05 leaf kernel forced
+    below its automatic threshold (1 and 3 patterns per wavelength) and in
+    passes of 16 patterns, the warp-level kernel forced above it.  Each
+    against the FP64 oracle; the tcgen05 passes of any size give the
+    automatic schedule's result bit for bit (every output column depends on
+    its own column of the currents only)."""
+    cloud = geometry.ellipsoid((1.5e-6, 1.0e-6, 0.8e-6), 3000)
+    box = [-1.65e-6, -1.1e-6, -0.88e-6, 1.65e-6, 1.1e-6, 0.88e-6]
+    th, ph = _many_incidences(n_inc, seed=5)
+    il = api.Illumination([520e-9], th, ph, api.PO_POL_TM, 1.55 + 0.1j, 2e-6)
+    cfg = api.Config.reference_rule(2, 24, 48, box[:3], box[3:], 1.6e-6, 3.0e-6, 1.2,
+                                    precision=api.PO_PREC_SPLIT_BF16, leaf_kernel=kernel, leaf_slots=slots)
+    out, rep = _solve(cloud, cfg, il)
+    out = out.reshape(n_inc, 24, 48)
+    per_pass = slots or 64
+    want = 2 * -(-n_inc // per_pass) if kernel == api.PO_LEAF_TCGEN05 else -(-n_inc // 4)
+    assert rep["n_leaf_launches"] == want, rep
+    ctr = [(box[i] + box[i + 3]) / 2 for i in range(3)]
+    for ii in sorted({0, n_inc - 1}):
+        o = oracle.solve_direct(cloud, oracle.make_illum(520e-9, th[ii], ph[ii], "M", 1.55 + 0.1j, 2e-6), 24, 48,
+                                center=ctr)
+        assert rel(out[ii], o) < TOL_TREE, (ii, rep)
+    if kernel == api.PO_LEAF_TCGEN05 and n_inc >= 8:
+        auto, _ = _solve(cloud, dataclasses.replace(cfg, leaf_kernel=api.PO_LEAF_AUTO, leaf_slots=0), il)
+        assert np.array_equal(out.reshape(auto.shape), auto)
 
 
 def test_reference_mode_tensor_path_on_large_grids():

@@ -18,6 +18,7 @@ PO_PREC_FP32, PO_PREC_FP64, PO_PREC_SPLIT_BF16, PO_PREC_SPLIT_FP16 = 0, 1, 2, 3
 PO_THETA_DOUBLE_COVER, PO_THETA_REFERENCE = 0, 1
 PO_POL_TM, PO_POL_TE = 1, 2
 PO_INTERP_FFT, PO_INTERP_TENSOR = 0, 1
+PO_LEAF_AUTO, PO_LEAF_WARP, PO_LEAF_TCGEN05 = 0, 1, 2
 
 STATUS_NAMES = {0: "PO_OK", 1: "PO_ERR_INVALID_ARGUMENT", 2: "PO_ERR_CUDA", 3: "PO_ERR_OUT_OF_MEMORY",
                 4: "PO_ERR_UNSUPPORTED", 5: "PO_ERR_TIMEOUT", 6: "PO_ERR_INTERNAL"}
@@ -36,7 +37,8 @@ class po_config(ctypes.Structure):
                 ("box_min", ctypes.c_float * 3), ("box_max", ctypes.c_float * 3),
                 ("precision", ctypes.c_int), ("theta_mode", ctypes.c_int), ("nyquist_quirk", ctypes.c_int),
                 ("distance", ctypes.c_double), ("interp_method", ctypes.c_int),
-                ("max_workspace_bytes", ctypes.c_int64), ("interp_tile", ctypes.c_int)]
+                ("max_workspace_bytes", ctypes.c_int64), ("interp_tile", ctypes.c_int),
+                ("leaf_kernel", ctypes.c_int), ("leaf_slots", ctypes.c_int)]
 
 
 class po_geometry(ctypes.Structure):

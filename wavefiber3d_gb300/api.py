@@ -25,13 +25,15 @@ from typing import Sequence
 import numpy as np
 
 from . import _lib
-from ._lib import (PO_INTERP_FFT, PO_INTERP_TENSOR, PO_POL_TE, PO_POL_TM, PO_PREC_FP32, PO_PREC_FP64,
-                   PO_PREC_SPLIT_BF16, PO_THETA_DOUBLE_COVER, PO_THETA_REFERENCE, WavePOError, check)
+from ._lib import (PO_INTERP_FFT, PO_INTERP_TENSOR, PO_LEAF_AUTO, PO_LEAF_TCGEN05, PO_LEAF_WARP, PO_POL_TE,
+                   PO_POL_TM, PO_PREC_FP32, PO_PREC_FP64, PO_PREC_SPLIT_BF16, PO_THETA_DOUBLE_COVER,
+                   PO_THETA_REFERENCE, WavePOError, check)
 
 __all__ = ["Config", "Illumination", "Solver", "compute_local_tangent_plane", "build_octree",
            "current_times_green_center", "copyandinterp", "compute_intensity", "wavelength_from_index",
            "incidence_from_index", "WavePOError", "PO_POL_TM", "PO_POL_TE", "PO_PREC_FP32", "PO_PREC_FP64", "PO_PREC_SPLIT_BF16",
-           "PO_THETA_DOUBLE_COVER", "PO_THETA_REFERENCE", "PO_INTERP_FFT", "PO_INTERP_TENSOR"]
+           "PO_THETA_DOUBLE_COVER", "PO_THETA_REFERENCE", "PO_INTERP_FFT", "PO_INTERP_TENSOR", "PO_LEAF_AUTO",
+           "PO_LEAF_WARP", "PO_LEAF_TCGEN05"]
 
 
 def _torch():
@@ -85,6 +87,8 @@ class Config:
     interp_method: int = PO_INTERP_TENSOR
     max_workspace_bytes: int = 0
     interp_tile: int = 0
+    leaf_kernel: int = PO_LEAF_AUTO
+    leaf_slots: int = 0
 
     @classmethod
     def reference_rule(cls, max_depth, n_theta_out, n_phi_out, box_min, box_max, theta_extent, phi_extent,
@@ -113,6 +117,8 @@ class Config:
         c.interp_method = int(self.interp_method)
         c.max_workspace_bytes = int(self.max_workspace_bytes)
         c.interp_tile = int(self.interp_tile)
+        c.leaf_kernel = int(self.leaf_kernel)
+        c.leaf_slots = int(self.leaf_slots)
         return c
 
 

@@ -53,7 +53,8 @@ bool leaf_row_fusion_fits(int Pc, int Pp, int Kp);
 // of 16: kc0[leaf] = first chunk of the leaf (kc0[n_leaves] = n_chunks),
 // chunk_leaf[chunk] = its leaf.  bop / uop: operand scratch of
 // n_lambda x n_chunks x leaf_tc_col_tiles(G) x leaf_tc_block_bytes() and of
-// n_lambda x n_chunks x 16 float4.
+// n_lambda x n_chunks x 16 float4.  group: slots per pass (a multiple of 8 up
+// to kLeafTcMaxSlots); each pass regenerates the phase operands of every leaf.
 constexpr int kLeafTcMaxSlots = 64;  // slots per operand pass (6 column tiles of 64 complex columns)
 constexpr int kLeafTcMinSlots = 8;   // fewer patterns per wavelength keep the warp-level kernel
 int leaf_tc_col_tiles(int G);
@@ -63,7 +64,8 @@ po_status launch_leaf_tc(const float *const g[7], const int32_t *leaf_begin, con
                          const int32_t *chunk_leaf, int64_t n_chunks, const double *leaf_center, int64_t n_leaves,
                          const SlotParams<float> *slots_dev, int n_lambda, int Gtot, int g0, int G,
                          const float4 *dirs, int ndir, uint8_t *bop, size_t bop_bytes, float4 *uop,
-                         size_t uop_bytes, float2 *out, int *err, cudaStream_t st, int withhold = 0);
+                         size_t uop_bytes, float2 *out, int *err, cudaStream_t st, int group = kLeafTcMaxSlots,
+                         int withhold = 0);
 
 int direct_splits(int64_t n, int ndir, int n_lambda, int sm_count);
 // FP32 depth-0 sum about c0: out[slot][comp][dir]; cur[slot][n][6]

@@ -375,17 +375,19 @@ po_status launch_leaf_tc(const float *const g[7], const int32_t *leaf_begin, con
                          const int32_t *chunk_leaf, int64_t n_chunks, const double *leaf_center, int64_t n_leaves,
                          const SlotParams<float> *slots_dev, int n_lambda, int Gtot, int g0, int G,
                          const float4 *dirs, int ndir, uint8_t *bop, size_t bop_bytes, float4 *uop,
-                         size_t uop_bytes, float2 *out, int *err, cudaStream_t st, int withhold) {
+                         size_t uop_bytes, float2 *out, int *err, cudaStream_t st, int group, int withhold) {
   if (n_leaves <= 0 || n_lambda <= 0 || G <= 0) return PO_OK;
+  if (group < 8 || group > kLeafTcMaxSlots || group % 8 != 0)
+    return fail(PO_ERR_INTERNAL, "tcgen05 leaf: slots per pass");
   if (n_chunks <= 0 || n_lambda > 65535 || n_leaves > 2147483647LL || n_chunks > 2147483647LL)
     return fail(PO_ERR_INTERNAL, "tcgen05 leaf: launch shape");
-  if ((size_t)n_lambda * n_chunks * leaf_tc_col_tiles(std::min(G, kLeafTcMaxSlots)) * kLtBBlock > bop_bytes ||
+  if ((size_t)n_lambda * n_chunks * leaf_tc_col_tiles(std::min(G, group)) * kLtBBlock > bop_bytes ||
       (size_t)n_lambda * n_chunks * kLtKC * sizeof(float4) > uop_bytes)
     return fail(PO_ERR_INTERNAL, "tcgen05 leaf: operand buffers");
-  // slots in groups of at most kLeafTcMaxSlots (6 column tiles); the operand
-  // buffers are reused group after group in stream order
-  for (int gs = 0; gs < G; gs += kLeafTcMaxSlots) {
-    const int gc = std::min(kLeafTcMaxSlots, G - gs), NT = leaf_tc_col_tiles(gc);
+  // slots in groups of at most `group` (kLeafTcMaxSlots = 6 column tiles); the
+  // operand buffers are reused group after group in stream order
+  for (int gs = 0; gs < G; gs += group) {
+    const int gc = std::min(group, G - gs), NT = leaf_tc_col_tiles(gc);
     k_leaf_tc_operands<<<dim3((unsigned)n_chunks, (unsigned)n_lambda), 256, NT * kLtBBlock, st>>>(
         g[0], g[1], g[2], g[3], g[4], g[5], g[6], leaf_begin, kc0, chunk_leaf, leaf_center, slots_dev, Gtot,
         g0 + gs, gc, NT, n_chunks, bop, uop);

@@ -96,7 +96,8 @@ po_status leaf_case(int *err, cudaStream_t st) {
   for (int q = 0; q < 7; ++q) gp[q] = (const float *)pts + q * npts;
   PO_TRY(launch_leaf_tc(gp, (const int32_t *)begin, (const int32_t *)kc0, (const int32_t *)chunk, 1,
                         (const double *)ctr, 1, (const SlotParams<float> *)slot, 1, 1, 0, 1, (const float4 *)dirs,
-                        ndir, (uint8_t *)bop, bop_bytes, (float4 *)uop, uop_bytes, (float2 *)out, err, st, 1));
+                        ndir, (uint8_t *)bop, bop_bytes, (float4 *)uop, uop_bytes, (float2 *)out, err, st,
+                        kLeafTcMaxSlots, 1));
   PO_CUDA(cudaStreamSynchronize(st));
   return PO_OK;
 }

@@ -285,6 +285,12 @@ po_status po_create(po_ctx **out, const po_config *cfg) {
     return fail(PO_ERR_INVALID_ARGUMENT, "unknown interpolation method");
   if (cfg->interp_tile != 0 && cfg->interp_tile != 8 && cfg->interp_tile != 16)
     return fail(PO_ERR_INVALID_ARGUMENT, "interp_tile must be 0, 8 or 16");
+  if (cfg->leaf_kernel < PO_LEAF_AUTO || cfg->leaf_kernel > PO_LEAF_TCGEN05)
+    return fail(PO_ERR_INVALID_ARGUMENT, "unknown leaf kernel");
+  if (cfg->leaf_kernel != PO_LEAF_AUTO && (cfg->precision != PO_PREC_SPLIT_BF16 || d == 0))
+    return fail(PO_ERR_INVALID_ARGUMENT, "the leaf kernel choice applies to split-BF16 tree solves");
+  if (cfg->leaf_slots != 0 && (cfg->leaf_slots < 8 || cfg->leaf_slots > kLeafTcMaxSlots || cfg->leaf_slots % 8))
+    return fail(PO_ERR_INVALID_ARGUMENT, "leaf_slots must be 0 or a multiple of 8 up to 64");
   int dev = 0;
   PO_CUDA(cudaGetDevice(&dev));
   PO_TRY(init_device_attributes(dev));
@@ -554,6 +560,7 @@ struct SolvePlan {
   const SlotParams<double> *sp64_dev = nullptr;
   const int32_t *perm_out = nullptr;  // sorted position -> input index of the gradient
   bool leaf_tc = false;               // leaf sums on tcgen05 (po_leaf_tc.cu)
+  int leaf_group = kLeafTcMaxSlots;   // slots per pass of the tcgen05 leaf kernel
   int64_t leaf_chunks = 0;            // 16-point chunks over all leaves
 };
 
@@ -720,7 +727,9 @@ static po_status prepare_solve(po_ctx *c, const po_geometry *g, const po_illum *
   }
   // tcgen05 leaf sums when a wavelength has many patterns: the leaves' points
   // in chunks of 16 (bases computed on the host from the leaf ranges)
-  P.leaf_tc = cfg.precision == PO_PREC_SPLIT_BF16 && G >= kLeafTcMinSlots && P.nleaf > 0;
+  P.leaf_tc = cfg.precision == PO_PREC_SPLIT_BF16 && P.nleaf > 0 &&
+              (cfg.leaf_kernel == PO_LEAF_TCGEN05 || (cfg.leaf_kernel == PO_LEAF_AUTO && G >= kLeafTcMinSlots));
+  P.leaf_group = cfg.leaf_slots ? cfg.leaf_slots : kLeafTcMaxSlots;
   double leaf_tc_per_slot = 0;
   if (P.leaf_tc) {
     std::vector<int32_t> lb((size_t)P.nleaf + 1);
@@ -763,7 +772,8 @@ static po_status prepare_solve(po_ctx *c, const po_geometry *g, const po_illum *
     size_t bop = 0;
     int nl_max = 1;
     for (const SlotChunk &ch : P.chunks) {
-      bop = std::max(bop, (size_t)ch.nl * P.leaf_chunks * leaf_tc_col_tiles(ch.gc) * leaf_tc_block_bytes());
+      bop = std::max(bop, (size_t)ch.nl * P.leaf_chunks * leaf_tc_col_tiles(std::min(ch.gc, P.leaf_group)) *
+                              leaf_tc_block_bytes());
       nl_max = std::max(nl_max, ch.nl);
     }
     PO_TRY(c->leaf_bop.ensure(bop));
@@ -901,7 +911,7 @@ static po_status enqueue_solve(po_ctx *c, const SolvePlan &P, float *out_dev, co
                               P.leaf_chunks, c->leaf_ctr.as<double>(), P.nleaf, sp, ch.nl, ch.gc, 0, ch.gc,
                               c->dirs.as<float4>(), c->R[d] * c->Phi[d], c->leaf_bop.as<uint8_t>(), c->leaf_bop.bytes,
                               c->leaf_uop.as<float4>(), c->leaf_uop.bytes, c->levelA.as<float2>(), c->tc_err.as<int>(),
-                              st));
+                              st, P.leaf_group));
       else if (cfg.precision == PO_PREC_SPLIT_BF16)
         PO_TRY(launch_leaf_mma(P.gsc, P.tree.level[d].begin, c->leaf_ctr.as<double>(), P.nleaf, sp, ch.nl, ch.gc,
                                c->dirs.as<float4>(), c->R[d] * c->Phi[d], c->levelA.as<float2>(), st,
@@ -912,7 +922,7 @@ static po_status enqueue_solve(po_ctx *c, const SolvePlan &P, float *out_dev, co
         PO_TRY(launch_leaf(P.gsc, P.tree.level[d].begin, c->leaf_ctr.as<double>(), P.nleaf, sp, ch.nl, ch.gc,
                            c->dirs.as<float4>(), c->R[d] * c->Phi[d], c->levelA.as<float2>(), st));
       PO_TRY(rec(c->kev[1]));
-      T.n_leaf += P.nleaf <= 0 ? 0 : P.leaf_tc ? 2 * ((ch.gc + kLeafTcMaxSlots - 1) / kLeafTcMaxSlots) : (ch.gc + 3) / 4;
+      T.n_leaf += P.nleaf <= 0 ? 0 : P.leaf_tc ? 2 * ((ch.gc + P.leaf_group - 1) / P.leaf_group) : (ch.gc + 3) / 4;
       float2 *cur_lvl = c->levelA.as<float2>(), *nxt = c->levelB.as<float2>();
       for (int l = d - 1; l >= 0; --l) {
         const int64_t nc = P.tree.level[l + 1].count, np = P.tree.level[l].count;
