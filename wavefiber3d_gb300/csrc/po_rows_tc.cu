@@ -16,8 +16,8 @@
 //    (3 tcgen05.mma of 128 x ntn x 16) into one of two accumulators in tensor
 //    memory (one per row block parity) and commits the chunk's stage and,
 //    after the last chunk, the accumulator;
-//  * 4 converter warps: load the FP32 rows of each K chunk (16-byte loads, two
-//    chunks ahead),
+//  * 4 converter warps: load the FP32 rows of each K chunk (16-byte loads,
+//    three chunks ahead into a ring of registers),
 //    split them into bf16 hi + lo and store them in the core-matrix A layout
 //    of a 4-stage ring (padding rows of the output patterns and columns past
 //    Pc are zero);
@@ -54,6 +54,12 @@ struct RtWarps {
   static constexpr int threads = 32 * (ctl + 1);
 };
 constexpr int kRtStages = 4;
+// converter register buffers (chunks of 4 x 16 B per thread): 4 with one CTA
+// per SM, 3 where two CTAs of the narrow-tile form share the register file
+template <int EW>
+struct RtBufs {
+  static constexpr int n = EW == 8 ? 4 : 3;
+};
 constexpr int kRtAStage = 2 * 128 * 16 * 2;  // bf16 hi + lo of 128 rows x 16: 8 KB
 constexpr int kRtMaxSmem = 216 * 1024;
 
@@ -212,35 +218,40 @@ __global__ void __launch_bounds__(RtWarps<EW>::threads, 1) k_rows_tc(
         if (rowok[pass & 1] && k < Pc) v[pass] = __ldg((const float4 *)(src + srow[pass & 1] * (int64_t)Pc + k));
       }
     };
-    float4 v0[4], v1[4], v2[4];
-    load_chunk(0, v0);
-    load_chunk(1, v1);
+    // a ring of kRtBufs register buffers, statically indexed (the loop over a
+    // ring turn is unrolled): kRtBufs - 1 chunks are loading while one is
+    // converted, and no buffer is copied, so no load is waited for early
+    constexpr int kRtBufs = RtBufs<EW>::n;
+    float4 v[kRtBufs][4];
+#pragma unroll
+    for (int b = 0; b < kRtBufs - 1; ++b) load_chunk(b, v[b]);
     bool ok = true;
-    for (int64_t g = 0; g < n_chunks; ++g) {
-      load_chunk(g + 2, v2);
-      const int s = (int)(g % kRtStages);
-      if (g >= kRtStages && !mbar_wait(smem_addr(&aempty[s]), (uint32_t)(((g / kRtStages) - 1) & 1), abort_flag)) {
-        ok = false;
-        break;
-      }
-      uint8_t *st = sA + s * kRtAStage;
+    for (int64_t g0 = 0; g0 < n_chunks && ok; g0 += kRtBufs) {
 #pragma unroll
-      for (int pass = 0; pass < 4; ++pass) {
-        const int i = (ct >> 2) + 32 * (pass & 1), kk = 2 * ((ct & 3) + 4 * (pass >> 1));
-        uint32_t rh, rl, ih, il;
-        split_bf16x2(v0[pass].x, v0[pass].z, rh, rl);  // real parts of columns k, k + 1
-        split_bf16x2(v0[pass].y, v0[pass].w, ih, il);  // imaginary parts
-        *(uint32_t *)(st + a_off(2 * i, kk)) = rh;
-        *(uint32_t *)(st + 4096 + a_off(2 * i, kk)) = rl;
-        *(uint32_t *)(st + a_off(2 * i + 1, kk)) = ih;
-        *(uint32_t *)(st + 4096 + a_off(2 * i + 1, kk)) = il;
-      }
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      mbar_arrive(smem_addr(&afull[s]));
+      for (int b = 0; b < kRtBufs; ++b) {
+        const int64_t g = g0 + b;
+        if (g >= n_chunks) break;
+        load_chunk(g + kRtBufs - 1, v[(b + kRtBufs - 1) % kRtBufs]);
+        const int s = (int)(g % kRtStages);
+        if (g >= kRtStages &&
+            !mbar_wait(smem_addr(&aempty[s]), (uint32_t)(((g / kRtStages) - 1) & 1), abort_flag)) {
+          ok = false;
+          break;
+        }
+        uint8_t *st = sA + s * kRtAStage;
 #pragma unroll
-      for (int pass = 0; pass < 4; ++pass) {
-        v0[pass] = v1[pass];
-        v1[pass] = v2[pass];
+        for (int pass = 0; pass < 4; ++pass) {
+          const int i = (ct >> 2) + 32 * (pass & 1), kk = 2 * ((ct & 3) + 4 * (pass >> 1));
+          uint32_t rh, rl, ih, il;
+          split_bf16x2(v[b][pass].x, v[b][pass].z, rh, rl);  // real parts of columns k, k + 1
+          split_bf16x2(v[b][pass].y, v[b][pass].w, ih, il);  // imaginary parts
+          *(uint32_t *)(st + a_off(2 * i, kk)) = rh;
+          *(uint32_t *)(st + 4096 + a_off(2 * i, kk)) = rl;
+          *(uint32_t *)(st + a_off(2 * i + 1, kk)) = ih;
+          *(uint32_t *)(st + 4096 + a_off(2 * i + 1, kk)) = il;
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        mbar_arrive(smem_addr(&afull[s]));
       }
     }
     if (!ok) *abort_flag = 1;
