@@ -831,6 +831,32 @@ def run_batch(args, world, rank, local):
     batch.close()
     npts = sum(int(g.shape[1]) for g in samples)
     pd = float(npts) * N_THETA * N_PHI
+    # baselines on the first solves of the batch, scaled to the whole batch by
+    # point-direction terms: the plain FP64 direct sum on this GPU (B1, full
+    # grid) and the FP64 oracle on the host cores (B0, seeded directions)
+    k = min(args.batch_baseline_items, len(items))
+    b1_ms, b1_pd, b0_s, b0_pd = 0.0, 0.0, 0.0, 0.0
+    dirs = sample_directions(args.cpu_dirs)
+    for (cloud, radii, lam, th, ph), g in zip(items[:k], samples[:k]):
+        il = api.Illumination([lam], [th], [ph], api.PO_POL_TM, ETA, 1.0)
+        cfg = api.Config(0, [N_THETA], [N_PHI], [-1.1 * a for a in radii], [1.1 * a for a in radii],
+                         precision=api.PO_PREC_FP64)
+        with api.Solver(cfg) as s64:
+            out = torch.empty(s64.out_shape(il), dtype=torch.float32, device=dev)
+            s64.solve(tuple(g[q] for q in range(7)), il, out=out)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            s64.solve(tuple(g[q] for q in range(7)), il, out=out, report=False)
+            e1.record(st)
+            torch.cuda.synchronize()
+        b1_ms += e0.elapsed_time(e1)
+        b1_pd += float(g.shape[1]) * N_THETA * N_PHI
+        il_o = oracle.make_illum(lam, th, ph, "M", ETA, 1.0)
+        t0 = time.perf_counter()
+        oracle.solve_sampled_f64(cloud.soa().astype(np.float64), il_o, N_THETA, N_PHI, dirs)
+        b0_s += time.perf_counter() - t0
+        b0_pd += float(g.shape[1]) * dirs.size
+    b1_rate, b0_rate = b1_pd / (b1_ms * 1e-3) / 1e9, b0_pd / b0_s / 1e9
     depth_hist = {d: sum(1 for c in choices if c["depth"] == d) for d in range(7)}
     return {
         "metric": "Gpoint-dirs/s (equivalent depth-0 terms) of a batch of independent solves in one CUDA graph",
@@ -852,6 +878,13 @@ def run_batch(args, world, rank, local):
         "per_solve_rel_l2_vs_fp64": {"max": max(errs), "median": float(np.median(errs)),
                                      "sample": f"{args.batch_dirs} seeded directions per solve, FP64 oracle"},
         "oracle_s": oracle_s,
+        "plain_fp64_gpu": {"value": b1_rate, "unit": "Gpoint-dirs/s", "ms_per_step_scaled": pd / b1_rate / 1e6,
+                           "sample": f"FP64 depth-0 sum (k_direct_f64) of the first {k} solves on the full grid, "
+                                     "scaled by point-direction terms"},
+        "speedup_vs_plain_fp64_gpu": (pd / b1_rate / 1e6) / ms_graph,
+        "cpu_baseline": {"value": b0_rate, "unit": "Gpoint-dirs/s", "cores": oracle.num_threads(), "kind": "port",
+                         "ms_per_step_scaled": pd / b0_rate / 1e6,
+                         "sample": f"FP64 oracle direct sum of the first {k} solves on {dirs.size} seeded directions"},
         "clocks": clk,
     }
 
@@ -1070,6 +1103,8 @@ def main():
     ap.add_argument("--batch-items", type=int, default=256, help="independent solves of the batch workload")
     ap.add_argument("--batch-streams", type=int, default=16, help="concurrent graph branches of the batch")
     ap.add_argument("--batch-dirs", type=int, default=64, help="FP64 check directions per batch solve")
+    ap.add_argument("--batch-baseline-items", type=int, default=4,
+                    help="solves of the batch timed for its FP64 GPU and host baselines")
     ap.add_argument("--tune-cache", default=None, help="JSON file of the autotuner's choices (read and written)")
     args = ap.parse_args()
     if args.precision is None:

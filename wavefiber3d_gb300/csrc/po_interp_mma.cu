@@ -665,6 +665,91 @@ __global__ void __launch_bounds__(128, 6) k_interp_rows_mma(const float2 *__rest
     rows_block<PACK, false>(blk, 0, nrows, src, dst_, Rc, Rc2, Pc, Pp, KS, B, ng, nq, npad);
 }
 
+// Packed row pass (k_theta_warp's operand) for narrow child grids, Pc <= 32
+// (two k-steps) and at most NG n-tiles of 4 mirror pairs: the same products
+// and output as rows_block<1, false>, but each warp keeps the whole input of
+// its next block of 8 rows in flight (both k-steps, statically indexed
+// ping-pong registers) while the current block multiplies, so that a warp has
+// about 2 KB of loads outstanding instead of one k-step.
+template <int NG>
+__global__ void __launch_bounds__(128, 5) k_rows_mma_narrow(const float2 *__restrict__ src,
+                                                                          uint4 *__restrict__ dst, int64_t nrows,
+                                                                          int Rc, int Pc, int Pp,
+                                                                          const uint4 *__restrict__ Bm) {
+  constexpr int KS = 2;
+  __shared__ uint4 bsm[NG * KS * 32];
+  const int half = Pp / 2, nq = (half + 3) / 4;
+  for (int e = threadIdx.x; e < NG * KS * 32; e += blockDim.x)
+    bsm[e] = e < nq * KS * 32 ? Bm[e] : make_uint4(0u, 0u, 0u, 0u);
+  __syncthreads();
+  const int lane = threadIdx.x & 31, g = lane >> 2, tq = lane & 3;
+  const bool odd = g & 1;
+  const int Rc2 = Rc + (Rc & 1);
+  const int64_t nblk = (nrows + 7) / 8, stride = (int64_t)gridDim.x * 4;
+  auto load = [&](int64_t blk, float2 (&v)[KS][4]) {
+    const int64_t r = blk * 8 + g;
+    const int64_t pattern = r / Rc2;
+    const int t = (int)(r - pattern * Rc2);
+    const bool ok = blk < nblk && r < nrows && t < Rc;
+    const float2 *in = src + (ok ? pattern * Rc + t : 0) * (int64_t)Pc;
+#pragma unroll
+    for (int ks = 0; ks < KS; ++ks)
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int k = ks * 16 + 2 * tq + (u & 1) + (u >> 1) * 8;
+        v[ks][u] = (ok && k < Pc) ? __ldg(in + k) : make_float2(0.f, 0.f);
+      }
+  };
+  auto block = [&](int64_t blk, const float2 (&v)[KS][4]) {
+    float acc[NG][4];
+#pragma unroll
+    for (int q = 0; q < NG; ++q) acc[q][0] = acc[q][1] = acc[q][2] = acc[q][3] = 0.f;
+#pragma unroll
+    for (int ks = 0; ks < KS; ++ks) {
+      uint32_t ahi[4], alo[4];
+      split_bf16x2(v[ks][0].x, v[ks][1].x, ahi[0], alo[0]);  // row g (real parts), k0, k0+1
+      split_bf16x2(v[ks][0].y, v[ks][1].y, ahi[1], alo[1]);  // row g+8 (imaginary parts)
+      split_bf16x2(v[ks][2].x, v[ks][3].x, ahi[2], alo[2]);  // row g, k0+8, k0+9
+      split_bf16x2(v[ks][2].y, v[ks][3].y, ahi[3], alo[3]);
+#pragma unroll
+      for (int q = 0; q < NG; ++q) {
+        const uint4 bv = bsm[(q * KS + ks) * 32 + lane];  // zero for the n-tiles past nq
+        const uint32_t bhi[2] = {bv.x, bv.y}, blo[2] = {bv.z, bv.w};
+        mma_bf16(acc[q], ahi, bhi);
+        mma_bf16(acc[q], ahi, blo);
+        mma_bf16(acc[q], alo, bhi);
+      }
+    }
+    const int64_t r = blk * 8 + g, pair_row = r >> 1;
+    const bool rok = r < nrows;
+#pragma unroll
+    for (int q = 0; q < NG; ++q) {
+      const float sr = acc[q][0] + acc[q][1], dr = acc[q][0] - acc[q][1];
+      const float si = acc[q][2] + acc[q][3], di = acc[q][2] - acc[q][3];
+      const float xs = __shfl_xor_sync(0xffffffffu, odd ? sr : si, 4);
+      const float xd = __shfl_xor_sync(0xffffffffu, odd ? dr : di, 4);
+      const float s0 = odd ? xs : sr, s1 = odd ? si : xs;
+      const float d0 = odd ? xd : dr, d1 = odd ? di : xd;
+      const int j = q * 4 + tq;
+      uint32_t sh, sl, dh, dl;
+      split_bf16x2(s0, s1, sh, sl);
+      split_bf16x2(d0, d1, dh, dl);
+      if (rok && j < half) dst[(pair_row * half + j) * 2 + (odd ? 1 : 0)] = make_uint4(sh, sl, dh, dl);
+    }
+  };
+  // every lane of a warp walks the same blocks (the epilogue shuffles need the whole warp)
+  int64_t blk = (int64_t)blockIdx.x * 4 + (threadIdx.x >> 5);
+  float2 va[KS][4], vb[KS][4];
+  load(blk, va);
+  for (; blk < nblk; blk += 2 * stride) {
+    load(blk + stride, vb);
+    block(blk, va);
+    if (blk + stride >= nblk) break;
+    load(blk + 2 * stride, va);
+    block(blk + stride, vb);
+  }
+}
+
 static po_status launch_rows(int pack, const float2 *src, void *dst, int64_t nrows, int Rc, int Pc, int Pp, int Kp,
                              const uint32_t *Bm, int sm_count, cudaStream_t st, int Rr = 0, int npad = 0) {
   if (nrows <= 0) return PO_OK;
@@ -679,7 +764,15 @@ static po_status launch_rows(int pack, const float2 *src, void *dst, int64_t nro
   if (blocks > cap) blocks = cap;
   if (ngroups > 65535) return fail(PO_ERR_UNSUPPORTED, "angular grid too large for the row pass");
   dim3 grid((unsigned)blocks, (unsigned)ngroups);
-  if (pack == 2)
+  if (pack == 1 && Kp == 32 && NTt <= 8) {
+    // narrow child grid: whole blocks in flight (k_rows_mma_narrow), grid of
+    // resident CTAs (5 per SM), each warp walking many blocks
+    const int64_t nb = std::min<int64_t>(((nrows + 7) / 8 + 3) / 4, (int64_t)sm_count * 5);
+    if (NTt <= 4)
+      k_rows_mma_narrow<4><<<(unsigned)nb, 128, 0, st>>>(src, (uint4 *)dst, nrows, Rc, Pc, Pp, (const uint4 *)Bm);
+    else
+      k_rows_mma_narrow<8><<<(unsigned)nb, 128, 0, st>>>(src, (uint4 *)dst, nrows, Rc, Pc, Pp, (const uint4 *)Bm);
+  } else if (pack == 2)
     k_interp_rows_mma<2><<<grid, 128, smem, st>>>(src, dst, nrows, Rc, Pc, Pp, Kp, (const uint4 *)Bm,
                                                   b_smem ? 1 : 0, Rr, npad);
   else if (pack == 1)
@@ -706,7 +799,8 @@ po_status launch_interp_rows_packed(const float2 *src, uint4 *dst, int64_t n_pat
 
 po_status launch_interp_rows_core(const float2 *src, uint8_t *dst, int64_t n_patterns, int Rc, int Rr, int npad,
                                   int Pc, int Pp, int Kp, const uint32_t *Bm, int sm_count, cudaStream_t st) {
-  if (Rr % 16 || Rr < Rc || npad % 8 || npad < Pp) return fail(PO_ERR_INTERNAL, "core-matrix row pass padding");
+  if (Rr % 16 || Rr < Rc || npad % 8 || npad < 6 * Pp || n_patterns % 6)
+    return fail(PO_ERR_INTERNAL, "core-matrix row pass padding");
   return launch_rows(2, src, dst, n_patterns * (int64_t)Rr, Rc, Pc, Pp, Kp, Bm, sm_count, st, Rr, npad);
 }
 

@@ -22,10 +22,11 @@ namespace wavepo {
 // Lane g and lane g^1 (4 apart) hold the two rows of a pair; the even lane
 // stores the real parts, the odd lane the imaginary parts.
 // PACK == 2 (forward pass feeding the tcgen05 theta pass, po_theta_tc.cu): the
-// same sums and differences as four bf16 matrices per pattern (S hi, S lo,
-// D hi, D lo) in chunks of 16 rows, [Rr/16][matrix][npad/8][2][8][8]: core
-// matrices of 8 columns x 8 rows (16 B per column row); element (column
-// n = 2j + part, row t) of matrix m at byte
+// same sums and differences as four bf16 matrices (S hi, S lo, D hi, D lo) per
+// child, whose six component patterns share one column space, in chunks of 16
+// rows, [Rr/16][matrix][npad/8][2][8][8]: core matrices of 8 columns x 8 rows
+// (16 B per column row); element (column n = comp Pp + 2j + part, row t) of
+// matrix m at byte
 // (t/16) 128 npad + m 32 npad + (n/8) 256 + ((t/8)%2) 128 + (n%8) 16 + (t%8) 2.
 // Patterns have Rr rows (rows Rc .. Rr-1 are zero); the 32 lanes of a warp
 // store one whole core matrix per matrix and n-tile.
@@ -103,7 +104,10 @@ __device__ __forceinline__ void rows_block(int64_t blk, int64_t row_lo, int64_t 
     const bool odd = g & 1;
     const int64_t pattern = r / Rc2;
     const int t0 = (int)(r - pattern * Rc2) & ~1;  // the pair's first row
-    uint8_t *base = (uint8_t *)dst_ + (size_t)pattern * 4 * npad * Rc2 * 2;
+    // the six component patterns of a child share one column space
+    const int64_t group = pattern / 6;
+    const int col0 = (int)(pattern - group * 6) * Pp;
+    uint8_t *base = (uint8_t *)dst_ + (size_t)group * 8 * npad * Rc2;
     const size_t mat = (size_t)npad * 32;  // matrix stride inside a 16-row chunk
 #pragma unroll
     for (int q = 0; q < kRowNG; ++q) {
@@ -119,7 +123,7 @@ __device__ __forceinline__ void rows_block(int64_t blk, int64_t row_lo, int64_t 
       split_bf16x2(s0, s1, sh, sl);
       split_bf16x2(d0, d1, dh, dl);
       if (rok && j < half) {
-        const int n = 2 * j + (odd ? 1 : 0);
+        const int n = col0 + 2 * j + (odd ? 1 : 0);
         const size_t off = (size_t)(t0 >> 4) * 128 * npad + (size_t)(n >> 3) * 256 + ((t0 >> 3) & 1) * 128 +
                            (n & 7) * 16 + (t0 & 7) * 2;
         *(uint32_t *)(base + off) = sh;

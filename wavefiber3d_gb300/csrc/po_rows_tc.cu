@@ -17,7 +17,8 @@
 //    memory (one per row block parity) and commits the chunk's stage and,
 //    after the last chunk, the accumulator;
 //  * 4 converter warps: load the FP32 rows of each K chunk (16-byte loads,
-//    three chunks ahead into a ring of registers),
+//    one to three chunks ahead into a statically indexed ring of registers,
+//    by the length of the K loop),
 //    split them into bf16 hi + lo and store them in the core-matrix A layout
 //    of a 4-stage ring (padding rows of the output patterns and columns past
 //    Pc are zero);
@@ -54,12 +55,6 @@ struct RtWarps {
   static constexpr int threads = 32 * (ctl + 1);
 };
 constexpr int kRtStages = 4;
-// converter register buffers (chunks of 4 x 16 B per thread): 4 with one CTA
-// per SM, 3 where two CTAs of the narrow-tile form share the register file
-template <int EW>
-struct RtBufs {
-  static constexpr int n = EW == 8 ? 4 : 3;
-};
 constexpr int kRtAStage = 2 * 128 * 16 * 2;  // bf16 hi + lo of 128 rows x 16: 8 KB
 constexpr int kRtMaxSmem = 216 * 1024;
 
@@ -85,7 +80,8 @@ bool rows_tc_plan(int Pc, int Pp, int &ntn, int &n_nt) {
   return false;
 }
 
-template <int EW>
+// NB: converter register buffers (chunks of 4 x 16 B per thread)
+template <int EW, int NB>
 __global__ void __launch_bounds__(RtWarps<EW>::threads, 1) k_rows_tc(
     const float2 *__restrict__ src, uint8_t *__restrict__ dst, int64_t n_rows_out, int Rc, int Rr, int Pc, int KC,
     int half, int npad, int ntn, int n_nt, const uint8_t *__restrict__ Bt, uint32_t tcols, int *__restrict__ err) {
@@ -221,7 +217,7 @@ __global__ void __launch_bounds__(RtWarps<EW>::threads, 1) k_rows_tc(
     // a ring of kRtBufs register buffers, statically indexed (the loop over a
     // ring turn is unrolled): kRtBufs - 1 chunks are loading while one is
     // converted, and no buffer is copied, so no load is waited for early
-    constexpr int kRtBufs = RtBufs<EW>::n;
+    constexpr int kRtBufs = NB;
     float4 v[kRtBufs][4];
 #pragma unroll
     for (int b = 0; b < kRtBufs - 1; ++b) load_chunk(b, v[b]);
@@ -269,7 +265,11 @@ __global__ void __launch_bounds__(RtWarps<EW>::threads, 1) k_rows_tc(
       const bool rok = r < n_rows_out;
       const int64_t pattern = rok ? r / Rr : 0;
       const int t = rok ? (int)(r - pattern * Rr) : 0;
-      uint8_t *pb = dst + pattern * (int64_t)8 * npad * Rr + (int64_t)(t >> 4) * 128 * npad + ((t >> 3) & 1) * 128 +
+      // the six component patterns of a child share one column space: column
+      // n' = comp 2 half + n of child group pattern / 6
+      const int64_t group = pattern / 6;
+      const int col0 = (int)(pattern - group * 6) * 2 * half;
+      uint8_t *pb = dst + group * (int64_t)8 * npad * Rr + (int64_t)(t >> 4) * 128 * npad + ((t >> 3) & 1) * 128 +
                     (t & 7) * 2;
       const int64_t mstride = (int64_t)32 * npad;  // matrix stride inside a 16-row chunk
       const uint32_t ta = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(buf * ntn);
@@ -283,7 +283,7 @@ __global__ void __launch_bounds__(RtWarps<EW>::threads, 1) k_rows_tc(
           const __nv_bfloat16 sh = __float2bfloat16_rn(sv), dh = __float2bfloat16_rn(dv);
           const __nv_bfloat16 sl = __float2bfloat16_rn(sv - __bfloat162float(sh));
           const __nv_bfloat16 dl = __float2bfloat16_rn(dv - __bfloat162float(dh));
-          const int n = 2 * j + part;
+          const int n = col0 + 2 * j + part;
           uint8_t *e = pb + (n >> 3) * 256 + (n & 7) * 16;
           *(__nv_bfloat16 *)e = sh;
           *(__nv_bfloat16 *)(e + mstride) = sl;
@@ -328,15 +328,21 @@ __global__ void __launch_bounds__(RtWarps<EW>::threads, 1) k_rows_tc(
   }
 }
 
+template <int EW, int NB>
+static po_status rows_tc_attributes() {
+  PO_CUDA(cudaFuncSetAttribute(k_rows_tc<EW, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize, kRtMaxSmem));
+  PO_CUDA(cudaFuncSetAttribute(k_rows_tc<EW, NB>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                               (int)cudaSharedmemCarveoutMaxShared));
+  return PO_OK;
+}
+
 po_status init_rows_tc_attributes() {
   // the whole shared-memory carveout, so that the occupancy query (and the
   // launch) can place two narrow-tile CTAs on an SM
-  PO_CUDA(cudaFuncSetAttribute(k_rows_tc<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, kRtMaxSmem));
-  PO_CUDA(cudaFuncSetAttribute(k_rows_tc<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, kRtMaxSmem));
-  PO_CUDA(cudaFuncSetAttribute(k_rows_tc<4>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                               (int)cudaSharedmemCarveoutMaxShared));
-  PO_CUDA(cudaFuncSetAttribute(k_rows_tc<8>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                               (int)cudaSharedmemCarveoutMaxShared));
+  PO_TRY((rows_tc_attributes<4, 2>()));
+  PO_TRY((rows_tc_attributes<4, 3>()));
+  PO_TRY((rows_tc_attributes<8, 3>()));
+  PO_TRY((rows_tc_attributes<8, 4>()));
   return PO_OK;
 }
 
@@ -346,9 +352,9 @@ po_status launch_rows_tc(const float2 *src, uint8_t *dst, size_t dst_bytes, int6
   if (n_patterns <= 0) return PO_OK;
   const int KC = (Pc + 15) / 16;
   const int64_t n_rows_out = n_patterns * (int64_t)Rr;
-  if ((Pc & 1) || (Pp & 1) || Rr % 16 || Rr < Rc || npad % 8 || npad < Pp || ntn % 16 || ntn > 256 || n_nt < 1 ||
-      (int64_t)n_nt * (ntn / 2) < Pp / 2 || (size_t)n_nt * KC * 64 * ntn > bt_bytes ||
-      (size_t)n_patterns * 8 * npad * Rr > dst_bytes)
+  if ((Pc & 1) || (Pp & 1) || Rr % 16 || Rr < Rc || npad % 8 || npad < 6 * Pp || n_patterns % 6 || ntn % 16 ||
+      ntn > 256 || n_nt < 1 || (int64_t)n_nt * (ntn / 2) < Pp / 2 || (size_t)n_nt * KC * 64 * ntn > bt_bytes ||
+      (size_t)(n_patterns / 6) * 8 * npad * Rr > dst_bytes)
     return fail(PO_ERR_INTERNAL, "tcgen05 row pass: tiling or buffer sizes");
   const int smem = rows_tc_smem(KC, ntn);
   if (smem > kRtMaxSmem) return fail(PO_ERR_INTERNAL, "tcgen05 row pass: shared memory");
@@ -358,8 +364,16 @@ po_status launch_rows_tc(const float2 *src, uint8_t *dst, size_t dst_bytes, int6
   // units of 8 per thread), shared memory (+1 KB reserved per CTA) and tensor
   // memory
   const bool wide = ntn > 128;
+  // converter buffers: deep prefetch pays on long K loops (fiber root, 34
+  // chunks: 57.8 -> 47.8 ms per wavelength with 3 buffers instead of 2) and
+  // costs on short ones, where the pass is bound by DRAM writes (fiber level
+  // 4, 3 chunks: 20.4 ms with 2 buffers, 28.0 with 3)
+  const int nb = KC >= 8 ? (wide ? 4 : 3) : (wide ? 3 : 2);
   cudaFuncAttributes fa;
-  PO_CUDA(wide ? cudaFuncGetAttributes(&fa, k_rows_tc<8>) : cudaFuncGetAttributes(&fa, k_rows_tc<4>));
+  if (wide)
+    PO_CUDA(nb == 4 ? cudaFuncGetAttributes(&fa, k_rows_tc<8, 4>) : cudaFuncGetAttributes(&fa, k_rows_tc<8, 3>));
+  else
+    PO_CUDA(nb == 3 ? cudaFuncGetAttributes(&fa, k_rows_tc<4, 3>) : cudaFuncGetAttributes(&fa, k_rows_tc<4, 2>));
   const int threads = wide ? RtWarps<8>::threads : RtWarps<4>::threads;
   const int reg_limit = 65536 / (std::max(1, (fa.numRegs + 7) / 8 * 8) * threads);
   const int smem_limit = 228 * 1024 / (smem + 1024);
@@ -368,12 +382,15 @@ po_status launch_rows_tc(const float2 *src, uint8_t *dst, size_t dst_bytes, int6
   const int64_t ctas_per_tile = std::min<int64_t>(n_rb, std::max(1, sm_count * per_sm / n_nt));
   const int64_t grid = ctas_per_tile * n_nt;
   if (grid > 2147483647LL) return fail(PO_ERR_UNSUPPORTED, "row pass grid");
-  if (wide)
-    k_rows_tc<8><<<(unsigned)grid, RtWarps<8>::threads, smem, st>>>(src, dst, n_rows_out, Rc, Rr, Pc, KC, Pp / 2,
-                                                                    npad, ntn, n_nt, Bt, tcols, err);
-  else
-    k_rows_tc<4><<<(unsigned)grid, RtWarps<4>::threads, smem, st>>>(src, dst, n_rows_out, Rc, Rr, Pc, KC, Pp / 2,
-                                                                    npad, ntn, n_nt, Bt, tcols, err);
+#define PO_RT_LAUNCH(E, N)                                                                                    \
+  k_rows_tc<E, N><<<(unsigned)grid, RtWarps<E>::threads, smem, st>>>(src, dst, n_rows_out, Rc, Rr, Pc, KC, Pp / 2, \
+                                                                     npad, ntn, n_nt, Bt, tcols, err)
+  if (wide) {
+    if (nb == 4) PO_RT_LAUNCH(8, 4); else PO_RT_LAUNCH(8, 3);
+  } else {
+    if (nb == 3) PO_RT_LAUNCH(4, 3); else PO_RT_LAUNCH(4, 2);
+  }
+#undef PO_RT_LAUNCH
   count_launch();
   PO_CUDA(cudaGetLastError());
   return PO_OK;

@@ -44,7 +44,7 @@ struct Scratch {
 po_status theta_case(bool withhold, int *err, cudaStream_t st) {
   Scratch S;
   const int phi = 128, Kr = 16, Rp = 128;
-  const size_t mid_bytes = (size_t)6 * 8 * theta_tc_npad(phi) * Kr, atc_bytes = theta_tc_bytes(Rp, Kr);
+  const size_t mid_bytes = (size_t)8 * theta_tc_npad(phi) * Kr, atc_bytes = theta_tc_bytes(Rp, Kr);
   void *mid, *atc, *trans, *parent, *child;
   PO_TRY(S.alloc(&mid, mid_bytes));
   PO_TRY(S.alloc(&atc, atc_bytes));

@@ -760,11 +760,12 @@ static po_status prepare_solve(po_ctx *c, const po_geometry *g, const po_illum *
   for (int l = 0; l <= d; ++l)
     lvl_max = std::max(lvl_max, (size_t)P.tree.level[l].count * 6 * (size_t)c->R[l] * c->Phi[l]);
   for (int l = 0; l < d; ++l) {
-    // float2 words per slot: R + 1 rows x Phi (packed pairs), or 4 bf16 matrices of
-    // tc_kr x npad (core matrices of the tcgen05 pass) = tc_kr x npad float2
+    // float2 words per slot and child: 6 components x R + 1 rows x Phi (packed
+    // pairs), or 4 bf16 matrices of tc_kr x npad (core matrices of the tcgen05
+    // pass, the six components in one column space) = tc_kr x npad float2
     const size_t per = c->tc_level[l] ? (size_t)c->tc_kr[l] * theta_tc_npad(c->Phi[l])
-                                      : (size_t)(c->R[l + 1] + 1) * c->Phi[l];
-    mid_max = std::max(mid_max, (size_t)P.tree.level[l + 1].count * 6 * per);
+                                      : (size_t)6 * (c->R[l + 1] + 1) * c->Phi[l];
+    mid_max = std::max(mid_max, (size_t)P.tree.level[l + 1].count * per);
   }
   P.chunks = plan_chunks(L, G, chunk_slot_count(budget, 8.0 * (2.0 * lvl_max + mid_max) + leaf_tc_per_slot, S));
   const int ns_max = P.chunks.front().ns;

@@ -7,9 +7,12 @@
 //   U = A_plus S,  V = A_minus D,  Y_j = U + V,  Y_j' = U - V,
 // rotated by the child's translation phasor and summed over the children.
 //
-// One CTA owns one (slot, parent, component), kTcPairs column pairs (N = 128
-// real columns of S and D) and one 128-row tile of the parent, and runs as
-// three roles:
+// The six component patterns of a child share one column space (packed pair
+// P = comp Phi/2 + j, real columns 2 P and 2 P + 1), so that a level's columns
+// are padded to whole chunks once per child instead of once per component.
+// One CTA owns one (slot, parent), kTcPairs packed column pairs (N = 128 real
+// columns of S and D) and one 128-row tile of the parent, and runs as three
+// roles:
 //  * copy warp (one thread): streams K chunks of 16 child rows -- the chunk of
 //    the four split theta matrices (A_plus hi, lo, A_minus hi, lo; 16 KB) and
 //    of the child's four split operands (S hi, lo, D hi, lo; 16 KB) -- with
@@ -37,9 +40,10 @@
 // a chunk of one matrix is [rows / 8][2][8][8] (row block, k8 block, row,
 // k), i.e. leading-dimension offset 128 B, stride offset 256 B.  The theta
 // matrices are stored as [tile][chunk][matrix][128 / 8][2][8][8]
-// (build_theta_tc); the row pass writes each child pattern as
-// [chunk][matrix][npad / 8][2][8][8] (launch_interp_rows_core), so that one
-// CTA's share of a chunk is one contiguous 4-KB run per matrix.
+// (build_theta_tc); the row pass writes each child's six packed component
+// patterns as [chunk][matrix][npad / 8][2][8][8] (launch_rows_tc,
+// launch_interp_rows_core), so that one CTA's share of a chunk is one
+// contiguous 4-KB run per matrix.
 //
 // Every wait is bounded in time: on a timeout the kernel records error word 1
 // and every role stops (`withhold`, a self-test switch, leaves the first
@@ -131,7 +135,7 @@ void build_theta_tc(const std::vector<double> &Mplus, const std::vector<double> 
       }
 }
 
-// grid.x = task * MT + tile (task = (slot, parent, component, column chunk)), kTcThreads threads
+// grid.x = task * MT + tile (task = (slot, parent, packed column chunk)), kTcThreads threads
 __global__ void __launch_bounds__(kTcThreads, 1) k_theta_tc(
     const uint8_t *__restrict__ mid, float2 *__restrict__ parent, const int32_t *__restrict__ child_table,
     int64_t n_parent, int64_t n_child, int phi, int Kr, int Npad, int Rp, const uint8_t *__restrict__ Atc,
@@ -156,12 +160,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_theta_tc(
   const int64_t task = blockIdx.x / MT;
   if (task >= n_task) return;
   const int nc = (int)(task % n_nc);
-  int64_t rest = task / n_nc;
-  const int comp = (int)(rest % 6);
-  rest /= 6;
+  const int64_t rest = task / n_nc;
   const int64_t p = rest % n_parent;
   const int slot = (int)(rest / n_parent), lam = slot / G;
-  const int span = phi / 2;
+  const int span = phi / 2, npairs = 6 * span;  // packed pairs of one child
 
   if (tid < 8) s_child[tid] = child_table[p * 8 + tid];
   if (tid == 0) {
@@ -190,7 +192,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_theta_tc(
   for (int o = 0; o < 8; ++o)
     if (s_child[o] >= 0) kids[nkids++] = o;
   const int nsteps = nkids * KC;
-  const size_t pat = (size_t)8 * Npad * Kr;  // bytes of one child pattern component (4 matrices)
+  const size_t pat = (size_t)8 * Npad * Kr;  // bytes of one child's six packed patterns (4 matrices)
 
   if (warp == kTcCopyWarp) {
     // ---- copy role ----
@@ -201,14 +203,14 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_theta_tc(
       bool ok = (size_t)(mtile + 1) * Kr * 1024 <= atc_bytes;
       for (int i = 0; i < nkids; ++i) {
         const int64_t ch = s_child[kids[i]];
-        ok = ok && ch < n_child && ((((size_t)slot * n_child + ch) * 6 + comp) + 1) * pat <= mid_bytes;
+        ok = ok && ch < n_child && (((size_t)slot * n_child + ch) + 1) * pat <= mid_bytes;
       }
       if (!ok) {
         atomicExch(err, 2);
         *abort_flag = 1;
       }
       const uint8_t *abase = Atc + (size_t)mtile * Kr * 1024;
-      const size_t comp_off = (size_t)nc * (kTcN / 8) * 256;
+      const size_t col_off = (size_t)nc * (kTcN / 8) * 256;
       constexpr uint32_t bmat = kTcN / 8 * 256;  // bytes of one matrix's share of a chunk
       for (int t = 0; t < nsteps && ok; ++t) {
         const int b = t % NST, ci = t / KC, kc = t % KC;
@@ -220,8 +222,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_theta_tc(
         const uint32_t fb = smem_addr(&full[b]);
         mbar_expect_tx(fb, kAStage + 4 * bmat);
         bulk_copy(smem_addr(sA + b * kAStage), abase + (size_t)kc * kAStage, kAStage, fb);
-        const uint8_t *cb = mid + (((size_t)slot * n_child + s_child[kids[ci]]) * 6 + comp) * pat +
-                            (size_t)kc * 128 * Npad + comp_off;
+        const uint8_t *cb = mid + ((size_t)slot * n_child + s_child[kids[ci]]) * pat + (size_t)kc * 128 * Npad +
+                            col_off;
 #pragma unroll
         for (int m = 0; m < 4; ++m)
           bulk_copy(smem_addr(sB + b * kBStage + m * bmat), cb + (size_t)m * 32 * Npad, bmat, fb);
@@ -293,7 +295,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_theta_tc(
       // and 16 rows, loaded 8 at a time
       const float4 *tr = trans + (int64_t)lam * Rp * phi;
       const int pl = tid & (kTcPairs - 1);
-      const int jq = nc * kTcPairs + pl < span ? nc * kTcPairs + pl : span - 1;
+      const int pp = nc * kTcPairs + pl < npairs ? nc * kTcPairs + pl : npairs - 1;
+      const int jq = pp % span;  // the pair's column within its component
 #pragma unroll
       for (int half = 0; half < 2; ++half) {
         float4 v[8];
@@ -377,16 +380,25 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_theta_tc(
         sO[rl * kTcLd + kTcPairs + 16 * wg + q] = make_float2(acc[q][1][0], acc[q][1][1]);
       }
       asm volatile("bar.sync 1, %0;" ::"r"(kTcEpiWarps * 32));
-      // warp w stores rows w, w + 16, ...: 64 consecutive pairs of j, then of j'
-      float2 *out = parent + (((int64_t)slot * n_parent + p) * 6 + comp) * (int64_t)Rp * phi;
+      // warp w stores rows w, w + 16, ...: 64 consecutive packed pairs of j,
+      // then of j' (a chunk's pairs may belong to several components)
+      float2 *out = parent + ((int64_t)slot * n_parent + p) * 6 * (int64_t)Rp * phi;
+      int64_t pofs[2];  // per lane half k & 1: component offset + column of the pair
+      bool pok[2];
+#pragma unroll
+      for (int k = 0; k < 2; ++k) {
+        const int pp = nc * kTcPairs + 32 * k + lane, comp = pp / span;
+        pok[k] = pp < npairs;
+        pofs[k] = (int64_t)comp * Rp * phi + (pp - comp * span);
+      }
       for (int row = warp; row < 128; row += kTcEpiWarps) {
         const int rg = mtile * 128 + row;
         if (rg >= Rp) break;
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
-          const int pair = 32 * (k & 1) + lane, jq = nc * kTcPairs + pair;
-          if (jq < span) out[(int64_t)rg * phi + jq + (k >> 1) * span] = sO[row * kTcLd + (k >> 1) * kTcPairs + pair];
-        }
+        for (int k = 0; k < 4; ++k)
+          if (pok[k & 1])
+            out[pofs[k & 1] + (int64_t)rg * phi + (k >> 1) * span] = sO[row * kTcLd + (k >> 1) * kTcPairs +
+                                                                         32 * (k & 1) + lane];
       }
     }
   }
@@ -403,9 +415,10 @@ po_status init_theta_tc_attributes() {
   return PO_OK;
 }
 
-// Columns of the core-matrix child operands: 2 x Phi/2 real columns rounded up
-// to whole column chunks of the CTA.
-int theta_tc_npad(int phi) { return (phi + kTcN - 1) / kTcN * kTcN; }
+// Columns of the core-matrix child operands: the six packed component patterns
+// of a child (6 x 2 x Phi/2 real columns) rounded up to whole column chunks of
+// the CTA.
+int theta_tc_npad(int phi) { return (6 * phi + kTcN - 1) / kTcN * kTcN; }
 
 po_status launch_theta_tc(const uint8_t *mid, float2 *parent, const int32_t *child_table, int64_t n_parent,
                           int64_t n_child, int phi, int Kr, int Rp, const uint8_t *Atc, const float4 *trans,
@@ -413,8 +426,8 @@ po_status launch_theta_tc(const uint8_t *mid, float2 *parent, const int32_t *chi
                           int withhold) {
   if (n_parent <= 0 || n_slots <= 0) return PO_OK;
   if (phi % 2 || Kr % kTcKC || Kr <= 0) return fail(PO_ERR_INTERNAL, "tcgen05 theta pass: grid");
-  const int MT = (Rp + 127) / 128, n_nc = (phi / 2 + kTcPairs - 1) / kTcPairs;
-  const int64_t n_task = (int64_t)n_slots * n_parent * 6 * n_nc;
+  const int MT = (Rp + 127) / 128, n_nc = (6 * (phi / 2) + kTcPairs - 1) / kTcPairs;
+  const int64_t n_task = (int64_t)n_slots * n_parent * n_nc;
   const int64_t gx = n_task * MT;
   if (gx > 2147483647LL) return fail(PO_ERR_UNSUPPORTED, "too many nodes for one launch");
   k_theta_tc<<<(unsigned)gx, kTcThreads, TcPlan::smem, st>>>(mid, parent, child_table, n_parent, n_child, phi, Kr,
