@@ -314,7 +314,15 @@ po_status po_create(po_ctx **out, const po_config *cfg) {
       lvl_ph[l] = smooth_at_least(lvl_ph[l], true);
     }
   }
-  if (d >= 1) {
+  // The root grid is the output grid times (mt, mp), so that the FFT
+  // interpolation only upsamples and the output is every mt-th row and mp-th
+  // column of the root (sphere.cu's copy of the root pattern).  The matrix
+  // passes of the double cover evaluate the trigonometric interpolant at any
+  // position, so they evaluate it at the output grid directly: the same values
+  // (row r of the output is at r / T on both grids) for 1 / (mt mp) of the
+  // root's work.
+  const bool direct_root = c->mirror && cfg->interp_method == PO_INTERP_TENSOR && lvl_ph[0] % 2 == 0;
+  if (d >= 1 && !direct_root) {
     c->mt = ceil_div(lvl_th[1], lvl_th[0]);
     c->mp = ceil_div(lvl_ph[1], lvl_ph[0]);
     if (c->mirror && (c->mp * lvl_ph[0]) % 2) ++c->mp;
