@@ -16,8 +16,9 @@
 //    (3 tcgen05.mma of 128 x ntn x 16) into one of two accumulators in tensor
 //    memory (one per row block parity) and commits the chunk's stage and,
 //    after the last chunk, the accumulator;
-//  * 4 converter warps: load the FP32 rows of each K chunk (16-byte loads,
-//    one to three chunks ahead into a statically indexed ring of registers,
+//  * 4 converter warps (8 with the wide tiles, two groups on alternate K
+//    chunks): load the FP32 rows of each K chunk (16-byte loads, one or two
+//    of the group's chunks ahead into a statically indexed ring of registers,
 //    by the length of the K loop),
 //    split them into bf16 hi + lo and store them in the core-matrix A layout
 //    of a 4-stage ring (padding rows of the output patterns and columns past
@@ -47,11 +48,14 @@ namespace {
 
 using namespace tc;
 
-constexpr int kRtCvtWarps = 4;
-// EW epilogue warps (4, or 8 = two per tensor-memory lane quarter for wide tiles)
+// EW epilogue warps (4, or 8 = two per tensor-memory lane quarter for wide
+// tiles); converter warps in groups of 4 that take alternate K chunks (two
+// groups with the wide tiles, one CTA per SM: twice the loads in flight)
 template <int EW>
 struct RtWarps {
-  static constexpr int ctl = EW + kRtCvtWarps;       // the phi-tile / MMA warp
+  static constexpr int cvt = EW == 8 ? 8 : 4;
+  static constexpr int groups = cvt / 4;
+  static constexpr int ctl = EW + cvt;  // the phi-tile / MMA warp
   static constexpr int threads = 32 * (ctl + 1);
 };
 constexpr int kRtStages = 4;
@@ -82,7 +86,7 @@ bool rows_tc_plan(int Pc, int Pp, int &ntn, int &n_nt) {
 
 // NB: converter register buffers (chunks of 4 x 16 B per thread)
 template <int EW, int NB>
-__global__ void __launch_bounds__(RtWarps<EW>::threads, 1) k_rows_tc(
+__global__ void __launch_bounds__(RtWarps<EW>::threads, EW == 4 ? 2 : 1) k_rows_tc(
     const float2 *__restrict__ src, uint8_t *__restrict__ dst, int64_t n_rows_out, int Rc, int Rr, int Pc, int KC,
     int half, int npad, int ntn, int n_nt, const uint8_t *__restrict__ Bt, uint32_t tcols, int *__restrict__ err) {
   extern __shared__ __align__(128) uint8_t smem_rt[];
@@ -101,7 +105,7 @@ __global__ void __launch_bounds__(RtWarps<EW>::threads, 1) k_rows_tc(
   if (tid == 0) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bfull)));
     for (int s = 0; s < kRtStages; ++s) {
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(&afull[s])), "r"(32 * kRtCvtWarps));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(&afull[s])), "r"(32 * 4));
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&aempty[s])));
     }
     for (int b = 0; b < 2; ++b) {
@@ -177,9 +181,11 @@ __global__ void __launch_bounds__(RtWarps<EW>::threads, 1) k_rows_tc(
     __syncwarp();
   } else if (warp >= kRtEpiWarps) {
     // ---- converter role: FP32 rows -> split bf16 A chunks ----
-    // the loads of the next two chunks are in flight while one is converted
-    const int ct = tid - 32 * kRtEpiWarps;
+    // group grp of 4 warps converts chunks grp, grp + NG, ...
+    constexpr int NG = RtWarps<EW>::groups;
+    const int grp = (tid - 32 * kRtEpiWarps) >> 7, ct = (tid - 32 * kRtEpiWarps) & 127;
     const int64_t n_chunks = (int64_t)n_it * KC;
+    const int64_t n_local = n_chunks > grp ? (n_chunks - grp + NG - 1) / NG : 0;
     // source rows of this thread's two output rows (i and i + 32) of row block
     // it: one division per row block, cached across its chunks
     int64_t row_it = -1, srow[2];
@@ -220,14 +226,14 @@ __global__ void __launch_bounds__(RtWarps<EW>::threads, 1) k_rows_tc(
     constexpr int kRtBufs = NB;
     float4 v[kRtBufs][4];
 #pragma unroll
-    for (int b = 0; b < kRtBufs - 1; ++b) load_chunk(b, v[b]);
+    for (int b = 0; b < kRtBufs - 1; ++b) load_chunk(grp + (int64_t)NG * b, v[b]);
     bool ok = true;
-    for (int64_t g0 = 0; g0 < n_chunks && ok; g0 += kRtBufs) {
+    for (int64_t i0 = 0; i0 < n_local && ok; i0 += kRtBufs) {
 #pragma unroll
       for (int b = 0; b < kRtBufs; ++b) {
-        const int64_t g = g0 + b;
-        if (g >= n_chunks) break;
-        load_chunk(g + kRtBufs - 1, v[(b + kRtBufs - 1) % kRtBufs]);
+        const int64_t il = i0 + b, g = grp + (int64_t)NG * il;
+        if (il >= n_local) break;
+        load_chunk(g + (int64_t)NG * (kRtBufs - 1), v[(b + kRtBufs - 1) % kRtBufs]);
         const int s = (int)(g % kRtStages);
         if (g >= kRtStages &&
             !mbar_wait(smem_addr(&aempty[s]), (uint32_t)(((g / kRtStages) - 1) & 1), abort_flag)) {
@@ -342,7 +348,6 @@ po_status init_rows_tc_attributes() {
   PO_TRY((rows_tc_attributes<4, 2>()));
   PO_TRY((rows_tc_attributes<4, 3>()));
   PO_TRY((rows_tc_attributes<8, 3>()));
-  PO_TRY((rows_tc_attributes<8, 4>()));
   return PO_OK;
 }
 
@@ -367,15 +372,21 @@ po_status launch_rows_tc(const float2 *src, uint8_t *dst, size_t dst_bytes, int6
   // converter buffers: deep prefetch pays on long K loops (fiber root, 34
   // chunks: 57.8 -> 47.8 ms per wavelength with 3 buffers instead of 2) and
   // costs on short ones, where the pass is bound by DRAM writes (fiber level
-  // 4, 3 chunks: 20.4 ms with 2 buffers, 28.0 with 3)
-  const int nb = KC >= 8 ? (wide ? 4 : 3) : (wide ? 3 : 2);
+  // 4, 3 chunks: 20.4 ms with 2 buffers, 28.0 with 3).  The wide tiles run two
+  // converter groups of 3 buffers (17 warps: 96 registers per thread).
+  const int nb = wide ? 3 : KC >= 8 ? 3 : 2;
   cudaFuncAttributes fa;
   if (wide)
-    PO_CUDA(nb == 4 ? cudaFuncGetAttributes(&fa, k_rows_tc<8, 4>) : cudaFuncGetAttributes(&fa, k_rows_tc<8, 3>));
+    PO_CUDA(cudaFuncGetAttributes(&fa, k_rows_tc<8, 3>));
   else
     PO_CUDA(nb == 3 ? cudaFuncGetAttributes(&fa, k_rows_tc<4, 3>) : cudaFuncGetAttributes(&fa, k_rows_tc<4, 2>));
   const int threads = wide ? RtWarps<8>::threads : RtWarps<4>::threads;
-  const int reg_limit = 65536 / (std::max(1, (fa.numRegs + 7) / 8 * 8) * threads);
+  // registers: each of the 4 SM sub-partitions holds 16K and takes every
+  // fourth warp of the resident CTAs (registers allocated 8 per thread)
+  const int warps = threads / 32, regs = std::max(8, (fa.numRegs + 7) / 8 * 8);
+  int reg_limit = 1;
+  for (int c = 2; c <= 8; ++c)
+    if ((c * warps + 3) / 4 * 32 * regs <= 16384) reg_limit = c;
   const int smem_limit = 228 * 1024 / (smem + 1024);
   const int per_sm = std::max(1, std::min(std::min(reg_limit, smem_limit), (int)(512 / tcols)));
   const int64_t n_rb = (n_rows_out + 63) / 64;
@@ -386,7 +397,7 @@ po_status launch_rows_tc(const float2 *src, uint8_t *dst, size_t dst_bytes, int6
   k_rows_tc<E, N><<<(unsigned)grid, RtWarps<E>::threads, smem, st>>>(src, dst, n_rows_out, Rc, Rr, Pc, KC, Pp / 2, \
                                                                      npad, ntn, n_nt, Bt, tcols, err)
   if (wide) {
-    if (nb == 4) PO_RT_LAUNCH(8, 4); else PO_RT_LAUNCH(8, 3);
+    PO_RT_LAUNCH(8, 3);
   } else {
     if (nb == 3) PO_RT_LAUNCH(4, 3); else PO_RT_LAUNCH(4, 2);
   }
