@@ -973,6 +973,20 @@ def run_reference_cuda(args, world, rank, local):
     t0 = time.perf_counter()
     oracle.solve_direct(sph, oracle.make_illum(500e-9, math.pi / 2, math.pi, "M", 1.55, 1e-2), N_THETA, N_PHI)
     eng["sphere_20k_depth0"]["b0_fp64_host_ms"] = (time.perf_counter() - t0) * 1e3
+    # plain vs tensor-core at depth 0: the split-BF16 tcgen05 direct sum (one leaf of all points), for the
+    # config's one pattern and per pattern at 64 incidences (where one phase tile serves 64 slots)
+    cfg1t = api.Config(0, [N_THETA], [N_PHI], box1[:3], box1[3:], precision=api.PO_PREC_SPLIT_BF16)
+    e1 = eng["sphere_20k_depth0"]
+    e1["b3_tensor_core_gpu_ms"] = engine_ms(cfg1t, g1, il1)
+    with api.Solver(cfg1t) as s, api.Solver(api.Config(0, [N_THETA], [N_PHI], box1[:3], box1[3:],
+                                                      precision=api.PO_PREC_FP64)) as s64:
+        ot = s.solve(sph, il1).reshape(-1).astype(np.float64)
+        o64 = s64.solve(sph, il1).reshape(-1).astype(np.float64)
+    e1["tensor_core_rel_l2_vs_fp64"] = float(np.linalg.norm(ot - o64) / np.linalg.norm(o64))
+    th64, ph64 = fiber_incidences(64)
+    il64 = api.Illumination([500e-9], th64, ph64, api.PO_POL_TM, 1.55 + 0j, 1e-2)
+    e1["per_pattern_ms_at_64_incidences"] = {"fp32": engine_ms(cfg1, g1, il64, reps=3) / 64,
+                                             "tensor_core": engine_ms(cfg1t, g1, il64, reps=3) / 64}
     eng["sphere_20k_depth0"]["b0_cores"] = oracle.num_threads()
 
     # ---- config 2: 400k-point ellipsoid, depth 5, one (wavelength, incidence) pair, capped loops

@@ -38,7 +38,7 @@ typedef enum po_precision {
   PO_PREC_FP32 = 0,       /* FP32 sums, FP64 phase arguments where they are large */
   PO_PREC_FP64 = 1,       /* plain FP64 everywhere (depth 0 only) */
   PO_PREC_SPLIT_BF16 = 2, /* leaf sums as tensor-core hi+lo BF16 products, FP32 accumulation
-                             (depth 0 keeps the FP32 direct sum) */
+                             (depth 0: the same tcgen05 sum over one leaf of all points) */
   PO_PREC_SPLIT_FP16 = 3  /* reserved: rejected with PO_ERR_UNSUPPORTED (the currents need
                              per-tile scaling to fit the FP16 range) */
 } po_precision;

@@ -2,8 +2,9 @@
 
   * the plain method (depth 0): sphere of radius 2 um, 20,000 Fibonacci
     points, n = 1.55, 500 nm, plane wave along +z polarised along x, on the
-    full 180 x 360 grid -- FP64 engine <= 1e-6, FP32 engine <= 1e-5 over all
-    64,800 directions; the engine's forward lobe against the Mie series;
+    full 180 x 360 grid -- FP64 engine <= 1e-6, FP32 engine <= 1e-5,
+    split-BF16 tcgen05 engine <= 1e-4 over all 64,800 directions; the
+    engine's forward lobe against the Mie series;
   * the fiber segment (3.40M points from the seeded height field, depth 7,
     reference level grids, 180 x 360, split-BF16 tcgen05 leaf sums): eight
     incidences of the 64-incidence sweep at 400 nm, two of them against the
@@ -52,6 +53,28 @@ def test_sphere_20k_depth0_full_grid(sphere20k, prec, tol):
     with api.Solver(cfg) as s:
         out = s.solve(cloud, il).reshape(NTH, NPH)
     assert rel(out, ref) <= tol
+
+
+def test_sphere_20k_depth0_tensor_core_full_grid(sphere20k):
+    """Config 1 on the tensor cores: the split-BF16 tcgen05 sum over one leaf of
+    all 20,000 points (its 507 direction tiles spread over CTAs) against the
+    FP64 oracle on all 64,800 directions; and with 70 patterns (two slot
+    groups) every pattern against the FP32 direct sum."""
+    cloud, ref = sphere20k
+    box = [-2.2e-6] * 3, [2.2e-6] * 3
+    il = api.Illumination([500e-9], [math.pi / 2], [math.pi], api.PO_POL_TM, 1.55 + 0j, 1e-2)
+    with api.Solver(api.Config(0, [NTH], [NPH], *box, precision=api.PO_PREC_SPLIT_BF16)) as s:
+        out = s.solve(cloud, il).reshape(NTH, NPH)
+        assert s.last_report["n_leaf_launches"] == 2, s.last_report  # operands + sums: the tcgen05 path
+    assert rel(out, ref) <= 1e-4
+    rng = np.random.default_rng(12)
+    th, ph = list(rng.uniform(-1.3, 1.3, 35)), list(rng.uniform(0, 2 * math.pi, 35))
+    il70 = api.Illumination([620e-9], th, ph, api.PO_POL_TM | api.PO_POL_TE, 1.55 + 0.1j, 1e-2)
+    outs = []
+    for prec in (api.PO_PREC_FP32, api.PO_PREC_SPLIT_BF16):
+        with api.Solver(api.Config(0, [90], [180], *box, precision=prec)) as s:
+            outs.append(s.solve(cloud, il70))
+    assert rel(outs[1], outs[0]) <= 1e-4
 
 
 def test_sphere_20k_forward_lobe_vs_mie(sphere20k):

@@ -65,7 +65,7 @@ po_status launch_leaf_tc(const float *const g[7], const int32_t *leaf_begin, con
                          const SlotParams<float> *slots_dev, int n_lambda, int Gtot, int g0, int G,
                          const float4 *dirs, int ndir, uint8_t *bop, size_t bop_bytes, float4 *uop,
                          size_t uop_bytes, float2 *out, int *err, cudaStream_t st, int group = kLeafTcMaxSlots,
-                         int withhold = 0);
+                         int withhold = 0, int msplit = 1);
 
 int direct_splits(int64_t n, int ndir, int n_lambda, int sm_count);
 // FP32 depth-0 sum about c0: out[slot][comp][dir]; cur[slot][n][6]

@@ -25,7 +25,8 @@
 //    UMMA K-major core-matrix layout, one contiguous 8-KB block per column
 //    tile, and the chunk's scaled offsets u = k (x - c) (zero for padding);
 //  * k_leaf_tc: one CTA per (leaf, wavelength) walking (direction tile m,
-//    column tile n, point chunk k) with four roles --
+//    column tile n, point chunk k) with four roles (a depth-0 solve is one
+//    leaf of all points, its direction tiles spread over msplit CTAs) --
 //      - 4 producer warps (thread = direction row): cos and sin of the
 //        chunk's phases, split, stored in the core-matrix A layout.  The
 //        phases do not depend on the column tile, so for a leaf of at most
@@ -177,7 +178,7 @@ template <class P>
 __global__ void __launch_bounds__(kLtThreads, P::ctas) k_leaf_tc(
     const uint8_t *__restrict__ bop, const float4 *__restrict__ uop, const int32_t *__restrict__ kc0,
     int64_t n_chunks, const float4 *__restrict__ dirs, int ndir, int64_t n_leaves, int Gtot, int g0, int G, int NT,
-    float2 *__restrict__ out, int *__restrict__ err, int withhold) {
+    float2 *__restrict__ out, int *__restrict__ err, int withhold, int msplit) {
   extern __shared__ __align__(1024) uint8_t smem_lt[];
   constexpr int kLtRes = P::res, kLtASlots = P::slots, kAcc = P::acc;
   uint8_t *sA = smem_lt;                                   // [kLtASlots][kLtAStage]
@@ -187,11 +188,15 @@ __global__ void __launch_bounds__(kLtThreads, P::ctas) k_leaf_tc(
   uint32_t *tmem_slot = (uint32_t *)(acce + kAcc);
   volatile int *abort_flag = (volatile int *)(tmem_slot + 1);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int64_t leaf = blockIdx.x;
+  // CTA = (leaf, direction tiles m0, m0 + msplit, ...): msplit > 1 spreads
+  // one large leaf (the whole point set of a depth-0 solve) over many CTAs
+  const int64_t leaf = blockIdx.x / msplit;
+  const int m0 = (int)(blockIdx.x % msplit);
   const int lam = blockIdx.y;
   const int c0 = kc0[leaf], KCl = kc0[leaf + 1] - c0;
   const int MT = (ndir + 127) / 128;
-  const int ntiles = MT * NT;
+  const int MTl = m0 < MT ? (MT - m0 + msplit - 1) / msplit : 0;  // direction tiles of this CTA
+  const int ntiles = MTl * NT;
   const bool resident = KCl <= kLtRes;
   if (tid == 0) {
     for (int q = 0; q < kLtASlots; ++q) {
@@ -269,7 +274,7 @@ __global__ void __launch_bounds__(kLtThreads, P::ctas) k_leaf_tc(
       for (int q = 0; q < kLtASlots; ++q) alast[q] = -1;
       int tiles_done = 0;
       for (int t = 0; t < ntiles && ok; ++t) {
-        const int m = t / NT, n = t % NT, buf = t % kAcc;
+        const int m = t / NT, n = t % NT, buf = t % kAcc;  // m: this CTA's tile index
         if (t >= kAcc && !mbar_wait(smem_addr(&acce[buf]), (uint32_t)(((t / kAcc) - 1) & 1), abort_flag)) {
           ok = false;
           break;
@@ -362,8 +367,8 @@ __global__ void __launch_bounds__(kLtThreads, P::ctas) k_leaf_tc(
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       mbar_arrive(smem_addr(&afull[slot]));
     };
-    for (int m = 0; m < MT && ok && KCl > 0; ++m) {
-      const float4 sd = __ldg(dirs + min(m * 128 + r, ndir - 1));
+    for (int m = 0; m < MTl && ok && KCl > 0; ++m) {  // this CTA's tile index
+      const float4 sd = __ldg(dirs + min((m0 + m * msplit) * 128 + r, ndir - 1));
       const int nrep = resident ? 1 : NT;  // a resident tile's chunks serve every column tile
       for (int rep = 0; rep < nrep && ok; ++rep)
         for (int kc = 0; kc < KCl; ++kc) {
@@ -384,7 +389,7 @@ __global__ void __launch_bounds__(kLtThreads, P::ctas) k_leaf_tc(
     const int quarter = warp & 3, eh = warp >> 2, r = 32 * quarter + lane;
     bool ok = true;
     for (int t = 0; t < ntiles && ok; ++t) {
-      const int m = t / NT, n = t % NT, d = m * 128 + r, buf = t % kAcc;
+      const int m = m0 + (t / NT) * msplit, n = t % NT, d = m * 128 + r, buf = t % kAcc;
       const uint32_t ta = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(buf * 2 * kLtN);
       if (KCl > 0) {
         ok = __all_sync(0xffffffffu, mbar_wait(smem_addr(&accf[buf]), (uint32_t)((t / kAcc) & 1), abort_flag)) != 0;
@@ -449,11 +454,13 @@ po_status launch_leaf_tc(const float *const g[7], const int32_t *leaf_begin, con
                          const int32_t *chunk_leaf, int64_t n_chunks, const double *leaf_center, int64_t n_leaves,
                          const SlotParams<float> *slots_dev, int n_lambda, int Gtot, int g0, int G,
                          const float4 *dirs, int ndir, uint8_t *bop, size_t bop_bytes, float4 *uop,
-                         size_t uop_bytes, float2 *out, int *err, cudaStream_t st, int group, int withhold) {
+                         size_t uop_bytes, float2 *out, int *err, cudaStream_t st, int group, int withhold,
+                         int msplit) {
   if (n_leaves <= 0 || n_lambda <= 0 || G <= 0) return PO_OK;
   if (group < 8 || group > kLeafTcMaxSlots || group % 8 != 0)
     return fail(PO_ERR_INTERNAL, "tcgen05 leaf: slots per pass");
-  if (n_chunks <= 0 || n_lambda > 65535 || n_leaves > 2147483647LL || n_chunks > 2147483647LL)
+  if (n_chunks <= 0 || n_lambda > 65535 || msplit < 1 || n_leaves * msplit > 2147483647LL ||
+      n_chunks > 2147483647LL)
     return fail(PO_ERR_INTERNAL, "tcgen05 leaf: launch shape");
   if ((size_t)n_lambda * n_chunks * leaf_tc_col_tiles(std::min(G, group)) * kLtBBlock > bop_bytes ||
       (size_t)n_lambda * n_chunks * kLtKC * sizeof(float4) > uop_bytes)
@@ -466,8 +473,8 @@ po_status launch_leaf_tc(const float *const g[7], const int32_t *leaf_begin, con
         g[0], g[1], g[2], g[3], g[4], g[5], g[6], leaf_begin, kc0, chunk_leaf, leaf_center, slots_dev, Gtot,
         g0 + gs, gc, NT, n_chunks, bop, uop);
     count_launch();
-    k_leaf_tc<LtMain><<<dim3((unsigned)n_leaves, (unsigned)n_lambda), kLtThreads, LtMain::smem, st>>>(
-        bop, uop, kc0, n_chunks, dirs, ndir, n_leaves, Gtot, g0 + gs, gc, NT, out, err, withhold);
+    k_leaf_tc<LtMain><<<dim3((unsigned)(n_leaves * msplit), (unsigned)n_lambda), kLtThreads, LtMain::smem, st>>>(
+        bop, uop, kc0, n_chunks, dirs, ndir, n_leaves, Gtot, g0 + gs, gc, NT, out, err, withhold, msplit);
     count_launch();
   }
   PO_CUDA(cudaGetLastError());

@@ -719,6 +719,32 @@ static po_status prepare_solve(po_ctx *c, const po_geometry *g, const po_illum *
     PO_TRY(c->partial.ensure(sizeof(float2) * 6 * (size_t)ns_max * nd_out * P.nsplit_max));
     PO_TRY(c->levelA.ensure(sizeof(float2) * 6 * (size_t)ns_max * nd_out));
     if (adj) PO_TRY(c->levelB.ensure(sizeof(float2) * 6 * (size_t)ns_max * nd_out));
+    // split BF16: the tcgen05 leaf kernel over one leaf of all points about
+    // the box centre (the direct sum's centre), its direction tiles spread
+    // over CTAs; tables [kc0: 0, chunks | begin: 0, n] and chunk -> leaf 0
+    P.leaf_tc = cfg.precision == PO_PREC_SPLIT_BF16 && n > 0;
+    P.leaf_group = cfg.leaf_slots ? cfg.leaf_slots : kLeafTcMaxSlots;
+    if (P.leaf_tc) {
+      const int64_t nchunks = (n + 15) / 16;
+      if (nchunks > 2147483647LL) return fail(PO_ERR_UNSUPPORTED, "too many points for the tcgen05 direct sum");
+      const int32_t tab[4] = {0, (int32_t)nchunks, 0, (int32_t)n};
+      PO_TRY(c->leaf_kc0.ensure(sizeof(tab)));
+      PO_TRY(c->leaf_chunk.ensure(sizeof(int32_t) * (size_t)nchunks));
+      PO_TRY(c->leaf_ctr.ensure(sizeof(double) * 3));
+      PO_CUDA(cudaMemcpyAsync(c->leaf_kc0.p, tab, sizeof(tab), cudaMemcpyHostToDevice, st));
+      PO_CUDA(cudaMemsetAsync(c->leaf_chunk.p, 0, sizeof(int32_t) * (size_t)nchunks, st));
+      PO_CUDA(cudaMemcpyAsync(c->leaf_ctr.p, P.c0, sizeof(P.c0), cudaMemcpyHostToDevice, st));
+      P.leaf_chunks = nchunks;
+      size_t bop = 0;
+      int nl_max = 1;
+      for (const SlotChunk &ch : P.chunks) {
+        bop = std::max(bop, (size_t)ch.nl * nchunks * leaf_tc_col_tiles(std::min(ch.gc, P.leaf_group)) *
+                                leaf_tc_block_bytes());
+        nl_max = std::max(nl_max, ch.nl);
+      }
+      PO_TRY(c->leaf_bop.ensure(bop));
+      PO_TRY(c->leaf_uop.ensure(sizeof(float4) * 16 * (size_t)nl_max * nchunks));
+    }
     PO_CUDA(cudaStreamSynchronize(st));
     return PO_OK;
   }
@@ -883,11 +909,21 @@ static po_status enqueue_solve(po_ctx *c, const SolvePlan &P, float *out_dev, co
   } else if (d == 0) {
     for (const SlotChunk &ch : P.chunks) {
       PO_TRY(rec(c->kev[0]));
-      PO_TRY(launch_currents_f32(n, P.gsc, c->slots.as<SlotParams<float>>() + ch.s0, ch.ns, c->cur.as<float>(), st));
-      int nsplit = direct_splits(n, (int)nd_out, ch.nl, c->sm_count);
-      PO_TRY(launch_direct_f32(n, P.gsc[0], P.gsc[1], P.gsc[2], c->cur.as<float2>(), c->tile_ctr.as<double>(),
-                               P.k_lambda + ch.l0, ch.nl, ch.gc, P.c0, c->dirs.as<float4>(), c->dirs_d.as<double>(),
-                               (int)nd_out, nsplit, c->partial.as<float2>(), c->levelA.as<float2>(), st));
+      if (P.leaf_tc) {
+        const int32_t *tab = c->leaf_kc0.as<int32_t>();
+        PO_TRY(launch_leaf_tc(P.gsc, tab + 2, tab, c->leaf_chunk.as<int32_t>(), P.leaf_chunks, c->leaf_ctr.as<double>(),
+                              1, c->slots.as<SlotParams<float>>() + ch.s0, ch.nl, ch.gc, 0, ch.gc,
+                              c->dirs.as<float4>(), (int)nd_out, c->leaf_bop.as<uint8_t>(), c->leaf_bop.bytes,
+                              c->leaf_uop.as<float4>(), c->leaf_uop.bytes, c->levelA.as<float2>(), c->tc_err.as<int>(),
+                              st, P.leaf_group, 0, ceil_div((int)nd_out, 128)));
+      } else {
+        PO_TRY(launch_currents_f32(n, P.gsc, c->slots.as<SlotParams<float>>() + ch.s0, ch.ns, c->cur.as<float>(),
+                                   st));
+        int nsplit = direct_splits(n, (int)nd_out, ch.nl, c->sm_count);
+        PO_TRY(launch_direct_f32(n, P.gsc[0], P.gsc[1], P.gsc[2], c->cur.as<float2>(), c->tile_ctr.as<double>(),
+                                 P.k_lambda + ch.l0, ch.nl, ch.gc, P.c0, c->dirs.as<float4>(), c->dirs_d.as<double>(),
+                                 (int)nd_out, nsplit, c->partial.as<float2>(), c->levelA.as<float2>(), st));
+      }
       PO_TRY(rec(c->kev[1]));
       PO_TRY(rec(c->ev[3]));
       PO_TRY(launch_intensity_f32(c->levelA.as<float2>(), ch.ns, nth_out, nph_out, nth_out, nph_out, 1, 1,
@@ -902,7 +938,7 @@ static po_status enqueue_solve(po_ctx *c, const SolvePlan &P, float *out_dev, co
                                         ch.nl, ch.gc, n, c->grad_acc.as<double>(), st));
       }
       PO_TRY(rec(c->ev[4]));
-      T.n_leaf += 3 + (ch.gc + 3) / 4;
+      T.n_leaf += P.leaf_tc ? 2 * ((ch.gc + P.leaf_group - 1) / P.leaf_group) : 3 + (ch.gc + 3) / 4;
       PO_TRY(chunk_done(false));
     }
     T.leaf_pd = (double)n * nd_out * P.S;
