@@ -359,7 +359,7 @@ FIBER_BOX_MAX = [-v for v in FIBER_BOX_MIN]
 # profiles/aggregation_traffic_fiber_8inc.md (dram__bytes_read.sum + dram__bytes_write.sum of every phi
 # and theta launch of one 8-incidence solve of this workload, 165.45 GB, over the per-level
 # algorithmic bytes of the same solve, 49.42 GB)
-FIBER_AGG_TRAFFIC_RATIO = 165.45 / 49.42
+FIBER_AGG_TRAFFIC_RATIO = 154.19 / 49.25
 
 
 def fiber_incidences(n: int = FIBER_INC):
