@@ -32,7 +32,9 @@
 // the mirror column e^{i (sz z - sx x - sy y)}, with the octant's signs s and
 // the reduced phases (x, y, z) of the translation table.  Once per CTA the
 // epilogue warps stage (x, y) per (row, pair) and e^{i z} per row; a child
-// then costs one sincos per (row, pair).  (Staging e^{i (x + y)} and
+// then costs one sincos per (row, pair), and the row's z phasor turns the
+// accumulator twice per task, since the children run in octant order (the
+// positive z sign first).  (Staging e^{i (x + y)} and
 // e^{i (x - y)} instead, which removes that sincos, needs twice the table
 // space, leaves room for one stage less and measured slower.)
 //
@@ -323,6 +325,23 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_theta_tc(
 #pragma unroll
     for (int q = 0; q < 16; ++q) acc[q][0][0] = acc[q][0][1] = acc[q][1][0] = acc[q][1][1] = 0.f;
     const float2 ez = sPz[rl];
+    // The z phasor e^{+-i z} depends on the row only (this thread's) and on
+    // the child's z sign; the children come in octant order, those with the
+    // positive z sign (o < 4) first.  So the accumulator collects sum Y e over
+    // the positive children, is turned by e^{2 i z} once before the first
+    // negative child, and by e^{-i z} once at the end:
+    // e^{-iz} (e^{2iz} S+ + S-) = e^{iz} S+ + e^{-iz} S-.
+    auto turn = [&](float cr, float ci_) {
+#pragma unroll
+      for (int q = 0; q < 16; ++q)
+#pragma unroll
+        for (int w = 0; w < 2; ++w) {
+          const float ar = acc[q][w][0], ai = acc[q][w][1];
+          acc[q][w][0] = ar * cr - ai * ci_;
+          acc[q][w][1] = ar * ci_ + ai * cr;
+        }
+    };
+    bool turned = false;
     bool ok = true;
     for (int ci = 0; ci < nkids && ok; ++ci) {
       const int b = ci & 1;
@@ -330,9 +349,12 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_theta_tc(
       if (!ok) break;
       asm volatile("tcgen05.fence::after_thread_sync;");
       const int o = kids[ci];
-      // octant signs: x + for o & 1, y + for !(o & 2), z + for !(o & 4)
+      if ((o & 4) && !turned) {
+        turn(ez.x * ez.x - ez.y * ez.y, 2.f * ez.x * ez.y);
+        turned = true;
+      }
+      // octant signs: x + for o & 1, y + for !(o & 2)
       const bool px = (o & 1) != 0, py = (o & 2) == 0;
-      const float pzr = ez.x, pzi = (o & 4) ? -ez.y : ez.y;
       const float sgx = px ? 1.f : -1.f, sgy = py ? 1.f : -1.f;
       const uint32_t ta = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(b * 2 * kTcN + 32 * wg);
 #pragma unroll
@@ -346,21 +368,23 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_theta_tc(
           float er, ei;
           const float2 xy = sT[pl * kTcLd + rl];
           __sincosf(fmaf(sgx, xy.x, sgy * xy.y), &ei, &er);
-          // column j: e^{i z'} e;  mirror column: e^{i z'} conj(e)
-          const float w1r = pzr * er - pzi * ei, w1i = pzr * ei + pzi * er;
-          const float w2r = pzr * er + pzi * ei, w2i = pzi * er - pzr * ei;
+          // column j: e;  mirror column: conj(e) (the z phasor is applied by turn)
           const float ur = __uint_as_float(u[2 * q]), ui = __uint_as_float(u[2 * q + 1]);
           const float vr = __uint_as_float(v[2 * q]), vi = __uint_as_float(v[2 * q + 1]);
           const float y1r = ur + vr, y1i = ui + vi, y2r = ur - vr, y2i = ui - vi;
-          acc[4 * h + q][0][0] += y1r * w1r - y1i * w1i;
-          acc[4 * h + q][0][1] += y1r * w1i + y1i * w1r;
-          acc[4 * h + q][1][0] += y2r * w2r - y2i * w2i;
-          acc[4 * h + q][1][1] += y2r * w2i + y2i * w2r;
+          acc[4 * h + q][0][0] += y1r * er - y1i * ei;
+          acc[4 * h + q][0][1] += y1r * ei + y1i * er;
+          acc[4 * h + q][1][0] += y2r * er + y2i * ei;
+          acc[4 * h + q][1][1] += y2i * er - y2r * ei;
         }
       }
       asm volatile("tcgen05.fence::before_thread_sync;");
       mbar_arrive(smem_addr(&acce[b]));
     }
+    if (turned)
+      turn(ez.x, -ez.y);
+    else
+      turn(ez.x, ez.y);
     if (!ok) {
       *abort_flag = 1;
       if (lane == 0) atomicCAS(err, 0, 1);
