@@ -62,17 +62,18 @@ WORKLOAD = "ellipsoid 8x5x5um, 400k points, depth 5, 25 wavelengths x 1 incidenc
 
 PRECISIONS = {"fp32": 0, "split_bf16": 2}
 INTERP = {"fft": 0, "tensor": 1}
+THETA_MODES = {"double_cover": 0, "reference": 1}
 
 
 def make_workload(precision: str = "fp32", interp: str = "tensor", tile: int = 0, n_lambda: int = 25,
-                  n_inc: int = 1):
+                  n_inc: int = 1, theta_mode: str = "double_cover"):
     from wavefiber3d_gb300 import api, geometry
     cloud = geometry.ellipsoid(RADII, N_POINTS)
     bmin = [-1.1 * r for r in RADII]
     bmax = [1.1 * r for r in RADII]
     cfg = api.Config.reference_rule(DEPTH, N_THETA, N_PHI, bmin, bmax, 16e-6, 16e-6, 1.3,
                                     precision=PRECISIONS[precision], interp_method=INTERP[interp],
-                                    interp_tile=tile)
+                                    interp_tile=tile, theta_mode=THETA_MODES[theta_mode])
     # one incidence along +x (the workload); more for profiling runs: a theta sweep at phi = 0.3
     th = [0.0] if n_inc == 1 else list(np.linspace(-1.0, 1.0, n_inc))
     ph = [0.0] if n_inc == 1 else [0.3] * n_inc
@@ -213,7 +214,8 @@ def run_engine(args, world, rank, local):
     bf16_peak = peaks.get("bf16_tflops", 1900.0)
     peak_src = "measured" if peaks else "fallback"
 
-    cloud, cfg, illum = make_workload(args.precision, args.interp, args.interp_tile, args.lambdas, args.incidences)
+    cloud, cfg, illum = make_workload(args.precision, args.interp, args.interp_tile, args.lambdas, args.incidences,
+                                      args.theta_mode)
     pd_step = point_dirs_per_step(illum)
     st = torch.cuda.current_stream()
     g_dev = torch.from_numpy(cloud.soa()).to(dev)
@@ -319,7 +321,8 @@ def run_engine(args, world, rank, local):
             "config": {"workload": WORKLOAD, "points": N_POINTS, "directions": N_THETA * N_PHI,
                        "wavelengths": len(illum.wavelengths_m), "incidences": len(illum.theta_i), "polarisations": 1,
                        "depth": DEPTH,
-                       "level_grids": [list(cfg.n_theta), list(cfg.n_phi)], "theta_mode": "double cover",
+                       "level_grids": [list(cfg.n_theta), list(cfg.n_phi)],
+                       "theta_mode": args.theta_mode.replace("_", " "),
                        "precision": args.precision, "theta_interpolation": args.interp,
                        "theta_tile": args.interp_tile,
                        "l2": "flushed between steps (256 MiB write, outside the timed events)",
@@ -1094,6 +1097,9 @@ def main():
     ap.add_argument("--interp", choices=sorted(INTERP), default="tensor")
     ap.add_argument("--interp-tile", type=int, choices=[0, 8, 16], default=0,
                     help="complex columns per CTA of the tensor-core theta pass (0: automatic)")
+    ap.add_argument("--theta-mode", choices=sorted(THETA_MODES), default="double_cover",
+                    help="ellipsoid workload: the engine's double-cover theta sampling, or the reference's "
+                         "pi-periodic theta interpolation (its drop-in mode)")
     ap.add_argument("--lambdas", type=int, default=25,
                     help="wavelengths of the ellipsoid workload (25 = the workload; fewer for profiling runs)")
     ap.add_argument("--incidences", type=int, default=1,

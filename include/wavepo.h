@@ -93,8 +93,10 @@ typedef enum po_interp_method {
   PO_INTERP_TENSOR = 1  /* the level's trigonometric interpolation matrices as split hi+lo
                            BF16 tensor-core products, for both passes: tcgen05 with
                            tensor-memory accumulators on levels whose rows fill 128-row
-                           tiles, warp-level mma.sync on the others (double-cover theta
-                           only; the reference theta mode falls back to the FFTs) */
+                           tiles, warp-level mma.sync on the others.  In the reference
+                           theta mode two kinds of level keep the FFTs: those where the
+                           Nyquist quirk of interpolation.h:66 reaches a parent column (a
+                           complex, column-dependent map) and those between equal sizes */
 } po_interp_method;
 
 typedef struct po_geometry {

@@ -483,3 +483,27 @@ def test_reference_mode_tensor_path_on_large_grids():
                           nth, nph, True)
     assert rel(outs[0], o) < TOL_TREE
     assert rel(outs[0], outs[1]) < TOL_TREE
+
+
+@pytest.mark.parametrize("prec", [api.PO_PREC_FP32, api.PO_PREC_SPLIT_BF16])
+def test_reference_mode_tensor_path_on_odd_phi_grids(prec):
+    """Odd parent phi grids in the reference theta mode, whose columns do not
+    pair up as phi and phi + pi: the tensor path pairs column j with
+    j + (Phi + 1)/2 (one phantom partner) and takes each partner's translation
+    from its own table entry.  Level 1 (45 columns) and level 2 (27 columns,
+    the deepest parent: its phi pass runs fused into the split-precision leaf
+    kernel) are odd; checked against the oracle's restatement of the
+    reference's FFT interpolation and against the FFT path."""
+    cloud = geometry.fibonacci_sphere(1.0e-6, 2000)
+    box = [-1.1e-6] * 3 + [1.1e-6] * 3
+    nth, nph = [48, 40, 26, 16], [96, 45, 27, 16]
+    il = api.Illumination([500e-9], [0.3], [0.7], api.PO_POL_TM, 1.55 + 0.1j, 2e-6)
+    outs = []
+    for interp in (api.PO_INTERP_TENSOR, api.PO_INTERP_FFT):
+        cfg = api.Config(3, nth, nph, box[:3], box[3:], theta_mode=api.PO_THETA_REFERENCE, nyquist_quirk=True,
+                         interp_method=interp, precision=prec)
+        outs.append(_solve(cloud, cfg, il)[0].reshape(nth[0], nph[0]))
+    o = oracle.solve_tree(cloud, oracle.make_illum(500e-9, 0.3, 0.7, "M", 1.55 + 0.1j, 2e-6), box[:3], box[3:], 3,
+                          nth, nph, True)
+    assert rel(outs[0], o) < TOL_TREE
+    assert rel(outs[0], outs[1]) < TOL_TREE

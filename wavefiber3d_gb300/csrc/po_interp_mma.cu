@@ -174,6 +174,9 @@ void build_theta_matrix_adj(int Tc, int Tp, int Rc, int Rp, int Kp, std::vector<
 // Theta pass as warp tasks (double cover).  A warp owns one (slot, parent,
 // component) and TW = 4 NPT column pairs (j, j + Phi/2), j = j0.., for the
 // CTA's 16-row tiles mt0 .. mt0+MTW-1 (blockIdx.y selects them).
+// ODD (reference theta mode, odd parent phi grid): the pairs are (j, j + H),
+// H = (Phi + 1)/2, whose partner is not at phi + pi: its translation phase
+// comes from its own table entry, and the phantom partner Phi is not stored.
 // mid (from k_interp_rows_mma<1>): per (slot, child, component)
 // [Rc2/2][Phi/2][re, im] uint4 {S hi pair, S lo pair, D hi pair, D lo pair} --
 // a lane's B registers for the S and the D n-tile in one 16-byte load.  The
@@ -181,7 +184,7 @@ void build_theta_matrix_adj(int Tc, int Tp, int Rc, int Rp, int Kp, std::vector<
 // that warps run independently: B fragments of the next k-step (or next
 // child) are loaded while the current one multiplies, and the parent tile
 // accumulates in registers across the children.
-template <int NPT, int MTW>
+template <int NPT, int MTW, bool ODD>
 __global__ void __launch_bounds__(256, (NPT == 1 && MTW <= 2) ? 3 : 2) k_theta_warp(const uint4 *__restrict__ mid, float2 *__restrict__ parent,
                                                        const int32_t *__restrict__ child_table, int64_t n_parent,
                                                        int64_t n_child, int phi, int Rch, int Rp, int KS, int MT,
@@ -213,7 +216,7 @@ __global__ void __launch_bounds__(256, (NPT == 1 && MTW <= 2) ? 3 : 2) k_theta_w
   rest /= 6;
   const int64_t p = rest % n_parent;
   const int slot = (int)(rest / n_parent), lam = slot / G;
-  const int span = phi / 2, j0 = ct * TW, part = g & 1;
+  const int span = (phi + 1) / 2, j0 = ct * TW, part = g & 1;
   const int64_t pat = (int64_t)Rch * span * 2;  // uint4 words of one child pattern component
   const uint4 *mbase = mid + ((int64_t)slot * n_child * 6 + comp) * pat;
   const int32_t cl = lane < 8 ? child_table[p * 8 + lane] : -1;
@@ -312,12 +315,18 @@ __global__ void __launch_bounds__(256, (NPT == 1 && MTW <= 2) ? 3 : 2) k_theta_w
           // the negatives of column j's, so one table entry serves both
           const float4 rr = __ldg(tr + (int64_t)r * phi + jc);
           const float pxy = fmaf(sgx, rr.x, sgy * rr.y), pz = sgz * rr.z;
+          float pxm = -pxy;
+          if (ODD) {  // the partner's own entry (same row: same z phase)
+            const int jm = jc + span < phi ? jc + span : phi - 1;
+            const float4 rm = __ldg(tr + (int64_t)r * phi + jm);
+            pxm = fmaf(sgx, rm.x, sgy * rm.y);
+          }
 #pragma unroll
           for (int w = 0; w < 2; ++w) {
             // each table phase is reduced to [-pi, pi], so |pz +- pxy| <= 3 pi:
             // the hardware sine / cosine need no further reduction (abs. error ~1e-6)
             float sn, cs;
-            __sincosf(w ? pz - pxy : pz + pxy, &sn, &cs);
+            __sincosf(pz + (w ? pxm : pxy), &sn, &cs);
             const float yr = w ? ur - vr : ur + vr, yi = w ? ui - vi : ui + vi;
             acc[i][pt][w][2 * h] += yr * cs - yi * sn;
             acc[i][pt][w][2 * h + 1] += yr * sn + yi * cs;
@@ -346,18 +355,19 @@ __global__ void __launch_bounds__(256, (NPT == 1 && MTW <= 2) ? 3 : 2) k_theta_w
         if (r >= Rp) continue;
 #pragma unroll
         for (int w = 0; w < 2; ++w)
-          out[(int64_t)r * phi + jq + w * span] = make_float2(acc[i][pt][w][2 * h], acc[i][pt][w][2 * h + 1]);
+          if (!ODD || jq + w * span < phi)
+            out[(int64_t)r * phi + jq + w * span] = make_float2(acc[i][pt][w][2 * h], acc[i][pt][w][2 * h + 1]);
       }
     }
   }
 }
 
-template <int NPT, int MTW>
+template <int NPT, int MTW, bool ODD>
 static void launch_theta_warp(dim3 grid, size_t smem, const uint4 *mid, float2 *parent, const int32_t *child_table,
                               int64_t n_parent, int64_t n_child, int phi, int Rch, int Rp, int KS, int MT,
                               const uint4 *A, const float4 *trans, int G, int n_ct, int64_t n_task, cudaStream_t st) {
-  k_theta_warp<NPT, MTW><<<grid, 256, smem, st>>>(mid, parent, child_table, n_parent, n_child, phi, Rch, Rp, KS, MT,
-                                                  A, trans, G, n_ct, n_task);
+  k_theta_warp<NPT, MTW, ODD><<<grid, 256, smem, st>>>(mid, parent, child_table, n_parent, n_child, phi, Rch, Rp, KS,
+                                                       MT, A, trans, G, n_ct, n_task);
 }
 
 po_status launch_interp_cols_mma(const uint4 *mid, float2 *parent, const int32_t *child_table, int64_t n_parent,
@@ -366,9 +376,9 @@ po_status launch_interp_cols_mma(const uint4 *mid, float2 *parent, const int32_t
   if (n_parent <= 0 || n_slots <= 0) return PO_OK;
   const int Rc2 = Rc + (Rc & 1);
   if (Kp % 16 || Kp < Rc2) return fail(PO_ERR_INTERNAL, "theta matrix K padding");
-  if (phi % 2) return fail(PO_ERR_INTERNAL, "mirrored storage needs an even phi grid");
+  const bool odd = phi % 2 != 0;  // reference theta mode only (no mirrored rows)
   const int KS = Kp / 16, MT = (Rp + 15) / 16;
-  const int NPT = tile == 16 ? 2 : 1;
+  const int NPT = tile == 16 && !odd ? 2 : 1;
   // 16-row tiles per warp: up to 4 (register budget of the accumulators), and
   // few enough that the CTA's matrix slice (2 KB per tile and k-step) leaves
   // room for two CTAs per SM; a single tile may use the whole opt-in limit
@@ -381,18 +391,19 @@ po_status launch_interp_cols_mma(const uint4 *mid, float2 *parent, const int32_t
   const int MTW = (MT + nmg - 1) / nmg;
   const size_t smem = (size_t)MTW * tile_bytes;
   const int TW = 4 * NPT;
-  const int n_ct = (phi / 2 + TW - 1) / TW;
+  const int n_ct = ((phi + 1) / 2 + TW - 1) / TW;
   const int64_t n_task = (int64_t)n_slots * n_parent * 6 * n_ct;
   const int64_t gx = (n_task + 7) / 8 * nmg;
   if (gx > 2147483647LL) return fail(PO_ERR_UNSUPPORTED, "too many nodes for one launch");
   dim3 grid((unsigned)gx, 1u, 1u);
   const uint4 *A = (const uint4 *)Afrag;
-#define PO_TW(N, M)                                                                                                 \
-  if (NPT == N && MTW == M) {                                                                                      \
-    launch_theta_warp<N, M>(grid, smem, mid, parent, child_table, n_parent, n_child, phi, Rc2 / 2, Rp, KS, MT, A, \
-                            trans, G, n_ct, n_task, st);                                                            \
+#define PO_TW(N, M, O)                                                                                             \
+  if (NPT == N && MTW == M && odd == O) {                                                                         \
+    launch_theta_warp<N, M, O>(grid, smem, mid, parent, child_table, n_parent, n_child, phi, Rc2 / 2, Rp, KS, MT, \
+                               A, trans, G, n_ct, n_task, st);                                                     \
   } else
-  PO_TW(1, 1) PO_TW(1, 2) PO_TW(1, 3) PO_TW(1, 4) PO_TW(2, 1) PO_TW(2, 2) {
+  PO_TW(1, 1, false) PO_TW(1, 2, false) PO_TW(1, 3, false) PO_TW(1, 4, false) PO_TW(2, 1, false) PO_TW(2, 2, false)
+  PO_TW(1, 1, true) PO_TW(1, 2, true) PO_TW(1, 3, true) PO_TW(1, 4, true) {
     return fail(PO_ERR_INTERNAL, "theta pass variant");
   }
 #undef PO_TW
@@ -597,15 +608,18 @@ static void b_fragments(int Pout, int Kin, int Kp, F W, std::vector<uint32_t> &o
 }
 
 // Forward phi matrix in mirror-pair column order (the packed row pass):
-// n-tile nt, slot 2q + w holds parent column nt*4 + q + w Pp/2, so a lane's
-// D fragment holds a column and its mirror for two rows.
+// n-tile nt, slot 2q + w holds parent column nt*4 + q + w H (H = ceil(Pp/2)
+// pairs), so a lane's D fragment holds a column and its partner for two rows.
+// An odd Pp (reference theta mode, where the columns of a level need not pair
+// up as phi and phi + pi) leaves one phantom partner, column Pp: a zero column.
 void build_phi_matrix(int Pc, int Pp, int Kp, std::vector<uint32_t> &out) {
-  const int half = Pp / 2, NTt = (half + 3) / 4;
+  const int half = (Pp + 1) / 2, NTt = (half + 3) / 4;
   b_fragments(NTt * 8, Pc, Kp,
               [&](int n, int k) {
                 const int j = (n >> 3) * 4 + ((n & 7) >> 1);
-                if (j >= half) return 0.0;
-                return trig_kernel(Pc, (double)(j + (n & 1) * half) / Pp - (double)k / Pc);
+                const int col = j + (n & 1) * half;
+                if (j >= half || col >= Pp) return 0.0;
+                return trig_kernel(Pc, (double)col / Pp - (double)k / Pc);
               },
               out);
 }
@@ -650,7 +664,7 @@ __global__ void __launch_bounds__(128, 6) k_interp_rows_mma(const float2 *__rest
                                                          const uint4 *__restrict__ Bm, int b_in_smem, int Rr,
                                                          int npad) {
   extern __shared__ uint4 bsm[];
-  const int KS = Kp / 16, NTt = PACK ? (Pp / 2 + 3) / 4 : (Pp + 7) / 8;
+  const int KS = Kp / 16, NTt = PACK ? ((Pp + 1) / 2 + 3) / 4 : (Pp + 7) / 8;
   const int ng = blockIdx.y * kRowNG;
   const int nq = NTt - ng < kRowNG ? NTt - ng : kRowNG;  // n-tiles in this group
   const uint4 *Bg = Bm + (size_t)ng * KS * 32;
@@ -678,7 +692,7 @@ __global__ void __launch_bounds__(128, 5) k_rows_mma_narrow(const float2 *__rest
                                                                           const uint4 *__restrict__ Bm) {
   constexpr int KS = 2;
   __shared__ uint4 bsm[NG * KS * 32];
-  const int half = Pp / 2, nq = (half + 3) / 4;
+  const int half = (Pp + 1) / 2, nq = (half + 3) / 4;
   for (int e = threadIdx.x; e < NG * KS * 32; e += blockDim.x)
     bsm[e] = e < nq * KS * 32 ? Bm[e] : make_uint4(0u, 0u, 0u, 0u);
   __syncthreads();
@@ -754,7 +768,7 @@ static po_status launch_rows(int pack, const float2 *src, void *dst, int64_t nro
                              const uint32_t *Bm, int sm_count, cudaStream_t st, int Rr = 0, int npad = 0) {
   if (nrows <= 0) return PO_OK;
   if (Kp % 16 || Kp < Pc) return fail(PO_ERR_INTERNAL, "phi matrix K padding");
-  const int NTt = pack ? (Pp / 2 + 3) / 4 : (Pp + 7) / 8;
+  const int NTt = pack ? ((Pp + 1) / 2 + 3) / 4 : (Pp + 7) / 8;
   const int ngroups = (NTt + kRowNG - 1) / kRowNG;
   const size_t bbytes = sizeof(uint4) * (size_t)kRowNG * (Kp / 16) * 32;
   const bool b_smem = bbytes <= 128 * 1024;
@@ -799,7 +813,7 @@ po_status launch_interp_rows_packed(const float2 *src, uint4 *dst, int64_t n_pat
 
 po_status launch_interp_rows_core(const float2 *src, uint8_t *dst, int64_t n_patterns, int Rc, int Rr, int npad,
                                   int Pc, int Pp, int Kp, const uint32_t *Bm, int sm_count, cudaStream_t st) {
-  if (Rr % 16 || Rr < Rc || npad % 8 || npad < 6 * Pp || n_patterns % 6)
+  if (Rr % 16 || Rr < Rc || npad % 8 || npad < 6 * Pp || n_patterns % 6 || Pp % 2)
     return fail(PO_ERR_INTERNAL, "core-matrix row pass padding");
   return launch_rows(2, src, dst, n_patterns * (int64_t)Rr, Rc, Pc, Pp, Kp, Bm, sm_count, st, Rr, npad);
 }
@@ -815,9 +829,11 @@ po_status init_interp_mma_attributes(int max_smem) {
   PO_CUDA(cudaFuncSetAttribute(k_interp_rows_mma<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
   PO_CUDA(cudaFuncSetAttribute(k_interp_rows_mma<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
   PO_CUDA(cudaFuncSetAttribute(k_interp_rows_mma<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
-#define PO_TW_ATTR(N, M) \
-  PO_CUDA(cudaFuncSetAttribute(k_theta_warp<N, M>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
-  PO_TW_ATTR(1, 1) PO_TW_ATTR(1, 2) PO_TW_ATTR(1, 3) PO_TW_ATTR(1, 4) PO_TW_ATTR(2, 1) PO_TW_ATTR(2, 2)
+#define PO_TW_ATTR(N, M, O) \
+  PO_CUDA(cudaFuncSetAttribute(k_theta_warp<N, M, O>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
+  PO_TW_ATTR(1, 1, false) PO_TW_ATTR(1, 2, false) PO_TW_ATTR(1, 3, false) PO_TW_ATTR(1, 4, false)
+  PO_TW_ATTR(2, 1, false) PO_TW_ATTR(2, 2, false)
+  PO_TW_ATTR(1, 1, true) PO_TW_ATTR(1, 2, true) PO_TW_ATTR(1, 3, true) PO_TW_ATTR(1, 4, true)
 #undef PO_TW_ATTR
   return PO_OK;
 }

@@ -232,7 +232,7 @@ po_status init_leaf_mma_attributes() {
 // Whether the phi pass from a leaf grid of Rc x Pc to Pp parent columns can run
 // fused in the leaf kernel: one n-tile group, fragments within s_b (GC = 1).
 bool leaf_row_fusion_fits(int Pc, int Pp, int Kp) {
-  const int NTt = (Pp / 2 + 3) / 4, KS = Kp / 16;
+  const int NTt = ((Pp + 1) / 2 + 3) / 4, KS = Kp / 16;
   return NTt <= kRowNG && Kp >= Pc && Kp % 16 == 0 && NTt * KS * 32 <= (kPC / 8) * ((12 + 7) / 8) * 32;
 }
 
@@ -245,7 +245,7 @@ po_status launch_leaf_mma(const float *const g[7], const int32_t *leaf_begin, co
   if (fuse_mid) {
     if (!leaf_row_fusion_fits(Pc, Pp, Kp) || (int64_t)Rc * Pc != ndir)
       return fail(PO_ERR_INTERNAL, "leaf/phi-pass fusion does not fit");
-    fz = LeafRowFusion{(const uint4 *)fuse_B, fuse_mid, Kp / 16, (Pp / 2 + 3) / 4, Rc, Pc, Pp};
+    fz = LeafRowFusion{(const uint4 *)fuse_B, fuse_mid, Kp / 16, ((Pp + 1) / 2 + 3) / 4, Rc, Pc, Pp};
   }
   if (n_lambda > 65535) return fail(PO_ERR_UNSUPPORTED, "too many wavelengths for one launch");
   dim3 grid((unsigned)n_leaves, (unsigned)n_lambda);

@@ -16,9 +16,11 @@ namespace wavepo {
 // PACK (forward pass feeding k_theta_warp): the phi matrix is in mirror-pair
 // column order (build_phi_matrix), rows are indexed over patterns of Rc2 = Rc
 // rounded up to even rows (row Rc of an odd Rc is a zero row), and the output
-// is S = h_j + h_j', D = h_j - h_j' (j' = j + Pp/2) split into bf16 hi + lo in
-// row pairs: per pattern [Rc2/2][Pp/2][re, im] uint4 {S hi pair, S lo pair,
-// D hi pair, D lo pair}, each pair holding rows 2 tp (low half) and 2 tp + 1.
+// is S = h_j + h_j', D = h_j - h_j' (j' = j + H, H = ceil(Pp/2) pairs; an odd
+// Pp has one phantom column j' = Pp, a zero column of the phi matrix) split
+// into bf16 hi + lo in row pairs: per pattern [Rc2/2][H][re, im] uint4 {S hi
+// pair, S lo pair, D hi pair, D lo pair}, each pair holding rows 2 tp (low
+// half) and 2 tp + 1.
 // Lane g and lane g^1 (4 apart) hold the two rows of a pair; the even lane
 // stores the real parts, the odd lane the imaginary parts.
 // PACK == 2 (forward pass feeding the tcgen05 theta pass, po_theta_tc.cu): the
@@ -43,7 +45,7 @@ __device__ __forceinline__ void rows_block(int64_t blk, int64_t row_lo, int64_t 
                                            void *__restrict__ dst_, int Rc, int Rc2, int Pc, int Pp, int KS,
                                            const uint4 *B, int ng, int nq, int npad) {
   const int lane = threadIdx.x & 31, g = lane >> 2, tq = lane & 3;
-  const int half = Pp / 2;
+  const int half = (Pp + 1) / 2;  // PACK == 2: Pp is even
   const int64_t r = blk * 8 + g;
   const bool rok = r >= row_lo && r < row_hi;
   int64_t srow = r;

@@ -380,16 +380,17 @@ po_status po_create(po_ctx **out, const po_config *cfg) {
   // Double cover: every level.  Reference theta mode: the levels whose maps are
   // real and column-independent -- not where the Nyquist quirk of
   // interpolation.h:66 reaches a parent column (columns past it keep the
-  // unsplit Nyquist bin: a complex, column-dependent map), not between equal
-  // sizes (the reference halves the Nyquist bin there) and only with an even
-  // parent phi grid (mirror column pairs); the other levels keep the FFTs.
+  // unsplit Nyquist bin: a complex, column-dependent map) and not between
+  // equal sizes (the reference halves the Nyquist bin there); the other levels
+  // keep the FFTs.  An odd parent phi grid pairs column j with j + (Phi+1)/2
+  // (one phantom partner) on the warp-level theta pass.
   for (int l = 0; l < d; ++l) {
     if (cfg->interp_method != PO_INTERP_TENSOR) break;
     if (c->mirror) {
       c->tt_level[l] = true;
     } else {
       const bool quirk = cfg->nyquist_quirk && c->T[l + 1] % 2 == 0 && c->Phi[l] > 256 * (c->T[l + 1] / 256 + 1);
-      c->tt_level[l] = !quirk && c->T[l + 1] != c->T[l] && c->Phi[l + 1] != c->Phi[l] && c->Phi[l] % 2 == 0;
+      c->tt_level[l] = !quirk && c->T[l + 1] != c->T[l] && c->Phi[l + 1] != c->Phi[l];
     }
     c->tensor_theta = c->tensor_theta || c->tt_level[l];
   }
@@ -407,7 +408,7 @@ po_status po_create(po_ctx **out, const po_config *cfg) {
       std::vector<uint16_t> tall, tone;
       std::vector<double> Mp, Mm;
       for (int l = 0; l < d; ++l) {
-        if (!c->tt_level[l] || !theta_on_tcgen05(c->R[l], c->Phi[l])) continue;
+        if (!c->tt_level[l] || c->Phi[l] % 2 || !theta_on_tcgen05(c->R[l], c->Phi[l])) continue;
         c->tc_level[l] = true;
         c->tc_kr[l] = (c->R[l + 1] + 15) / 16 * 16;
         theta_plus_minus(c->T[l + 1], c->T[l], c->R[l + 1], c->R[l], c->tc_kr[l], Mp, Mm, c->mirror != 0);
@@ -794,11 +795,11 @@ static po_status prepare_solve(po_ctx *c, const po_geometry *g, const po_illum *
   for (int l = 0; l <= d; ++l)
     lvl_max = std::max(lvl_max, (size_t)P.tree.level[l].count * 6 * (size_t)c->R[l] * c->Phi[l]);
   for (int l = 0; l < d; ++l) {
-    // float2 words per slot and child: 6 components x R + 1 rows x Phi (packed
-    // pairs), or 4 bf16 matrices of tc_kr x npad (core matrices of the tcgen05
+    // float2 words per slot and child: 6 components x R + 1 rows x Phi rounded
+    // up to even (packed pairs), or 4 bf16 matrices of tc_kr x npad (core matrices of the tcgen05
     // pass, the six components in one column space) = tc_kr x npad float2
     const size_t per = c->tc_level[l] ? (size_t)c->tc_kr[l] * theta_tc_npad(c->Phi[l])
-                                      : (size_t)6 * (c->R[l + 1] + 1) * c->Phi[l];
+                                      : (size_t)6 * (c->R[l + 1] + 1) * (c->Phi[l] + (c->Phi[l] & 1));
     mid_max = std::max(mid_max, (size_t)P.tree.level[l + 1].count * per);
   }
   P.chunks = plan_chunks(L, G, chunk_slot_count(budget, 8.0 * (2.0 * lvl_max + mid_max) + leaf_tc_per_slot, S));
