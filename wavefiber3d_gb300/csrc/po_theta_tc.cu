@@ -214,8 +214,13 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_theta_tc(
       const uint8_t *abase = Atc + (size_t)mtile * Kr * 1024;
       const size_t col_off = (size_t)nc * (kTcN / 8) * 256;
       constexpr uint32_t bmat = kTcN / 8 * 256;  // bytes of one matrix's share of a chunk
+      int ci = 0, kc = -1;  // child and K chunk of step t (no division on this thread's path)
       for (int t = 0; t < nsteps && ok; ++t) {
-        const int b = t % NST, ci = t / KC, kc = t % KC;
+        if (++kc == KC) {
+          kc = 0;
+          ++ci;
+        }
+        const int b = t % NST;
         if (t >= NST && !mbar_wait(smem_addr(&empty[b]), ((t / NST) - 1) & 1, abort_flag)) {
           ok = false;
           break;
@@ -250,8 +255,13 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_theta_tc(
       constexpr uint64_t mA = (kAStage / 4) >> 4, mB = (kBStage / 4) >> 4;  // one matrix, in descriptor units
       bool ok = true;
       int committed = 0;
+      int ci = 0, kc = -1;  // child and K chunk of step s (no division on the issuing path)
       for (int s = 0; s < nsteps; ++s) {
-        const int b = s % NST, ci = s / KC, kc = s % KC;
+        if (++kc == KC) {
+          kc = 0;
+          ++ci;
+        }
+        const int b = s % NST;
         if (kc == 0 && ci >= 2 && !mbar_wait(smem_addr(&acce[ci & 1]), ((ci >> 1) - 1) & 1, abort_flag)) {
           ok = false;
           break;
