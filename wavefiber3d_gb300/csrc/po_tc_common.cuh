@@ -45,8 +45,11 @@ __device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
 }
 
 // true once the mbarrier has completed the phase of the given parity; false
-// after the time limit, or as soon as another role has given up (abort)
+// after the time limit, or as soon as another role has given up (abort).  The
+// clock is read only once the first try has failed: a phase that is already
+// complete costs one try on the issuing threads' per-step path.
 __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, const volatile int *abort) {
+  if (mbar_try(bar, parity)) return true;
   const unsigned long long t0 = global_ns();
   for (int it = 0;; ++it) {
     if (mbar_try(bar, parity)) return true;
