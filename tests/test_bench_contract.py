@@ -30,3 +30,13 @@ def test_point_dirs_per_step_is_the_headline_unit():
     illum = api.Illumination(bench.LAMBDAS, [0.0], [0.0], api.PO_POL_TM, bench.ETA, bench.SIGMA)
     # N points x 180 x 360 directions x 25 wavelengths x 1 incidence x 1 polarisation
     assert bench.point_dirs_per_step(illum) == 400000 * 180 * 360 * 25
+
+
+def test_ellipsoid_workload_in_the_reference_theta_mode():
+    # --theta-mode reference: the reference's own grids, whose odd levels
+    # (197 and 37 columns) run on the tensor path with a phantom partner column
+    from wavefiber3d_gb300 import api
+    _, cfg, illum = bench.make_workload("split_bf16", "tensor", 0, 1, 1, "reference")
+    assert cfg.theta_mode == api.PO_THETA_REFERENCE and cfg.interp_method == api.PO_INTERP_TENSOR
+    assert list(cfg.n_phi) == [360, 197, 108, 62, 37, 24]
+    assert illum.n_patterns == 1
