@@ -91,8 +91,10 @@ po_status launch_interp_cols(const float2 *mid, float2 *parent, const int32_t *c
                              int64_t n_child, int phi, int Rc, int Rp, const FftPlan &pin, const FftPlan &pout,
                              const float2 *twiddles, const float4 *trans, int n_slots, int G, int quirk_reach,
                              float scale, int ncomp, int mirror, int ref_nyquist, cudaStream_t st);
-// tensor-core theta pass, double cover (po_interp_mma.cu).  mid: the packed
-// output of launch_interp_rows_packed; Kp = Rc rounded up to even, then to 16.
+// tensor-core theta pass (po_interp_mma.cu): double cover, or the reference
+// theta mode's real column-independent map (an odd phi pairs column j with
+// j + (phi+1)/2).  mid: the packed output of launch_interp_rows_packed; Kp =
+// Rc rounded up to even, then to 16.
 size_t theta_matrix_words(int Rp, int Kp);
 size_t theta_pair_words(int Rp, int Kp);
 void build_theta_matrix(int Tc, int Tp, int Rc, int Rp, int Kp, std::vector<uint32_t> &out, bool mirror = true);
