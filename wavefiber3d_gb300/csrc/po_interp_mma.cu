@@ -178,7 +178,7 @@ void build_theta_matrix_adj(int Tc, int Tp, int Rc, int Rp, int Kp, std::vector<
 // H = (Phi + 1)/2, whose partner is not at phi + pi: its translation phase
 // comes from its own table entry, and the phantom partner Phi is not stored.
 // mid (from k_interp_rows_mma<1>): per (slot, child, component)
-// [Rc2/2][Phi/2][re, im] uint4 {S hi pair, S lo pair, D hi pair, D lo pair} --
+// [Rc2/2][(Phi+1)/2][re, im] uint4 {S hi pair, S lo pair, D hi pair, D lo pair} --
 // a lane's B registers for the S and the D n-tile in one 16-byte load.  The
 // CTA stages its slice of the theta matrices in shared memory once; after
 // that warps run independently: B fragments of the next k-step (or next
