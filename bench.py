@@ -370,11 +370,12 @@ def fiber_incidences(n: int = FIBER_INC):
     return list(-math.pi / 2 + 1e-10 + math.pi / 180 * idx), [0.0] * n
 
 
-def fiber_config(precision: str, interp: str = "tensor"):
+def fiber_config(precision: str, interp: str = "tensor", workspace_gb: float = 0.0):
     from wavefiber3d_gb300 import api
     return api.Config.reference_rule(FIBER_DEPTH, N_THETA, N_PHI, FIBER_BOX_MIN, FIBER_BOX_MAX, FIBER_LENGTH,
                                      2 * max(FIBER_RADII), 1.2, precision=PRECISIONS[precision],
-                                     interp_method=INTERP[interp])  # treePO.cu:353-359
+                                     interp_method=INTERP[interp],
+                                     max_workspace_bytes=int(workspace_gb * 1e9))  # treePO.cu:353-359
 
 
 def run_fiber(args, world, rank, local):
@@ -408,7 +409,7 @@ def run_fiber(args, world, rank, local):
     n_inc = max(1, min(FIBER_INC, args.fiber_incidences))
     th, ph = fiber_incidences(n_inc)
     illum = api.Illumination(lams, th, ph, api.PO_POL_TM, ETA, FIBER_SIGMA)
-    cfg = fiber_config(args.precision, args.interp)
+    cfg = fiber_config(args.precision, args.interp, args.workspace_gb)
     solver = api.Solver(cfg)
     out = torch.empty(solver.out_shape(illum), dtype=torch.float32, device=dev)
     out_host = torch.empty(solver.out_shape(illum), dtype=torch.float32).pin_memory()
@@ -530,6 +531,7 @@ def run_fiber(args, world, rank, local):
                    "directions": N_THETA * N_PHI, "level_grids": [list(cfg.n_theta), list(cfg.n_phi)],
                    "precision": args.precision, "theta_mode": "double cover", "theta_interpolation": args.interp,
                    "beam_sigma_m": FIBER_SIGMA,
+                   "workspace_cap_gb": args.workspace_gb if args.workspace_gb > 0 else "half the device",
                    "l2": "no flush: inputs (95 MB), tree and level buffers (>100 GB) are far larger than L2",
                    "parallelism": f"replicas x{world}"},
         "patterns_per_s": illum.n_patterns * world / (ms_step_max * 1e-3),
@@ -1115,6 +1117,9 @@ def main():
     ap.add_argument("--ref-leaf-dirs", type=int, default=24, help="reference-cuda: leaf directions timed")
     ap.add_argument("--ref-children", type=int, default=48, help="reference-cuda: children timed per level")
     ap.add_argument("--fiber-lambdas", type=int, default=25, help="wavelengths per fiber step (25 = the workload)")
+    ap.add_argument("--workspace-gb", type=float, default=0.0,
+                    help="fiber: the solver's workspace cap in GB, which sets how many patterns go through the tree "
+                         "at once (0: the library default, half the device)")
     ap.add_argument("--e2e-steps", type=int, default=2, help="steps of the end-to-end (host buffers) timing")
     ap.add_argument("--ref-dirs", type=int, default=256, help="directions per step of the --impl reference arm")
     ap.add_argument("--fiber-dirs", type=int, default=512, help="directions of the fiber accuracy sample")

@@ -493,20 +493,27 @@ struct SlotChunk {
   int gc;      // slots per wavelength inside the chunk
 };
 
+// Contiguous slot ranges of at most chunk_slots slots: whole wavelengths when
+// one fits, else runs of one wavelength's incidences.  The ranges are as even
+// as the count allows (64 incidences under a cap of 27: 22 + 21 + 21, not
+// 27 + 27 + 10), so that no chunk leaves the upper levels' launches short of
+// work; the first range is the largest (the buffers are sized by it).
 static std::vector<SlotChunk> plan_chunks(int L, int G, int chunk_slots) {
   std::vector<SlotChunk> v;
-  const int S = L * G;
   if (chunk_slots >= G) {
-    chunk_slots = (chunk_slots / G) * G;
-    for (int s0 = 0; s0 < S; s0 += chunk_slots) {
-      int ns = std::min(chunk_slots, S - s0);
-      v.push_back({s0, ns, s0 / G, ns / G, G});
+    const int cap = chunk_slots / G, n = (L + cap - 1) / cap;  // wavelengths per chunk, chunks
+    for (int i = 0, l0 = 0; i < n; ++i) {
+      const int nl = (L - l0 + n - i - 1) / (n - i);  // the remaining wavelengths over the remaining chunks
+      v.push_back({l0 * G, nl * G, l0, nl, G});
+      l0 += nl;
     }
   } else {
+    const int n = (G + chunk_slots - 1) / chunk_slots;
     for (int l = 0; l < L; ++l)
-      for (int g0 = 0; g0 < G; g0 += chunk_slots) {
-        int ns = std::min(chunk_slots, G - g0);
+      for (int i = 0, g0 = 0; i < n; ++i) {
+        const int ns = (G - g0 + n - i - 1) / (n - i);
         v.push_back({l * G + g0, ns, l, 1, ns});
+        g0 += ns;
       }
   }
   return v;
